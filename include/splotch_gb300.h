@@ -1,0 +1,147 @@
+/*
+ * splotch_gb300.h -- C ABI of the GB300 particle renderer (libsplgpu.so).
+ *
+ * Drop-in boundary for Splotch's host renderer.  The C++ shim in
+ * splotch_gb300/shim/ implements
+ *     void host_rendering(paramfile&, std::vector<particle_sim>&, render_context&)
+ * (splotch/splotch_host.h:43, defined at splotch/splotch_host.cc:711) on top
+ * of these entry points; ctypes / cgo-style callers bind them directly.
+ *
+ * Conventions: every entry point returns spl_status (0 = success), never
+ * throws and never traps the GPU; on failure spl_last_error_string() holds a
+ * one-line reason.  Plain pointers and sizes only.  Images are x-major like
+ * the reference's arr2<COLOUR> (cxxsupport/arr.h:429): pixel (x,y) channel c
+ * lives at pic[(x*yres + y)*3 + c].
+ */
+#ifndef SPLOTCH_GB300_H
+#define SPLOTCH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPL_MAX_TYPES 8
+
+typedef int spl_status;
+enum {
+  SPL_OK = 0,
+  SPL_ERR_INVALID = 1,     /* bad argument (planck_fail in the reference) */
+  SPL_ERR_CUDA = 2,        /* CUDA runtime error */
+  SPL_ERR_ALLOC = 3,       /* device or pinned allocation failed */
+  SPL_ERR_CAPACITY = 4,    /* a fixed-capacity buffer overflowed */
+  SPL_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  SPL_ERR_UNSUPPORTED = 6  /* option not implemented on this path */
+};
+
+/* Memory space of a caller buffer. */
+enum { SPL_MEM_HOST = 0, SPL_MEM_DEVICE = 1 };
+/* Particle layout: AoS = particle_sim records (splotch/splotchutils.h:52-72,
+   36-byte stride); SoA = one array per field. */
+enum { SPL_LAYOUT_AOS = 0, SPL_LAYOUT_SOA = 1 };
+/* What spl_render writes back into an AoS input.  FULL reproduces the
+   reference's in-place side effects (projected x,y,z,r,I, colourised e,
+   active, z-sorted order when a_eq_e is false); NONE leaves it untouched. */
+enum { SPL_WRITEBACK_NONE = 0, SPL_WRITEBACK_FULL = 1 };
+/* Compositing order for the ordered (a_eq_e=false) splat.  BACK_TO_FRONT
+   applies particles in list order exactly like render_new; FRONT_TO_BACK
+   evaluates the same sum in reverse with early exit once every channel's
+   transmittance is below spl_frame_desc.ftb_epsilon. */
+enum { SPL_ORDER_BACK_TO_FRONT = 0, SPL_ORDER_FRONT_TO_BACK = 1 };
+
+typedef struct spl_context spl_context;
+
+/* Camera quantities of particle_project's set-up (splotch_host.cc:62-110),
+   computed on the host bit-for-bit like the reference. */
+typedef struct {
+  float mat[12]; /* TRANSFORM matrix in TRANSMAT::p order */
+  float res2, ycorr, fovfct, xfac;
+  double xshift, yshift;
+} spl_camera;
+
+/* Everything host_rendering() reads from the paramfile and render_context.
+   Fill with spl_frame_desc_defaults() (the reference defaults), then set. */
+typedef struct {
+  int xres, yres;           /* "xres" (800), "yres" (=xres) */
+  float fov;                /* "fov" (45), degrees */
+  float zmin, zmax;         /* "zmin" (0), "zmax" (1e23) */
+  float minrad_pix;         /* "minrad_pix" (1) */
+  int projection;           /* "projection" (true) */
+  int ptypes;               /* "ptypes" (1) */
+  float smooth_factor[SPL_MAX_TYPES];  /* "smooth_factor{t}" (1) */
+  float brightness[SPL_MAX_TYPES];     /* "brightness{t}" (1) */
+  int color_is_vector[SPL_MAX_TYPES];  /* "color_is_vector{t}" (false) */
+  float b_brightness;       /* render_context::b_brightness */
+  int pal_n[SPL_MAX_TYPES];            /* palette of type t (rc.amap[t]) */
+  const double *pal_x[SPL_MAX_TYPES];  /* host: n knot positions, ascending */
+  const float *pal_rgb[SPL_MAX_TYPES]; /* host: 3n floats, r,g,b per knot */
+  int a_eq_e;               /* "a_eq_e" (true) */
+  float gray_absorption;    /* "gray_absorption" (0.2) */
+  int sort_type;            /* "sort_type" (1) */
+  int tile_size;            /* "tile_size_cpu" (50); 1..64 on the GPU */
+  double campos[3], lookat[3], sky[3], centerpos[3]; /* render_context */
+  /* GPU-only knobs (no reference counterpart) */
+  int order_mode;           /* SPL_ORDER_* (default BACK_TO_FRONT) */
+  float ftb_epsilon;        /* transmittance cut for FRONT_TO_BACK (1e-9) */
+} spl_frame_desc;
+
+/* Particle input.  AoS: aos points at n particle_sim records.  SoA: x..I,
+   cr/cg/cb (e.r/e.g/e.b) are float arrays; type may be NULL (all type 0). */
+typedef struct {
+  int64_t n;
+  int layout;   /* SPL_LAYOUT_* */
+  int memspace; /* SPL_MEM_* */
+  void *aos;
+  const float *x, *y, *z, *r, *I, *cr, *cg, *cb;
+  const uint16_t *type;
+} spl_particles;
+
+typedef struct {
+  float *pic;   /* x-major xres*yres*3 floats */
+  int memspace; /* SPL_MEM_* */
+} spl_image;
+
+/* Per-stage device times of the last spl_render call (CUDA events). */
+typedef struct {
+  float h2d_ms, project_ms, sort_ms, bin_ms, splat_ms, d2h_ms, total_ms;
+  int64_t n_active;
+  int64_t n_entries;   /* (particle, tile) bin entries */
+  int64_t n_tiles;
+  int kernel_launches; /* kernels launched by the call */
+} spl_stats;
+
+/* ---- context ---------------------------------------------------------- */
+spl_status spl_context_create(spl_context **ctx, int device);
+spl_status spl_context_destroy(spl_context *ctx);
+/* Bind the context to a CUDA stream (cudaStream_t as void*; NULL = legacy). */
+spl_status spl_context_set_stream(spl_context *ctx, void *stream);
+const char *spl_last_error_string(void);
+const char *spl_version(void);
+
+/* ---- frame set-up ----------------------------------------------------- */
+void spl_frame_desc_defaults(spl_frame_desc *d);
+/* The camera set-up of particle_project (splotch/splotch_host.cc:62-110). */
+spl_status spl_camera_setup(const spl_frame_desc *d, spl_camera *cam);
+
+/* ---- plain render: replaces host_rendering (splotch_host.cc:711-834) --- */
+spl_status spl_render(spl_context *ctx, const spl_frame_desc *d,
+                      const spl_particles *p, spl_image *out, int writeback);
+spl_status spl_get_stats(const spl_context *ctx, spl_stats *s);
+
+/* ---- test hooks: state of the last spl_render (host destinations) ----- */
+/* Projected + colourised particles in original order (particle_sim layout):
+   the reference's particle_project + particle_colorize side effects. */
+spl_status spl_debug_get_projected(spl_context *ctx, void *aos_out, int64_t n);
+/* Visiting order (stable sort permutation); identity when a_eq_e. */
+spl_status spl_debug_get_order(spl_context *ctx, uint32_t *perm_out, int64_t n);
+/* Tile bins: tile_start has ntiles+1 entries; entries hold particle indices. */
+spl_status spl_debug_get_bins(spl_context *ctx, int64_t *tile_start_out,
+                              int64_t ntiles_plus_one, uint32_t *entries_out,
+                              int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

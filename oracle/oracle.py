@@ -1,0 +1,321 @@
+"""ctypes front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Two checkers:
+
+* ``Port``  -- liboracle.so, the plain-C restatement in spl_oracle.c (builds
+  anywhere, including the AArch64 GPU host), with an FP64 splat and FP64 adjoint.
+* ``Ref``   -- oracle/_ref/libsplotch_ref*.so, the reference's own
+  host_rendering/particle_project/render_new compiled from its sources by
+  build_ref.sh (only where those sources exist).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module.  The product path (splotch_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+PORT_LIB = BUILD / "liboracle.so"
+REF_DIR = HERE / "_ref"
+MAXT = 8
+
+PARTICLE_DTYPE = np.dtype({
+    "names": ["er", "eg", "eb", "x", "y", "z", "r", "I", "type", "active", "pad"],
+    "formats": ["<f4"] * 8 + ["<u2", "u1", "u1"],
+    "offsets": [0, 4, 8, 12, 16, 20, 24, 28, 32, 34, 35],
+    "itemsize": 36,
+})
+
+
+def build_port(force: bool = False) -> Path:
+    """Compile spl_oracle.c (plain C, OpenMP, no fused multiply-add)."""
+    BUILD.mkdir(exist_ok=True)
+    src = HERE / "spl_oracle.c"
+    hdr = HERE / "spl_oracle.h"
+    if (not force and PORT_LIB.exists()
+            and PORT_LIB.stat().st_mtime >= max(src.stat().st_mtime, hdr.stat().st_mtime)):
+        return PORT_LIB
+    cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
+           str(src), "-o", str(PORT_LIB), "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        raise RuntimeError(f"oracle build failed:\n{r.stderr}")
+    return PORT_LIB
+
+
+def build_ref() -> bool:
+    """Compile the reference sources into oracle/_ref (no-op without them)."""
+    r = subprocess.run(["bash", str(HERE / "build_ref.sh")], capture_output=True, text=True)
+    return r.returncode == 0 and (REF_DIR / "libsplotch_ref.so").exists()
+
+
+class SpoParams(C.Structure):
+    _fields_ = [
+        ("xres", C.c_int), ("yres", C.c_int), ("fov", C.c_float), ("zmin", C.c_float),
+        ("zmax", C.c_float), ("minrad_pix", C.c_float), ("projection", C.c_int),
+        ("ptypes", C.c_int), ("smooth_factor", C.c_float * MAXT),
+        ("brightness", C.c_float * MAXT), ("color_is_vector", C.c_int * MAXT),
+        ("b_brightness", C.c_float), ("pal_n", C.c_int * MAXT),
+        ("pal_x", C.c_void_p * MAXT), ("pal_rgb", C.c_void_p * MAXT), ("a_eq_e", C.c_int),
+        ("gray_absorption", C.c_float), ("sort_type", C.c_int), ("tile_size", C.c_int),
+        ("campos", C.c_double * 3), ("lookat", C.c_double * 3), ("sky", C.c_double * 3),
+        ("centerpos", C.c_double * 3),
+    ]
+
+
+class SpoCamera(C.Structure):
+    _fields_ = [("mat", C.c_float * 12), ("res2", C.c_float), ("ycorr", C.c_float),
+                ("fovfct", C.c_float), ("xfac", C.c_float), ("xshift", C.c_double),
+                ("yshift", C.c_double)]
+
+
+def _get(params: dict, key: str, default):
+    """paramfile::find semantics on a plain dict of strings (no insertion)."""
+    if key not in params:
+        return default
+    s = str(params[key]).strip()
+    if isinstance(default, bool):
+        return s.lower() in ("t", "y", "true", ".true.")
+    if isinstance(default, int):
+        return int(s)
+    if isinstance(default, float):
+        return float(s)
+    return s
+
+
+def make_params(params: dict, rc, keep: list) -> SpoParams:
+    """Everything host_rendering reads (splotch_host.cc:62-109, 256-265, 806-825)."""
+    p = SpoParams()
+    p.xres = _get(params, "xres", 800)
+    p.yres = _get(params, "yres", p.xres)
+    p.fov = _get(params, "fov", 45.0)
+    p.zmin = _get(params, "zmin", 0.0)
+    p.zmax = _get(params, "zmax", 1e23)
+    p.minrad_pix = _get(params, "minrad_pix", 1.0)
+    p.projection = 1 if _get(params, "projection", True) else 0
+    p.ptypes = _get(params, "ptypes", 1)
+    for t in range(p.ptypes):
+        p.smooth_factor[t] = _get(params, f"smooth_factor{t}", 1.0)
+        p.brightness[t] = _get(params, f"brightness{t}", 1.0)
+        p.color_is_vector[t] = 1 if _get(params, f"color_is_vector{t}", False) else 0
+        if not p.color_is_vector[t]:
+            pal = rc.amap[t]
+            x = np.ascontiguousarray(pal.x, np.float64)
+            rgb = np.ascontiguousarray(pal.rgb, np.float32)
+            keep += [x, rgb]
+            p.pal_n[t] = len(x)
+            p.pal_x[t] = x.ctypes.data
+            p.pal_rgb[t] = rgb.ctypes.data
+    p.b_brightness = float(rc.b_brightness)
+    p.a_eq_e = 1 if _get(params, "a_eq_e", True) else 0
+    p.gray_absorption = _get(params, "gray_absorption", 0.2)
+    p.sort_type = _get(params, "sort_type", 1)
+    p.tile_size = int(_get(params, "tile_size_cpu", 50.0))
+    for i in range(3):
+        p.campos[i] = float(rc.campos[i])
+        p.lookat[i] = float(rc.lookat[i])
+        p.sky[i] = float(rc.sky[i])
+        p.centerpos[i] = float(rc.centerpos[i])
+    return p
+
+
+def _vp(a):
+    return None if a is None else a.ctypes.data
+
+
+class Port:
+    """The C restatement (spl_oracle.c)."""
+
+    def __init__(self, threads: int = 0):
+        lib = C.CDLL(str(build_port()))
+        vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int
+        for name, res, args in [
+            ("spo_set_threads", None, [i32]),
+            ("spo_get_threads", i32, []),
+            ("spo_camera_setup", i32, [vp, vp]),
+            ("spo_project", None, [vp, vp, vp, i64]),
+            ("spo_colorize", None, [vp, vp, i64]),
+            ("spo_sort_perm", i32, [vp, i64, i32, vp]),
+            ("spo_apply_perm", None, [vp, vp, i64, vp]),
+            ("spo_bin", i64, [vp, vp, i64, i32, i32, i32, vp, vp]),
+            ("spo_render_fp32", i64, [vp, vp, i64, i32, i32, i32, i32, C.c_float, i32, vp]),
+            ("spo_render_fp64", i64, [vp, vp, i64, i32, i32, i32, i32, C.c_double, vp]),
+            ("spo_host_rendering", i32, [vp, vp, i64, i32, vp]),
+            ("spo_splat_adjoint_fp64", i32,
+             [vp, vp, i64, i32, i32, i32, i32, C.c_double, vp, vp, vp, vp, vp]),
+        ]:
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        self.lib = lib
+        if threads:
+            lib.spo_set_threads(threads)
+
+    @property
+    def threads(self) -> int:
+        return self.lib.spo_get_threads()
+
+    def camera(self, params: dict, rc) -> SpoCamera:
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        cam = SpoCamera()
+        if self.lib.spo_camera_setup(C.byref(prm), C.byref(cam)):
+            raise ValueError("degenerate matrix")
+        return cam
+
+    def project_colorize(self, params: dict, rc, p: np.ndarray, colorize: bool = True) -> None:
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        cam = SpoCamera()
+        if self.lib.spo_camera_setup(C.byref(prm), C.byref(cam)):
+            raise ValueError("degenerate matrix")
+        self.lib.spo_project(C.byref(prm), C.byref(cam), _vp(p), len(p))
+        if colorize:
+            self.lib.spo_colorize(C.byref(prm), _vp(p), len(p))
+
+    def sort_perm(self, p: np.ndarray, sort_type: int) -> np.ndarray:
+        perm = np.zeros(len(p), dtype=np.uint32)
+        if self.lib.spo_sort_perm(_vp(p), len(p), sort_type, _vp(perm)):
+            raise ValueError("unknown sorting chosen ...")
+        return perm
+
+    def bins(self, p: np.ndarray, order, xres: int, yres: int, T: int):
+        ncx, ncy = (xres + T - 1) // T, (yres + T - 1) // T
+        ts = np.zeros(ncx * ncy + 1, dtype=np.int64)
+        tot = self.lib.spo_bin(_vp(p), _vp(order), len(p), xres, yres, T, _vp(ts), None)
+        ent = np.zeros(max(1, tot), dtype=np.uint32)
+        self.lib.spo_bin(_vp(p), _vp(order), len(p), xres, yres, T, _vp(ts), _vp(ent))
+        return ts, ent[:tot]
+
+    def render_fp32(self, p, order, xres, yres, T, a_eq_e, gray, simd=False):
+        pic = np.zeros((xres, yres, 3), dtype=np.float32)
+        fr = self.lib.spo_render_fp32(_vp(p), _vp(order), len(p), xres, yres, T, int(a_eq_e),
+                                      float(gray), int(simd), _vp(pic))
+        return pic, fr
+
+    def render_fp64(self, p, order, xres, yres, T, a_eq_e, gray):
+        pic = np.zeros((xres, yres, 3), dtype=np.float64)
+        fr = self.lib.spo_render_fp64(_vp(p), _vp(order), len(p), xres, yres, T, int(a_eq_e),
+                                      float(np.float32(gray)), _vp(pic))
+        return pic, fr
+
+    def host_rendering(self, params: dict, rc, p: np.ndarray, simd: bool = False) -> np.ndarray:
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        pic = np.zeros((prm.xres, prm.yres, 3), dtype=np.float32)
+        if self.lib.spo_host_rendering(C.byref(prm), _vp(p), len(p), int(simd), _vp(pic)):
+            raise RuntimeError("oracle host_rendering failed")
+        return pic
+
+    def splat_adjoint_fp64(self, p, order, xres, yres, T, a_eq_e, gray, gpic):
+        n = len(p)
+        gx, gy, gr = (np.zeros(n) for _ in range(3))
+        ge = np.zeros((n, 3))
+        g = np.ascontiguousarray(gpic, dtype=np.float64)
+        self.lib.spo_splat_adjoint_fp64(_vp(p), _vp(order), n, xres, yres, T, int(a_eq_e),
+                                        float(np.float32(gray)), _vp(g), _vp(gx), _vp(gy),
+                                        _vp(gr), _vp(ge))
+        return gx, gy, gr, ge
+
+
+class Ref:
+    """The reference's own compiled host renderer (oracle/_ref)."""
+
+    def __init__(self, scalar: bool = False):
+        name = "libsplotch_ref_scalar.so" if scalar else "libsplotch_ref.so"
+        path = REF_DIR / name
+        if not path.exists():
+            raise FileNotFoundError(path)
+        lib = C.CDLL(str(path))
+        vp, i32, i64, f32 = C.c_void_p, C.c_int, C.c_long, C.c_float
+        lib.ref_simd_branch.restype = i32
+        lib.ref_project_colorize.restype = i32
+        lib.ref_project_colorize.argtypes = [vp, vp, i32, vp, i64, vp, vp, vp, vp, i32, vp, vp, vp,
+                                             f32, i32]
+        lib.ref_render_new.restype = i32
+        lib.ref_render_new.argtypes = [vp, i32, i32, i32, i32, f32, i32, vp]
+        lib.ref_particle_sort.restype = i32
+        lib.ref_particle_sort.argtypes = [vp, i32, i32]
+        lib.ref_host_rendering.restype = i32
+        lib.ref_host_rendering.argtypes = [vp, vp, i32, vp, i64, vp, vp, vp, vp, i32, vp, vp, vp,
+                                           f32, i32, i32, vp]
+        self.lib = lib
+        self.simd = bool(lib.ref_simd_branch())
+
+    @staticmethod
+    def _kv(params: dict):
+        keys = [k.encode() for k in params]
+        vals = [str(v).encode() for v in params.values()]
+        ka = (C.c_char_p * len(keys))(*keys)
+        va = (C.c_char_p * len(vals))(*vals)
+        return ka, va, len(keys)
+
+    @staticmethod
+    def _cam(rc):
+        return [np.ascontiguousarray(a, np.float64) for a in (rc.campos, rc.lookat, rc.sky,
+                                                             rc.centerpos)]
+
+    @staticmethod
+    def _pals(rc, ntypes):
+        n = (C.c_int * ntypes)()
+        xs = (C.c_void_p * ntypes)()
+        rgbs = (C.c_void_p * ntypes)()
+        keep = []
+        for t in range(ntypes):
+            pal = rc.amap[t] if t < len(rc.amap) else None
+            if pal is None:
+                n[t] = 0
+                continue
+            x = np.ascontiguousarray(pal.x, np.float64)
+            rgb = np.ascontiguousarray(pal.rgb, np.float32)
+            keep += [x, rgb]
+            n[t], xs[t], rgbs[t] = len(x), x.ctypes.data, rgb.ctypes.data
+        return n, xs, rgbs, keep
+
+    def project_colorize(self, params: dict, rc, p: np.ndarray, colorize: bool = True) -> None:
+        ka, va, nkv = self._kv(params)
+        cams = self._cam(rc)
+        nt = int(params.get("ptypes", 1))
+        n, xs, rgbs, keep = self._pals(rc, nt)
+        if self.lib.ref_project_colorize(ka, va, nkv, _vp(p), len(p), *[_vp(c) for c in cams],
+                                         nt, n, xs, rgbs, float(rc.b_brightness), int(colorize)):
+            raise RuntimeError("reference particle_project failed")
+
+    def render_new(self, p, xres, yres, a_eq_e, gray, T) -> np.ndarray:
+        pic = np.zeros((xres, yres, 3), dtype=np.float32)
+        if self.lib.ref_render_new(_vp(p), len(p), xres, yres, int(a_eq_e), float(gray), T,
+                                   _vp(pic)):
+            raise RuntimeError("reference render_new failed")
+        return pic
+
+    def particle_sort(self, p, sort_type: int) -> None:
+        if self.lib.ref_particle_sort(_vp(p), len(p), sort_type):
+            raise RuntimeError("reference particle_sort failed")
+
+    def host_rendering(self, params: dict, rc, p: np.ndarray) -> np.ndarray:
+        ka, va, nkv = self._kv(params)
+        cams = self._cam(rc)
+        nt = int(params.get("ptypes", 1))
+        n, xs, rgbs, keep = self._pals(rc, nt)
+        xres = int(params.get("xres", 800))
+        yres = int(params.get("yres", xres))
+        pic = np.zeros((xres, yres, 3), dtype=np.float32)
+        if self.lib.ref_host_rendering(ka, va, nkv, _vp(p), len(p), *[_vp(c) for c in cams], nt,
+                                       n, xs, rgbs, float(rc.b_brightness), xres, yres, _vp(pic)):
+            raise RuntimeError("reference host_rendering failed")
+        return pic
+
+
+def rel_linf(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-6) -> float:
+    """max |a-b| / max(|b|, floor), floor = floor_frac * max|b| (per image)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    m = float(np.max(np.abs(b))) if b.size else 0.0
+    floor = max(floor_frac * m, 1e-30)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if b.size else 0.0

@@ -1,0 +1,768 @@
+/*
+ * spl_oracle.c -- CPU oracle for the Splotch particle-render path.
+ *
+ * TEST INFRASTRUCTURE ONLY (see spl_oracle.h).  A plain-C restatement of the
+ * reference host renderer, written to reproduce its float/double arithmetic
+ * operation by operation.  Build with -ffp-contract=off and without
+ * -ffast-math: the reference is only reproducible without fused multiply-add.
+ *
+ * Integer conversion: the reference truncates with int(float).  For NaN and
+ * out-of-range values that is undefined in C++; this restatement (like the CUDA
+ * cvt.rzi.s32.f32 instruction and AArch64 fcvtzs) maps NaN to 0 and saturates.
+ */
+#include "spl_oracle.h"
+
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* cxxsupport/lsconstants.h:35,51 */
+static const double SPO_PI = 3.141592653589793238462643383279502884197;
+#define SPO_DEGR2RAD (SPO_PI / 180.0)
+
+static int g_threads = 0;
+
+void spo_set_threads(int n) { g_threads = n; }
+
+int spo_get_threads(void) {
+#ifdef _OPENMP
+  return g_threads > 0 ? g_threads : omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+static inline int f2i(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483648.0f) return INT_MAX;
+  if (v <= -2147483904.0f) return INT_MIN;
+  return (int)v;
+}
+static inline int imax(int a, int b) { return a > b ? a : b; }
+static inline int imin(int a, int b) { return a < b ? a : b; }
+
+/* splotch/splotch_host.cc:44-49 (SPLOTCH_CLASSIC) */
+static float h2sigma_f(void) { return (float)(0.5 * pow(SPO_PI, -1. / 6.)); }
+static float bfak_f(void) { return (float)(0.5 * pow(SPO_PI, -5. / 6.)); }
+static const float RFAC = 0.75f;
+
+/* ---------------------------------------------------------------------- */
+/* vec3 (double) and TRANSMAT (float) -- cxxsupport/vec3.h, kernel/transform.cxx */
+
+typedef struct { double x, y, z; } v3;
+
+static v3 v3_sub(v3 a, v3 b) { v3 r = {a.x - b.x, a.y - b.y, a.z - b.z}; return r; }
+static v3 v3_normed(v3 a) { /* vec3.h:72-83 */
+  double l = 1.0 / sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  v3 r = {a.x * l, a.y * l, a.z * l};
+  return r;
+}
+static double v3_len(v3 a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+static v3 v3_cross(v3 a, v3 b) { /* vec3.h:129-131 */
+  v3 r = {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+  return r;
+}
+
+typedef struct { float e[3][4]; } tmat;
+
+static void tmat_identity(tmat *m) {
+  memset(m, 0, sizeof(*m));
+  m->e[0][0] = m->e[1][1] = m->e[2][2] = 1.f;
+}
+
+/* TRANSMAT::Inverse, kernel/transform.cxx:64-112 */
+static int tmat_inverse(const tmat *a, tmat *t) {
+  const float (*e)[4] = a->e;
+  t->e[0][0] = e[1][1] * e[2][2] - e[2][1] * e[1][2];
+  t->e[0][1] = e[0][1] * e[2][2] - e[2][1] * e[0][2];
+  t->e[0][2] = e[0][1] * e[1][2] - e[1][1] * e[0][2];
+  t->e[1][0] = e[1][0] * e[2][2] - e[2][0] * e[1][2];
+  t->e[1][1] = e[0][0] * e[2][2] - e[2][0] * e[0][2];
+  t->e[1][2] = e[0][0] * e[1][2] - e[1][0] * e[0][2];
+  t->e[2][0] = e[1][0] * e[2][1] - e[2][0] * e[1][1];
+  t->e[2][1] = e[0][0] * e[2][1] - e[2][0] * e[0][1];
+  t->e[2][2] = e[0][0] * e[1][1] - e[1][0] * e[0][1];
+  float df = e[0][0] * t->e[0][0] - e[1][0] * t->e[0][1] + e[2][0] * t->e[0][2];
+  double d = (double)df;
+  if (!(fabs(d) > 1e-10)) return -1;
+  d = 1. / d;
+  t->e[0][0] = (float)(t->e[0][0] * d);
+  t->e[2][0] = (float)(t->e[2][0] * d);
+  t->e[1][1] = (float)(t->e[1][1] * d);
+  t->e[0][2] = (float)(t->e[0][2] * d);
+  t->e[2][2] = (float)(t->e[2][2] * d);
+  d = -d;
+  t->e[1][0] = (float)(t->e[1][0] * d);
+  t->e[0][1] = (float)(t->e[0][1] * d);
+  t->e[2][1] = (float)(t->e[2][1] * d);
+  t->e[1][2] = (float)(t->e[1][2] * d);
+  for (int j = 0; j < 3; ++j)
+    t->e[j][3] = -(t->e[j][0] * e[0][3] + t->e[j][1] * e[1][3] + t->e[j][2] * e[2][3]);
+  return 0;
+}
+
+/* TRANSMAT::operator*=, kernel/transform.cxx:50-62 */
+static void tmat_mul_inplace(tmat *self, const tmat *b) {
+  tmat a = *self;
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 3; ++j)
+      self->e[j][i] = a.e[0][i] * b->e[j][0] + a.e[1][i] * b->e[j][1] + a.e[2][i] * b->e[j][2];
+  self->e[0][3] += b->e[0][3];
+  self->e[1][3] += b->e[1][3];
+  self->e[2][3] += b->e[2][3];
+}
+
+/* camera set-up of particle_project, splotch/splotch_host.cc:62-110 */
+int spo_camera_setup(const spo_params *prm, spo_camera *cam) {
+  int xres = prm->xres, yres = prm->yres;
+  cam->ycorr = .5f * (yres - xres);
+  cam->res2 = 0.5f * xres;
+  cam->fovfct = (float)tan((double)(prm->fov * 0.5f) * SPO_DEGR2RAD);
+
+  v3 campos = {prm->campos[0], prm->campos[1], prm->campos[2]};
+  v3 lookat = {prm->lookat[0], prm->lookat[1], prm->lookat[2]};
+  v3 sky = {prm->sky[0], prm->sky[1], prm->sky[2]};
+  v3 centerpos = {prm->centerpos[0], prm->centerpos[1], prm->centerpos[2]};
+
+  sky = v3_normed(sky);
+  v3 zaxis = v3_normed(v3_sub(centerpos, lookat));
+  v3 xaxis = v3_normed(v3_cross(sky, zaxis));
+  v3 yaxis = v3_cross(zaxis, xaxis);
+
+  /* TRANSMAT ctor stores its 12 arguments transposed (transform.cxx:28-48) */
+  tmat gen;
+  gen.e[0][0] = (float)xaxis.x; gen.e[1][0] = (float)xaxis.y; gen.e[2][0] = (float)xaxis.z;
+  gen.e[0][1] = (float)yaxis.x; gen.e[1][1] = (float)yaxis.y; gen.e[2][1] = (float)yaxis.z;
+  gen.e[0][2] = (float)zaxis.x; gen.e[1][2] = (float)zaxis.y; gen.e[2][2] = (float)zaxis.z;
+  gen.e[0][3] = 0.f; gen.e[1][3] = 0.f; gen.e[2][3] = 0.f;
+  tmat gen_inv;
+  if (tmat_inverse(&gen, &gen_inv)) return -1;
+  /* trans.Invert() swaps matrix and inverse: matrix = gen_inv */
+  tmat trans_matrix = gen_inv;
+
+  /* trans2 = translation(-campos); trans2.Add_Transform(trans) */
+  tmat t2;
+  tmat_identity(&t2);
+  t2.e[0][3] = (float)(-campos.x);
+  t2.e[1][3] = (float)(-campos.y);
+  t2.e[2][3] = (float)(-campos.z);
+  tmat_mul_inplace(&t2, &trans_matrix);
+  memcpy(cam->mat, t2.e, sizeof(cam->mat));
+
+  const float *p = cam->mat; /* TRANSFORM::TransPoint, transform.cxx:212-219 */
+  double tcx = centerpos.x * p[0] + centerpos.y * p[1] + centerpos.z * p[2] + p[3];
+  double tcy = centerpos.x * p[4] + centerpos.y * p[5] + centerpos.z * p[6] + p[7];
+
+  float dist = (float)v3_len(v3_sub(centerpos, lookat));
+  cam->xfac = cam->res2 / (cam->fovfct * dist);
+  cam->xshift = -cam->xfac * tcx;
+  cam->yshift = -cam->xfac * tcy;
+  return 0;
+}
+
+/* per-particle loop of particle_project, splotch/splotch_host.cc:111-178 */
+void spo_project(const spo_params *prm, const spo_camera *cam, spo_particle *pp,
+                 int64_t n) {
+  const int xres = prm->xres, yres = prm->yres;
+  const float zmax = prm->zmax;
+  const float zmin = prm->zmin > 0.f ? prm->zmin : 0.f;
+  const float res2 = cam->res2, ycorr = cam->ycorr, fovfct = cam->fovfct;
+  const double xshift = cam->xshift, yshift = cam->yshift;
+  const float *m = cam->mat;
+  const float bfak = bfak_f();
+  const float minrad = prm->minrad_pix;
+  const int projection = prm->projection;
+
+#pragma omp parallel for schedule(guided, 1000) num_threads(spo_get_threads())
+  for (int64_t i = 0; i < n; ++i) {
+    spo_particle *p = &pp[i];
+    double vx = p->x, vy = p->y, vz = p->z;
+    double tx = vx * m[0] + vy * m[1] + vz * m[2] + m[3];
+    double ty = vx * m[4] + vy * m[5] + vz * m[6] + m[7];
+    double tz = vx * m[8] + vy * m[9] + vz * m[10] + m[11];
+    p->x = (float)tx; p->y = (float)ty; p->z = (float)tz;
+    p->active = 0;
+    if (-p->z <= zmin) continue;
+    if (-p->z >= zmax) continue;
+    float xfac2 = cam->xfac;
+    if (!projection) {
+      p->x = res2 + p->x * xfac2;
+      p->y = res2 + ycorr + p->y * xfac2;
+    } else {
+      xfac2 = -res2 / (fovfct * p->z);
+      float px = p->x * xfac2, py = p->y * xfac2;
+      p->x = (float)((double)res2 + xshift + (double)px);
+      p->y = (float)((double)res2 + yshift + (double)ycorr + (double)py);
+    }
+    p->I *= 0.5f * bfak / p->r;
+    p->r *= 2;
+    p->r *= xfac2 * prm->smooth_factor[p->type];
+    float rcorr = sqrtf(p->r * p->r + minrad * minrad) / p->r;
+    p->r *= rcorr;
+    p->I /= rcorr;
+
+    float posx = p->x, posy = p->y;
+    float rfacr = RFAC * p->r;
+    int minx = f2i(posx - rfacr + 1);
+    if (minx >= xres) continue;
+    minx = imax(minx, 0);
+    int maxx = f2i(posx + rfacr + 1);
+    if (maxx <= 0) continue;
+    maxx = imin(maxx, xres);
+    if (minx >= maxx) continue;
+    int miny = f2i(posy - rfacr + 1);
+    if (miny >= yres) continue;
+    miny = imax(miny, 0);
+    int maxy = f2i(posy + rfacr + 1);
+    if (maxy <= 0) continue;
+    maxy = imin(maxy, yres);
+    if (miny >= maxy) continue;
+    p->active = 1;
+  }
+}
+
+/* linearMap<COLOUR>::getVal_const, cxxsupport/linear_map.h:71-84, with
+   interpol_helper, cxxsupport/math_utils.h:186-196 */
+static void palette_lookup(int n, const double *x, const float *rgb, double xv,
+                           float out[3]) {
+  int idx;
+  if (n == 1 || xv <= x[0]) { idx = 0; goto ends; }
+  if (xv >= x[n - 1]) { idx = n - 1; goto ends; }
+  {
+    int lo = 0, hi = n; /* lower_bound: first x[i] >= xv */
+    while (lo < hi) {
+      int mid = lo + (hi - lo) / 2;
+      if (x[mid] < xv) lo = mid + 1; else hi = mid;
+    }
+    idx = lo;
+    if (idx > 0) --idx;
+    if (idx > n - 2) idx = n - 2;
+    double frac = (xv - x[idx]) / (x[idx + 1] - x[idx]);
+    for (int c = 0; c < 3; ++c) {
+      float a = (float)(rgb[3 * idx + c] * (1. - frac));
+      float b = (float)(rgb[3 * (idx + 1) + c] * frac);
+      out[c] = a + b;
+    }
+    return;
+  }
+ends:
+  out[0] = rgb[3 * idx]; out[1] = rgb[3 * idx + 1]; out[2] = rgb[3 * idx + 2];
+}
+
+/* particle_colorize, splotch/splotch_host.cc:252-287 */
+void spo_colorize(const spo_params *prm, spo_particle *pp, int64_t n) {
+  float bright[SPO_MAX_TYPES];
+  for (int t = 0; t < prm->ptypes && t < SPO_MAX_TYPES; ++t)
+    bright[t] = prm->brightness[t] * prm->b_brightness;
+#pragma omp parallel for schedule(guided, 1000) num_threads(spo_get_threads())
+  for (int64_t i = 0; i < n; ++i) {
+    spo_particle *p = &pp[i];
+    if (!p->active) continue;
+    int t = p->type;
+    if (!prm->color_is_vector[t]) {
+      float c[3];
+      palette_lookup(prm->pal_n[t], prm->pal_x[t], prm->pal_rgb[t], (double)p->er, c);
+      p->er = c[0]; p->eg = c[1]; p->eb = c[2];
+    }
+    float fac = p->I * bright[t];
+    p->er *= fac; p->eg *= fac; p->eb *= fac;
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* stable sort, splotch/splotch_host.cc:289-321 with the comparators of
+   splotch/splotchutils.h:74-96 (stable, i.e. ties keep the original order) */
+
+static int less_by(const spo_particle *p, int st, uint32_t a, uint32_t b) {
+  switch (st) {
+    case 1: return p[a].z < p[b].z;
+    case 2: return p[a].er > p[b].er;
+    case 3: return p[a].er < p[b].er;
+    case 4: return p[a].r > p[b].r;
+  }
+  return 0;
+}
+
+int spo_sort_perm(const spo_particle *p, int64_t n, int sort_type, uint32_t *perm) {
+  for (int64_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
+  if (sort_type == 0 || n < 2) return 0;
+  if (sort_type < 0 || sort_type > 4) return -1;
+  uint32_t *tmp = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+  if (!tmp) return -2;
+  uint32_t *src = perm, *dst = tmp;
+  for (int64_t w = 1; w < n; w *= 2) { /* bottom-up merge sort (serial) */
+    for (int64_t lo = 0; lo < n; lo += 2 * w) {
+      int64_t mid = lo + w < n ? lo + w : n, hi = lo + 2 * w < n ? lo + 2 * w : n;
+      int64_t i = lo, j = mid, k = lo;
+      while (i < mid && j < hi)
+        dst[k++] = less_by(p, sort_type, src[j], src[i]) ? src[j++] : src[i++];
+      while (i < mid) dst[k++] = src[i++];
+      while (j < hi) dst[k++] = src[j++];
+    }
+    uint32_t *s = src; src = dst; dst = s;
+  }
+  if (src != perm) memcpy(perm, src, (size_t)n * sizeof(uint32_t));
+  free(tmp);
+  return 0;
+}
+
+void spo_apply_perm(const spo_particle *in, const uint32_t *perm, int64_t n,
+                    spo_particle *out) {
+#pragma omp parallel for num_threads(spo_get_threads())
+  for (int64_t i = 0; i < n; ++i) out[i] = in[perm[i]];
+}
+
+/* ---------------------------------------------------------------------- */
+/* binning, render_new region A, splotch/splotch_host.cc:339-406 */
+
+typedef struct {
+  int T, ncx, ncy;
+  float rcell, cmid0;
+} tiling;
+
+static tiling make_tiling(int xres, int yres, int T) {
+  tiling g;
+  g.T = T;
+  g.ncx = (xres + T - 1) / T;
+  g.ncy = (yres + T - 1) / T;
+  g.rcell = sqrtf(2.f) * (T * 0.5f - 0.5f);
+  g.cmid0 = 0.5f * (T - 1);
+  return g;
+}
+
+/* visits the tiles of one particle; returns count, optionally writes ids */
+static int particle_tiles(const spo_particle *pp, const tiling *g, uint32_t *ids) {
+  if (!pp->active) return 0;
+  const int T = g->T;
+  float rfacr = RFAC * pp->r;
+  int minx = imax(0, f2i(pp->x - rfacr + 1) / T);
+  int maxx = imin(g->ncx - 1, f2i(pp->x + rfacr) / T);
+  int miny = imax(0, f2i(pp->y - rfacr + 1) / T);
+  int maxy = imin(g->ncy - 1, f2i(pp->y + rfacr) / T);
+  float sumsq = (g->rcell + rfacr) * (g->rcell + rfacr);
+  int cnt = 0;
+  for (int ix = minx; ix <= maxx; ++ix) {
+    float cx = g->cmid0 + ix * T;
+    for (int iy = miny; iy <= maxy; ++iy) {
+      float cy = g->cmid0 + iy * T;
+      float rtot2 = (pp->x - cx) * (pp->x - cx) + (pp->y - cy) * (pp->y - cy);
+      if (rtot2 < sumsq) {
+        if (ids) ids[cnt] = (uint32_t)(iy * g->ncx + ix);
+        ++cnt;
+      }
+    }
+  }
+  return cnt;
+}
+
+int64_t spo_bin(const spo_particle *p, const uint32_t *order, int64_t n, int xres,
+                int yres, int T, int64_t *tile_start, uint32_t *entries) {
+  tiling g = make_tiling(xres, yres, T);
+  const int64_t ntiles = (int64_t)g.ncx * g.ncy;
+  const int nth = spo_get_threads();
+  int64_t *cnt = (int64_t *)calloc((size_t)(nth * ntiles), sizeof(int64_t));
+  if (!cnt) return -1;
+  /* pass 1: per-thread per-tile counts over contiguous shares (like the
+     per-thread lists of the reference, concatenated in thread order) */
+#pragma omp parallel num_threads(nth)
+  {
+    int th = 0;
+#ifdef _OPENMP
+    th = omp_get_thread_num();
+#endif
+    int64_t lo = n * th / nth, hi = n * (th + 1) / nth;
+    int64_t *c = cnt + (int64_t)th * ntiles;
+    uint32_t ids[4096];
+    for (int64_t s = lo; s < hi; ++s) {
+      const spo_particle *pp = &p[order ? order[s] : s];
+      int k = particle_tiles(pp, &g, NULL);
+      if (k <= 4096) {
+        particle_tiles(pp, &g, ids);
+        for (int j = 0; j < k; ++j) c[ids[j]]++;
+      } else {
+        uint32_t *big = (uint32_t *)malloc((size_t)k * sizeof(uint32_t));
+        particle_tiles(pp, &g, big);
+        for (int j = 0; j < k; ++j) c[big[j]]++;
+        free(big);
+      }
+    }
+  }
+  /* exclusive scan, tile-major then thread order */
+  int64_t run = 0;
+  for (int64_t t = 0; t < ntiles; ++t) {
+    if (tile_start) tile_start[t] = run;
+    for (int th = 0; th < nth; ++th) {
+      int64_t v = cnt[(int64_t)th * ntiles + t];
+      cnt[(int64_t)th * ntiles + t] = run;
+      run += v;
+    }
+  }
+  if (tile_start) tile_start[ntiles] = run;
+  if (entries) {
+#pragma omp parallel num_threads(nth)
+    {
+      int th = 0;
+#ifdef _OPENMP
+      th = omp_get_thread_num();
+#endif
+      int64_t lo = n * th / nth, hi = n * (th + 1) / nth;
+      int64_t *c = cnt + (int64_t)th * ntiles;
+      uint32_t ids[4096];
+      for (int64_t s = lo; s < hi; ++s) {
+        uint32_t i = (uint32_t)(order ? order[s] : s);
+        int k = particle_tiles(&p[i], &g, NULL);
+        uint32_t *buf = k <= 4096 ? ids : (uint32_t *)malloc((size_t)k * sizeof(uint32_t));
+        particle_tiles(&p[i], &g, buf);
+        for (int j = 0; j < k; ++j) entries[c[buf[j]]++] = i;
+        if (buf != ids) free(buf);
+      }
+    }
+  }
+  free(cnt);
+  return run;
+}
+
+/* ---------------------------------------------------------------------- */
+/* exptable<float32>(-20), splotch/splotchutils.h:174-215 */
+
+typedef struct {
+  float expfac, taylorlimit;
+  float tab1[1024], tab2[1024];
+} exptab;
+
+static void exptab_init(exptab *t, float maxexp) {
+  t->expfac = 1048576 / maxexp;
+  for (int m = 0; m < 1024; ++m) {
+    t->tab1[m] = expf(m * 1024 / t->expfac);
+    t->tab2[m] = expf(m / t->expfac);
+  }
+  t->taylorlimit = sqrtf(2.f * fabsf(maxexp) / 1048576);
+}
+
+static inline float exptab_exp(const exptab *t, float arg) {
+  int iarg = f2i(arg * t->expfac);
+  if (iarg & ~((1 << 20) - 1)) return (iarg < 0) ? 1.f : 0.f;
+  return t->tab1[iarg >> 10] * t->tab2[iarg & 1023];
+}
+
+static inline float exptab_expm1(const exptab *t, float arg) {
+  if (fabsf(arg) < t->taylorlimit) return arg;
+  return exptab_exp(t, arg) - 1.f;
+}
+
+/* tile lists for the splat: built with spo_bin */
+typedef struct {
+  tiling g;
+  int64_t ntiles;
+  int64_t *start;
+  uint32_t *ent;
+} bins;
+
+static int make_bins(const spo_particle *p, const uint32_t *order, int64_t n, int xres,
+                     int yres, int T, bins *b) {
+  b->g = make_tiling(xres, yres, T);
+  b->ntiles = (int64_t)b->g.ncx * b->g.ncy;
+  b->start = (int64_t *)malloc((size_t)(b->ntiles + 1) * sizeof(int64_t));
+  int64_t tot = spo_bin(p, order, n, xres, yres, T, b->start, NULL);
+  if (tot < 0) return -1;
+  b->ent = (uint32_t *)malloc((size_t)(tot > 0 ? tot : 1) * sizeof(uint32_t));
+  spo_bin(p, order, n, xres, yres, T, b->start, b->ent);
+  return 0;
+}
+static void free_bins(bins *b) { free(b->start); free(b->ent); }
+
+/* per-particle, per-tile coverage of render_new (splotch_host.cc:461-476) */
+typedef struct {
+  float posx, posy, rfacr, radsq, stp;
+  int minx, maxx, miny, maxy;
+} pcov;
+
+static inline void particle_cover(const spo_particle *pp, int x0s, int y0s, int x1, int y1,
+                                  float h2sigma, pcov *c) {
+  c->rfacr = pp->r * RFAC;
+  c->posx = pp->x - x0s;
+  c->posy = pp->y - y0s;
+  c->minx = imax(f2i(c->posx - c->rfacr + 1), 0);
+  c->maxx = imin(f2i(c->posx + c->rfacr + 1), x1);
+  c->miny = imax(f2i(c->posy - c->rfacr + 1), 0);
+  c->maxy = imin(f2i(c->posy + c->rfacr + 1), y1);
+  c->radsq = c->rfacr * c->rfacr;
+  float sigma = h2sigma * pp->r;
+  c->stp = -1.f / (sigma * sigma);
+}
+
+/* column run of render_new (splotch_host.cc:603-606) */
+static inline void column_run(const pcov *c, int x, int *lo, int *hi, float *dxsq) {
+  float dx = x - c->posx;
+  *dxsq = dx * dx;
+  float dy = sqrtf(c->radsq - *dxsq);
+  *lo = imax(c->miny, f2i(c->posy - dy + 1));
+  *hi = imin(c->maxy, f2i(c->posy + dy + 1));
+}
+
+int64_t spo_render_fp32(const spo_particle *p, const uint32_t *order, int64_t n,
+                        int xres, int yres, int T, int a_eq_e, float gray,
+                        int simd_branch, float *pic) {
+  bins b;
+  if (make_bins(p, order, n, xres, yres, T, &b)) return -1;
+  exptab xexp;
+  exptab_init(&xexp, -20.f);
+  const float taylorlimit = xexp.taylorlimit;
+  const float h2sigma = h2sigma_f();
+  int64_t frags = 0;
+
+#pragma omp parallel num_threads(spo_get_threads()) reduction(+ : frags)
+  {
+    float *lpic = (float *)malloc((size_t)T * T * 3 * sizeof(float));
+    float *pre1 = (float *)malloc((size_t)T * sizeof(float));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t chunk = 0; chunk < b.ntiles; ++chunk) {
+      int ix = (int)(chunk % b.g.ncx), iy = (int)(chunk / b.g.ncx);
+      int x0s = ix * T, y0s = iy * T;
+      int x1 = imin(x0s + T, xres) - x0s, y1 = imin(y0s + T, yres) - y0s;
+      memset(lpic, 0, (size_t)x1 * y1 * 3 * sizeof(float));
+      for (int64_t k = b.start[chunk]; k < b.start[chunk + 1]; ++k) {
+        const spo_particle *pp = &p[b.ent[k]];
+        pcov c;
+        particle_cover(pp, x0s, y0s, x1, y1, h2sigma, &c);
+        float ar = -pp->er, ag = -pp->eg, ab = -pp->eb;
+        for (int y = c.miny; y < c.maxy; ++y) {
+          float t = y - c.posy;
+          pre1[y] = exptab_exp(&xexp, c.stp * t * t);
+        }
+        if (a_eq_e) {
+          for (int x = c.minx; x < c.maxx; ++x) {
+            int lo, hi; float dxsq;
+            column_run(&c, x, &lo, &hi, &dxsq);
+            float pre2 = exptab_exp(&xexp, c.stp * dxsq);
+            float *col = lpic + (size_t)x * y1 * 3;
+            for (int y = lo; y < hi; ++y) {
+              float att = pre1[y] * pre2;
+              col[3 * y] += att * ar;
+              col[3 * y + 1] += att * ag;
+              col[3 * y + 2] += att * ab;
+            }
+            if (hi > lo) frags += hi - lo;
+          }
+        } else {
+          float qr = pp->er / (pp->er + gray), qg = pp->eg / (pp->eg + gray),
+                qb = pp->eb / (pp->eb + gray);
+          float maxa = fabsf(ar);
+          if (fabsf(ag) > maxa) maxa = fabsf(ag);
+          if (fabsf(ab) > maxa) maxa = fabsf(ab);
+          for (int x = c.minx; x < c.maxx; ++x) {
+            int lo, hi; float dxsq;
+            column_run(&c, x, &lo, &hi, &dxsq);
+            float pre2 = exptab_exp(&xexp, c.stp * dxsq);
+            float *col = lpic + (size_t)x * y1 * 3;
+            for (int y = lo; y < hi; ++y) {
+              float att = pre1[y] * pre2;
+              float *v = col + 3 * y;
+              if (simd_branch && (maxa * att) < taylorlimit) {
+                v[0] += ((v[0] - qr) * ar) * att;
+                v[1] += ((v[1] - qg) * ag) * att;
+                v[2] += ((v[2] - qb) * ab) * att;
+              } else {
+                v[0] += exptab_expm1(&xexp, att * ar) * (v[0] - qr);
+                v[1] += exptab_expm1(&xexp, att * ag) * (v[1] - qg);
+                v[2] += exptab_expm1(&xexp, att * ab) * (v[2] - qb);
+              }
+            }
+            if (hi > lo) frags += hi - lo;
+          }
+        }
+      }
+      for (int x = 0; x < x1; ++x)
+        memcpy(pic + ((size_t)(x + x0s) * yres + y0s) * 3, lpic + (size_t)x * y1 * 3,
+               (size_t)y1 * 3 * sizeof(float));
+    }
+    free(lpic);
+    free(pre1);
+  }
+  free_bins(&b);
+  return frags;
+}
+
+int64_t spo_render_fp64(const spo_particle *p, const uint32_t *order, int64_t n,
+                        int xres, int yres, int T, int a_eq_e, double gray,
+                        double *pic) {
+  bins b;
+  if (make_bins(p, order, n, xres, yres, T, &b)) return -1;
+  const float h2sigma = h2sigma_f();
+  int64_t frags = 0;
+#pragma omp parallel num_threads(spo_get_threads()) reduction(+ : frags)
+  {
+    double *lpic = (double *)malloc((size_t)T * T * 3 * sizeof(double));
+    double *pre1 = (double *)malloc((size_t)T * sizeof(double));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t chunk = 0; chunk < b.ntiles; ++chunk) {
+      int ix = (int)(chunk % b.g.ncx), iy = (int)(chunk / b.g.ncx);
+      int x0s = ix * T, y0s = iy * T;
+      int x1 = imin(x0s + T, xres) - x0s, y1 = imin(y0s + T, yres) - y0s;
+      memset(lpic, 0, (size_t)x1 * y1 * 3 * sizeof(double));
+      for (int64_t k = b.start[chunk]; k < b.start[chunk + 1]; ++k) {
+        const spo_particle *pp = &p[b.ent[k]];
+        pcov c;
+        particle_cover(pp, x0s, y0s, x1, y1, h2sigma, &c);
+        double sigma = (double)h2sigma * pp->r;
+        double stp = -1.0 / (sigma * sigma);
+        double px = (double)pp->x - x0s, py = (double)pp->y - y0s;
+        double e[3] = {pp->er, pp->eg, pp->eb};
+        double q[3];
+        for (int ch = 0; ch < 3; ++ch) q[ch] = e[ch] / (e[ch] + gray);
+        for (int y = c.miny; y < c.maxy; ++y) pre1[y] = exp(stp * (y - py) * (y - py));
+        for (int x = c.minx; x < c.maxx; ++x) {
+          int lo, hi; float dxsq;
+          column_run(&c, x, &lo, &hi, &dxsq);
+          double pre2 = exp(stp * (x - px) * (x - px));
+          double *col = lpic + (size_t)x * y1 * 3;
+          for (int y = lo; y < hi; ++y) {
+            double att = pre1[y] * pre2;
+            double *v = col + 3 * y;
+            if (a_eq_e) {
+              for (int ch = 0; ch < 3; ++ch) v[ch] += -e[ch] * att;
+            } else {
+              for (int ch = 0; ch < 3; ++ch) v[ch] += expm1(-e[ch] * att) * (v[ch] - q[ch]);
+            }
+          }
+          if (hi > lo) frags += hi - lo;
+        }
+      }
+      for (int x = 0; x < x1; ++x)
+        memcpy(pic + ((size_t)(x + x0s) * yres + y0s) * 3, lpic + (size_t)x * y1 * 3,
+               (size_t)y1 * 3 * sizeof(double));
+    }
+    free(lpic);
+    free(pre1);
+  }
+  free_bins(&b);
+  return frags;
+}
+
+/* ---------------------------------------------------------------------- */
+/* FP64 adjoint of the splat.  Per tile and pixel: replay the ordered layer
+   list forward (storing every intermediate value), then walk it backwards. */
+
+int spo_splat_adjoint_fp64(const spo_particle *p, const uint32_t *order, int64_t n,
+                           int xres, int yres, int T, int a_eq_e, double gray,
+                           const double *gpic, double *gx, double *gy, double *gr,
+                           double *ge) {
+  bins b;
+  if (make_bins(p, order, n, xres, yres, T, &b)) return -1;
+  const float h2sigma = h2sigma_f();
+  memset(gx, 0, (size_t)n * sizeof(double));
+  memset(gy, 0, (size_t)n * sizeof(double));
+  memset(gr, 0, (size_t)n * sizeof(double));
+  memset(ge, 0, (size_t)n * 3 * sizeof(double));
+  /* serial over tiles keeps the per-particle accumulation deterministic */
+  for (int64_t chunk = 0; chunk < b.ntiles; ++chunk) {
+    int ix = (int)(chunk % b.g.ncx), iy = (int)(chunk / b.g.ncx);
+    int x0s = ix * T, y0s = iy * T;
+    int x1 = imin(x0s + T, xres) - x0s, y1 = imin(y0s + T, yres) - y0s;
+    int64_t k0 = b.start[chunk], k1 = b.start[chunk + 1];
+    int64_t L = k1 - k0;
+    if (L == 0) continue;
+    double *att = (double *)malloc((size_t)L * sizeof(double));
+    double *hist = (double *)malloc((size_t)(L + 1) * 3 * sizeof(double));
+    pcov *cv = (pcov *)malloc((size_t)L * sizeof(pcov));
+    for (int64_t k = 0; k < L; ++k)
+      particle_cover(&p[b.ent[k0 + k]], x0s, y0s, x1, y1, h2sigma, &cv[k]);
+    for (int x = 0; x < x1; ++x)
+      for (int y = 0; y < y1; ++y) {
+        const double *G = gpic + ((size_t)(x + x0s) * yres + (y + y0s)) * 3;
+        /* forward replay */
+        hist[0] = hist[1] = hist[2] = 0.0;
+        for (int64_t k = 0; k < L; ++k) {
+          const spo_particle *pp = &p[b.ent[k0 + k]];
+          const pcov *c = &cv[k];
+          double *h0 = hist + 3 * k, *h1 = hist + 3 * (k + 1);
+          att[k] = 0.0;
+          int inside = 0;
+          if (x >= c->minx && x < c->maxx) {
+            int lo, hi; float dxsq;
+            column_run(c, x, &lo, &hi, &dxsq);
+            inside = (y >= lo && y < hi);
+          }
+          if (inside) {
+            double sigma = (double)h2sigma * pp->r;
+            double stp = -1.0 / (sigma * sigma);
+            double dx = (double)(x + x0s) - pp->x, dy = (double)(y + y0s) - pp->y;
+            att[k] = exp(stp * dy * dy) * exp(stp * dx * dx);
+          }
+          double e[3] = {pp->er, pp->eg, pp->eb};
+          for (int ch = 0; ch < 3; ++ch) {
+            if (!inside) { h1[ch] = h0[ch]; continue; }
+            if (a_eq_e) h1[ch] = h0[ch] - e[ch] * att[k];
+            else {
+              double q = e[ch] / (e[ch] + gray);
+              h1[ch] = h0[ch] + expm1(-e[ch] * att[k]) * (h0[ch] - q);
+            }
+          }
+        }
+        /* reverse sweep */
+        double lam[3] = {G[0], G[1], G[2]};
+        for (int64_t k = L - 1; k >= 0; --k) {
+          if (att[k] == 0.0) continue;
+          uint32_t i = b.ent[k0 + k];
+          const spo_particle *pp = &p[i];
+          double sigma = (double)h2sigma * pp->r;
+          double stp = -1.0 / (sigma * sigma);
+          double dx = (double)(x + x0s) - pp->x, dy = (double)(y + y0s) - pp->y;
+          double e[3] = {pp->er, pp->eg, pp->eb};
+          double gatt = 0.0;
+          for (int ch = 0; ch < 3; ++ch) {
+            if (a_eq_e) {
+              ge[3 * (size_t)i + ch] += -lam[ch] * att[k];
+              gatt += -lam[ch] * e[ch];
+            } else {
+              double Cprev = hist[3 * k + ch];
+              double q = e[ch] / (e[ch] + gray);
+              double Tk = exp(-e[ch] * att[k]);
+              double dT = lam[ch] * (Cprev - q);
+              double dq = lam[ch] * (1.0 - Tk);
+              ge[3 * (size_t)i + ch] += dT * (-att[k] * Tk) + dq * gray / ((e[ch] + gray) * (e[ch] + gray));
+              gatt += dT * (-e[ch] * Tk);
+              lam[ch] *= Tk;
+            }
+          }
+          double a = att[k];
+          gx[i] += gatt * a * (-2.0 * stp) * dx;
+          gy[i] += gatt * a * (-2.0 * stp) * dy;
+          gr[i] += gatt * a * (dx * dx + dy * dy) * (-2.0 * stp / pp->r);
+        }
+      }
+    free(att);
+    free(hist);
+    free(cv);
+  }
+  free_bins(&b);
+  return 0;
+}
+
+/* ---------------------------------------------------------------------- */
+/* host_rendering, splotch/splotch_host.cc:711-834 (non-MPI, classic path) */
+int spo_host_rendering(const spo_params *prm, spo_particle *p, int64_t n,
+                       int simd_branch, float *pic) {
+  spo_camera cam;
+  if (spo_camera_setup(prm, &cam)) return -1;
+  spo_project(prm, &cam, p, n);
+  spo_colorize(prm, p, n);
+  if (!prm->a_eq_e && prm->sort_type != 0) {
+    uint32_t *perm = (uint32_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(uint32_t));
+    spo_particle *tmp = (spo_particle *)malloc((size_t)(n > 0 ? n : 1) * sizeof(spo_particle));
+    if (!perm || !tmp) { free(perm); free(tmp); return -2; }
+    if (spo_sort_perm(p, n, prm->sort_type, perm)) { free(perm); free(tmp); return -3; }
+    spo_apply_perm(p, perm, n, tmp);
+    memcpy(p, tmp, (size_t)n * sizeof(spo_particle));
+    free(perm);
+    free(tmp);
+  }
+  int64_t r = spo_render_fp32(p, NULL, n, prm->xres, prm->yres, prm->tile_size,
+                              prm->a_eq_e, prm->gray_absorption, simd_branch, pic);
+  return r < 0 ? -4 : 0;
+}

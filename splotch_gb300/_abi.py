@@ -1,0 +1,130 @@
+"""ctypes binding of the C ABI declared in include/splotch_gb300.h.
+
+Loads the in-tree ``libsplgpu.so``.  There is no fallback: if the library is
+missing or fails to load, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+SPL_MAX_TYPES = 8
+SPL_OK, SPL_ERR_INVALID, SPL_ERR_CUDA, SPL_ERR_ALLOC, SPL_ERR_CAPACITY, SPL_ERR_TIMEOUT, \
+    SPL_ERR_UNSUPPORTED = range(7)
+SPL_MEM_HOST, SPL_MEM_DEVICE = 0, 1
+SPL_LAYOUT_AOS, SPL_LAYOUT_SOA = 0, 1
+SPL_WRITEBACK_NONE, SPL_WRITEBACK_FULL = 0, 1
+SPL_ORDER_BACK_TO_FRONT, SPL_ORDER_FRONT_TO_BACK = 0, 1
+
+LIB_PATH = Path(__file__).resolve().parent / "libsplgpu.so"
+
+# Every symbol include/splotch_gb300.h declares (checked by the CPU tests).
+EXPORTED = [
+    "spl_context_create", "spl_context_destroy", "spl_context_set_stream",
+    "spl_last_error_string", "spl_version", "spl_frame_desc_defaults", "spl_camera_setup",
+    "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
+    "spl_debug_get_bins",
+]
+
+
+class Camera(C.Structure):
+    _fields_ = [("mat", C.c_float * 12), ("res2", C.c_float), ("ycorr", C.c_float),
+                ("fovfct", C.c_float), ("xfac", C.c_float), ("xshift", C.c_double),
+                ("yshift", C.c_double)]
+
+
+class FrameDesc(C.Structure):
+    _fields_ = [
+        ("xres", C.c_int), ("yres", C.c_int), ("fov", C.c_float), ("zmin", C.c_float),
+        ("zmax", C.c_float), ("minrad_pix", C.c_float), ("projection", C.c_int),
+        ("ptypes", C.c_int), ("smooth_factor", C.c_float * SPL_MAX_TYPES),
+        ("brightness", C.c_float * SPL_MAX_TYPES),
+        ("color_is_vector", C.c_int * SPL_MAX_TYPES), ("b_brightness", C.c_float),
+        ("pal_n", C.c_int * SPL_MAX_TYPES), ("pal_x", C.c_void_p * SPL_MAX_TYPES),
+        ("pal_rgb", C.c_void_p * SPL_MAX_TYPES), ("a_eq_e", C.c_int),
+        ("gray_absorption", C.c_float), ("sort_type", C.c_int), ("tile_size", C.c_int),
+        ("campos", C.c_double * 3), ("lookat", C.c_double * 3), ("sky", C.c_double * 3),
+        ("centerpos", C.c_double * 3), ("order_mode", C.c_int), ("ftb_epsilon", C.c_float),
+    ]
+
+
+class Particles(C.Structure):
+    _fields_ = [("n", C.c_int64), ("layout", C.c_int), ("memspace", C.c_int),
+                ("aos", C.c_void_p), ("x", C.c_void_p), ("y", C.c_void_p), ("z", C.c_void_p),
+                ("r", C.c_void_p), ("I", C.c_void_p), ("cr", C.c_void_p), ("cg", C.c_void_p),
+                ("cb", C.c_void_p), ("type", C.c_void_p)]
+
+
+class Image(C.Structure):
+    _fields_ = [("pic", C.c_void_p), ("memspace", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("h2d_ms", C.c_float), ("project_ms", C.c_float), ("sort_ms", C.c_float),
+                ("bin_ms", C.c_float), ("splat_ms", C.c_float), ("d2h_ms", C.c_float),
+                ("total_ms", C.c_float), ("n_active", C.c_int64), ("n_entries", C.c_int64),
+                ("n_tiles", C.c_int64), ("kernel_launches", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SplotchError(RuntimeError):
+    """A non-zero spl_status; the message is spl_last_error_string()."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"spl_status {code}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def load(path: Path | str | None = None) -> C.CDLL:
+    """Load libsplgpu.so (once).  Raises if it is absent: no CPU fallback."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"{p} is not built; run splotch_gb300.build.build() first")
+    lib = C.CDLL(str(p))
+    vp, i64 = C.c_void_p, C.c_int64
+    sig = {
+        "spl_context_create": (C.c_int, [C.POINTER(vp), C.c_int]),
+        "spl_context_destroy": (C.c_int, [vp]),
+        "spl_context_set_stream": (C.c_int, [vp, vp]),
+        "spl_last_error_string": (C.c_char_p, []),
+        "spl_version": (C.c_char_p, []),
+        "spl_frame_desc_defaults": (None, [C.POINTER(FrameDesc)]),
+        "spl_camera_setup": (C.c_int, [C.POINTER(FrameDesc), C.POINTER(Camera)]),
+        "spl_render": (C.c_int, [vp, C.POINTER(FrameDesc), C.POINTER(Particles),
+                                 C.POINTER(Image), C.c_int]),
+        "spl_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
+        "spl_debug_get_projected": (C.c_int, [vp, vp, i64]),
+        "spl_debug_get_order": (C.c_int, [vp, vp, i64]),
+        "spl_debug_get_bins": (C.c_int, [vp, vp, i64, vp, i64]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(code: int) -> None:
+    if code != SPL_OK:
+        msg = load().spl_last_error_string()
+        raise SplotchError(code, msg.decode() if msg else "")
+
+
+def ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return int(a.data_ptr())

@@ -1,0 +1,483 @@
+// spl_api.cu -- the C ABI of libsplgpu.so: context, buffer pool and the
+// plain-render pipeline that replaces host_rendering()
+// (splotch/splotch_host.cc:711-834):
+//
+//   H2D (host inputs) -> project+colourise -> [stable depth sort] ->
+//   count scan -> bin emission -> stable tile sort -> tile ranges ->
+//   tiled splat -> D2H (host outputs) [-> particle writeback]
+//
+// All device memory is owned by the context and grows on demand; a frame that
+// fits the current capacity allocates nothing.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "../../include/splotch_gb300.h"
+#include "spl_internal.cuh"
+
+struct spl_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  struct Buf {
+    void *p = nullptr;
+    size_t cap = 0;
+  };
+  Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
+      tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
+      aos_out;
+  // state of the last frame (for the debug getters)
+  int64_t n = 0, ne = 0, ntiles = 0;
+  bool has_order = false;
+  int last_T = 0;
+  spl_stats stats{};
+  cudaEvent_t ev[8]{};
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+spl_status fail(spl_status code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define SPL_CK(call)                                                                    \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return fail(SPL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+spl_status ensure(spl_context::Buf &b, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (b.cap >= bytes) return SPL_OK;
+  if (b.p) cudaFree(b.p);
+  b.p = nullptr;
+  b.cap = 0;
+  size_t want = bytes + bytes / 8;  // headroom for slowly growing frames
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SPL_ERR_ALLOC, "cudaMalloc(" + std::to_string(want) + "): " +
+                                   cudaGetErrorString(e));
+  }
+  b.cap = want;
+  return SPL_OK;
+}
+
+template <typename T>
+T *as(spl_context::Buf &b) {
+  return static_cast<T *>(b.p);
+}
+
+int is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+spl_status validate(const spl_frame_desc *d, const spl_particles *p, const spl_image *o) {
+  if (!d || !p || !o) return fail(SPL_ERR_INVALID, "null argument");
+  if (d->xres <= 0 || d->yres <= 0 || d->xres > 65536 || d->yres > 65536)
+    return fail(SPL_ERR_INVALID, "xres/yres out of range");
+  if (d->tile_size < 1 || d->tile_size > 64)
+    return fail(SPL_ERR_UNSUPPORTED, "tile size must be in [1,64] on the GPU path");
+  if (d->ptypes < 1 || d->ptypes > SPL_MAX_TYPES)
+    return fail(SPL_ERR_INVALID, "ptypes must be in [1,8]");
+  if (d->sort_type < 0 || d->sort_type > 4)
+    return fail(SPL_ERR_INVALID, "unknown sorting chosen ...");  // splotch_host.cc:318
+  for (int t = 0; t < d->ptypes; ++t)
+    if (!d->color_is_vector[t] && (d->pal_n[t] < 1 || !d->pal_x[t] || !d->pal_rgb[t]))
+      return fail(SPL_ERR_INVALID, "trying to access an empty map (palette of type " +
+                                       std::to_string(t) + ")");
+  if (p->n < 0 || p->n > 0xffffffffLL) return fail(SPL_ERR_INVALID, "particle count out of range");
+  if (p->layout == SPL_LAYOUT_AOS) {
+    if (p->n > 0 && !p->aos) return fail(SPL_ERR_INVALID, "null AoS pointer");
+  } else if (p->layout == SPL_LAYOUT_SOA) {
+    if (p->n > 0 && (!p->x || !p->y || !p->z || !p->r || !p->I || !p->cr))
+      return fail(SPL_ERR_INVALID, "null SoA pointer");
+  } else {
+    return fail(SPL_ERR_INVALID, "unknown layout");
+  }
+  if (!o->pic) return fail(SPL_ERR_INVALID, "null image pointer");
+  if (o->memspace == SPL_MEM_DEVICE && !is_device_ptr(o->pic))
+    return fail(SPL_ERR_INVALID, "image marked device but pointer is not device memory");
+  if (p->memspace == SPL_MEM_DEVICE && p->n > 0) {
+    const void *probe = p->layout == SPL_LAYOUT_AOS ? p->aos : (const void *)p->x;
+    if (!is_device_ptr(probe))
+      return fail(SPL_ERR_INVALID, "particles marked device but pointer is not device memory");
+  }
+  return SPL_OK;
+}
+
+int bits_for(int64_t v) {  // bits needed to represent 0..v-1
+  int b = 0;
+  while (b < 32 && ((int64_t)1 << b) < v) ++b;
+  return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *spl_last_error_string(void) { return g_err.c_str(); }
+
+const char *spl_version(void) { return "splotch_gb300 0.1 (sm_103a)"; }
+
+spl_status spl_context_create(spl_context **ctx, int device) {
+  if (!ctx) return fail(SPL_ERR_INVALID, "null ctx");
+  *ctx = nullptr;
+  int ndev = 0;
+  SPL_CK(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(SPL_ERR_INVALID, "no such device");
+  SPL_CK(cudaSetDevice(device));
+  spl_context *c = new spl_context();
+  c->device = device;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return fail(SPL_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  c->own_stream = true;
+  for (auto &e : c->ev) cudaEventCreate(&e);
+  *ctx = c;
+  return SPL_OK;
+}
+
+spl_status spl_context_destroy(spl_context *c) {
+  if (!c) return SPL_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  spl_context::Buf *bufs[] = {&c->aos_in, &c->pos, &c->col, &c->active, &c->count, &c->key,
+                              &c->perm, &c->ktmp, &c->vtmp, &c->off, &c->scratch, &c->tkey,
+                              &c->tval, &c->tkey2, &c->tval2, &c->tkey_s, &c->tval_s,
+                              &c->tile_start, &c->wide_list, &c->small, &c->pic, &c->pal_x,
+                              &c->pal_rgb, &c->aos_out};
+  for (auto *b : bufs)
+    if (b->p) cudaFree(b->p);
+  for (auto &b : c->soa_in)
+    if (b.p) cudaFree(b.p);
+  for (auto &e : c->ev)
+    if (e) cudaEventDestroy(e);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return SPL_OK;
+}
+
+spl_status spl_context_set_stream(spl_context *c, void *stream) {
+  if (!c) return fail(SPL_ERR_INVALID, "null ctx");
+  SPL_CK(cudaSetDevice(c->device));
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  c->stream = static_cast<cudaStream_t>(stream);
+  c->own_stream = false;
+  return SPL_OK;
+}
+
+spl_status spl_get_stats(const spl_context *c, spl_stats *s) {
+  if (!c || !s) return fail(SPL_ERR_INVALID, "null argument");
+  *s = c->stats;
+  return SPL_OK;
+}
+
+spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particles *p,
+                      spl_image *out, int writeback) {
+  if (!c) return fail(SPL_ERR_INVALID, "null ctx");
+  SPL_CK(cudaSetDevice(c->device));
+  spl_status st = validate(d, p, out);
+  if (st) return st;
+  if (writeback == SPL_WRITEBACK_FULL && p->layout != SPL_LAYOUT_AOS)
+    return fail(SPL_ERR_UNSUPPORTED, "writeback needs the AoS (particle_sim) layout");
+  cudaStream_t s = c->stream;
+  const int64_t n = p->n;
+  const int xres = d->xres, yres = d->yres, T = d->tile_size;
+  int launches = 0;
+
+  spl_camera cam;
+  if (spl_camera_setup(d, &cam)) return fail(SPL_ERR_INVALID, "degenerate matrix in TRANSMAT::Inverse()");
+
+  // ---- frame constants ---------------------------------------------------
+  spl::ProjConst pc;
+  std::memset(&pc, 0, sizeof(pc));
+  std::memcpy(pc.mat, cam.mat, sizeof(pc.mat));
+  pc.res2 = cam.res2;
+  pc.ycorr = cam.ycorr;
+  pc.fovfct = cam.fovfct;
+  pc.xfac = cam.xfac;
+  pc.xsum = (double)cam.res2 + cam.xshift;
+  pc.ysum = (double)cam.res2 + cam.yshift + (double)cam.ycorr;
+  pc.zmin = d->zmin > 0.f ? d->zmin : 0.f;
+  pc.zmax = d->zmax;
+  pc.minrad2 = d->minrad_pix * d->minrad_pix;
+  const float bfak = (float)(0.5 * std::pow(3.141592653589793238462643383279502884197, -5. / 6.));
+  pc.half_bfak = 0.5f * bfak;
+  pc.xres = xres;
+  pc.yres = yres;
+  pc.projection = d->projection ? 1 : 0;
+  pc.ptypes = d->ptypes;
+  int npal = 0;
+  for (int t = 0; t < d->ptypes; ++t) {
+    pc.smooth[t] = d->smooth_factor[t];
+    pc.bright[t] = d->brightness[t] * d->b_brightness;
+    pc.colvec[t] = d->color_is_vector[t] ? 1 : 0;
+    pc.pal_off[t] = npal;
+    pc.pal_n[t] = d->color_is_vector[t] ? 0 : d->pal_n[t];
+    npal += pc.pal_n[t];
+  }
+  spl::Tiling g;
+  g.T = T;
+  g.ncx = (xres + T - 1) / T;
+  g.ncy = (yres + T - 1) / T;
+  g.rcell = std::sqrt(2.f) * (T * 0.5f - 0.5f);
+  g.cmid0 = 0.5f * (T - 1);
+  pc.T = g.T;
+  pc.ncx = g.ncx;
+  pc.ncy = g.ncy;
+  pc.rcell = g.rcell;
+  pc.cmid0 = g.cmid0;
+  const bool do_sort = !d->a_eq_e && d->sort_type != 0;
+  pc.sort_type = do_sort ? d->sort_type : 0;
+  const int64_t ntiles = (int64_t)g.ncx * g.ncy;
+  if (ntiles >= 0xffffffffLL) return fail(SPL_ERR_INVALID, "too many tiles");
+
+  // ---- buffers -------------------------------------------------------------
+  if ((st = ensure(c->pos, n * sizeof(float4))) || (st = ensure(c->col, n * sizeof(float4))) ||
+      (st = ensure(c->active, n)) || (st = ensure(c->count, n * 4)) ||
+      (st = ensure(c->off, (n + 1) * 8)) || (st = ensure(c->wide_list, n * 4)) ||
+      (st = ensure(c->small, 256)) || (st = ensure(c->tile_start, (ntiles + 1) * 4)) ||
+      (st = ensure(c->pic, (size_t)xres * yres * 3 * 4)) ||
+      (st = ensure(c->pal_x, (npal + 1) * 8)) || (st = ensure(c->pal_rgb, (npal + 1) * 12)))
+    return st;
+  if (do_sort) {
+    if ((st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
+        (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)))
+      return st;
+  }
+  size_t scr = spl::scan_scratch_bytes(n + 1);
+  size_t rs = spl::radix_scratch_bytes(n);
+  if (rs > scr) scr = rs;
+  if ((st = ensure(c->scratch, scr))) return st;
+  uint32_t *d_err = as<uint32_t>(c->small);
+  uint32_t *d_wide_n = d_err + 1;
+
+  // palettes (a few KB)
+  for (int t = 0; t < d->ptypes; ++t) {
+    if (!pc.pal_n[t]) continue;
+    SPL_CK(cudaMemcpyAsync(as<double>(c->pal_x) + pc.pal_off[t], d->pal_x[t], pc.pal_n[t] * 8,
+                           cudaMemcpyHostToDevice, s));
+    SPL_CK(cudaMemcpyAsync(as<float>(c->pal_rgb) + 3 * pc.pal_off[t], d->pal_rgb[t],
+                           pc.pal_n[t] * 12, cudaMemcpyHostToDevice, s));
+  }
+  pc.pal_x = as<double>(c->pal_x);
+  pc.pal_rgb = as<float>(c->pal_rgb);
+  SPL_CK(cudaMemsetAsync(d_err, 0, 8, s));
+
+  cudaEventRecord(c->ev[0], s);
+  // ---- inputs --------------------------------------------------------------
+  const void *aos_dev = nullptr;
+  const float *soa[8] = {p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb};
+  const uint16_t *type_dev = p->type;
+  if (p->layout == SPL_LAYOUT_AOS) {
+    if (p->memspace == SPL_MEM_HOST) {
+      if ((st = ensure(c->aos_in, n * 36))) return st;
+      SPL_CK(cudaMemcpyAsync(c->aos_in.p, p->aos, n * 36, cudaMemcpyHostToDevice, s));
+      aos_dev = c->aos_in.p;
+    } else {
+      aos_dev = p->aos;
+    }
+  } else if (p->memspace == SPL_MEM_HOST) {
+    for (int f = 0; f < 8; ++f) {
+      if (!soa[f]) continue;
+      if ((st = ensure(c->soa_in[f], n * 4))) return st;
+      SPL_CK(cudaMemcpyAsync(c->soa_in[f].p, soa[f], n * 4, cudaMemcpyHostToDevice, s));
+      soa[f] = as<float>(c->soa_in[f]);
+    }
+    if (p->type) {
+      if ((st = ensure(c->soa_in[8], n * 2))) return st;
+      SPL_CK(cudaMemcpyAsync(c->soa_in[8].p, p->type, n * 2, cudaMemcpyHostToDevice, s));
+      type_dev = as<uint16_t>(c->soa_in[8]);
+    }
+  }
+  cudaEventRecord(c->ev[1], s);
+
+  // ---- project + colourise ------------------------------------------------
+  spl::ProjectOut po;
+  po.pos = as<float4>(c->pos);
+  po.col = as<float4>(c->col);
+  po.active = as<uint8_t>(c->active);
+  po.count = as<uint32_t>(c->count);
+  po.key = do_sort ? as<uint32_t>(c->key) : nullptr;
+  po.err = d_err;
+  if (p->layout == SPL_LAYOUT_AOS)
+    spl::launch_project_aos(aos_dev, n, pc, po, s);
+  else
+    spl::launch_project_soa(soa[0], soa[1], soa[2], soa[3], soa[4], soa[5], soa[6], soa[7],
+                            type_dev, n, pc, po, s);
+  if (n > 0) ++launches;
+  cudaEventRecord(c->ev[2], s);
+
+  // ---- depth sort (a_eq_e=false), splotch_host.cc:805-815 ------------------
+  const uint32_t *order = nullptr;
+  if (do_sort && n > 0) {
+    spl::radix_sort_pairs(as<uint32_t>(c->key), nullptr, as<uint32_t>(c->ktmp),
+                          as<uint32_t>(c->vtmp), as<uint32_t>(c->key) /*unused out*/,
+                          as<uint32_t>(c->perm), n, 0, 32, false, c->scratch.p, s, &launches);
+    order = as<uint32_t>(c->perm);
+  }
+  cudaEventRecord(c->ev[3], s);
+
+  // ---- binning ---------------------------------------------------------------
+  uint64_t *off = as<uint64_t>(c->off);
+  spl::scan_counts(as<uint32_t>(c->count), order, n, off, c->scratch.p, s, &launches);
+  uint64_t ne = 0;
+  SPL_CK(cudaMemcpyAsync(&ne, off + n, 8, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));
+  if (ne >= 0xffffffffULL) return fail(SPL_ERR_CAPACITY, "more than 2^32-1 bin entries");
+  if ((st = ensure(c->tkey, ne * 4)) || (st = ensure(c->tval, ne * 4)) ||
+      (st = ensure(c->tkey2, ne * 4)) || (st = ensure(c->tval2, ne * 4)) ||
+      (st = ensure(c->tkey_s, ne * 4)) || (st = ensure(c->tval_s, ne * 4)))
+    return st;
+  size_t rs2 = spl::radix_scratch_bytes((int64_t)ne);
+  if ((st = ensure(c->scratch, rs2))) return st;
+  if (ne > 0) {
+    spl::launch_emit(as<float4>(c->pos), as<uint32_t>(c->count), order, off, n, g,
+                     as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->wide_list),
+                     d_wide_n, s);
+    launches += 2;
+    const int tb = bits_for(ntiles);
+    if (tb > 0) {
+      spl::radix_sort_pairs(as<uint32_t>(c->tkey), as<uint32_t>(c->tval),
+                            as<uint32_t>(c->tkey2), as<uint32_t>(c->tval2),
+                            as<uint32_t>(c->tkey_s), as<uint32_t>(c->tval_s), (int64_t)ne, 0,
+                            tb, true, c->scratch.p, s, &launches);
+    } else {
+      SPL_CK(cudaMemcpyAsync(c->tkey_s.p, c->tkey.p, ne * 4, cudaMemcpyDeviceToDevice, s));
+      SPL_CK(cudaMemcpyAsync(c->tval_s.p, c->tval.p, ne * 4, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  spl::launch_tile_ranges(as<uint32_t>(c->tkey_s), (int64_t)ne, ntiles,
+                          as<uint32_t>(c->tile_start), s);
+  ++launches;
+  cudaEventRecord(c->ev[4], s);
+
+  // ---- splat ---------------------------------------------------------------------
+  spl::SplatArgs sa;
+  sa.pos = as<float4>(c->pos);
+  sa.col = as<float4>(c->col);
+  sa.entries = as<uint32_t>(c->tval_s);
+  sa.tile_start = as<uint32_t>(c->tile_start);
+  sa.T = T;
+  sa.ncx = g.ncx;
+  sa.ncy = g.ncy;
+  sa.xres = xres;
+  sa.yres = yres;
+  sa.gray = d->gray_absorption;
+  sa.h2sigma = (float)(0.5 * std::pow(3.141592653589793238462643383279502884197, -1. / 6.));
+  sa.a_eq_e = d->a_eq_e ? 1 : 0;
+  sa.order_mode = d->order_mode;
+  sa.ftb_eps = d->ftb_epsilon;
+  sa.pic = out->memspace == SPL_MEM_DEVICE ? out->pic : as<float>(c->pic);
+  launches += spl::launch_splat(sa, s);
+  SPL_CK(cudaGetLastError());
+  cudaEventRecord(c->ev[5], s);
+
+  // ---- outputs -------------------------------------------------------------------
+  if (out->memspace == SPL_MEM_HOST)
+    SPL_CK(cudaMemcpyAsync(out->pic, c->pic.p, (size_t)xres * yres * 12, cudaMemcpyDeviceToHost,
+                           s));
+  if (writeback == SPL_WRITEBACK_FULL && n > 0) {
+    void *dst = p->memspace == SPL_MEM_DEVICE ? p->aos : nullptr;
+    if (!dst) {
+      if ((st = ensure(c->aos_out, n * 36))) return st;
+      dst = c->aos_out.p;
+    }
+    // a device-resident AoS is read by the project kernel already; the
+    // writeback permutes, so it goes through a separate buffer first
+    if (p->memspace == SPL_MEM_DEVICE) {
+      if ((st = ensure(c->aos_out, n * 36))) return st;
+      spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
+                                aos_dev, 1, order, n, c->aos_out.p, s);
+      SPL_CK(cudaMemcpyAsync(p->aos, c->aos_out.p, n * 36, cudaMemcpyDeviceToDevice, s));
+    } else {
+      spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
+                                aos_dev, 1, order, n, dst, s);
+      SPL_CK(cudaMemcpyAsync(p->aos, dst, n * 36, cudaMemcpyDeviceToHost, s));
+    }
+    ++launches;
+  }
+  cudaEventRecord(c->ev[6], s);
+  uint32_t err = 0;
+  SPL_CK(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));
+  SPL_CK(cudaGetLastError());
+  if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
+
+  c->n = n;
+  c->ne = (int64_t)ne;
+  c->ntiles = ntiles;
+  c->has_order = order != nullptr;
+  c->last_T = T;
+  spl_stats &S = c->stats;
+  cudaEventElapsedTime(&S.h2d_ms, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&S.project_ms, c->ev[1], c->ev[2]);
+  cudaEventElapsedTime(&S.sort_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&S.bin_ms, c->ev[3], c->ev[4]);
+  cudaEventElapsedTime(&S.splat_ms, c->ev[4], c->ev[5]);
+  cudaEventElapsedTime(&S.d2h_ms, c->ev[5], c->ev[6]);
+  cudaEventElapsedTime(&S.total_ms, c->ev[0], c->ev[6]);
+  S.n_entries = (int64_t)ne;
+  S.n_tiles = ntiles;
+  S.kernel_launches = launches;
+  S.n_active = -1;
+  return SPL_OK;
+}
+
+spl_status spl_debug_get_projected(spl_context *c, void *aos_out, int64_t n) {
+  if (!c || !aos_out || n != c->n) return fail(SPL_ERR_INVALID, "bad arguments");
+  SPL_CK(cudaSetDevice(c->device));
+  spl_status st;
+  if ((st = ensure(c->aos_out, n * 36))) return st;
+  // type comes from the AoS input copy when there is one; SoA types from soa_in
+  const void *tsrc = c->aos_in.p;
+  int kind = 1;
+  if (!tsrc) { tsrc = c->soa_in[8].p; kind = tsrc ? 2 : 0; }
+  spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
+                            tsrc, kind, nullptr, n, c->aos_out.p, c->stream);
+  SPL_CK(cudaMemcpyAsync(aos_out, c->aos_out.p, n * 36, cudaMemcpyDeviceToHost, c->stream));
+  SPL_CK(cudaStreamSynchronize(c->stream));
+  return SPL_OK;
+}
+
+spl_status spl_debug_get_order(spl_context *c, uint32_t *perm_out, int64_t n) {
+  if (!c || !perm_out || n != c->n) return fail(SPL_ERR_INVALID, "bad arguments");
+  SPL_CK(cudaSetDevice(c->device));
+  if (!c->has_order) {
+    for (int64_t i = 0; i < n; ++i) perm_out[i] = (uint32_t)i;
+    return SPL_OK;
+  }
+  SPL_CK(cudaMemcpy(perm_out, c->perm.p, n * 4, cudaMemcpyDeviceToHost));
+  return SPL_OK;
+}
+
+spl_status spl_debug_get_bins(spl_context *c, int64_t *tile_start_out, int64_t ntp1,
+                              uint32_t *entries_out, int64_t cap) {
+  if (!c || !tile_start_out || ntp1 != c->ntiles + 1)
+    return fail(SPL_ERR_INVALID, "bad arguments (need ntiles+1 tile starts)");
+  if (cap < c->ne || (c->ne > 0 && !entries_out))
+    return fail(SPL_ERR_CAPACITY, "entries buffer too small: need " + std::to_string(c->ne));
+  SPL_CK(cudaSetDevice(c->device));
+  std::string tmp;
+  uint32_t *ts = new uint32_t[ntp1];
+  cudaError_t e = cudaMemcpy(ts, c->tile_start.p, ntp1 * 4, cudaMemcpyDeviceToHost);
+  for (int64_t i = 0; i < ntp1; ++i) tile_start_out[i] = ts[i];
+  delete[] ts;
+  if (e != cudaSuccess) return fail(SPL_ERR_CUDA, cudaGetErrorString(e));
+  if (c->ne > 0) SPL_CK(cudaMemcpy(entries_out, c->tval_s.p, c->ne * 4, cudaMemcpyDeviceToHost));
+  return SPL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,156 @@
+// spl_bin.cu -- particle-to-tile binning (render_new region A,
+// splotch/splotch_host.cc:339-406) as count -> exclusive scan -> emit ->
+// stable sort by tile id.
+//
+// The reference builds one list per tile; because each OpenMP thread scans a
+// contiguous, ascending share of the particle array and the lists are read in
+// thread order (splotch_host.cc:455), every tile's list is in ascending array
+// position.  Here entries are emitted in visiting order (scan offsets) and a
+// stable radix sort by tile id groups them without reordering, which gives the
+// same per-tile order bit-for-bit.
+//
+// Two emission paths: one thread per particle for footprints of up to
+// kWideTiles tiles, and one warp per particle (rows of its tile rectangle
+// spread over the lanes) for wide particles, so a particle covering thousands
+// of tiles does not serialise a whole warp behind one thread.
+#include "spl_internal.cuh"
+
+namespace spl {
+
+namespace {
+
+constexpr int kWideTiles = 64;
+
+__global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ pos,
+                                                     const uint32_t *__restrict__ count,
+                                                     const uint32_t *__restrict__ order,
+                                                     const uint64_t *__restrict__ off,
+                                                     int64_t n, Tiling g,
+                                                     uint32_t *__restrict__ tkey,
+                                                     uint32_t *__restrict__ tval,
+                                                     uint32_t *__restrict__ wide_list,
+                                                     uint32_t *__restrict__ wide_n) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
+    const uint32_t c = __ldg(count + i);
+    if (c == 0) continue;
+    if (c > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
+      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+      continue;
+    }
+    const uint64_t o = __ldg(off + s);
+    const float4 p = __ldg(pos + i);
+    for_each_tile(p.x, p.y, p.z, g, [&](int tile, int j) {
+      tkey[o + j] = (uint32_t)tile;
+      tval[o + j] = i;
+    });
+  }
+}
+
+// One warp per wide particle.  Lane l takes tile rows iy = miny + l, +32, ...;
+// each row's passing tiles are counted first, a warp scan gives each row its
+// slot, then the row is written.  The order of a particle's entries inside its
+// slot range does not matter: the stable tile sort only orders entries of the
+// same tile, and a particle contributes at most one entry per tile.
+__global__ void __launch_bounds__(256) k_emit_wide(const float4 *__restrict__ pos,
+                                                   const uint32_t *__restrict__ order,
+                                                   const uint64_t *__restrict__ off,
+                                                   const uint32_t *__restrict__ wide_list,
+                                                   const uint32_t *__restrict__ wide_n,
+                                                   Tiling g, uint32_t *__restrict__ tkey,
+                                                   uint32_t *__restrict__ tval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nw = *wide_n;
+  for (int64_t w = warp0; w < nw; w += nwarps) {
+    const uint32_t s = wide_list[w];
+    const uint32_t i = order ? __ldg(order + s) : s;
+    const uint64_t o = __ldg(off + s);
+    const float4 p = __ldg(pos + i);
+    const int T = g.T;
+    const float rfacr = fmul(0.75f, p.z);
+    const int minx = max(0, f2i(fadd(fsub(p.x, rfacr), 1.f)) / T);
+    const int maxx = min(g.ncx - 1, f2i(fadd(p.x, rfacr)) / T);
+    const int miny = max(0, f2i(fadd(fsub(p.y, rfacr), 1.f)) / T);
+    const int maxy = min(g.ncy - 1, f2i(fadd(p.y, rfacr)) / T);
+    const float rs = fadd(g.rcell, rfacr);
+    const float sumsq = fmul(rs, rs);
+    uint64_t base = o;
+    for (int iy0 = miny; iy0 <= maxy; iy0 += 32) {
+      const int iy = iy0 + lane;
+      int rc = 0;
+      float dy2 = 0.f;
+      if (iy <= maxy) {
+        const float cy = fadd(g.cmid0, (float)(iy * T));
+        const float dy = fsub(p.y, cy);
+        dy2 = fmul(dy, dy);
+        for (int ix = minx; ix <= maxx; ++ix) {
+          const float cx = fadd(g.cmid0, (float)(ix * T));
+          const float dx = fsub(p.x, cx);
+          if (fadd(fmul(dx, dx), dy2) < sumsq) ++rc;
+        }
+      }
+      // exclusive warp scan of row counts
+      int incl = rc;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += t;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      uint64_t slot = base + (uint64_t)(incl - rc);
+      if (iy <= maxy && rc > 0) {
+        for (int ix = minx; ix <= maxx; ++ix) {
+          const float cx = fadd(g.cmid0, (float)(ix * T));
+          const float dx = fsub(p.x, cx);
+          if (fadd(fmul(dx, dx), dy2) < sumsq) {
+            tkey[slot] = (uint32_t)(iy * g.ncx + ix);
+            tval[slot] = i;
+            ++slot;
+          }
+        }
+      }
+      base += (uint64_t)total;
+    }
+  }
+}
+
+// tile_start[t] = first sorted position whose key is >= t.
+__global__ void __launch_bounds__(256) k_tile_ranges(const uint32_t *__restrict__ key,
+                                                     int64_t ne, int64_t ntiles,
+                                                     uint32_t *__restrict__ tile_start) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= ne;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t kprev = p > 0 ? (int64_t)key[p - 1] : -1;
+    const int64_t kcur = p < ne ? (int64_t)key[p] : ntiles;
+    for (int64_t t = kprev + 1; t <= kcur; ++t) tile_start[t] = (uint32_t)p;
+  }
+}
+
+int grid_for(int64_t n, int per_block) {
+  int64_t b = (n + per_block - 1) / per_block;
+  const int64_t cap = 152LL * 16;
+  if (b > cap) b = cap;
+  return (int)(b > 0 ? b : 1);
+}
+
+}  // namespace
+
+void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order,
+                 const uint64_t *off, int64_t n, Tiling g, uint32_t *tkey, uint32_t *tval,
+                 uint32_t *wide_list, uint32_t *wide_n, cudaStream_t s) {
+  if (n <= 0) return;
+  cudaMemsetAsync(wide_n, 0, sizeof(uint32_t), s);
+  k_emit_narrow<<<grid_for(n, 256), 256, 0, s>>>(pos, count, order, off, n, g, tkey, tval,
+                                                 wide_list, wide_n);
+  k_emit_wide<<<152 * 4, 256, 0, s>>>(pos, order, off, wide_list, wide_n, g, tkey, tval);
+}
+
+void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
+                        uint32_t *tile_start, cudaStream_t s) {
+  k_tile_ranges<<<grid_for(ne + 1, 256), 256, 0, s>>>(sorted_tkey, ne, ntiles, tile_start);
+}
+
+}  // namespace spl

@@ -1,0 +1,277 @@
+// spl_sort.cu -- stable LSD radix sort of (uint32 key, uint32 value) pairs
+// and the exclusive scans used by binning.
+//
+// The depth sort replaces particle_sort (splotch/splotch_host.cc:289-321).
+// The reference calls std::sort, which is not stable; this sort is stable, so
+// equal keys keep ascending particle index (= std::stable_sort with the same
+// comparator), the tie-break the renderer specifies.
+//
+// Structure per 8-bit digit pass (reduce-then-scan, no inter-block waits):
+//   upsweep   : per-block digit histogram -> counts[digit][block]
+//   scan      : exclusive scan over the digit-major counts array
+//   downsweep : stable in-block ranking with warp match/ballot, then scatter
+#include "spl_internal.cuh"
+
+namespace spl {
+
+namespace {
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_WARPS = RS_THREADS / 32;
+constexpr int RS_ITEMS = 16;
+constexpr int RS_TILE = RS_THREADS * RS_ITEMS;  // keys per block
+constexpr int RS_BINS = 256;
+
+constexpr int SC_THREADS = 256;
+constexpr int SC_ITEMS = 16;
+constexpr int SC_TILE = SC_THREADS * SC_ITEMS;
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t *__restrict__ keys,
+                                                           int64_t n, int shift, int nbits,
+                                                           uint32_t *__restrict__ counts,
+                                                           int nblocks) {
+  __shared__ uint32_t hist[RS_BINS];
+  hist[threadIdx.x] = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t mask = (1u << nbits) - 1u;
+  const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * 32 * RS_ITEMS;
+#pragma unroll 4
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const int64_t idx = base + j * 32 + lane;
+    const bool valid = idx < n;
+    const uint32_t d = valid ? (__ldg(keys + idx) >> shift) & mask : RS_BINS + lane;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    if (valid && (__ffs(peers) - 1) == lane) atomicAdd(&hist[d], __popc(peers));
+  }
+  __syncthreads();
+  counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = hist[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
+    const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+    uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n, int shift,
+    int nbits, const uint32_t *__restrict__ offsets, int nblocks) {
+  __shared__ uint32_t whist[RS_WARPS][RS_BINS];
+  __shared__ uint32_t boff[RS_BINS];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&whist[0][0])[i] = 0;
+  boff[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  __syncthreads();
+  const uint32_t mask = (1u << nbits) - 1u;
+  const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * 32 * RS_ITEMS;
+  uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const int64_t idx = base + j * 32 + lane;
+    const bool valid = idx < n;
+    key[j] = valid ? __ldg(keys_in + idx) : 0xffffffffu;
+    val[j] = valid ? (vals_in ? __ldg(vals_in + idx) : (uint32_t)idx) : 0u;
+    const uint32_t d = valid ? (key[j] >> shift) & mask : RS_BINS + lane;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    uint32_t prior = 0;
+    if (valid) prior = whist[w][d];
+    __syncwarp();
+    if (valid && (__ffs(peers) - 1) == lane) whist[w][d] = prior + __popc(peers);
+    __syncwarp();
+    rank[j] = prior + __popc(peers & lanemask_lt());
+  }
+  __syncthreads();
+  {  // exclusive prefix over warps for each digit
+    const int d = threadIdx.x;
+    uint32_t run = 0;
+#pragma unroll
+    for (int ww = 0; ww < RS_WARPS; ++ww) {
+      const uint32_t t = whist[ww][d];
+      whist[ww][d] = run;
+      run += t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const int64_t idx = base + j * 32 + lane;
+    if (idx < n) {
+      const uint32_t d = (key[j] >> shift) & mask;
+      const uint32_t dst = boff[d] + whist[w][d] + rank[j];
+      if (keys_out) keys_out[dst] = key[j];
+      vals_out[dst] = val[j];
+    }
+  }
+}
+
+// ---- generic exclusive scan (three kernels) ------------------------------
+
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan(T v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// block-wide exclusive scan of one value per thread; returns exclusive
+// prefix and writes the block total
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T *sm_warp, T &total) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T inc = warp_incl_scan(v, lane);
+  if (lane == 31) sm_warp[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    T x = lane < (int)(blockDim.x >> 5) ? sm_warp[lane] : T(0);
+    T xi = warp_incl_scan(x, lane);
+    if (lane < (int)(blockDim.x >> 5)) sm_warp[lane] = xi - x;
+    if (lane == 31) sm_warp[32] = xi;
+  }
+  __syncthreads();
+  total = sm_warp[32];
+  T r = sm_warp[w] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+template <typename T, typename L>
+__global__ void __launch_bounds__(SC_THREADS) k_scan_reduce(L load, int64_t n, T *partials) {
+  __shared__ T sm[33];
+  const int64_t base = (int64_t)blockIdx.x * SC_TILE;
+  T s = 0;
+  for (int j = 0; j < SC_ITEMS; ++j) {
+    const int64_t i = base + j * SC_THREADS + threadIdx.x;
+    if (i < n) s += load(i);
+  }
+  T total;
+  block_excl_scan<T>(s, sm, total);
+  if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+// single block: exclusive scan of m partials in place; total to *total_out
+template <typename T>
+__global__ void __launch_bounds__(SC_THREADS) k_scan_partials(T *partials, int64_t m,
+                                                              T *total_out) {
+  __shared__ T sm[33];
+  T carry = 0;
+  for (int64_t b = 0; b < m; b += SC_THREADS) {
+    const int64_t i = b + threadIdx.x;
+    T v = i < m ? partials[i] : T(0);
+    T tot;
+    T ex = block_excl_scan<T>(v, sm, tot);
+    if (i < m) partials[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0 && total_out) *total_out = carry;
+}
+
+template <typename T, typename L>
+__global__ void __launch_bounds__(SC_THREADS) k_scan_apply(L load, int64_t n,
+                                                           const T *partials, T *out) {
+  __shared__ T sm[33];
+  const int64_t base = (int64_t)blockIdx.x * SC_TILE;
+  // each thread owns SC_ITEMS consecutive elements
+  const int64_t my = base + (int64_t)threadIdx.x * SC_ITEMS;
+  T v[SC_ITEMS];
+  T s = 0;
+#pragma unroll
+  for (int j = 0; j < SC_ITEMS; ++j) {
+    const int64_t i = my + j;
+    v[j] = i < n ? load(i) : T(0);
+    s += v[j];
+  }
+  T tot;
+  T ex = block_excl_scan<T>(s, sm, tot) + partials[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < SC_ITEMS; ++j) {
+    const int64_t i = my + j;
+    if (i < n) out[i] = ex;
+    ex += v[j];
+  }
+}
+
+struct LoadU32 {
+  const uint32_t *p;
+  __device__ __forceinline__ uint32_t operator()(int64_t i) const { return __ldg(p + i); }
+};
+struct LoadCountOrdered {
+  const uint32_t *count;
+  const uint32_t *order;
+  __device__ __forceinline__ uint64_t operator()(int64_t i) const {
+    return (uint64_t)__ldg(count + (order ? __ldg(order + i) : (uint32_t)i));
+  }
+};
+
+template <typename T, typename L>
+void exclusive_scan(L load, int64_t n, T *out, T *total_out, void *scratch, cudaStream_t s,
+                    int *launches) {
+  const int64_t nb = (n + SC_TILE - 1) / SC_TILE;
+  T *partials = static_cast<T *>(scratch);
+  if (nb > 0) {
+    k_scan_reduce<T, L><<<(unsigned)nb, SC_THREADS, 0, s>>>(load, n, partials);
+    k_scan_partials<T><<<1, SC_THREADS, 0, s>>>(partials, nb, total_out);
+    k_scan_apply<T, L><<<(unsigned)nb, SC_THREADS, 0, s>>>(load, n, partials, out);
+    if (launches) *launches += 3;
+  } else if (total_out) {
+    cudaMemsetAsync(total_out, 0, sizeof(T), s);
+  }
+}
+
+}  // namespace
+
+size_t radix_scratch_bytes(int64_t n) {
+  const int64_t nb = (n + RS_TILE - 1) / RS_TILE;
+  const int64_t m = nb * RS_BINS;
+  const int64_t np = (m + SC_TILE - 1) / SC_TILE;
+  return (size_t)(2 * m + np + 64) * sizeof(uint32_t);
+}
+
+int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_tmp,
+                     uint32_t *vals_tmp, uint32_t *keys_out, uint32_t *vals_out, int64_t n,
+                     int bit0, int bit1, bool keys_needed, void *scratch, cudaStream_t s,
+                     int *launches) {
+  if (n <= 0) return 0;
+  const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
+  const int64_t m = (int64_t)nblocks * RS_BINS;
+  uint32_t *counts = static_cast<uint32_t *>(scratch);
+  uint32_t *offsets = counts + m;
+  uint32_t *sc = offsets + m;
+  int npass = 0;
+  for (int b = bit0; b < bit1; b += 8) ++npass;
+  // ping-pong so that the last pass lands in (keys_out, vals_out)
+  const uint32_t *kin = keys_in;
+  const uint32_t *vin = vals_in;
+  int pass = 0;
+  for (int b = bit0; b < bit1; b += 8, ++pass) {
+    const int nbits = (bit1 - b) < 8 ? (bit1 - b) : 8;
+    const bool last = pass == npass - 1;
+    const bool to_out = ((npass - 1 - pass) % 2) == 0;
+    uint32_t *ko = to_out ? keys_out : keys_tmp;
+    uint32_t *vo = to_out ? vals_out : vals_tmp;
+    k_rs_upsweep<<<nblocks, RS_THREADS, 0, s>>>(kin, n, b, nbits, counts, nblocks);
+    exclusive_scan<uint32_t>(LoadU32{counts}, m, offsets, (uint32_t *)nullptr, sc, s, launches);
+    k_rs_downsweep<<<nblocks, RS_THREADS, 0, s>>>(kin, vin, (last && !keys_needed) ? nullptr : ko,
+                                                  vo, n, b, nbits, offsets, nblocks);
+    if (launches) *launches += 2;
+    kin = ko;
+    vin = vo;
+  }
+  return npass;
+}
+
+size_t scan_scratch_bytes(int64_t n) {
+  return (size_t)((n + SC_TILE - 1) / SC_TILE + 64) * sizeof(uint64_t);
+}
+
+void scan_counts(const uint32_t *count, const uint32_t *order, int64_t n, uint64_t *off,
+                 void *scratch, cudaStream_t s, int *launches) {
+  exclusive_scan<uint64_t>(LoadCountOrdered{count, order}, n, off, off + n, scratch, s,
+                           launches);
+}
+
+}  // namespace spl
