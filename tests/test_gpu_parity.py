@@ -1,0 +1,177 @@
+"""Parity of the CUDA path with the oracle, stage by stage.
+
+Bit-exact: projected particles (x, y, z, r, I, e, active), the visiting order
+(stable sort permutation), tile ranges and tile bin entries.  Images: per-pixel
+relative L-inf <= 1e-4 against the FP64 oracle (floor 1e-6 * max|pixel|).
+"""
+import numpy as np
+import pytest
+
+import splotch_gb300 as sg
+from oracle.oracle import rel_linf
+from splotch_gb300 import synth
+
+from .helpers import IMAGE_TOL, assert_parity, gpu_frame, oracle_frame
+
+pytestmark = pytest.mark.gpu
+
+
+def _additive(**kw):
+    return synth.plain_additive(**kw)
+
+
+def _absorption(**kw):
+    return synth.plain_absorption(**kw)
+
+
+CASES = {
+    "add_T16": lambda: _additive(n=40000, xres=160, yres=120, tile=16),
+    "add_T50": lambda: _additive(n=40000, xres=200, yres=150, tile=50),
+    "add_T7_odd": lambda: _additive(n=20000, xres=101, yres=77, tile=7),
+    "add_T32": lambda: _additive(n=40000, xres=256, yres=200, tile=32),
+    "add_T64": lambda: _additive(n=20000, xres=200, yres=130, tile=64),
+    "abs_btf_T16": lambda: _absorption(n_gas=40000, n_star=10000, xres=192, yres=108, tile=16,
+                                       order="btf"),
+    "abs_ftb_T16": lambda: _absorption(n_gas=40000, n_star=10000, xres=192, yres=108, tile=16,
+                                       order="ftb"),
+    "abs_btf_T50": lambda: _absorption(n_gas=40000, n_star=10000, xres=192, yres=108, tile=50,
+                                       order="btf"),
+    "abs_ftb_T32": lambda: _absorption(n_gas=40000, n_star=10000, xres=256, yres=144, tile=32,
+                                       order="ftb"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_stage_parity(name, renderer, port):
+    w = CASES[name]()
+    prm = dict(w.params.params)
+    g = gpu_frame(renderer, prm, w.rc, w.particles)
+    o = oracle_frame(port, prm, w.rc, w.particles)
+    info = assert_parity(g, o)
+    assert o.frags > 0
+    print(name, info)
+
+
+def _edge_setup(xres=96, yres=80, tile=16, a_eq_e=True, **extra):
+    rc = sg.RenderContext(campos=np.array([0.0, 0.0, 100.0]),
+                          centerpos=np.array([0.0, 0.0, 100.0]), lookat=np.zeros(3),
+                          sky=np.array([0.0, 1.0, 0.0]), amap=[synth.blue_white_palette()])
+    prm = {"xres": xres, "yres": yres, "fov": 45.0, "a_eq_e": a_eq_e, "tile_size_cpu": tile,
+           "ptypes": 1, "sort_type": 1}
+    prm.update(extra)
+    return sg.ParamFile(prm).params, rc
+
+
+def _place(prm, px, py, rpix, zw=0.0):
+    """World position / hsml that lands near pixel (px, py) with radius rpix
+    for the edge-case camera (campos (0,0,100) looking at the origin)."""
+    xres, yres = int(prm["xres"]), int(prm["yres"])
+    res2 = 0.5 * xres
+    fovfct = np.tan(np.radians(45.0) / 2)
+    xfac2 = res2 / (fovfct * (100.0 - zw))
+    ycorr = 0.5 * (yres - xres)
+    return (px - res2) / xfac2, (py - res2 - ycorr) / xfac2, rpix / (2 * xfac2)
+
+
+def _particles(prm, specs):
+    p = sg.make_particles(len(specs))
+    for i, (px, py, rpix, zw, I, c) in enumerate(specs):
+        x, y, h = _place(prm, px, py, rpix, zw)
+        p[i]["x"], p[i]["y"], p[i]["z"], p[i]["r"] = x, y, zw, h
+        p[i]["I"], p[i]["er"] = I, c
+    return p
+
+
+EDGE = {
+    "single_centre": [(40.0, 40.0, 6.0, 0.0, 1.0, 0.5)],
+    "tile_edge_straddle": [(16.0 + d, 16.0 + d, 5.0, 0.0, 1.0, 0.3) for d in (-0.5, 0.0, 0.49)]
+    + [(31.5, 47.99, 3.0, 0.0, 2.0, 0.7)],
+    "clipped_borders": [(-3.0, 10.0, 8.0, 0.0, 1.0, 0.2), (95.5, 79.7, 6.0, 0.0, 1.0, 0.9),
+                        (50.0, -7.5, 9.0, 0.0, 1.0, 0.4), (120.0, 40.0, 10.0, 0.0, 1.0, 0.5)],
+    "minrad_floor": [(20.3 + 3 * i, 30.7 + 2 * i, 0.05 * (i + 1), 0.0, 1.0, 0.5) for i in range(12)],
+    "huge_wide_path": [(48.0, 40.0, 400.0, 0.0, 0.3, 0.6), (10.0, 70.0, 150.0, 1.0, 0.2, 0.1)],
+    "equal_z_ties": [(30.0 + i, 35.0 + (i % 3), 7.0, 5.0, 1.0 + 0.1 * i, i / 20) for i in range(20)],
+    "behind_camera": [(40.0, 40.0, 5.0, 150.0, 1.0, 0.5), (41.0, 40.0, 5.0, 99.999, 1.0, 0.5)],
+}
+
+
+@pytest.mark.parametrize("mode", ["add", "btf", "ftb"])
+@pytest.mark.parametrize("name", sorted(EDGE))
+def test_edge_cases(name, mode, renderer, port):
+    prm, rc = _edge_setup(a_eq_e=(mode == "add"), gpu_order=mode if mode != "add" else "btf")
+    p = _particles(prm, EDGE[name])
+    g = gpu_frame(renderer, prm, rc, p)
+    o = oracle_frame(port, prm, rc, p)
+    assert_parity(g, o)
+
+
+def test_zmin_and_all_culled(renderer, port):
+    # both particles sit at depth -z = 100 and 99.5 in camera space: zmin=100.5
+    # culls them (splotch_host.cc:123, cull when -z <= zmin)
+    prm, rc = _edge_setup(zmin=100.5)
+    p = _particles(prm, [(40.0, 40.0, 5.0, 0.0, 1.0, 0.5), (60.0, 20.0, 5.0, 0.5, 1.0, 0.5)])
+    g = gpu_frame(renderer, prm, rc, p)
+    o = oracle_frame(port, prm, rc, p)
+    assert_parity(g, o)
+    assert not g.projected["active"].any()
+    assert not g.pic.any()
+
+
+def test_empty_input(renderer, port):
+    prm, rc = _edge_setup(a_eq_e=False)
+    p = sg.make_particles(0)
+    g = gpu_frame(renderer, prm, rc, p)
+    assert g.entries.size == 0 and not g.pic.any()
+
+
+def test_host_rendering_mirror(built, port):
+    """The drop-in: same keys/defaults, rc.pic overwritten, particles mutated in
+    place (projected, colourised, stable z order) like the reference."""
+    w = synth.plain_absorption(n_gas=8000, n_star=2000, xres=128, yres=96, tile=16, order="btf")
+    parts = w.particles.copy()
+    rc = w.rc
+    sg.update_res(w.params, rc)
+    sg.host_rendering(w.params, parts, rc)
+    prm = dict(w.params.params)
+    ref = w.particles.copy()
+    port.project_colorize(prm, rc, ref)
+    perm = port.sort_perm(ref, 1)
+    ref = ref[perm]
+    assert np.array_equal(parts.view(np.uint8), ref.view(np.uint8))
+    pic64, _ = port.render_fp64(ref, None, 128, 96, 16, False, 0.2)
+    assert rel_linf(rc.pic, pic64) <= IMAGE_TOL
+
+
+def test_soa_device_matches_aos(renderer):
+    torch = pytest.importorskip("torch")
+    w = synth.plain_additive(n=30000, xres=128, yres=128, tile=16)
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    pic_h = np.zeros((128, 128, 3), np.float32)
+    renderer.render_aos(desc, w.particles.copy(), pic_h)
+    soa = {k: torch.from_numpy(v).cuda() for k, v in synth.soa_from_aos(w.particles).items()}
+    pic_d = torch.zeros((128, 128, 3), dtype=torch.float32, device="cuda")
+    renderer.render_soa(desc, soa, pic_d, device=True)
+    torch.cuda.synchronize()
+    assert np.array_equal(pic_d.cpu().numpy(), pic_h)
+
+
+def test_determinism(renderer):
+    w = synth.plain_absorption(n_gas=40000, n_star=10000, xres=192, yres=108, tile=16)
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    a = np.zeros((192, 108, 3), np.float32)
+    b = np.zeros_like(a)
+    renderer.render_aos(desc, w.particles.copy(), a)
+    renderer.render_aos(desc, w.particles.copy(), b)
+    assert np.array_equal(a, b)
+
+
+def test_full_size_additive_1M(renderer, port):
+    """The plain additive workload at full size (1M particles, 800x800)."""
+    w = synth.plain_additive()
+    prm = dict(w.params.params)
+    g = gpu_frame(renderer, prm, w.rc, w.particles)
+    o = oracle_frame(port, prm, w.rc, w.particles, fp32=False)
+    info = assert_parity(g, o)
+    print("full additive", info, g.stats)
