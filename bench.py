@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""bench.py -- throughput of the Splotch particle-render path on GB300.
+
+Workload (one step = one frame): the plain ordered emission-absorption render,
+40M gas + 10M star particles from the seeded halo-mixture generator in a
+[0,500]^3 box, 1920x1080 float32 image, camera (250,250,-50) -> (250,250,250),
+fov 45, depth sort on (sort_type 1), gray_absorption 0.2.  Synthetic data: the
+reference's demo snapshot is not available.
+
+value : Mparticles/s with the SoA inputs already resident in HBM (CUDA events
+        on the render stream around K frames; 1.8 GB of inputs per frame, far
+        larger than L2, so no flush is needed).
+e2e   : the same metric through the C ABI with HOST buffers: particle_sim
+        records in pinned host memory, H2D + image D2H inside every timed call.
+roofline: the dominant kernel of the frame, algorithmic work / its CUDA-event
+        time, against MEASURED_PEAKS.json.
+cpu_baseline: the CPU restatement of the reference (bit-exact with it) timed
+        on this host's cores on a 1-in-5 subsample of the same frame.
+
+--impl reference runs that CPU implementation alone (rank 0) on the same
+config and prints its own line.  Multi-GPU (torchrun): replicas -- every rank
+renders its own seeded frame, value = all ranks' particles / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Mparticles/s & frames/s (plain, batched, fwd+bwd) on 1 GB300 at ≤1e-4 rel err"
+CPU_SAMPLE_STRIDE = 5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--workload", default="absorption", choices=["absorption", "additive"])
+    ap.add_argument("--tile", type=int, default=16)
+    ap.add_argument("--order", default="ftb", choices=["ftb", "btf"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="particle-count multiplier (profiling runs use a smaller frame)")
+    return ap.parse_args()
+
+
+def make_workload(args, seed_offset: int = 0):
+    from splotch_gb300 import synth
+
+    s = args.scale
+    if args.workload == "additive":
+        n = int(1_000_000 * s)
+        w = synth.plain_additive(n=n, seed=0 + seed_offset, tile=args.tile)
+        cfg = {"workload": f"plain additive: {n} particles, 800x800, halo mixture [0,100]^3, "
+                           "fov 30", "particles": n, "image": [800, 800]}
+    else:
+        ng, ns = int(40_000_000 * s), int(10_000_000 * s)
+        w = synth.plain_absorption(n_gas=ng, n_star=ns, seed=1 + seed_offset, tile=args.tile,
+                                   order=args.order)
+        cfg = {"workload": f"plain ordered emission-absorption: {ng} gas + {ns} stars, "
+                           "1920x1080, halo mixture [0,500]^3, fov 45, depth sort",
+               "particles": ng + ns, "image": [1920, 1080]}
+    cfg.update({"tile_size": args.tile, "absorption_order": args.order,
+                "l2": "inputs (36 B/particle) larger than the 129 MB L2; no flush"})
+    return w, cfg
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "sm_max_mhz": d.get("sm_max_mhz", 2070.0),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.tmp,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = [r.split(",") for r in Path(self.tmp.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+                for k, nm in enumerate(names):
+                    if r[5 + k].strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(w, steps: int = 2, warmup: int = 1) -> dict:
+    """The oracle's restatement of host_rendering (bit-exact with the
+    reference) on this host's cores, on a 1-in-5 particle subsample."""
+    from oracle.oracle import Port
+
+    port = Port()
+    prm = dict(w.params.params)
+    prm["tile_size_cpu"] = "50"  # the reference's own default tile size
+    sample = np.ascontiguousarray(w.particles[::CPU_SAMPLE_STRIDE])
+    ts = []
+    for i in range(warmup + steps):
+        p = sample.copy()
+        t0 = time.perf_counter()
+        port.host_rendering(prm, w.rc, p)
+        if i >= warmup:
+            ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    return {"value": len(sample) / t / 1e6, "unit": "Mparticles/s", "cores": port.threads,
+            "kind": "port", "seconds_per_frame": t,
+            "sample": f"every {CPU_SAMPLE_STRIDE}th particle ({len(sample)}) of the same frame, "
+                      f"same image and camera, reference default tile_size_cpu=50; median of "
+                      f"{steps} after {warmup} warm-up"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    w, cfg = make_workload(args)
+    from oracle.oracle import Port
+
+    port = Port()
+    prm = dict(w.params.params)
+    prm["tile_size_cpu"] = "50"  # the reference's own default tile size
+    sample = np.ascontiguousarray(w.particles[::CPU_SAMPLE_STRIDE])
+    ts = []
+    for i in range(args.warmup + args.steps):
+        p = sample.copy()
+        t0 = time.perf_counter()
+        port.host_rendering(prm, w.rc, p)
+        if i >= args.warmup:
+            ts.append(time.perf_counter() - t0)
+    t = sum(ts) / len(ts)
+    v = len(sample) / t / 1e6
+    cb = {"value": v, "unit": "Mparticles/s", "cores": port.threads, "kind": "port",
+          "sample": f"every {CPU_SAMPLE_STRIDE}th particle ({len(sample)}) of the frame per "
+                    f"step; the reference itself cannot be compiled on this host, its "
+                    f"bit-exact C restatement (oracle/spl_oracle.c) runs instead"}
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mparticles/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "frames_per_s": 1.0 / t, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "Mparticles/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def roofline(stage_ms: dict, n: int, n_entries: int, frags: int, args, pk: dict,
+             a_eq_e: bool) -> tuple[dict, dict]:
+    """Per-stage rooflines; the top-level one is the dominant stage's."""
+    hbm = pk["hbm_gbs"]
+    fp32_peak = 2 * 128 * 152 * pk["sm_max_mhz"] * 1e6 / 1e12  # TFLOP/s, nominal issue
+    st = {}
+    # project+colourise: read SoA x,y,z,r,I,e(3),type (34 B), write x,y,r,z + rgb,I
+    # (32 B), active (1), tile count (4), sort key (4 when sorting)
+    proj_bytes = n * (34 + 32 + 1 + 4 + (0 if a_eq_e else 4))
+    st["project"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": proj_bytes,
+                     "achieved": proj_bytes / (stage_ms["project_ms"] * 1e-3) / 1e9}
+    if not a_eq_e and stage_ms["sort_ms"] > 0:
+        sort_bytes = n * 16  # read key+index once, write once
+        st["sort"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": sort_bytes,
+                      "achieved": sort_bytes / (stage_ms["sort_ms"] * 1e-3) / 1e9}
+    bin_bytes = n * 12 + n_entries * 4
+    st["bin"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": bin_bytes,
+                 "achieved": bin_bytes / (stage_ms["bin_ms"] * 1e-3) / 1e9}
+    # splat: reference fragments x useful FP32 work per fragment
+    ops = 7 if a_eq_e else 12
+    flops = frags * ops
+    st["splat"] = {"bound": "fp32", "unit": "TFLOP/s", "algorithmic_flops": flops,
+                   "fragments": frags, "ops_per_fragment": ops,
+                   "achieved": flops / (stage_ms["splat_ms"] * 1e-3) / 1e12}
+    for k, v in st.items():
+        v["ms"] = stage_ms[k + "_ms"]
+        v["peak"] = hbm if v["bound"] == "hbm" else fp32_peak
+        v["frac"] = v["achieved"] / v["peak"]
+    dom = max(st, key=lambda k: st[k]["ms"])
+    d = st[dom]
+    top = {"kernel": {"project": "k_project_soa", "sort": "k_rs_downsweep+k_rs_upsweep+scan",
+                      "bin": "k_emit_*+tile sort+k_tile_ranges", "splat": "k_splat"}[dom],
+           "stage": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
+           "unit": d["unit"], "frac": d["frac"], "traffic": None,
+           "peak_source": (pk["source"] if d["bound"] == "hbm"
+                           else "nominal FP32 issue rate at max SM clock")}
+    return top, st
+
+
+def run_gpu(args):
+    import torch
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    import splotch_gb300 as sg
+    from splotch_gb300 import synth
+
+    w, cfg = make_workload(args, seed_offset=rank * 1000)
+    cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
+    n = len(w.particles)
+    r = sg.Renderer(local)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    soa = {k: torch.from_numpy(v).to(f"cuda:{local}") for k, v in synth.soa_from_aos(
+        w.particles).items()}
+    pic = torch.zeros((desc.xres, desc.yres, 3), dtype=torch.float32, device=f"cuda:{local}")
+
+    for _ in range(args.warmup):
+        r.render_soa(desc, soa, pic)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stages = {k: 0.0 for k in ("project_ms", "sort_ms", "bin_ms", "splat_ms")}
+    launches = 0
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        r.render_soa(desc, soa, pic)
+        s = r.stats()
+        for k in stages:
+            stages[k] += s[k]
+        launches += s["kernel_launches"]
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    for k in stages:
+        stages[k] /= args.steps
+    last = r.stats()
+    frags = r.fragments()
+
+    # ---- e2e through the C ABI with host buffers --------------------------------
+    host_aos = torch.empty(n * 36, dtype=torch.uint8, pin_memory=True)
+    host_aos.numpy()[:] = w.particles.view(np.uint8)
+    host_pic = torch.empty((desc.xres, desc.yres, 3), dtype=torch.float32, pin_memory=True)
+    r.set_stream(stream.cuda_stream)
+    r.render_aos(desc, host_aos, host_pic)  # warm the AoS path
+    e2e_t = []
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r.render_aos(desc, host_aos, host_pic)
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    if dist:
+        t = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    pal_bytes = sum(int(desc.pal_n[t]) * 20 for t in range(desc.ptypes))
+    e2e = {"value": world * n / e2e_s / 1e6, "unit": "Mparticles/s",
+           "h2d_bytes_per_step": n * 36 + pal_bytes,
+           "d2h_bytes_per_step": desc.xres * desc.yres * 12 + 12,
+           "ms_per_step": e2e_s * 1e3}
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    pk = peaks()
+    top, st = roofline(stages, n, int(last["n_entries"]), frags, args, pk, bool(desc.a_eq_e))
+    cb = None
+    if world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(w)
+    line = {"metric": METRIC, "value": world * n / (ms * 1e-3) / 1e6, "unit": "Mparticles/s",
+            "frames_per_s": world * 1e3 / ms, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded halo mixture; no snapshot available)", "config": cfg,
+            "e2e": e2e, "gpu_launches": launches, "clocks": clk, "roofline": top,
+            "stages": st, "fragments": frags, "bin_entries": int(last["n_entries"]),
+            "cpu_baseline": cb}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

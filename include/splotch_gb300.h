@@ -141,6 +141,11 @@ spl_status spl_debug_get_bins(spl_context *ctx, int64_t *tile_start_out,
                               int64_t ntiles_plus_one, uint32_t *entries_out,
                               int64_t cap);
 
+/* Exact fragment count of the reference splat loop for the last frame: the
+   number of (pixel, particle) pairs render_new visits (splotch_host.cc:601-622).
+   The algorithmic work behind the splat's roofline figure. */
+spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -278,36 +278,51 @@ void spo_colorize(const spo_params *prm, spo_particle *pp, int64_t n) {
 /* stable sort, splotch/splotch_host.cc:289-321 with the comparators of
    splotch/splotchutils.h:74-96 (stable, i.e. ties keep the original order) */
 
-static int less_by(const spo_particle *p, int st, uint32_t a, uint32_t b) {
-  switch (st) {
-    case 1: return p[a].z < p[b].z;
-    case 2: return p[a].er > p[b].er;
-    case 3: return p[a].er < p[b].er;
-    case 4: return p[a].r > p[b].r;
-  }
-  return 0;
+typedef struct {
+  float key;
+  uint32_t idx;
+} kv;
+
+/* a goes strictly before b under the comparator (ties: not before) */
+static inline int kv_before(const kv *a, const kv *b, int desc) {
+  return desc ? a->key > b->key : a->key < b->key;
 }
 
 int spo_sort_perm(const spo_particle *p, int64_t n, int sort_type, uint32_t *perm) {
   for (int64_t i = 0; i < n; ++i) perm[i] = (uint32_t)i;
   if (sort_type == 0 || n < 2) return 0;
   if (sort_type < 0 || sort_type > 4) return -1;
-  uint32_t *tmp = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
-  if (!tmp) return -2;
-  uint32_t *src = perm, *dst = tmp;
-  for (int64_t w = 1; w < n; w *= 2) { /* bottom-up merge sort (serial) */
+  kv *a = (kv *)malloc((size_t)n * sizeof(kv)), *b = (kv *)malloc((size_t)n * sizeof(kv));
+  if (!a || !b) { free(a); free(b); return -2; }
+  const int desc = sort_type == 2 || sort_type == 4;
+  for (int64_t i = 0; i < n; ++i) {
+    a[i].idx = (uint32_t)i;
+    a[i].key = sort_type == 1 ? p[i].z : (sort_type == 4 ? p[i].r : p[i].er);
+  }
+  /* bottom-up merge sort (serial, stable): runs of 16 by insertion first */
+  for (int64_t lo = 0; lo < n; lo += 16) {
+    int64_t hi = lo + 16 < n ? lo + 16 : n;
+    for (int64_t i = lo + 1; i < hi; ++i) {
+      kv t = a[i];
+      int64_t j = i;
+      while (j > lo && kv_before(&t, &a[j - 1], desc)) { a[j] = a[j - 1]; --j; }
+      a[j] = t;
+    }
+  }
+  kv *src = a, *dst = b;
+  for (int64_t w = 16; w < n; w *= 2) {
     for (int64_t lo = 0; lo < n; lo += 2 * w) {
       int64_t mid = lo + w < n ? lo + w : n, hi = lo + 2 * w < n ? lo + 2 * w : n;
       int64_t i = lo, j = mid, k = lo;
-      while (i < mid && j < hi)
-        dst[k++] = less_by(p, sort_type, src[j], src[i]) ? src[j++] : src[i++];
+      while (i < mid && j < hi) dst[k++] = kv_before(&src[j], &src[i], desc) ? src[j++] : src[i++];
       while (i < mid) dst[k++] = src[i++];
       while (j < hi) dst[k++] = src[j++];
     }
-    uint32_t *s = src; src = dst; dst = s;
+    kv *s = src; src = dst; dst = s;
   }
-  if (src != perm) memcpy(perm, src, (size_t)n * sizeof(uint32_t));
-  free(tmp);
+  for (int64_t i = 0; i < n; ++i) perm[i] = src[i].idx;
+  free(a);
+  free(b);
   return 0;
 }
 

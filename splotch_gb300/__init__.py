@@ -326,6 +326,12 @@ class Renderer:
         _abi.check(self.lib.spl_debug_get_order(self.ctx, out.ctypes.data, n))
         return out
 
+    def fragments(self) -> int:
+        """Exact reference fragment count of the last frame."""
+        v = C.c_int64()
+        _abi.check(self.lib.spl_debug_count_fragments(self.ctx, C.byref(v)))
+        return int(v.value)
+
     def bins(self, ntiles: int) -> tuple[np.ndarray, np.ndarray]:
         ts = np.zeros(ntiles + 1, dtype=np.int64)
         s = self.stats()

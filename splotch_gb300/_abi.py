@@ -25,7 +25,7 @@ EXPORTED = [
     "spl_context_create", "spl_context_destroy", "spl_context_set_stream",
     "spl_last_error_string", "spl_version", "spl_frame_desc_defaults", "spl_camera_setup",
     "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
-    "spl_debug_get_bins",
+    "spl_debug_get_bins", "spl_debug_count_fragments",
 ]
 
 
@@ -106,6 +106,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_debug_get_projected": (C.c_int, [vp, vp, i64]),
         "spl_debug_get_order": (C.c_int, [vp, vp, i64]),
         "spl_debug_get_bins": (C.c_int, [vp, vp, i64, vp, i64]),
+        "spl_debug_count_fragments": (C.c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

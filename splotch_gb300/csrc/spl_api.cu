@@ -31,6 +31,7 @@ struct spl_context {
   int64_t n = 0, ne = 0, ntiles = 0;
   bool has_order = false;
   int last_T = 0;
+  spl::SplatArgs last_splat{};
   spl_stats stats{};
   cudaEvent_t ev[8]{};
 };
@@ -383,6 +384,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   sa.pic = out->memspace == SPL_MEM_DEVICE ? out->pic : as<float>(c->pic);
   launches += spl::launch_splat(sa, s);
   SPL_CK(cudaGetLastError());
+  c->last_splat = sa;
   cudaEventRecord(c->ev[5], s);
 
   // ---- outputs -------------------------------------------------------------------
@@ -449,6 +451,20 @@ spl_status spl_debug_get_projected(spl_context *c, void *aos_out, int64_t n) {
                             tsrc, kind, nullptr, n, c->aos_out.p, c->stream);
   SPL_CK(cudaMemcpyAsync(aos_out, c->aos_out.p, n * 36, cudaMemcpyDeviceToHost, c->stream));
   SPL_CK(cudaStreamSynchronize(c->stream));
+  return SPL_OK;
+}
+
+spl_status spl_debug_count_fragments(spl_context *c, int64_t *frags_out) {
+  if (!c || !frags_out) return fail(SPL_ERR_INVALID, "bad arguments");
+  SPL_CK(cudaSetDevice(c->device));
+  spl_status st;
+  if ((st = ensure(c->small, 256))) return st;
+  unsigned long long *d = reinterpret_cast<unsigned long long *>(as<uint8_t>(c->small) + 64);
+  spl::launch_count_fragments(c->last_splat, d, c->stream);
+  unsigned long long h = 0;
+  SPL_CK(cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, c->stream));
+  SPL_CK(cudaStreamSynchronize(c->stream));
+  *frags_out = (int64_t)h;
   return SPL_OK;
 }
 

@@ -182,5 +182,6 @@ struct SplatArgs {
   float *pic;                  // device, x-major xres*yres*3
 };
 int launch_splat(const SplatArgs &a, cudaStream_t s);
+void launch_count_fragments(const SplatArgs &a, unsigned long long *total, cudaStream_t s);
 
 }  // namespace spl

@@ -233,6 +233,39 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
   }
 }
 
+// Exact fragment count of the reference loop (sum over tile entries of the
+// column runs, splotch_host.cc:601-606): the algorithmic work of the splat.
+__global__ void __launch_bounds__(256) k_count_fragments(SplatArgs a,
+                                                         unsigned long long *total) {
+  const int T = a.T;
+  const int tile = blockIdx.x;
+  const int ix = tile % a.ncx, iy = tile / a.ncx;
+  const int x0s = ix * T, y0s = iy * T;
+  const int tw = min(x0s + T, a.xres) - x0s;
+  const int th = min(y0s + T, a.yres) - y0s;
+  const uint32_t start = a.tile_start[tile], end = a.tile_start[tile + 1];
+  unsigned long long cnt = 0;
+  for (uint32_t jj = start + threadIdx.x; jj < end; jj += blockDim.x) {
+    const float4 p = __ldg(a.pos + __ldg(a.entries + jj));
+    const float rfacr = fmul(p.z, 0.75f);
+    const float posx = fsub(p.x, (float)x0s), posy = fsub(p.y, (float)y0s);
+    const int minx = max(f2i(fadd(fsub(posx, rfacr), 1.f)), 0);
+    const int maxx = min(f2i(fadd(fadd(posx, rfacr), 1.f)), tw);
+    const int miny = max(f2i(fadd(fsub(posy, rfacr), 1.f)), 0);
+    const int maxy = min(f2i(fadd(fadd(posy, rfacr), 1.f)), th);
+    const float radsq = fmul(rfacr, rfacr);
+    for (int x = minx; x < maxx; ++x) {
+      const float dx = fsub((float)x, posx);
+      const float dy = fsqrt(fsub(radsq, fmul(dx, dx)));
+      const int lo = max(miny, f2i(fadd(fsub(posy, dy), 1.f)));
+      const int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
+      if (hi > lo) cnt += (unsigned long long)(hi - lo);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(total, cnt);
+}
+
 template <int K>
 int launch_k(const SplatArgs &a, cudaStream_t s) {
   const int ntiles = a.ncx * a.ncy;
@@ -248,6 +281,11 @@ int launch_k(const SplatArgs &a, cudaStream_t s) {
 }
 
 }  // namespace
+
+void launch_count_fragments(const SplatArgs &a, unsigned long long *total, cudaStream_t s) {
+  cudaMemsetAsync(total, 0, sizeof(unsigned long long), s);
+  if (a.ncx * a.ncy > 0) k_count_fragments<<<a.ncx * a.ncy, 256, 0, s>>>(a, total);
+}
 
 int launch_splat(const SplatArgs &a, cudaStream_t s) {
   const int need = (a.T * a.T + kThreads - 1) / kThreads;  // pixels per lane

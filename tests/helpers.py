@@ -31,8 +31,10 @@ def gpu_frame(renderer: sg.Renderer, params: dict, rc, particles: np.ndarray) ->
     T = desc.tile_size
     ntiles = ((desc.xres + T - 1) // T) * ((desc.yres + T - 1) // T)
     ts, ent = renderer.bins(ntiles)
+    st = renderer.stats()
+    st["fragments"] = renderer.fragments()
     return FrameResult(pic, renderer.projected(len(parts)), renderer.order(len(parts)), ts, ent,
-                       renderer.stats())
+                       st)
 
 
 @dataclass
@@ -73,6 +75,7 @@ def assert_parity(g: FrameResult, o: OracleResult, tol: float = IMAGE_TOL) -> di
     assert np.array_equal(g.order, want_order), "visiting order (sort permutation) differs"
     assert np.array_equal(g.tile_start, o.tile_start), "tile ranges differ"
     assert np.array_equal(g.entries, o.entries), "tile bin entries differ"
+    assert g.stats["fragments"] == o.frags, "fragment count differs from the reference loop"
     err = rel_linf(g.pic, o.pic64)
     ref_err = rel_linf(o.pic32, o.pic64) if o.pic32 is not None else None
     assert err <= tol, f"image rel Linf vs FP64 oracle {err:.3e} > {tol:.0e} (reference FP32: {ref_err})"
