@@ -110,6 +110,8 @@ typedef struct {
   int64_t n_entries;   /* (particle, tile) bin entries */
   int64_t n_tiles;
   int kernel_launches; /* kernels launched by the call */
+  int64_t n_fallback;  /* particles projected through the exact FP64 fallback */
+  int64_t n_wide;      /* particles binned by the wide (many-tile) path */
 } spl_stats;
 
 /* ---- context ---------------------------------------------------------- */
@@ -145,6 +147,12 @@ spl_status spl_debug_get_bins(spl_context *ctx, int64_t *tile_start_out,
    number of (pixel, particle) pairs render_new visits (splotch_host.cc:601-622).
    The algorithmic work behind the splat's roofline figure. */
 spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
+
+/* Debug options for later spl_render calls.  Bit 0: project through the
+   exact FP64 arithmetic only (no float-float fast path); the two must agree
+   bit for bit. */
+#define SPL_DEBUG_EXACT_FP64 1
+spl_status spl_debug_set_options(spl_context *ctx, int flags);
 
 #ifdef __cplusplus
 }

@@ -326,6 +326,10 @@ class Renderer:
         _abi.check(self.lib.spl_debug_get_order(self.ctx, out.ctypes.data, n))
         return out
 
+    def set_debug(self, flags: int) -> None:
+        """spl_debug_set_options: bit 0 forces the exact FP64 projection."""
+        _abi.check(self.lib.spl_debug_set_options(self.ctx, flags))
+
     def fragments(self) -> int:
         """Exact reference fragment count of the last frame."""
         v = C.c_int64()

@@ -25,8 +25,9 @@ EXPORTED = [
     "spl_context_create", "spl_context_destroy", "spl_context_set_stream",
     "spl_last_error_string", "spl_version", "spl_frame_desc_defaults", "spl_camera_setup",
     "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
-    "spl_debug_get_bins", "spl_debug_count_fragments",
+    "spl_debug_get_bins", "spl_debug_count_fragments", "spl_debug_set_options",
 ]
+SPL_DEBUG_EXACT_FP64 = 1
 
 
 class Camera(C.Structure):
@@ -65,7 +66,8 @@ class Stats(C.Structure):
     _fields_ = [("h2d_ms", C.c_float), ("project_ms", C.c_float), ("sort_ms", C.c_float),
                 ("bin_ms", C.c_float), ("splat_ms", C.c_float), ("d2h_ms", C.c_float),
                 ("total_ms", C.c_float), ("n_active", C.c_int64), ("n_entries", C.c_int64),
-                ("n_tiles", C.c_int64), ("kernel_launches", C.c_int)]
+                ("n_tiles", C.c_int64), ("kernel_launches", C.c_int),
+                ("n_fallback", C.c_int64), ("n_wide", C.c_int64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -107,6 +109,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_debug_get_order": (C.c_int, [vp, vp, i64]),
         "spl_debug_get_bins": (C.c_int, [vp, vp, i64, vp, i64]),
         "spl_debug_count_fragments": (C.c_int, [vp, vp]),
+        "spl_debug_set_options": (C.c_int, [vp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "../../include/splotch_gb300.h"
 #include "spl_internal.cuh"
@@ -26,7 +27,8 @@ struct spl_context {
   };
   Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
-      aos_out;
+      aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord;
+  int debug_flags = 0;  // bit 0: exact FP64 projection only
   // state of the last frame (for the debug getters)
   int64_t n = 0, ne = 0, ntiles = 0;
   bool has_order = false;
@@ -115,6 +117,29 @@ spl_status validate(const spl_frame_desc *d, const spl_particles *p, const spl_i
       return fail(SPL_ERR_INVALID, "particles marked device but pointer is not device memory");
   }
   return SPL_OK;
+}
+
+float2 split_ff(double v) {  // v as a float-float pair (hi, lo)
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
+float least_float_above(double v) {  // least float f with f > v
+  float f = (float)v;
+  if ((double)f <= v) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
+float least_float_not_below(double v) {  // least float f with f >= v
+  float f = (float)v;
+  if ((double)f < v) f = std::nextafter(f, INFINITY);
+  return f;
+}
+
+float greatest_float_not_above(double v) {  // greatest float f with f <= v
+  float f = (float)v;
+  if ((double)f > v) f = std::nextafter(f, -INFINITY);
+  return f;
 }
 
 int bits_for(int64_t v) {  // bits needed to represent 0..v-1
@@ -211,6 +236,12 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   pc.xfac = cam.xfac;
   pc.xsum = (double)cam.res2 + cam.xshift;
   pc.ysum = (double)cam.res2 + cam.yshift + (double)cam.ycorr;
+  {
+    const float2 xs = split_ff(pc.xsum), ys = split_ff(pc.ysum);
+    pc.xsum_ff = spl::ff{xs.x, xs.y};
+    pc.ysum_ff = spl::ff{ys.x, ys.y};
+  }
+  pc.exact_fp64 = (c->debug_flags & 1) ? 1 : 0;
   pc.zmin = d->zmin > 0.f ? d->zmin : 0.f;
   pc.zmax = d->zmax;
   pc.minrad2 = d->minrad_pix * d->minrad_pix;
@@ -275,7 +306,37 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   }
   pc.pal_x = as<double>(c->pal_x);
   pc.pal_rgb = as<float>(c->pal_rgb);
-  SPL_CK(cudaMemsetAsync(d_err, 0, 8, s));
+  // float-float palette tables for the fast colourisation path
+  {
+    std::vector<float> thr(npal + 1);
+    std::vector<float2> xff(npal + 1), invff(npal + 1);
+    for (int t = 0; t < d->ptypes; ++t) {
+      const int nk = pc.pal_n[t], o = pc.pal_off[t];
+      if (!nk) continue;
+      const double *x = d->pal_x[t];
+      for (int k = 0; k < nk; ++k) {
+        thr[o + k] = least_float_above(x[k]);
+        xff[o + k] = split_ff(x[k]);
+        invff[o + k] = k + 1 < nk ? split_ff(1.0 / (x[k + 1] - x[k])) : make_float2(0.f, 0.f);
+      }
+      pc.pal_lo_f[t] = greatest_float_not_above(x[0]);
+      pc.pal_hi_f[t] = least_float_not_below(x[nk - 1]);
+    }
+    if ((st = ensure(c->pal_thr, (npal + 1) * 4)) || (st = ensure(c->pal_xff, (npal + 1) * 8)) ||
+        (st = ensure(c->pal_invff, (npal + 1) * 8)))
+      return st;
+    SPL_CK(cudaMemcpyAsync(c->pal_thr.p, thr.data(), (npal + 1) * 4, cudaMemcpyHostToDevice, s));
+    SPL_CK(cudaMemcpyAsync(c->pal_xff.p, xff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+    SPL_CK(cudaMemcpyAsync(c->pal_invff.p, invff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice,
+                           s));
+    // the host vectors die at scope end: wait for the copies
+    SPL_CK(cudaStreamSynchronize(s));
+    pc.pal_thr = as<float>(c->pal_thr);
+    pc.pal_xff = as<float2>(c->pal_xff);
+    pc.pal_invff = as<float2>(c->pal_invff);
+  }
+  SPL_CK(cudaMemsetAsync(d_err, 0, 12, s));
+  pc.n_fallback = d_err + 2;
 
   cudaEventRecord(c->ev[0], s);
   // ---- inputs --------------------------------------------------------------
@@ -332,8 +393,15 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   cudaEventRecord(c->ev[3], s);
 
   // ---- binning ---------------------------------------------------------------
+  // tile counts in visiting order (one gather; the sort's key scratch is free)
+  const uint32_t *count_seq = as<uint32_t>(c->count);
+  if (order) {
+    spl::launch_gather_u32(as<uint32_t>(c->count), order, n, as<uint32_t>(c->ktmp), s);
+    ++launches;
+    count_seq = as<uint32_t>(c->ktmp);
+  }
   uint64_t *off = as<uint64_t>(c->off);
-  spl::scan_counts(as<uint32_t>(c->count), order, n, off, c->scratch.p, s, &launches);
+  spl::scan_counts(count_seq, nullptr, n, off, c->scratch.p, s, &launches);
   uint64_t ne = 0;
   SPL_CK(cudaMemcpyAsync(&ne, off + n, 8, cudaMemcpyDeviceToHost, s));
   SPL_CK(cudaStreamSynchronize(s));
@@ -345,7 +413,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   size_t rs2 = spl::radix_scratch_bytes((int64_t)ne);
   if ((st = ensure(c->scratch, rs2))) return st;
   if (ne > 0) {
-    spl::launch_emit(as<float4>(c->pos), as<uint32_t>(c->count), order, off, n, g,
+    spl::launch_emit(as<float4>(c->pos), count_seq, order, off, n, g,
                      as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->wide_list),
                      d_wide_n, s);
     launches += 2;
@@ -363,6 +431,16 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   spl::launch_tile_ranges(as<uint32_t>(c->tkey_s), (int64_t)ne, ntiles,
                           as<uint32_t>(c->tile_start), s);
   ++launches;
+  // longest lists first: the splat's tail is set by its heaviest tiles
+  if ((st = ensure(c->tcost, ntiles * 4)) || (st = ensure(c->tcost_s, ntiles * 4)) ||
+      (st = ensure(c->tord, ntiles * 4)) ||
+      (st = ensure(c->scratch, spl::radix_scratch_bytes(ntiles))))
+    return st;
+  spl::launch_tile_cost(as<uint32_t>(c->tile_start), ntiles, as<uint32_t>(c->tcost), s);
+  spl::radix_sort_pairs(as<uint32_t>(c->tcost), nullptr, as<uint32_t>(c->tcost_s),
+                        as<uint32_t>(c->tord), as<uint32_t>(c->tcost_s), as<uint32_t>(c->tord),
+                        ntiles, 0, 8, false, c->scratch.p, s, &launches);
+  ++launches;
   cudaEventRecord(c->ev[4], s);
 
   // ---- splat ---------------------------------------------------------------------
@@ -371,6 +449,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   sa.col = as<float4>(c->col);
   sa.entries = as<uint32_t>(c->tval_s);
   sa.tile_start = as<uint32_t>(c->tile_start);
+  sa.tile_order = as<uint32_t>(c->tord);
   sa.T = T;
   sa.ncx = g.ncx;
   sa.ncy = g.ncy;
@@ -412,11 +491,14 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     ++launches;
   }
   cudaEventRecord(c->ev[6], s);
-  uint32_t err = 0;
-  SPL_CK(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s));
+  uint32_t words[3] = {0, 0, 0};  // error word, wide-particle count, FP64 fallbacks
+  SPL_CK(cudaMemcpyAsync(words, d_err, 12, cudaMemcpyDeviceToHost, s));
   SPL_CK(cudaStreamSynchronize(s));
   SPL_CK(cudaGetLastError());
+  const uint32_t err = words[0];
   if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
+  c->stats.n_fallback = words[2];
+  c->stats.n_wide = words[1];
 
   c->n = n;
   c->ne = (int64_t)ne;
@@ -451,6 +533,12 @@ spl_status spl_debug_get_projected(spl_context *c, void *aos_out, int64_t n) {
                             tsrc, kind, nullptr, n, c->aos_out.p, c->stream);
   SPL_CK(cudaMemcpyAsync(aos_out, c->aos_out.p, n * 36, cudaMemcpyDeviceToHost, c->stream));
   SPL_CK(cudaStreamSynchronize(c->stream));
+  return SPL_OK;
+}
+
+spl_status spl_debug_set_options(spl_context *c, int flags) {
+  if (!c) return fail(SPL_ERR_INVALID, "null ctx");
+  c->debug_flags = flags;
   return SPL_OK;
 }
 

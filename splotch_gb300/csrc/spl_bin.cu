@@ -32,9 +32,9 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
                                                      uint32_t *__restrict__ wide_n) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
        s += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
-    const uint32_t c = __ldg(count + i);
+    const uint32_t c = __ldg(count + s);  // counts are in visiting order
     if (c == 0) continue;
+    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
     if (c > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
       wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
       continue;
@@ -129,6 +129,18 @@ __global__ void __launch_bounds__(256) k_tile_ranges(const uint32_t *__restrict_
   }
 }
 
+// Scheduling key per tile: 8-bit log-scale of the list length, inverted so an
+// ascending sort puts the longest lists first (longest-processing-time order).
+__global__ void __launch_bounds__(256) k_tile_cost(const uint32_t *__restrict__ tile_start,
+                                                   int64_t ntiles, uint32_t *__restrict__ key) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t cnt = tile_start[t + 1] - tile_start[t];
+    const int lg = (int)(8.f * __log2f((float)cnt + 1.f));
+    key[t] = 255u - (uint32_t)min(lg, 255);
+  }
+}
+
 int grid_for(int64_t n, int per_block) {
   int64_t b = (n + per_block - 1) / per_block;
   const int64_t cap = 152LL * 16;
@@ -151,6 +163,24 @@ void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order
 void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
                         uint32_t *tile_start, cudaStream_t s) {
   k_tile_ranges<<<grid_for(ne + 1, 256), 256, 0, s>>>(sorted_tkey, ne, ntiles, tile_start);
+}
+
+__global__ void __launch_bounds__(256) k_gather_u32(const uint32_t *__restrict__ src,
+                                                    const uint32_t *__restrict__ perm,
+                                                    int64_t n, uint32_t *__restrict__ out) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x)
+    out[s] = __ldg(src + __ldg(perm + s));
+}
+
+void launch_gather_u32(const uint32_t *src, const uint32_t *perm, int64_t n, uint32_t *out,
+                       cudaStream_t s) {
+  if (n > 0) k_gather_u32<<<grid_for(n, 256), 256, 0, s>>>(src, perm, n, out);
+}
+
+void launch_tile_cost(const uint32_t *tile_start, int64_t ntiles, uint32_t *key,
+                      cudaStream_t s) {
+  if (ntiles > 0) k_tile_cost<<<grid_for(ntiles, 256), 256, 0, s>>>(tile_start, ntiles, key);
 }
 
 }  // namespace spl

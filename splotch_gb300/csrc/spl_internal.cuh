@@ -36,21 +36,68 @@ __device__ __forceinline__ float ex2(float x) {
 
 constexpr float kLog2e = 1.4426950408889634f;
 
-// expm1(x) for x <= 0 in float with ~1e-7 relative error everywhere:
-// Taylor series (degree 7, Horner form) near zero where exp(x)-1 cancels,
-// ex2-based exp(x)-1 elsewhere.
+// expm1(x) for x <= 0 in float, branch-free: the Taylor polynomial of degree
+// 4 for -0.05 < x (truncation below 5e-8 relative) where exp(x)-1 would
+// cancel, and ex2(x*log2e)-1 elsewhere (relative error below 4e-6 there,
+// from the ~2^-22.5 error of ex2.approx).
 __device__ __forceinline__ float expm1_neg(float x) {
-  if (x > -0.25f) {
-    float p = 1.f / 5040.f;
-    p = fmaf(p, x, 1.f / 720.f);
-    p = fmaf(p, x, 1.f / 120.f);
-    p = fmaf(p, x, 1.f / 24.f);
-    p = fmaf(p, x, 1.f / 6.f);
-    p = fmaf(p, x, 0.5f);
-    p = fmaf(p, x, 1.f);
-    return p * x;
-  }
-  return ex2(x * kLog2e) - 1.f;
+  float p = fmaf(x, 1.f / 24.f, 1.f / 6.f);
+  p = fmaf(p, x, 0.5f);
+  p = fmaf(p, x, 1.f);
+  p *= x;
+  const float e = ex2(x * kLog2e) - 1.f;
+  return x > -0.05f ? p : e;
+}
+
+// ---------------------------------------------------------------------------
+// Float-float ("double-float") arithmetic for reproducing double results.
+// GB300's FP64 rate is a small fraction of its FP32 rate, so the reference's
+// double-precision steps (transform, screen shift, palette interpolation) are
+// evaluated in float-float with a rigorous error bound; when the bound cannot
+// decide the final float rounding, the caller redoes the particle in FP64.
+// Algorithms: TwoSum / Fast2Sum (Knuth, Dekker), TwoProd via FMA, and
+// AccurateDWPlusDW (Joldes, Muller, Popescu, ACM TOMS 2017, relative error
+// <= 3u^2 with u = 2^-24).
+struct ff {
+  float h, l;
+};
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  const float p = __fmul_rn(a, b);
+  return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  const ff s = two_sum(a.h, b.h);
+  const ff t = two_sum(a.l, b.l);
+  const ff v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+  return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
+}
+// (a.h + a.l) * (b.h + b.l), relative error about 2^-45
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  ff p = two_prod(a.h, b.h);
+  const float c = __fmaf_rn(a.h, b.l, __fmul_rn(a.l, b.h));
+  return fast_two_sum(p.h, __fadd_rn(p.l, c));
+}
+
+// True when every real number within `delta` of v.h + v.l rounds to v.h in
+// float round-to-nearest-even, i.e. the float result is decided.
+__device__ __forceinline__ bool rn24_decided(ff v, float delta) {
+  const uint32_t b = __float_as_uint(v.h) & 0x7fffffffu;
+  const uint32_t E = b >> 23;
+  if (E < 30u || E > 250u) return false;  // tiny, huge, inf or nan: no fast verdict
+  const float ulp = __uint_as_float((E - 23u) << 23);
+  const bool toward_zero = v.l != 0.f && ((__float_as_uint(v.l) ^ __float_as_uint(v.h)) >> 31);
+  const float half = (toward_zero && (b & 0x7fffffu) == 0) ? 0.25f * ulp : 0.5f * ulp;
+  return fabsf(v.l) + delta < half;
 }
 
 // Canonical radix keys: ascending unsigned order == ascending float order,
@@ -69,6 +116,16 @@ struct ProjConst {
   float res2, ycorr, fovfct, xfac;
   double xsum;  // (double)res2 + xshift                (splotch_host.cc:134)
   double ysum;  // ((double)res2 + yshift) + ycorr       (splotch_host.cc:135)
+  ff xsum_ff, ysum_ff;  // the same as float-float pairs
+  int exact_fp64;       // 1: skip the float-float fast path (test hook)
+  uint32_t *n_fallback; // particles that took the FP64 path (may be null)
+  // palette acceleration, per knot k: thr_gt[k] = least float > x[k];
+  // x_ff[k] = x[k] as float-float; per segment k: inv_ff[k] = 1/(x[k+1]-x[k]);
+  // per palette: lo_f = largest float <= x[0], hi_f = least float >= x[n-1]
+  const float *pal_thr;
+  const float2 *pal_xff;
+  const float2 *pal_invff;
+  float pal_lo_f[SPL_MAXT], pal_hi_f[SPL_MAXT];
   float zmin, zmax, minrad2, half_bfak;
   int xres, yres, projection, ptypes;
   float smooth[SPL_MAXT];
@@ -159,13 +216,21 @@ void scan_counts(const uint32_t *count, const uint32_t *order, int64_t n, uint64
                  void *scratch, cudaStream_t s, int *launches);
 
 // Bin emission and tile ranges.
-// wide_list must hold n entries, wide_n one counter (particles with more than
-// 64 tiles go to the warp-per-particle emitter through this list).
+// count[s] is the tile count of the s-th particle in visiting order (order[s]
+// its index; order null = identity).  wide_list must hold n entries, wide_n
+// one counter (particles with more than 64 tiles go to the warp-per-particle
+// emitter through this list).
+void launch_gather_u32(const uint32_t *src, const uint32_t *perm, int64_t n, uint32_t *out,
+                       cudaStream_t s);
 void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order,
                  const uint64_t *off, int64_t n, Tiling g, uint32_t *tkey, uint32_t *tval,
                  uint32_t *wide_list, uint32_t *wide_n, cudaStream_t s);
 void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
                         uint32_t *tile_start, cudaStream_t s);
+// 8-bit longest-first scheduling key per tile (sort ascending with
+// radix_sort_pairs over bits [0,8) to get the launch order).
+void launch_tile_cost(const uint32_t *tile_start, int64_t ntiles, uint32_t *key,
+                      cudaStream_t s);
 
 // Splat.
 struct SplatArgs {
@@ -173,6 +238,7 @@ struct SplatArgs {
   const float4 *col;
   const uint32_t *entries;     // particle index per bin entry, tile-major
   const uint32_t *tile_start;  // ntiles+1
+  const uint32_t *tile_order;  // launch order of the tiles (null: row order)
   int T, ncx, ncy, xres, yres;
   float gray;
   float h2sigma;

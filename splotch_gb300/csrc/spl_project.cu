@@ -20,6 +20,99 @@ struct PIn {
   int type;
 };
 
+// ---- exact FP64 forms (the reference's arithmetic; fallback and test path) ----
+
+// TRANSFORM::TransPoint (kernel/transform.cxx:212-219) in double.
+__device__ __forceinline__ float transpoint_fp64(const float *m, float x, float y, float z) {
+  const double vx = x, vy = y, vz = z;
+  return __double2float_rn(
+      dadd(dadd(dadd(dmul(vx, m[0]), dmul(vy, m[1])), dmul(vz, m[2])), (double)m[3]));
+}
+
+// ---- float-float fast forms ----------------------------------------------------
+
+// One row of the transform; false when the float rounding is undecided.
+__device__ __forceinline__ bool transpoint_fast(const float *m, float x, float y, float z,
+                                                float &out) {
+  const ff s1 = ff_add(two_prod(x, m[0]), two_prod(y, m[1]));
+  const ff s2 = ff_add(s1, two_prod(z, m[2]));
+  const ff s3 = ff_add(s2, ff{m[3], 0.f});
+  // reference rounding (2^-53 per double add) + float-float error (3*2^-48
+  // per add), with a factor-4 margin
+  const float delta = 0x1p-44f * (fabsf(s1.h) + fabsf(s2.h) + fabsf(s3.h));
+  out = s3.h;
+  return rn24_decided(s3, delta);
+}
+
+// (float)(A + (double)p) for a double A given as float-float.
+__device__ __forceinline__ bool shift_fast(ff A, float p, float &out) {
+  const ff s = ff_add(A, ff{p, 0.f});
+  const float delta = 0x1p-44f * (fabsf(A.h) + fabsf(s.h));
+  out = s.h;
+  return s.h != 0.f && rn24_decided(s, delta);
+}
+
+// One channel of (1-frac)*y0 + frac*y1 with the reference's roundings:
+// RN24(RN53(y0*RN53(1-frac))) + RN24(RN53(y1*frac)) in float.
+__device__ __forceinline__ bool lerp_channel_fast(float y0, float y1, ff omf, ff frac,
+                                                  float efrac, float &out) {
+  float p0 = 0.f, p1 = 0.f;
+  if (y0 != 0.f) {
+    const ff P = ff_mul(ff{y0, 0.f}, omf);
+    if (!rn24_decided(P, fabsf(y0) * efrac + 0x1p-42f * fabsf(P.h))) return false;
+    p0 = P.h;
+  }
+  if (y1 != 0.f) {
+    const ff P = ff_mul(ff{y1, 0.f}, frac);
+    if (!rn24_decided(P, fabsf(y1) * efrac + 0x1p-42f * fabsf(P.h))) return false;
+    p1 = P.h;
+  }
+  out = fadd(p0, p1);
+  return true;
+}
+
+// linearMap<COLOUR>::getVal_const (cxxsupport/linear_map.h:71-84) with
+// interpol_helper (cxxsupport/math_utils.h:186-196), float-float form.
+// Knot comparisons use precomputed float thresholds, which is exact for a
+// float argument; the interpolation is decided or reported undecided.
+__device__ __forceinline__ bool palette_fast(const ProjConst &c, int t, float v, float &r,
+                                             float &g, float &b) {
+  const int n = c.pal_n[t];
+  const int off = c.pal_off[t];
+  const float *rgb = c.pal_rgb + 3 * off;
+  int idx;
+  if (n == 1 || v <= c.pal_lo_f[t]) {
+    idx = 0;
+  } else if (v >= c.pal_hi_f[t]) {
+    idx = n - 1;
+  } else {
+    const float *thr = c.pal_thr + off;
+    int lo = 0, hi = n;
+    while (lo < hi) {  // lower_bound: first knot with !(x[k] < v)
+      const int mid = (lo + hi) >> 1;
+      if (v >= __ldg(thr + mid)) lo = mid + 1; else hi = mid;
+    }
+    idx = lo > 0 ? lo - 1 : 0;
+    if (idx > n - 2) idx = n - 2;
+    const float2 xk = __ldg(c.pal_xff + off + idx);
+    const float2 ik = __ldg(c.pal_invff + off + idx);
+    const ff num = ff_add(ff{v, 0.f}, ff{-xk.x, -xk.y});
+    const ff frac = ff_mul(num, ff{ik.x, ik.y});
+    const ff omf = ff_add(ff{1.f, 0.f}, ff{-frac.h, -frac.l});
+    // |frac - reference frac|: float-float and double roundings of the
+    // quotient plus the float-float representation error of x[k]
+    const float efrac = 0x1p-43f * fabsf(frac.h) + 0x1p-46f * fabsf(xk.x) * fabsf(ik.x);
+    const float *y0 = rgb + 3 * idx;
+    return lerp_channel_fast(__ldg(y0), __ldg(y0 + 3), omf, frac, efrac, r) &&
+           lerp_channel_fast(__ldg(y0 + 1), __ldg(y0 + 4), omf, frac, efrac, g) &&
+           lerp_channel_fast(__ldg(y0 + 2), __ldg(y0 + 5), omf, frac, efrac, b);
+  }
+  r = __ldg(rgb + 3 * idx);
+  g = __ldg(rgb + 3 * idx + 1);
+  b = __ldg(rgb + 3 * idx + 2);
+  return true;
+}
+
 // linearMap<COLOUR>::getVal_const (cxxsupport/linear_map.h:71-84) with
 // interpol_helper (cxxsupport/math_utils.h:186-196), in double like the
 // reference.
@@ -60,12 +153,18 @@ __device__ __forceinline__ void palette(const ProjConst &c, int t, float v, floa
 __device__ __forceinline__ void project_one(const ProjConst &c, const PIn &in, int64_t i,
                                             const ProjectOut &o) {
   const float *m = c.mat;
-  const double vx = in.x, vy = in.y, vz = in.z;
-  // TRANSFORM::TransPoint (kernel/transform.cxx:212-219)
-  double tx = dadd(dadd(dadd(dmul(vx, m[0]), dmul(vy, m[1])), dmul(vz, m[2])), (double)m[3]);
-  double ty = dadd(dadd(dadd(dmul(vx, m[4]), dmul(vy, m[5])), dmul(vz, m[6])), (double)m[7]);
-  double tz = dadd(dadd(dadd(dmul(vx, m[8]), dmul(vy, m[9])), dmul(vz, m[10])), (double)m[11]);
-  float x = __double2float_rn(tx), y = __double2float_rn(ty), z = __double2float_rn(tz);
+  const bool fast = !c.exact_fp64;
+  bool fell_back = false;
+  // TRANSFORM::TransPoint (kernel/transform.cxx:212-219), double in the reference
+  float x, y, z;
+  if (!(fast && transpoint_fast(m, in.x, in.y, in.z, x) &&
+        transpoint_fast(m + 4, in.x, in.y, in.z, y) &&
+        transpoint_fast(m + 8, in.x, in.y, in.z, z))) {
+    fell_back = fast;
+    x = transpoint_fp64(m, in.x, in.y, in.z);
+    y = transpoint_fp64(m + 4, in.x, in.y, in.z);
+    z = transpoint_fp64(m + 8, in.x, in.y, in.z);
+  }
   float r = in.r, I = in.I;
   float er = in.er, eg = in.eg, eb = in.eb;
   bool active = false;
@@ -79,8 +178,13 @@ __device__ __forceinline__ void project_one(const ProjConst &c, const PIn &in, i
       y = fadd(fadd(c.res2, c.ycorr), fmul(y, xfac2));
     } else {
       xfac2 = fdiv(-c.res2, fmul(c.fovfct, z));
-      x = __double2float_rn(dadd(c.xsum, (double)fmul(x, xfac2)));
-      y = __double2float_rn(dadd(c.ysum, (double)fmul(y, xfac2)));
+      const float px = fmul(x, xfac2), py = fmul(y, xfac2);
+      // res2 + xshift + x*xfac2 in double, stored to float (splotch_host.cc:134-135)
+      if (!(fast && shift_fast(c.xsum_ff, px, x) && shift_fast(c.ysum_ff, py, y))) {
+        fell_back = fell_back || fast;
+        x = __double2float_rn(dadd(c.xsum, (double)px));
+        y = __double2float_rn(dadd(c.ysum, (double)py));
+      }
     }
     I = fmul(I, fdiv(c.half_bfak, r));
     r = fmul(r, 2.f);
@@ -96,12 +200,27 @@ __device__ __forceinline__ void project_one(const ProjConst &c, const PIn &in, i
     active = !(minx >= c.xres) && !(maxx <= 0) && max(minx, 0) < min(maxx, c.xres) &&
              !(miny >= c.yres) && !(maxy <= 0) && max(miny, 0) < min(maxy, c.yres);
     if (active) {  // particle_colorize (splotch_host.cc:276-282)
-      if (!c.colvec[t]) palette(c, t, er, er, eg, eb);
+      if (!c.colvec[t]) {
+        float pr, pg, pb;
+        if (fast && palette_fast(c, t, er, pr, pg, pb)) {
+          er = pr;
+          eg = pg;
+          eb = pb;
+        } else {
+          fell_back = fell_back || fast;
+          palette(c, t, er, er, eg, eb);
+        }
+      }
       const float fac = fmul(I, c.bright[t]);
       er = fmul(er, fac);
       eg = fmul(eg, fac);
       eb = fmul(eb, fac);
     }
+  }
+  if (c.n_fallback) {
+    const uint32_t am = __activemask();
+    const uint32_t fb = __ballot_sync(am, fell_back);
+    if (fb && (int)(threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(c.n_fallback, __popc(fb));
   }
   o.pos[i] = make_float4(x, y, r, z);
   o.col[i] = make_float4(er, eg, eb, I);

@@ -60,6 +60,10 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
     int nbits, const uint32_t *__restrict__ offsets, int nblocks) {
   __shared__ uint32_t whist[RS_WARPS][RS_BINS];
   __shared__ uint32_t boff[RS_BINS];
+  __shared__ uint32_t lstart[RS_BINS];
+  __shared__ uint32_t wtot[RS_WARPS];
+  __shared__ uint32_t skey[RS_TILE];
+  __shared__ uint32_t sval[RS_TILE];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&whist[0][0])[i] = 0;
   boff[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
@@ -83,7 +87,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
     rank[j] = prior + __popc(peers & lanemask_lt());
   }
   __syncthreads();
-  {  // exclusive prefix over warps for each digit
+  {  // per digit: exclusive prefix over warps, then over digits (block-local)
     const int d = threadIdx.x;
     uint32_t run = 0;
 #pragma unroll
@@ -92,17 +96,40 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
       whist[ww][d] = run;
       run += t;
     }
+    // exclusive scan of the block's digit totals across the 256 threads
+    uint32_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) wtot[w] = inc;
+    __syncthreads();
+    uint32_t wpre = 0;
+    for (int ww = 0; ww < w; ++ww) wpre += wtot[ww];
+    lstart[d] = wpre + inc - run;
   }
   __syncthreads();
+  // stable local sort into shared memory ...
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; ++j) {
     const int64_t idx = base + j * 32 + lane;
     if (idx < n) {
       const uint32_t d = (key[j] >> shift) & mask;
-      const uint32_t dst = boff[d] + whist[w][d] + rank[j];
-      if (keys_out) keys_out[dst] = key[j];
-      vals_out[dst] = val[j];
+      const uint32_t lpos = lstart[d] + whist[w][d] + rank[j];
+      skey[lpos] = key[j];
+      sval[lpos] = val[j];
     }
+  }
+  __syncthreads();
+  // ... then consecutive threads write consecutive slots of each digit run
+  const int nloc = (int)min((int64_t)RS_TILE, n - (int64_t)blockIdx.x * RS_TILE);
+  for (int i = threadIdx.x; i < nloc; i += RS_THREADS) {
+    const uint32_t k = skey[i];
+    const uint32_t d = (k >> shift) & mask;
+    const uint32_t dst = boff[d] + (uint32_t)i - lstart[d];
+    if (keys_out) keys_out[dst] = k;
+    vals_out[dst] = sval[i];
   }
 }
 

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const SmemLayout L = smem_layout(smem_raw);
   const int T = a.T;
-  const int tile = blockIdx.x;
+  const int tile = a.tile_order ? (int)__ldg(a.tile_order + blockIdx.x) : (int)blockIdx.x;
   const int ix = tile % a.ncx, iy = tile / a.ncx;
   const int x0s = ix * T, y0s = iy * T;
   const int tw = min(x0s + T, a.xres) - x0s;
@@ -75,6 +75,7 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
   const int wc1 = warp_has_pixels ? (min(wbase + 32 * K, P) - 1) / th : -1;
 
   int pxy[K];
+  float pxf[K], pyf[K];  // tile-local pixel coordinates as floats
   int ic0[K], ic1[K];
   float acc[K][3];
   float tr[K][3];
@@ -83,6 +84,8 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
     const int p0 = wbase + k * 32;
     const int p = p0 + lane;
     pxy[k] = p < P ? (((p / th) << 8) | (p % th)) : -1;
+    pxf[k] = (float)(pxy[k] >> 8);
+    pyf[k] = (float)(pxy[k] & 255);
     ic0[k] = p0 < P ? p0 / th : 1 << 20;
     ic1[k] = p0 < P ? (min(p0 + 31, P - 1)) / th : -1;
 #pragma unroll
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
                 in = y >= (int)(rr & 255) && y < (int)(rr >> 8);
               }
               if (in) {
-                const float dx = (float)x - posx, dy = (float)y - posy;
+                const float dx = pxf[k] - posx, dy = pyf[k] - posy;
                 const float s2 = fmaf(dy, dy, dx * dx);
                 const float att = ex2(stp2 * s2);
                 if (ADD) {

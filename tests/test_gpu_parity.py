@@ -167,6 +167,35 @@ def test_determinism(renderer):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("camera", ["outside", "inside_cluster"])
+def test_fast_projection_equals_fp64(camera, renderer):
+    """The float-float projection (with per-particle FP64 fallback) is bit-identical
+    to the exact FP64 arithmetic over millions of particles."""
+    w = synth.plain_absorption(n_gas=1_600_000, n_star=400_000, xres=640, yres=360, tile=16)
+    if camera == "inside_cluster":  # many particles near the camera axis and plane
+        p = w.particles
+        c = np.array([p["x"][0], p["y"][0], p["z"][0]], dtype=np.float64)
+        w.rc.campos = c + np.array([0.3, -0.2, -2.0])
+        w.rc.centerpos = w.rc.campos.copy()
+        w.rc.lookat = c + np.array([1.0, 0.5, 40.0])
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    pic = np.zeros((640, 360, 3), np.float32)
+    out = {}
+    for flags in (0, 1):
+        renderer.set_debug(flags)
+        try:
+            renderer.render_aos(desc, w.particles.copy(), pic)
+        finally:
+            renderer.set_debug(0)
+        out[flags] = (renderer.projected(len(w.particles)), renderer.stats()["n_fallback"])
+    a, b = out[0][0].view(np.uint8), out[1][0].view(np.uint8)
+    assert np.array_equal(a, b)
+    assert out[1][1] == 0
+    assert out[0][1] < 0.01 * len(w.particles), f"{out[0][1]} FP64 fallbacks"
+    print(camera, "fallbacks", out[0][1], "of", len(w.particles))
+
+
 def test_full_size_additive_1M(renderer, port):
     """The plain additive workload at full size (1M particles, 800x800)."""
     w = synth.plain_additive()
