@@ -34,8 +34,20 @@ __device__ __forceinline__ float transpoint_fp64(const float *m, float x, float 
 // One row of the transform; false when the float rounding is undecided.
 __device__ __forceinline__ bool transpoint_fast(const float *m, float x, float y, float z,
                                                 float &out) {
-  const ff s1 = ff_add(two_prod(x, m[0]), two_prod(y, m[1]));
-  const ff s2 = ff_add(s1, two_prod(z, m[2]));
+  const ff a = two_prod(x, m[0]), b = two_prod(y, m[1]), c = two_prod(z, m[2]);
+  if (a.l == 0.f && b.l == 0.f && c.l == 0.f) {
+    // Products and the first two partial sums exact in float (axis-aligned
+    // cameras): the double sum is then exactly representable up to the last
+    // add, whose single rounding to float -- ties included -- is one float add.
+    const ff t1 = two_sum(a.h, b.h);
+    const ff t2 = two_sum(t1.h, c.h);
+    if (t1.l == 0.f && t2.l == 0.f) {
+      out = fadd(t2.h, m[3]);
+      return true;
+    }
+  }
+  const ff s1 = ff_add(a, b);
+  const ff s2 = ff_add(s1, c);
   const ff s3 = ff_add(s2, ff{m[3], 0.f});
   // reference rounding (2^-53 per double add) + float-float error (3*2^-48
   // per add), with a factor-4 margin
@@ -46,6 +58,12 @@ __device__ __forceinline__ bool transpoint_fast(const float *m, float x, float y
 
 // (float)(A + (double)p) for a double A given as float-float.
 __device__ __forceinline__ bool shift_fast(ff A, float p, float &out) {
+  if (A.l == 0.f) {
+    // A is a float: A + p is exact in double unless p is far below A's last
+    // bit, where it cannot move the float rounding; one float add is exact.
+    out = fadd(A.h, p);
+    return true;
+  }
   const ff s = ff_add(A, ff{p, 0.f});
   const float delta = 0x1p-44f * (fabsf(A.h) + fabsf(s.h));
   out = s.h;

@@ -36,22 +36,33 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t *__res
                                                            int64_t n, int shift, int nbits,
                                                            uint32_t *__restrict__ counts,
                                                            int nblocks) {
-  __shared__ uint32_t hist[RS_BINS];
-  hist[threadIdx.x] = 0;
+  __shared__ uint32_t whist[RS_WARPS][RS_BINS];  // per-warp privatised histograms
+  for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&whist[0][0])[i] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t mask = (1u << nbits) - 1u;
   const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * 32 * RS_ITEMS;
-#pragma unroll 4
-  for (int j = 0; j < RS_ITEMS; ++j) {
-    const int64_t idx = base + j * 32 + lane;
-    const bool valid = idx < n;
-    const uint32_t d = valid ? (__ldg(keys + idx) >> shift) & mask : RS_BINS + lane;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    if (valid && (__ffs(peers) - 1) == lane) atomicAdd(&hist[d], __popc(peers));
+  if (base + 32 * RS_ITEMS <= n) {
+    const uint4 *k4 = reinterpret_cast<const uint4 *>(keys + base);
+#pragma unroll
+    for (int j = 0; j < RS_ITEMS / 4; ++j) {
+      const uint4 v = __ldg(k4 + j * 32 + lane);
+      atomicAdd(&whist[w][(v.x >> shift) & mask], 1u);
+      atomicAdd(&whist[w][(v.y >> shift) & mask], 1u);
+      atomicAdd(&whist[w][(v.z >> shift) & mask], 1u);
+      atomicAdd(&whist[w][(v.w >> shift) & mask], 1u);
+    }
+  } else {
+    for (int j = 0; j < RS_ITEMS; ++j) {
+      const int64_t idx = base + j * 32 + lane;
+      if (idx < n) atomicAdd(&whist[w][(__ldg(keys + idx) >> shift) & mask], 1u);
+    }
   }
   __syncthreads();
-  counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = hist[threadIdx.x];
+  uint32_t tot = 0;
+#pragma unroll
+  for (int ww = 0; ww < RS_WARPS; ++ww) tot += whist[ww][threadIdx.x];
+  counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = tot;
 }
 
 __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
