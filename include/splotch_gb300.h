@@ -85,6 +85,8 @@ typedef struct {
   /* GPU-only knobs (no reference counterpart) */
   int order_mode;           /* SPL_ORDER_* (default BACK_TO_FRONT) */
   float ftb_epsilon;        /* transmittance cut for FRONT_TO_BACK (1e-9) */
+  int splat_config;         /* splat launch configuration, -1 = default for the
+                               tile size (see spl_splat_config_valid) */
 } spl_frame_desc;
 
 /* Particle input.  AoS: aos points at n particle_sim records.  SoA: x..I,
@@ -127,6 +129,12 @@ void spl_frame_desc_defaults(spl_frame_desc *d);
 /* The camera set-up of particle_project (splotch/splotch_host.cc:62-110). */
 spl_status spl_camera_setup(const spl_frame_desc *d, spl_camera *cam);
 
+/* Splat launch configurations (threads per tile x pixels per lane); the
+   autotuner picks one per (tile size, workload).  Returns the number of
+   configurations / whether cfg can cover a tile_size x tile_size tile. */
+int spl_splat_config_count(void);
+int spl_splat_config_valid(int cfg, int tile_size);
+
 /* ---- plain render: replaces host_rendering (splotch_host.cc:711-834) --- */
 spl_status spl_render(spl_context *ctx, const spl_frame_desc *d,
                       const spl_particles *p, spl_image *out, int writeback);
@@ -150,8 +158,10 @@ spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
 
 /* Debug options for later spl_render calls.  Bit 0: project through the
    exact FP64 arithmetic only (no float-float fast path); the two must agree
-   bit for bit. */
+   bit for bit.  Bit 1: radix sorts in the reduce-then-scan form instead of
+   onesweep (no inter-block waits); results are identical. */
 #define SPL_DEBUG_EXACT_FP64 1
+#define SPL_DEBUG_RADIX_REDUCE_SCAN 2
 spl_status spl_debug_set_options(spl_context *ctx, int flags);
 
 #ifdef __cplusplus

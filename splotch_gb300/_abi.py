@@ -26,6 +26,7 @@ EXPORTED = [
     "spl_last_error_string", "spl_version", "spl_frame_desc_defaults", "spl_camera_setup",
     "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
     "spl_debug_get_bins", "spl_debug_count_fragments", "spl_debug_set_options",
+    "spl_splat_config_count", "spl_splat_config_valid",
 ]
 SPL_DEBUG_EXACT_FP64 = 1
 
@@ -48,6 +49,7 @@ class FrameDesc(C.Structure):
         ("gray_absorption", C.c_float), ("sort_type", C.c_int), ("tile_size", C.c_int),
         ("campos", C.c_double * 3), ("lookat", C.c_double * 3), ("sky", C.c_double * 3),
         ("centerpos", C.c_double * 3), ("order_mode", C.c_int), ("ftb_epsilon", C.c_float),
+        ("splat_config", C.c_int),
     ]
 
 
@@ -110,6 +112,8 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_debug_get_bins": (C.c_int, [vp, vp, i64, vp, i64]),
         "spl_debug_count_fragments": (C.c_int, [vp, vp]),
         "spl_debug_set_options": (C.c_int, [vp, C.c_int]),
+        "spl_splat_config_count": (C.c_int, []),
+        "spl_splat_config_valid": (C.c_int, [C.c_int, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -183,7 +183,8 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->perm, &c->ktmp, &c->vtmp, &c->off, &c->scratch, &c->tkey,
                               &c->tval, &c->tkey2, &c->tval2, &c->tkey_s, &c->tval_s,
                               &c->tile_start, &c->wide_list, &c->small, &c->pic, &c->pal_x,
-                              &c->pal_rgb, &c->aos_out};
+                              &c->pal_rgb, &c->aos_out, &c->pal_thr, &c->pal_xff,
+                              &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
@@ -242,6 +243,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     pc.ysum_ff = spl::ff{ys.x, ys.y};
   }
   pc.exact_fp64 = (c->debug_flags & 1) ? 1 : 0;
+  const bool onesweep = (c->debug_flags & 2) == 0;
   pc.zmin = d->zmin > 0.f ? d->zmin : 0.f;
   pc.zmax = d->zmax;
   pc.minrad2 = d->minrad_pix * d->minrad_pix;
@@ -387,7 +389,8 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   if (do_sort && n > 0) {
     spl::radix_sort_pairs(as<uint32_t>(c->key), nullptr, as<uint32_t>(c->ktmp),
                           as<uint32_t>(c->vtmp), as<uint32_t>(c->key) /*unused out*/,
-                          as<uint32_t>(c->perm), n, 0, 32, false, c->scratch.p, s, &launches);
+                          as<uint32_t>(c->perm), n, 0, 32, false, c->scratch.p, s, &launches,
+                          d_err, onesweep);
     order = as<uint32_t>(c->perm);
   }
   cudaEventRecord(c->ev[3], s);
@@ -422,7 +425,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
       spl::radix_sort_pairs(as<uint32_t>(c->tkey), as<uint32_t>(c->tval),
                             as<uint32_t>(c->tkey2), as<uint32_t>(c->tval2),
                             as<uint32_t>(c->tkey_s), as<uint32_t>(c->tval_s), (int64_t)ne, 0,
-                            tb, true, c->scratch.p, s, &launches);
+                            tb, true, c->scratch.p, s, &launches, d_err, onesweep);
     } else {
       SPL_CK(cudaMemcpyAsync(c->tkey_s.p, c->tkey.p, ne * 4, cudaMemcpyDeviceToDevice, s));
       SPL_CK(cudaMemcpyAsync(c->tval_s.p, c->tval.p, ne * 4, cudaMemcpyDeviceToDevice, s));
@@ -439,7 +442,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   spl::launch_tile_cost(as<uint32_t>(c->tile_start), ntiles, as<uint32_t>(c->tcost), s);
   spl::radix_sort_pairs(as<uint32_t>(c->tcost), nullptr, as<uint32_t>(c->tcost_s),
                         as<uint32_t>(c->tord), as<uint32_t>(c->tcost_s), as<uint32_t>(c->tord),
-                        ntiles, 0, 8, false, c->scratch.p, s, &launches);
+                        ntiles, 0, 8, false, c->scratch.p, s, &launches, d_err, onesweep);
   ++launches;
   cudaEventRecord(c->ev[4], s);
 
@@ -460,6 +463,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   sa.a_eq_e = d->a_eq_e ? 1 : 0;
   sa.order_mode = d->order_mode;
   sa.ftb_eps = d->ftb_epsilon;
+  sa.config = d->splat_config;
   sa.pic = out->memspace == SPL_MEM_DEVICE ? out->pic : as<float>(c->pic);
   launches += spl::launch_splat(sa, s);
   SPL_CK(cudaGetLastError());
@@ -497,6 +501,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   SPL_CK(cudaGetLastError());
   const uint32_t err = words[0];
   if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
+  if (err & 2u) return fail(SPL_ERR_TIMEOUT, "radix sort look-back wait gave up");
   c->stats.n_fallback = words[2];
   c->stats.n_wide = words[1];
 
@@ -534,6 +539,15 @@ spl_status spl_debug_get_projected(spl_context *c, void *aos_out, int64_t n) {
   SPL_CK(cudaMemcpyAsync(aos_out, c->aos_out.p, n * 36, cudaMemcpyDeviceToHost, c->stream));
   SPL_CK(cudaStreamSynchronize(c->stream));
   return SPL_OK;
+}
+
+int spl_splat_config_count(void) { return spl::splat_config_count(); }
+
+int spl_splat_config_valid(int cfg, int tile_size) {
+  return (cfg >= 0 && cfg < spl::splat_config_count() && tile_size >= 1 && tile_size <= 64 &&
+          spl::splat_config_valid(cfg, tile_size))
+             ? 1
+             : 0;
 }
 
 spl_status spl_debug_set_options(spl_context *c, int flags) {

@@ -97,6 +97,7 @@ extern "C" void spl_frame_desc_defaults(spl_frame_desc *d) {
   d->sky[1] = 1.0;
   d->order_mode = SPL_ORDER_BACK_TO_FRONT;
   d->ftb_epsilon = 1e-9f;
+  d->splat_config = -1;
 }
 
 extern "C" spl_status spl_camera_setup(const spl_frame_desc *d, spl_camera *cam) {

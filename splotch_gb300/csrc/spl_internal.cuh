@@ -204,10 +204,13 @@ void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *a
 // buffers distinct from keys_in/vals_in); sorted keys are written only when
 // keys_needed.
 size_t radix_scratch_bytes(int64_t n);
+// onesweep: one histogram pass then one decoupled-look-back pass per digit
+// (bounded waits; a wait that gives up sets bit 1 of *err); otherwise the
+// reduce-then-scan form (no inter-block waits).
 int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_tmp,
                      uint32_t *vals_tmp, uint32_t *keys_out, uint32_t *vals_out, int64_t n,
                      int bit0, int bit1, bool keys_needed, void *scratch, cudaStream_t s,
-                     int *launches);
+                     int *launches, uint32_t *err, bool onesweep);
 
 // Exclusive scan of count[order[s]] (order may be null) into off (n+1 slots;
 // off[n] = total).
@@ -245,9 +248,13 @@ struct SplatArgs {
   int a_eq_e;
   int order_mode;
   float ftb_eps;
+  int config;                  // launch configuration (-1: default for T)
   float *pic;                  // device, x-major xres*yres*3
 };
 int launch_splat(const SplatArgs &a, cudaStream_t s);
+int splat_config_count();
+bool splat_config_valid(int cfg, int T);
+int splat_default_config(int T, bool additive);
 void launch_count_fragments(const SplatArgs &a, unsigned long long *total, cudaStream_t s);
 
 }  // namespace spl

@@ -65,22 +65,48 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t *__res
   counts[(int64_t)threadIdx.x * nblocks + blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
+// Look-back state word (one per tile and digit): epoch (8 bits) | kind (2 bits)
+// | count (54 bits).  kind 1 = this tile's own count, 2 = inclusive prefix.
+constexpr int OS_EPOCH_SHIFT = 56, OS_KIND_SHIFT = 54;
+constexpr unsigned long long OS_VALUE_MASK = (1ull << OS_KIND_SHIFT) - 1ull;
+constexpr uint32_t OS_SPIN_LIMIT = 1u << 22;  // bounded wait, then error flag
+
+__device__ __forceinline__ unsigned long long os_word(uint32_t epoch, uint32_t kind,
+                                                      unsigned long long v) {
+  return ((unsigned long long)epoch << OS_EPOCH_SHIFT) |
+         ((unsigned long long)kind << OS_KIND_SHIFT) | v;
+}
+
+// Scatter pass.  OS=false: reduce-then-scan (offsets from the upsweep and a
+// scan).  OS=true: onesweep -- tiles are taken in launch order from a counter
+// and each digit's global offset comes from the global digit base plus a
+// decoupled look-back over earlier tiles' published counts.  A tile only ever
+// waits on tiles that started before it, and every wait is bounded.
+template <bool OS>
+__global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n, int shift,
-    int nbits, const uint32_t *__restrict__ offsets, int nblocks) {
+    int nbits, const uint32_t *__restrict__ offsets, int nblocks,
+    const unsigned long long *__restrict__ digit_base, unsigned long long *state,
+    uint32_t *tile_ctr, uint32_t *err, uint32_t epoch) {
   __shared__ uint32_t whist[RS_WARPS][RS_BINS];
   __shared__ uint32_t boff[RS_BINS];
   __shared__ uint32_t lstart[RS_BINS];
   __shared__ uint32_t wtot[RS_WARPS];
   __shared__ uint32_t skey[RS_TILE];
   __shared__ uint32_t sval[RS_TILE];
+  __shared__ uint32_t tile_sh;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&whist[0][0])[i] = 0;
-  boff[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  if (OS) {
+    if (threadIdx.x == 0) tile_sh = atomicAdd(tile_ctr, 1u);
+  } else {
+    boff[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  }
   __syncthreads();
+  const int blk = OS ? (int)tile_sh : (int)blockIdx.x;
   const uint32_t mask = (1u << nbits) - 1u;
-  const int64_t base = (int64_t)blockIdx.x * RS_TILE + (int64_t)w * 32 * RS_ITEMS;
+  const int64_t base = (int64_t)blk * RS_TILE + (int64_t)w * 32 * RS_ITEMS;
   uint32_t key[RS_ITEMS], val[RS_ITEMS], rank[RS_ITEMS];
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; ++j) {
@@ -119,6 +145,35 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
     uint32_t wpre = 0;
     for (int ww = 0; ww < w; ++ww) wpre += wtot[ww];
     lstart[d] = wpre + inc - run;
+    if (OS) {  // decoupled look-back for digit d
+      volatile unsigned long long *st = state + (size_t)blk * RS_BINS + d;
+      unsigned long long excl = 0;
+      if (blk == 0) {
+        *st = os_word(epoch, 2u, run);
+      } else {
+        *st = os_word(epoch, 1u, run);
+        int t = blk - 1;
+        uint32_t spins = 0;
+        while (t >= 0) {
+          const unsigned long long v =
+              reinterpret_cast<volatile unsigned long long *>(state)[(size_t)t * RS_BINS + d];
+          const uint32_t kind = (uint32_t)(v >> OS_KIND_SHIFT) & 3u;
+          if ((uint32_t)(v >> OS_EPOCH_SHIFT) != epoch || kind == 0u) {
+            if (++spins > OS_SPIN_LIMIT) {  // give up: results invalid, host reports it
+              atomicOr(err, 2u);
+              break;
+            }
+            if (spins > 64) __nanosleep(64);
+            continue;
+          }
+          excl += v & OS_VALUE_MASK;
+          if (kind == 2u) break;
+          --t;
+        }
+        *st = os_word(epoch, 2u, excl + run);
+      }
+      boff[d] = (uint32_t)(digit_base[d] + excl);
+    }
   }
   __syncthreads();
   // stable local sort into shared memory ...
@@ -134,13 +189,58 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_downsweep(
   }
   __syncthreads();
   // ... then consecutive threads write consecutive slots of each digit run
-  const int nloc = (int)min((int64_t)RS_TILE, n - (int64_t)blockIdx.x * RS_TILE);
+  const int nloc = (int)min((int64_t)RS_TILE, n - (int64_t)blk * RS_TILE);
   for (int i = threadIdx.x; i < nloc; i += RS_THREADS) {
     const uint32_t k = skey[i];
     const uint32_t d = (k >> shift) & mask;
     const uint32_t dst = boff[d] + (uint32_t)i - lstart[d];
     if (keys_out) keys_out[dst] = k;
     vals_out[dst] = sval[i];
+  }
+}
+
+// All digit histograms of the onesweep passes in one read of the keys.
+constexpr int OS_MAX_PASS = 4;
+__global__ void __launch_bounds__(RS_THREADS) k_os_hist(const uint32_t *__restrict__ keys,
+                                                        int64_t n, int bit0, int bit1,
+                                                        unsigned long long *hist) {
+  __shared__ uint32_t h[OS_MAX_PASS][RS_BINS];
+  for (int i = threadIdx.x; i < OS_MAX_PASS * RS_BINS; i += RS_THREADS) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const int npass = (bit1 - bit0 + 7) / 8;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t k = __ldg(keys + i);
+    for (int p = 0; p < npass; ++p) {
+      const int sh = bit0 + 8 * p;
+      const int nb = min(8, bit1 - sh);
+      atomicAdd(&h[p][(k >> sh) & ((1u << nb) - 1u)], 1u);
+    }
+  }
+  __syncthreads();
+  for (int p = 0; p < npass; ++p)
+    if (h[p][threadIdx.x]) atomicAdd(hist + p * RS_BINS + threadIdx.x, (unsigned long long)h[p][threadIdx.x]);
+}
+
+// Exclusive scan of each pass's 256 digit counts (one block).
+__global__ void __launch_bounds__(RS_THREADS) k_os_prefix(unsigned long long *hist, int npass) {
+  __shared__ unsigned long long sm[33];
+  for (int p = 0; p < npass; ++p) {
+    const unsigned long long v = hist[p * RS_BINS + threadIdx.x];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned long long inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += t;
+    }
+    if (lane == 31) sm[w] = inc;
+    __syncthreads();
+    unsigned long long pre = 0;
+    for (int ww = 0; ww < w; ++ww) pre += sm[ww];
+    __syncthreads();
+    hist[p * RS_BINS + threadIdx.x] = pre + inc - v;
+    __syncthreads();
   }
 }
 
@@ -266,21 +366,38 @@ size_t radix_scratch_bytes(int64_t n) {
   const int64_t nb = (n + RS_TILE - 1) / RS_TILE;
   const int64_t m = nb * RS_BINS;
   const int64_t np = (m + SC_TILE - 1) / SC_TILE;
-  return (size_t)(2 * m + np + 64) * sizeof(uint32_t);
+  const size_t rts = (size_t)(2 * m + np + 64) * sizeof(uint32_t);
+  const size_t os = (size_t)OS_MAX_PASS * RS_BINS * 8 + 256 + (size_t)m * 8;
+  return (rts > os ? rts : os) + 256;
 }
 
 int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_tmp,
                      uint32_t *vals_tmp, uint32_t *keys_out, uint32_t *vals_out, int64_t n,
                      int bit0, int bit1, bool keys_needed, void *scratch, cudaStream_t s,
-                     int *launches) {
+                     int *launches, uint32_t *err, bool onesweep) {
   if (n <= 0) return 0;
   const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
   const int64_t m = (int64_t)nblocks * RS_BINS;
+  int npass = 0;
+  for (int b = bit0; b < bit1; b += 8) ++npass;
+  if (npass > OS_MAX_PASS) onesweep = false;
+  // onesweep scratch: digit bases, per-pass tile counters, look-back state
+  unsigned long long *hist = static_cast<unsigned long long *>(scratch);
+  uint32_t *tile_ctr = reinterpret_cast<uint32_t *>(hist + OS_MAX_PASS * RS_BINS);
+  unsigned long long *state = reinterpret_cast<unsigned long long *>(
+      reinterpret_cast<uint8_t *>(tile_ctr) + 256);
+  // reduce-then-scan scratch
   uint32_t *counts = static_cast<uint32_t *>(scratch);
   uint32_t *offsets = counts + m;
   uint32_t *sc = offsets + m;
-  int npass = 0;
-  for (int b = bit0; b < bit1; b += 8) ++npass;
+  if (onesweep) {
+    cudaMemsetAsync(scratch, 0, (size_t)OS_MAX_PASS * RS_BINS * 8 + 256 + (size_t)m * 8, s);
+    int hb = (int)((n + RS_THREADS * 16 - 1) / (RS_THREADS * 16));
+    if (hb > 152 * 8) hb = 152 * 8;
+    k_os_hist<<<hb, RS_THREADS, 0, s>>>(keys_in, n, bit0, bit1, hist);
+    k_os_prefix<<<1, RS_THREADS, 0, s>>>(hist, npass);
+    if (launches) *launches += 2;
+  }
   // ping-pong so that the last pass lands in (keys_out, vals_out)
   const uint32_t *kin = keys_in;
   const uint32_t *vin = vals_in;
@@ -291,11 +408,20 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
     const bool to_out = ((npass - 1 - pass) % 2) == 0;
     uint32_t *ko = to_out ? keys_out : keys_tmp;
     uint32_t *vo = to_out ? vals_out : vals_tmp;
-    k_rs_upsweep<<<nblocks, RS_THREADS, 0, s>>>(kin, n, b, nbits, counts, nblocks);
-    exclusive_scan<uint32_t>(LoadU32{counts}, m, offsets, (uint32_t *)nullptr, sc, s, launches);
-    k_rs_downsweep<<<nblocks, RS_THREADS, 0, s>>>(kin, vin, (last && !keys_needed) ? nullptr : ko,
-                                                  vo, n, b, nbits, offsets, nblocks);
-    if (launches) *launches += 2;
+    uint32_t *kout = (last && !keys_needed) ? nullptr : ko;
+    if (onesweep) {
+      k_rs_downsweep<true><<<nblocks, RS_THREADS, 0, s>>>(
+          kin, vin, kout, vo, n, b, nbits, nullptr, nblocks, hist + pass * RS_BINS, state,
+          tile_ctr + pass, err, (uint32_t)(pass + 1));
+      if (launches) *launches += 1;
+    } else {
+      k_rs_upsweep<<<nblocks, RS_THREADS, 0, s>>>(kin, n, b, nbits, counts, nblocks);
+      exclusive_scan<uint32_t>(LoadU32{counts}, m, offsets, (uint32_t *)nullptr, sc, s,
+                               launches);
+      k_rs_downsweep<false><<<nblocks, RS_THREADS, 0, s>>>(
+          kin, vin, kout, vo, n, b, nbits, offsets, nblocks, nullptr, nullptr, nullptr, nullptr, 0);
+      if (launches) *launches += 2;
+    }
     kin = ko;
     vin = vo;
   }

@@ -1,15 +1,19 @@
 // spl_splat.cu -- tiled Gaussian splat (render_new region B,
 // splotch/splotch_host.cc:434-692), additive and ordered emission-absorption.
 //
-// One CTA (256 threads, 8 warps) per tile.  The tile's pixels are numbered
-// column-major (p = x*th + y, tile-local) and dealt out in contiguous spans:
-// warp w owns pixels [w*32K, (w+1)*32K), lane l of item k owns pixel
-// w*32K + 32k + l, and keeps its three channels in registers for the whole
-// tile.  The tile's particle list is streamed through shared memory 256
-// entries at a time: each thread stages one particle (tile-local position,
-// Gaussian width, clipped bounding box) and the exact column runs of its
-// footprint inside the tile.  Each warp then ballots the 256 staged particles
-// against its own column range and walks only the hits, in list order.
+// One CTA per tile.  The tile is cut into 8x4-pixel items; lane l of an item
+// owns pixel (l%8, l/8) of it and keeps its three channels in registers for
+// the whole tile.  Each warp owns a WX x WY group of items (K = WX*WY pixels
+// per lane), so one particle's per-warp cost (parameter loads, bounding-box
+// tests) is shared by up to 32*K pixels and an item the particle misses costs
+// one uniform branch.
+//
+// The tile's particle list is streamed through shared memory B entries at a
+// time: each thread stages particles (tile-local position, Gaussian width,
+// clipped bounding box, colour) and the exact column runs of their footprint
+// inside the tile.  Each warp ballots the staged particles against its own
+// bounding box and walks only the hits, in list order (or reverse list order
+// front-to-back).
 //
 // Coverage is decided exactly as the reference decides it (tile-local
 // coordinates, truncating int conversion, the column run
@@ -17,77 +21,70 @@
 // non-contracted float arithmetic, so every pixel receives exactly the
 // reference's fragments.  The Gaussian weight exp(stp*dx^2)*exp(stp*dy^2) is
 // evaluated as one ex2(stp*log2e*(dx^2+dy^2)) instead of the reference's
-// exptable<float> (splotch/splotchutils.h:174-215), which is closer to the
-// exact weight than the table.
+// exptable<float> (splotch/splotchutils.h:174-215), closer to the exact weight.
 //
 // Absorption: back-to-front applies C += expm1(-e*att)*(C - q) in list order
 // (splotch_host.cc:663-665).  Front-to-back visits the list in reverse and
-// accumulates C += Tr*q*(1-T), Tr *= T, the same sum term by term, and stops a
-// tile once every pixel's transmittance in all channels is below epsilon.
+// accumulates C += Tr*q*(1-T), Tr *= T -- the same sum term by term -- and stops
+// a warp once every pixel's transmittance in all channels is below epsilon,
+// and the tile once every warp has stopped.
 #include "spl_internal.cuh"
 
 namespace spl {
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kWarps = kThreads / 32;
-constexpr int kBatch = kThreads;
+constexpr int IW = 8, IH = 4;  // item: 8 columns x 4 rows, one pixel per lane
 
-struct SmemLayout {
-  float *px, *py, *stp;
-  uint32_t *bb;
-  float4 *e, *q;
-  uint16_t *run;
+template <int B>
+struct Smem {
+  float4 p0[B];  // posx, posy, stp*log2e, bbox bits
+  float4 e[B];   // e.r, e.g, e.b, q.r
+  float2 q[B];   // q.g, q.b
+  // followed by uint16_t run[B*T]: column runs lo | hi<<8
 };
 
-__device__ __forceinline__ SmemLayout smem_layout(uint8_t *base) {
-  SmemLayout L;
-  L.e = reinterpret_cast<float4 *>(base);
-  L.q = L.e + kBatch;
-  L.px = reinterpret_cast<float *>(L.q + kBatch);
-  L.py = L.px + kBatch;
-  L.stp = L.py + kBatch;
-  L.bb = reinterpret_cast<uint32_t *>(L.stp + kBatch);
-  L.run = reinterpret_cast<uint16_t *>(L.bb + kBatch);
-  return L;
-}
-
+template <int B>
 size_t smem_bytes(int T) {
-  return (size_t)kBatch * (16 + 16 + 4 + 4 + 4 + 4) + (size_t)kBatch * T * 2;
+  return sizeof(Smem<B>) + (size_t)B * T * 2;
 }
 
-template <int K, bool ADD, bool FTB>
-__global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB>
+__global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
+  constexpr int K = WX * WY;
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  const SmemLayout L = smem_layout(smem_raw);
+  Smem<B> &S = *reinterpret_cast<Smem<B> *>(smem_raw);
+  uint16_t *srun = reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem<B>));
+
   const int T = a.T;
   const int tile = a.tile_order ? (int)__ldg(a.tile_order + blockIdx.x) : (int)blockIdx.x;
   const int ix = tile % a.ncx, iy = tile / a.ncx;
   const int x0s = ix * T, y0s = iy * T;
   const int tw = min(x0s + T, a.xres) - x0s;
   const int th = min(y0s + T, a.yres) - y0s;
-  const int P = tw * th;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int wbase = w * 32 * K;
-  const bool warp_has_pixels = wbase < P;
-  const int wc0 = warp_has_pixels ? wbase / th : 0;
-  const int wc1 = warp_has_pixels ? (min(wbase + 32 * K, P) - 1) / th : -1;
 
-  int pxy[K];
-  float pxf[K], pyf[K];  // tile-local pixel coordinates as floats
-  int ic0[K], ic1[K];
-  float acc[K][3];
-  float tr[K][3];
+  // ---- this warp's items ------------------------------------------------
+  const int nbx = (tw + IW - 1) / IW, nby = (th + IH - 1) / IH;
+  const int nwx = (nbx + WX - 1) / WX, nwy = (nby + WY - 1) / WY;
+  const int wx = w % nwx, wy = w / nwx;
+  const bool warp_has_pixels = wy < nwy;
+  const int wbx0 = wx * WX * IW, wby0 = wy * WY * IH;  // warp box, tile-local
+  const int wbx1 = min(wbx0 + WX * IW, tw), wby1 = min(wby0 + WY * IH, th);
+
+  float pxf[K], pyf[K];
+  int pxi[K], pyi[K];
+  bool valid[K];
+  float acc[K][3], tr[K][3];
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    const int p0 = wbase + k * 32;
-    const int p = p0 + lane;
-    pxy[k] = p < P ? (((p / th) << 8) | (p % th)) : -1;
-    pxf[k] = (float)(pxy[k] >> 8);
-    pyf[k] = (float)(pxy[k] & 255);
-    ic0[k] = p0 < P ? p0 / th : 1 << 20;
-    ic1[k] = p0 < P ? (min(p0 + 31, P - 1)) / th : -1;
+    const int x = wbx0 + (k % WX) * IW + (lane & 7);
+    const int y = wby0 + (k / WX) * IH + (lane >> 3);
+    valid[k] = warp_has_pixels && x < tw && y < th;
+    pxi[k] = x;
+    pyi[k] = y;
+    pxf[k] = (float)x;
+    pyf[k] = (float)y;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       acc[k][c] = 0.f;
@@ -96,15 +93,17 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
   }
 
   const uint32_t start = a.tile_start[tile], end = a.tile_start[tile + 1];
-  const int nbatch = (int)((end - start + kBatch - 1) / kBatch);
+  const int nbatch = (int)((end - start + B - 1) / B);
   bool warp_done = !warp_has_pixels;
 
   for (int b = 0; b < nbatch; ++b) {
     const int bi = FTB ? nbatch - 1 - b : b;
-    // ---- stage one particle per thread ---------------------------------
-    {
-      const uint32_t jj = start + (uint32_t)bi * kBatch + threadIdx.x;
+    // ---- stage B particles ------------------------------------------------
+#pragma unroll 1
+    for (int slot = threadIdx.x; slot < B; slot += NT) {
+      const uint32_t jj = start + (uint32_t)bi * B + slot;
       uint32_t bb = 0;
+      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f);
       if (jj < end) {
         const uint32_t idx = __ldg(a.entries + jj);
         const float4 p = __ldg(a.pos + idx);
@@ -121,7 +120,7 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
         if (minx < maxx && miny < maxy) {
           bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((uint32_t)miny << 16) |
                ((uint32_t)maxy << 24);
-          uint16_t *run = L.run + threadIdx.x * T;
+          uint16_t *run = srun + slot * T;
           for (int x = minx; x < maxx; ++x) {  // splotch_host.cc:603-606
             const float dx = fsub((float)x, posx);
             const float dxsq = fmul(dx, dx);
@@ -132,53 +131,54 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
             run[x] = (uint16_t)(lo | (hi << 8));
           }
         }
-        L.px[threadIdx.x] = posx;
-        L.py[threadIdx.x] = posy;
-        L.stp[threadIdx.x] = stp * kLog2e;
-        L.e[threadIdx.x] = make_float4(c.x, c.y, c.z, 0.f);
-        if (!ADD) {
+        p0 = make_float4(posx, posy, stp * kLog2e, 0.f);
+        if (ADD) {
+          S.e[slot] = make_float4(c.x, c.y, c.z, 0.f);
+        } else {
           // q = e/(e+grayabsorb), splotch_host.cc:626-628
-          L.q[threadIdx.x] = make_float4(fdiv(c.x, fadd(c.x, a.gray)),
-                                         fdiv(c.y, fadd(c.y, a.gray)),
-                                         fdiv(c.z, fadd(c.z, a.gray)), 0.f);
+          S.e[slot] = make_float4(c.x, c.y, c.z, fdiv(c.x, fadd(c.x, a.gray)));
+          S.q[slot] = make_float2(fdiv(c.y, fadd(c.y, a.gray)), fdiv(c.z, fadd(c.z, a.gray)));
         }
       }
-      L.bb[threadIdx.x] = bb;
+      p0.w = __uint_as_float(bb);
+      S.p0[slot] = p0;
     }
     __syncthreads();
-    // ---- accumulate ------------------------------------------------------
+    // ---- accumulate ---------------------------------------------------------
     if (!warp_done) {
 #pragma unroll 1
-      for (int cc = 0; cc < kBatch / 32; ++cc) {
-        const int ch = FTB ? kBatch / 32 - 1 - cc : cc;
-        const uint32_t bbl = L.bb[ch * 32 + lane];
+      for (int cc = 0; cc < B / 32; ++cc) {
+        const int ch = FTB ? B / 32 - 1 - cc : cc;
+        const uint32_t bbl = __float_as_uint(S.p0[ch * 32 + lane].w);
         const int mnx = bbl & 255, mxx = (bbl >> 8) & 255;
-        const bool hit = (mnx < mxx) && (mxx > wc0) && (mnx <= wc1);
+        const int mny = (bbl >> 16) & 255, mxy = bbl >> 24;
+        const bool hit = (mnx < mxx) && (mnx < wbx1) && (mxx > wbx0) && (mny < wby1) &&
+                         (mxy > wby0);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
           const int bit = FTB ? 31 - __clz(mask) : __ffs(mask) - 1;
           mask &= ~(1u << bit);
           const int j = ch * 32 + bit;
-          const uint32_t bbj = L.bb[j];
+          const float4 p0 = S.p0[j];
+          const uint32_t bbj = __float_as_uint(p0.w);
           const int jmnx = bbj & 255, jmxx = (bbj >> 8) & 255;
-          const float posx = L.px[j], posy = L.py[j], stp2 = L.stp[j];
-          const float4 e = L.e[j];
-          float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (!ADD) q = L.q[j];
-          const uint16_t *run = L.run + j * T;
+          const int jmny = (bbj >> 16) & 255, jmxy = bbj >> 24;
+          const float4 e = S.e[j];
+          float2 q2 = make_float2(0.f, 0.f);
+          if (!ADD) q2 = S.q[j];
+          const uint16_t *run = srun + j * T;
 #pragma unroll
           for (int k = 0; k < K; ++k) {
-            if (ic1[k] >= jmnx && ic0[k] < jmxx) {  // warp-uniform
-              const int x = pxy[k] >> 8, y = pxy[k] & 255;
-              bool in = pxy[k] >= 0 && x >= jmnx && x < jmxx;
+            const int ix0 = wbx0 + (k % WX) * IW, iy0 = wby0 + (k / WX) * IH;
+            if (jmnx < ix0 + IW && jmxx > ix0 && jmny < iy0 + IH && jmxy > iy0) {  // uniform
+              bool in = valid[k] && pxi[k] >= jmnx && pxi[k] < jmxx;
               if (in) {
-                const uint32_t rr = run[x];
-                in = y >= (int)(rr & 255) && y < (int)(rr >> 8);
+                const uint32_t rr = run[pxi[k]];
+                in = pyi[k] >= (int)(rr & 255) && pyi[k] < (int)(rr >> 8);
               }
               if (in) {
-                const float dx = pxf[k] - posx, dy = pyf[k] - posy;
-                const float s2 = fmaf(dy, dy, dx * dx);
-                const float att = ex2(stp2 * s2);
+                const float dx = pxf[k] - p0.x, dy = pyf[k] - p0.y;
+                const float att = ex2(p0.z * fmaf(dy, dy, dx * dx));
                 if (ADD) {
                   acc[k][0] = fmaf(-e.x, att, acc[k][0]);
                   acc[k][1] = fmaf(-e.y, att, acc[k][1]);
@@ -187,19 +187,20 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
                   const float m0 = expm1_neg(-e.x * att);
                   const float m1 = expm1_neg(-e.y * att);
                   const float m2 = expm1_neg(-e.z * att);
-                  acc[k][0] = fmaf(m0, acc[k][0] - q.x, acc[k][0]);
-                  acc[k][1] = fmaf(m1, acc[k][1] - q.y, acc[k][1]);
-                  acc[k][2] = fmaf(m2, acc[k][2] - q.z, acc[k][2]);
+                  acc[k][0] = fmaf(m0, acc[k][0] - e.w, acc[k][0]);
+                  acc[k][1] = fmaf(m1, acc[k][1] - q2.x, acc[k][1]);
+                  acc[k][2] = fmaf(m2, acc[k][2] - q2.y, acc[k][2]);
                 } else {
-                  const float m0 = expm1_neg(-e.x * att);
-                  const float m1 = expm1_neg(-e.y * att);
-                  const float m2 = expm1_neg(-e.z * att);
-                  acc[k][0] = fmaf(-tr[k][0] * q.x, m0, acc[k][0]);
-                  acc[k][1] = fmaf(-tr[k][1] * q.y, m1, acc[k][1]);
-                  acc[k][2] = fmaf(-tr[k][2] * q.z, m2, acc[k][2]);
-                  tr[k][0] = fmaf(tr[k][0], m0, tr[k][0]);
-                  tr[k][1] = fmaf(tr[k][1], m1, tr[k][1]);
-                  tr[k][2] = fmaf(tr[k][2], m2, tr[k][2]);
+                  // w = Tr*(1-T) = -Tr*expm1(-e*att); C += w*q; Tr -= w
+                  const float w0 = -tr[k][0] * expm1_neg(-e.x * att);
+                  const float w1 = -tr[k][1] * expm1_neg(-e.y * att);
+                  const float w2 = -tr[k][2] * expm1_neg(-e.z * att);
+                  acc[k][0] = fmaf(w0, e.w, acc[k][0]);
+                  acc[k][1] = fmaf(w1, q2.x, acc[k][1]);
+                  acc[k][2] = fmaf(w2, q2.y, acc[k][2]);
+                  tr[k][0] -= w0;
+                  tr[k][1] -= w1;
+                  tr[k][2] -= w2;
                 }
               }
             }
@@ -210,7 +211,7 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
         bool mine_done = true;
 #pragma unroll
         for (int k = 0; k < K; ++k)
-          if (pxy[k] >= 0)
+          if (valid[k])
             mine_done = mine_done && tr[k][0] < a.ftb_eps && tr[k][1] < a.ftb_eps &&
                         tr[k][2] < a.ftb_eps;
         warp_done = __all_sync(0xffffffffu, mine_done);
@@ -226,9 +227,8 @@ __global__ void __launch_bounds__(kThreads) k_splat(SplatArgs a) {
   // ---- write the tile (pic is x-major: pixel (x,y) at (x*yres + y)*3) ----
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    if (pxy[k] >= 0) {
-      const int x = pxy[k] >> 8, y = pxy[k] & 255;
-      float *o = a.pic + ((size_t)(x0s + x) * a.yres + (y0s + y)) * 3;
+    if (valid[k]) {
+      float *o = a.pic + ((size_t)(x0s + pxi[k]) * a.yres + (y0s + pyi[k])) * 3;
       o[0] = acc[k][0];
       o[1] = acc[k][1];
       o[2] = acc[k][2];
@@ -269,18 +269,31 @@ __global__ void __launch_bounds__(256) k_count_fragments(SplatArgs a,
   if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(total, cnt);
 }
 
-template <int K>
-int launch_k(const SplatArgs &a, cudaStream_t s) {
+template <int NT, int WX, int WY, int B>
+int launch_cfg(const SplatArgs &a, cudaStream_t s) {
   const int ntiles = a.ncx * a.ncy;
-  const size_t sm = smem_bytes(a.T);
+  const size_t sm = smem_bytes<B>(a.T);
   if (a.a_eq_e) {
-    k_splat<K, true, false><<<ntiles, kThreads, sm, s>>>(a);
+    auto k = k_splat<NT, WX, WY, B, true, false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<ntiles, NT, sm, s>>>(a);
   } else if (a.order_mode == 1) {
-    k_splat<K, false, true><<<ntiles, kThreads, sm, s>>>(a);
+    auto k = k_splat<NT, WX, WY, B, false, true>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<ntiles, NT, sm, s>>>(a);
   } else {
-    k_splat<K, false, false><<<ntiles, kThreads, sm, s>>>(a);
+    auto k = k_splat<NT, WX, WY, B, false, false>;
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k<<<ntiles, NT, sm, s>>>(a);
   }
   return 1;
+}
+
+// Does a (threads, WX, WY) configuration cover a T x T tile?
+bool covers(int T, int nt, int wxi, int wyi) {
+  const int nbx = (T + IW - 1) / IW, nby = (T + IH - 1) / IH;
+  const int nwx = (nbx + wxi - 1) / wxi, nwy = (nby + wyi - 1) / wyi;
+  return nwx * nwy <= nt / 32;
 }
 
 }  // namespace
@@ -290,15 +303,43 @@ void launch_count_fragments(const SplatArgs &a, unsigned long long *total, cudaS
   if (a.ncx * a.ncy > 0) k_count_fragments<<<a.ncx * a.ncy, 256, 0, s>>>(a, total);
 }
 
+// Launch configurations (threads per tile, items per warp): the autotuner
+// chooses among those that cover the tile size.
+int splat_config_count() { return 5; }
+
+bool splat_config_valid(int cfg, int T) {
+  switch (cfg) {
+    case 0: return covers(T, 256, 1, 1);  // 8 warps x (8x4)
+    case 1: return covers(T, 64, 2, 2);   // 2 warps x (16x8)
+    case 2: return covers(T, 128, 2, 1);  // 4 warps x (16x4)
+    case 3: return covers(T, 256, 2, 2);  // 8 warps x (16x8)
+    case 4: return covers(T, 256, 4, 4);  // 8 warps x (32x16)
+  }
+  return false;
+}
+
+// Measured on GB300 (50M-particle absorption frame and 1M additive frame at
+// T=16): 4 warps x 16x4 is fastest for the absorption splat, 8 warps x 8x4 for
+// the additive one; larger tiles need the wider configurations.
+int splat_default_config(int T, bool additive) {
+  if (!additive && splat_config_valid(2, T)) return 2;
+  if (splat_config_valid(0, T)) return 0;
+  if (splat_config_valid(3, T)) return 3;
+  return 4;
+}
+
 int launch_splat(const SplatArgs &a, cudaStream_t s) {
-  const int need = (a.T * a.T + kThreads - 1) / kThreads;  // pixels per lane
   if (a.ncx * a.ncy <= 0) return 0;
-  if (need <= 1) return launch_k<1>(a, s);
-  if (need <= 2) return launch_k<2>(a, s);
-  if (need <= 4) return launch_k<4>(a, s);
-  if (need <= 8) return launch_k<8>(a, s);
-  if (need <= 10) return launch_k<10>(a, s);
-  return launch_k<16>(a, s);
+  int cfg = a.config >= 0 && splat_config_valid(a.config, a.T)
+                ? a.config
+                : splat_default_config(a.T, a.a_eq_e != 0);
+  switch (cfg) {
+    case 0: return launch_cfg<256, 1, 1, 256>(a, s);
+    case 1: return launch_cfg<64, 2, 2, 128>(a, s);
+    case 2: return launch_cfg<128, 2, 1, 128>(a, s);
+    case 3: return launch_cfg<256, 2, 2, 256>(a, s);
+    default: return launch_cfg<256, 4, 4, 256>(a, s);
+  }
 }
 
 }  // namespace spl

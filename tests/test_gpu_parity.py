@@ -52,6 +52,29 @@ def test_stage_parity(name, renderer, port):
     print(name, info)
 
 
+@pytest.mark.parametrize("mode", ["add", "btf", "ftb"])
+@pytest.mark.parametrize("tile", [8, 16, 32, 50])
+def test_every_splat_config(tile, mode, renderer, port):
+    """Every launch configuration that covers the tile size gives a parity image."""
+    from splotch_gb300 import _abi
+
+    lib = _abi.load()
+    if mode == "add":
+        w = _additive(n=20000, xres=120, yres=88, tile=tile)
+    else:
+        w = _absorption(n_gas=16000, n_star=4000, xres=128, yres=72, tile=tile, order=mode)
+    prm = dict(w.params.params)
+    o = oracle_frame(port, prm, w.rc, w.particles, fp32=False)
+    ran = 0
+    for cfg in range(lib.spl_splat_config_count()):
+        if not lib.spl_splat_config_valid(cfg, tile):
+            continue
+        prm["gpu_splat_config"] = str(cfg)
+        assert_parity(gpu_frame(renderer, prm, w.rc, w.particles), o)
+        ran += 1
+    assert ran >= 1
+
+
 def _edge_setup(xres=96, yres=80, tile=16, a_eq_e=True, **extra):
     rc = sg.RenderContext(campos=np.array([0.0, 0.0, 100.0]),
                           centerpos=np.array([0.0, 0.0, 100.0]), lookat=np.zeros(3),
@@ -194,6 +217,26 @@ def test_fast_projection_equals_fp64(camera, renderer):
     assert out[1][1] == 0
     assert out[0][1] < 0.01 * len(w.particles), f"{out[0][1]} FP64 fallbacks"
     print(camera, "fallbacks", out[0][1], "of", len(w.particles))
+
+
+def test_onesweep_equals_reduce_then_scan(renderer):
+    """The onesweep radix sorts (decoupled look-back) and the reduce-then-scan
+    sorts give the same permutation and bins on a few million keys."""
+    w = synth.plain_absorption(n_gas=3_200_000, n_star=800_000, xres=960, yres=540, tile=16)
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    pic = np.zeros((960, 540, 3), np.float32)
+    ntiles = 60 * 34
+    got = {}
+    for flags in (0, 2):
+        renderer.set_debug(flags)
+        try:
+            renderer.render_aos(desc, w.particles.copy(), pic)
+        finally:
+            renderer.set_debug(0)
+        got[flags] = (renderer.order(len(w.particles)), *renderer.bins(ntiles), pic.copy())
+    for a, b in zip(got[0], got[2]):
+        assert np.array_equal(a, b)
 
 
 def test_full_size_additive_1M(renderer, port):
