@@ -144,8 +144,11 @@ spl_status spl_get_stats(const spl_context *ctx, spl_stats *s);
 /* Projected + colourised particles in original order (particle_sim layout):
    the reference's particle_project + particle_colorize side effects. */
 spl_status spl_debug_get_projected(spl_context *ctx, void *aos_out, int64_t n);
-/* Visiting order (stable sort permutation); identity when a_eq_e. */
-spl_status spl_debug_get_order(spl_context *ctx, uint32_t *perm_out, int64_t n);
+/* Visiting order of the active particles (particle indices, *n_out of them):
+   ascending index when a_eq_e, else the stable sort order -- the order in
+   which the reference's stably sorted array meets its active particles. */
+spl_status spl_debug_get_order(spl_context *ctx, uint32_t *order_out, int64_t cap,
+                               int64_t *n_out);
 /* Tile bins: tile_start has ntiles+1 entries; entries hold particle indices. */
 spl_status spl_debug_get_bins(spl_context *ctx, int64_t *tile_start_out,
                               int64_t ntiles_plus_one, uint32_t *entries_out,

@@ -324,9 +324,11 @@ class Renderer:
         return out
 
     def order(self, n: int) -> np.ndarray:
-        out = np.zeros(n, dtype=np.uint32)
-        _abi.check(self.lib.spl_debug_get_order(self.ctx, out.ctypes.data, n))
-        return out
+        """Visiting order of the active particles of the last frame."""
+        out = np.zeros(max(n, 1), dtype=np.uint32)
+        na = C.c_int64()
+        _abi.check(self.lib.spl_debug_get_order(self.ctx, out.ctypes.data, n, C.byref(na)))
+        return out[: na.value]
 
     def set_debug(self, flags: int) -> None:
         """spl_debug_set_options: bit 0 forces the exact FP64 projection."""

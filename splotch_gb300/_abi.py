@@ -108,7 +108,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
                                  C.POINTER(Image), C.c_int]),
         "spl_get_stats": (C.c_int, [vp, C.POINTER(Stats)]),
         "spl_debug_get_projected": (C.c_int, [vp, vp, i64]),
-        "spl_debug_get_order": (C.c_int, [vp, vp, i64]),
+        "spl_debug_get_order": (C.c_int, [vp, vp, i64, vp]),
         "spl_debug_get_bins": (C.c_int, [vp, vp, i64, vp, i64]),
         "spl_debug_count_fragments": (C.c_int, [vp, vp]),
         "spl_debug_set_options": (C.c_int, [vp, C.c_int]),

@@ -27,13 +27,16 @@ struct spl_context {
   };
   Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
-      aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord;
-  int debug_flags = 0;  // bit 0: exact FP64 projection only
+      aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate;
+  int debug_flags = 0;  // SPL_DEBUG_* bits
   // state of the last frame (for the debug getters)
-  int64_t n = 0, ne = 0, ntiles = 0;
-  bool has_order = false;
+  int64_t n = 0, na = 0, ne = 0, ntiles = 0;
+  bool has_order = false, writeback_done = false;
   int last_T = 0;
   spl::SplatArgs last_splat{};
+  spl::ProjConst last_pc{};
+  const void *last_aos = nullptr;
+  spl::SoAIn last_soa{};
   spl_stats stats{};
   cudaEvent_t ev[8]{};
 };
@@ -148,6 +151,27 @@ int bits_for(int64_t v) {  // bits needed to represent 0..v-1
   return b;
 }
 
+// Every particle's projected state (indexed by particle) from the last
+// frame's inputs and constants: the writeback and the projection test hook.
+spl_status project_full(spl_context *c, int64_t n, bool with_key, int *launches) {
+  spl_status st;
+  if ((st = ensure(c->pos, n * sizeof(float4))) || (st = ensure(c->col, n * sizeof(float4))) ||
+      (st = ensure(c->active, n)) || (with_key && (st = ensure(c->key, n * 4))))
+    return st;
+  spl::ProjectOut po;
+  std::memset(&po, 0, sizeof(po));
+  po.pos = as<float4>(c->pos);
+  po.col = as<float4>(c->col);
+  po.active = as<uint8_t>(c->active);
+  po.key = with_key ? as<uint32_t>(c->key) : nullptr;
+  po.err = as<uint32_t>(c->small);
+  spl::ProjConst pc = c->last_pc;
+  pc.n_fallback = nullptr;
+  spl::launch_project(c->last_aos, &c->last_soa, n, pc, po, false, c->stream);
+  if (n > 0) ++*launches;
+  return SPL_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -184,7 +208,8 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->tval, &c->tkey2, &c->tval2, &c->tkey_s, &c->tval_s,
                               &c->tile_start, &c->wide_list, &c->small, &c->pic, &c->pal_x,
                               &c->pal_rgb, &c->aos_out, &c->pal_thr, &c->pal_xff,
-                              &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord};
+                              &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord, &c->pos_c,
+                              &c->col_c, &c->idx_c, &c->pstate};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
@@ -279,24 +304,30 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   if (ntiles >= 0xffffffffLL) return fail(SPL_ERR_INVALID, "too many tiles");
 
   // ---- buffers -------------------------------------------------------------
-  if ((st = ensure(c->pos, n * sizeof(float4))) || (st = ensure(c->col, n * sizeof(float4))) ||
-      (st = ensure(c->active, n)) || (st = ensure(c->count, n * 4)) ||
+  // compact (active-only) arrays are sized for n: the active count is known
+  // only after projection
+  const int64_t nprojtiles = (n + 255) / 256;
+  if ((st = ensure(c->pos_c, n * sizeof(float4))) || (st = ensure(c->col_c, n * sizeof(float4))) ||
+      (st = ensure(c->idx_c, n * 4)) || (st = ensure(c->count, n * 4)) ||
       (st = ensure(c->off, (n + 1) * 8)) || (st = ensure(c->wide_list, n * 4)) ||
       (st = ensure(c->small, 256)) || (st = ensure(c->tile_start, (ntiles + 1) * 4)) ||
+      (st = ensure(c->pstate, (nprojtiles + 1) * 8)) ||
       (st = ensure(c->pic, (size_t)xres * yres * 3 * 4)) ||
       (st = ensure(c->pal_x, (npal + 1) * 8)) || (st = ensure(c->pal_rgb, (npal + 1) * 12)))
     return st;
-  if (do_sort) {
-    if ((st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
-        (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)))
-      return st;
-  }
+  if ((st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
+      (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)))
+    return st;
   size_t scr = spl::scan_scratch_bytes(n + 1);
   size_t rs = spl::radix_scratch_bytes(n);
   if (rs > scr) scr = rs;
   if ((st = ensure(c->scratch, scr))) return st;
+  // small words: 0 error, 1 wide-particle count, 2 FP64 fallbacks, 3 active
+  // count, 4 projection tile counter
   uint32_t *d_err = as<uint32_t>(c->small);
   uint32_t *d_wide_n = d_err + 1;
+  uint32_t *d_nact = d_err + 3;
+  uint32_t *d_ptile = d_err + 4;
 
   // palettes (a few KB)
   for (int t = 0; t < d->ptypes; ++t) {
@@ -337,14 +368,14 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     pc.pal_xff = as<float2>(c->pal_xff);
     pc.pal_invff = as<float2>(c->pal_invff);
   }
-  SPL_CK(cudaMemsetAsync(d_err, 0, 12, s));
+  SPL_CK(cudaMemsetAsync(d_err, 0, 32, s));
+  SPL_CK(cudaMemsetAsync(c->pstate.p, 0, (nprojtiles + 1) * 8, s));
   pc.n_fallback = d_err + 2;
 
   cudaEventRecord(c->ev[0], s);
   // ---- inputs --------------------------------------------------------------
   const void *aos_dev = nullptr;
-  const float *soa[8] = {p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb};
-  const uint16_t *type_dev = p->type;
+  spl::SoAIn soa{p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb, p->type};
   if (p->layout == SPL_LAYOUT_AOS) {
     if (p->memspace == SPL_MEM_HOST) {
       if ((st = ensure(c->aos_in, n * 36))) return st;
@@ -354,42 +385,49 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
       aos_dev = p->aos;
     }
   } else if (p->memspace == SPL_MEM_HOST) {
-    for (int f = 0; f < 8; ++f) {
-      if (!soa[f]) continue;
-      if ((st = ensure(c->soa_in[f], n * 4))) return st;
-      SPL_CK(cudaMemcpyAsync(c->soa_in[f].p, soa[f], n * 4, cudaMemcpyHostToDevice, s));
-      soa[f] = as<float>(c->soa_in[f]);
+    const float **f[8] = {&soa.x, &soa.y, &soa.z, &soa.r, &soa.I, &soa.cr, &soa.cg, &soa.cb};
+    for (int k = 0; k < 8; ++k) {
+      if (!*f[k]) continue;
+      if ((st = ensure(c->soa_in[k], n * 4))) return st;
+      SPL_CK(cudaMemcpyAsync(c->soa_in[k].p, *f[k], n * 4, cudaMemcpyHostToDevice, s));
+      *f[k] = as<float>(c->soa_in[k]);
     }
     if (p->type) {
       if ((st = ensure(c->soa_in[8], n * 2))) return st;
       SPL_CK(cudaMemcpyAsync(c->soa_in[8].p, p->type, n * 2, cudaMemcpyHostToDevice, s));
-      type_dev = as<uint16_t>(c->soa_in[8]);
+      soa.type = as<uint16_t>(c->soa_in[8]);
     }
   }
   cudaEventRecord(c->ev[1], s);
 
-  // ---- project + colourise ------------------------------------------------
+  // ---- project + colourise, active particles compacted -----------------------
   spl::ProjectOut po;
-  po.pos = as<float4>(c->pos);
-  po.col = as<float4>(c->col);
-  po.active = as<uint8_t>(c->active);
-  po.count = as<uint32_t>(c->count);
-  po.key = do_sort ? as<uint32_t>(c->key) : nullptr;
+  std::memset(&po, 0, sizeof(po));
+  po.pos_c = as<float4>(c->pos_c);
+  po.col_c = as<float4>(c->col_c);
+  po.idx_c = as<uint32_t>(c->idx_c);
+  po.count_c = as<uint32_t>(c->count);
+  po.key_c = do_sort ? as<uint32_t>(c->key) : nullptr;
+  po.n_act = d_nact;
+  po.state = as<unsigned long long>(c->pstate);
+  po.tile_ctr = d_ptile;
   po.err = d_err;
-  if (p->layout == SPL_LAYOUT_AOS)
-    spl::launch_project_aos(aos_dev, n, pc, po, s);
-  else
-    spl::launch_project_soa(soa[0], soa[1], soa[2], soa[3], soa[4], soa[5], soa[6], soa[7],
-                            type_dev, n, pc, po, s);
+  spl::launch_project(aos_dev, &soa, n, pc, po, true, s);
   if (n > 0) ++launches;
+  uint32_t nact_h = 0;
+  SPL_CK(cudaMemcpyAsync(&nact_h, d_nact, 4, cudaMemcpyDeviceToHost, s));
   cudaEventRecord(c->ev[2], s);
+  SPL_CK(cudaStreamSynchronize(s));
+  const int64_t na = nact_h;
 
-  // ---- depth sort (a_eq_e=false), splotch_host.cc:805-815 ------------------
+  // ---- depth sort of the active particles (a_eq_e=false), splotch_host.cc:805-815
+  // The reference sorts every particle; a stable sort of all of them visits the
+  // active ones in exactly the order of this stable sort of the active subset.
   const uint32_t *order = nullptr;
-  if (do_sort && n > 0) {
+  if (do_sort && na > 0) {
     spl::radix_sort_pairs(as<uint32_t>(c->key), nullptr, as<uint32_t>(c->ktmp),
                           as<uint32_t>(c->vtmp), as<uint32_t>(c->key) /*unused out*/,
-                          as<uint32_t>(c->perm), n, 0, 32, false, c->scratch.p, s, &launches,
+                          as<uint32_t>(c->perm), na, 0, 32, false, c->scratch.p, s, &launches,
                           d_err, onesweep);
     order = as<uint32_t>(c->perm);
   }
@@ -399,14 +437,14 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   // tile counts in visiting order (one gather; the sort's key scratch is free)
   const uint32_t *count_seq = as<uint32_t>(c->count);
   if (order) {
-    spl::launch_gather_u32(as<uint32_t>(c->count), order, n, as<uint32_t>(c->ktmp), s);
+    spl::launch_gather_u32(as<uint32_t>(c->count), order, na, as<uint32_t>(c->ktmp), s);
     ++launches;
     count_seq = as<uint32_t>(c->ktmp);
   }
   uint64_t *off = as<uint64_t>(c->off);
-  spl::scan_counts(count_seq, nullptr, n, off, c->scratch.p, s, &launches);
+  spl::scan_counts(count_seq, nullptr, na, off, c->scratch.p, s, &launches);
   uint64_t ne = 0;
-  SPL_CK(cudaMemcpyAsync(&ne, off + n, 8, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaMemcpyAsync(&ne, off + na, 8, cudaMemcpyDeviceToHost, s));
   SPL_CK(cudaStreamSynchronize(s));
   if (ne >= 0xffffffffULL) return fail(SPL_ERR_CAPACITY, "more than 2^32-1 bin entries");
   if ((st = ensure(c->tkey, ne * 4)) || (st = ensure(c->tval, ne * 4)) ||
@@ -416,7 +454,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   size_t rs2 = spl::radix_scratch_bytes((int64_t)ne);
   if ((st = ensure(c->scratch, rs2))) return st;
   if (ne > 0) {
-    spl::launch_emit(as<float4>(c->pos), count_seq, order, off, n, g,
+    spl::launch_emit(as<float4>(c->pos_c), count_seq, order, off, na, g,
                      as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->wide_list),
                      d_wide_n, s);
     launches += 2;
@@ -448,8 +486,8 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
 
   // ---- splat ---------------------------------------------------------------------
   spl::SplatArgs sa;
-  sa.pos = as<float4>(c->pos);
-  sa.col = as<float4>(c->col);
+  sa.pos = as<float4>(c->pos_c);
+  sa.col = as<float4>(c->col_c);
   sa.entries = as<uint32_t>(c->tval_s);
   sa.tile_start = as<uint32_t>(c->tile_start);
   sa.tile_order = as<uint32_t>(c->tord);
@@ -474,25 +512,33 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   if (out->memspace == SPL_MEM_HOST)
     SPL_CK(cudaMemcpyAsync(out->pic, c->pic.p, (size_t)xres * yres * 12, cudaMemcpyDeviceToHost,
                            s));
+  // remembered for the test hooks (full-form projection on demand)
+  c->last_pc = pc;
+  c->last_aos = aos_dev;
+  c->last_soa = soa;
   if (writeback == SPL_WRITEBACK_FULL && n > 0) {
-    void *dst = p->memspace == SPL_MEM_DEVICE ? p->aos : nullptr;
-    if (!dst) {
-      if ((st = ensure(c->aos_out, n * 36))) return st;
-      dst = c->aos_out.p;
+    // the reference's side effects: every particle projected and colourised,
+    // the whole array stably sorted when a_eq_e is false
+    if ((st = project_full(c, n, do_sort, &launches))) return st;
+    const uint32_t *perm_all = nullptr;
+    if (do_sort) {
+      spl::radix_sort_pairs(as<uint32_t>(c->key), nullptr, as<uint32_t>(c->ktmp),
+                            as<uint32_t>(c->vtmp), as<uint32_t>(c->key), as<uint32_t>(c->perm),
+                            n, 0, 32, false, c->scratch.p, s, &launches, d_err, onesweep);
+      perm_all = as<uint32_t>(c->perm);
     }
-    // a device-resident AoS is read by the project kernel already; the
-    // writeback permutes, so it goes through a separate buffer first
-    if (p->memspace == SPL_MEM_DEVICE) {
-      if ((st = ensure(c->aos_out, n * 36))) return st;
-      spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
-                                aos_dev, 1, order, n, c->aos_out.p, s);
-      SPL_CK(cudaMemcpyAsync(p->aos, c->aos_out.p, n * 36, cudaMemcpyDeviceToDevice, s));
-    } else {
-      spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
-                                aos_dev, 1, order, n, dst, s);
-      SPL_CK(cudaMemcpyAsync(p->aos, dst, n * 36, cudaMemcpyDeviceToHost, s));
-    }
+    if ((st = ensure(c->aos_out, n * 36))) return st;
+    spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
+                              aos_dev ? aos_dev : (const void *)soa.type,
+                              aos_dev ? 1 : (soa.type ? 2 : 0), perm_all, n, c->aos_out.p, s);
     ++launches;
+    SPL_CK(cudaMemcpyAsync(p->aos, c->aos_out.p, n * 36,
+                           p->memspace == SPL_MEM_DEVICE ? cudaMemcpyDeviceToDevice
+                                                         : cudaMemcpyDeviceToHost,
+                           s));
+    c->has_order = false;  // the compact order buffers were reused
+  } else {
+    c->has_order = order != nullptr;
   }
   cudaEventRecord(c->ev[6], s);
   uint32_t words[3] = {0, 0, 0};  // error word, wide-particle count, FP64 fallbacks
@@ -501,15 +547,16 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   SPL_CK(cudaGetLastError());
   const uint32_t err = words[0];
   if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
-  if (err & 2u) return fail(SPL_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  if (err & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
   c->stats.n_fallback = words[2];
   c->stats.n_wide = words[1];
 
   c->n = n;
+  c->na = na;
   c->ne = (int64_t)ne;
   c->ntiles = ntiles;
-  c->has_order = order != nullptr;
   c->last_T = T;
+  c->writeback_done = writeback == SPL_WRITEBACK_FULL;
   spl_stats &S = c->stats;
   cudaEventElapsedTime(&S.h2d_ms, c->ev[0], c->ev[1]);
   cudaEventElapsedTime(&S.project_ms, c->ev[1], c->ev[2]);
@@ -521,7 +568,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   S.n_entries = (int64_t)ne;
   S.n_tiles = ntiles;
   S.kernel_launches = launches;
-  S.n_active = -1;
+  S.n_active = na;
   return SPL_OK;
 }
 
@@ -529,11 +576,11 @@ spl_status spl_debug_get_projected(spl_context *c, void *aos_out, int64_t n) {
   if (!c || !aos_out || n != c->n) return fail(SPL_ERR_INVALID, "bad arguments");
   SPL_CK(cudaSetDevice(c->device));
   spl_status st;
+  int launches = 0;
+  if ((st = project_full(c, n, false, &launches))) return st;
   if ((st = ensure(c->aos_out, n * 36))) return st;
-  // type comes from the AoS input copy when there is one; SoA types from soa_in
-  const void *tsrc = c->aos_in.p;
-  int kind = 1;
-  if (!tsrc) { tsrc = c->soa_in[8].p; kind = tsrc ? 2 : 0; }
+  const void *tsrc = c->last_aos ? c->last_aos : (const void *)c->last_soa.type;
+  const int kind = c->last_aos ? 1 : (c->last_soa.type ? 2 : 0);
   spl::launch_writeback_aos(as<float4>(c->pos), as<float4>(c->col), as<uint8_t>(c->active),
                             tsrc, kind, nullptr, n, c->aos_out.p, c->stream);
   SPL_CK(cudaMemcpyAsync(aos_out, c->aos_out.p, n * 36, cudaMemcpyDeviceToHost, c->stream));
@@ -570,14 +617,21 @@ spl_status spl_debug_count_fragments(spl_context *c, int64_t *frags_out) {
   return SPL_OK;
 }
 
-spl_status spl_debug_get_order(spl_context *c, uint32_t *perm_out, int64_t n) {
-  if (!c || !perm_out || n != c->n) return fail(SPL_ERR_INVALID, "bad arguments");
+spl_status spl_debug_get_order(spl_context *c, uint32_t *order_out, int64_t cap,
+                               int64_t *n_out) {
+  if (!c || !n_out) return fail(SPL_ERR_INVALID, "bad arguments");
   SPL_CK(cudaSetDevice(c->device));
-  if (!c->has_order) {
-    for (int64_t i = 0; i < n; ++i) perm_out[i] = (uint32_t)i;
-    return SPL_OK;
+  *n_out = c->na;
+  if (c->na == 0) return SPL_OK;
+  if (!order_out || cap < c->na) return fail(SPL_ERR_CAPACITY, "order buffer too small");
+  if (c->writeback_done) return fail(SPL_ERR_UNSUPPORTED, "order not kept after a writeback");
+  std::vector<uint32_t> idx(c->na), perm;
+  SPL_CK(cudaMemcpy(idx.data(), c->idx_c.p, c->na * 4, cudaMemcpyDeviceToHost));
+  if (c->has_order) {
+    perm.resize(c->na);
+    SPL_CK(cudaMemcpy(perm.data(), c->perm.p, c->na * 4, cudaMemcpyDeviceToHost));
   }
-  SPL_CK(cudaMemcpy(perm_out, c->perm.p, n * 4, cudaMemcpyDeviceToHost));
+  for (int64_t s = 0; s < c->na; ++s) order_out[s] = idx[c->has_order ? perm[s] : s];
   return SPL_OK;
 }
 
@@ -588,13 +642,16 @@ spl_status spl_debug_get_bins(spl_context *c, int64_t *tile_start_out, int64_t n
   if (cap < c->ne || (c->ne > 0 && !entries_out))
     return fail(SPL_ERR_CAPACITY, "entries buffer too small: need " + std::to_string(c->ne));
   SPL_CK(cudaSetDevice(c->device));
-  std::string tmp;
-  uint32_t *ts = new uint32_t[ntp1];
-  cudaError_t e = cudaMemcpy(ts, c->tile_start.p, ntp1 * 4, cudaMemcpyDeviceToHost);
+  std::vector<uint32_t> ts(ntp1);
+  SPL_CK(cudaMemcpy(ts.data(), c->tile_start.p, ntp1 * 4, cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < ntp1; ++i) tile_start_out[i] = ts[i];
-  delete[] ts;
-  if (e != cudaSuccess) return fail(SPL_ERR_CUDA, cudaGetErrorString(e));
-  if (c->ne > 0) SPL_CK(cudaMemcpy(entries_out, c->tval_s.p, c->ne * 4, cudaMemcpyDeviceToHost));
+  if (c->ne > 0) {
+    // entries hold ranks among active particles; report particle indices
+    std::vector<uint32_t> idx(c->na);
+    SPL_CK(cudaMemcpy(idx.data(), c->idx_c.p, c->na * 4, cudaMemcpyDeviceToHost));
+    SPL_CK(cudaMemcpy(entries_out, c->tval_s.p, c->ne * 4, cudaMemcpyDeviceToHost));
+    for (int64_t i = 0; i < c->ne; ++i) entries_out[i] = idx[entries_out[i]];
+  }
   return SPL_OK;
 }
 

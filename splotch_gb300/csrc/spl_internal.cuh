@@ -179,20 +179,32 @@ __device__ __forceinline__ int for_each_tile(float x, float y, float r, const Ti
 // ---------------------------------------------------------------------------
 // Launch wrappers (defined in the .cu files).
 struct ProjectOut {
+  // full form, indexed by particle
   float4 *pos;      // x, y, r, z   (projected)
   float4 *col;      // e.r, e.g, e.b, I (colourised)
   uint8_t *active;
-  uint32_t *count;  // tiles per particle (binning circle test)
-  uint32_t *key;    // sort key (when sort_type != 0)
+  uint32_t *count;  // tiles per particle (binning circle test), may be null
+  uint32_t *key;    // sort key (when sort_type != 0), may be null
+  // compact form, indexed by rank among active particles (ascending index)
+  float4 *pos_c, *col_c;
+  uint32_t *idx_c;    // particle index of each active particle
+  uint32_t *count_c;
+  uint32_t *key_c;    // may be null
+  uint32_t *n_act;    // number of active particles (zeroed by the caller)
+  unsigned long long *state;  // one word per 256-particle tile, zeroed
+  uint32_t *tile_ctr;         // zeroed
   uint32_t *err;    // device error word
 };
 
-void launch_project_aos(const void *aos, int64_t n, const ProjConst &c, ProjectOut o,
-                        cudaStream_t s);
-void launch_project_soa(const float *x, const float *y, const float *z, const float *r,
-                        const float *I, const float *cr, const float *cg, const float *cb,
-                        const uint16_t *type, int64_t n, const ProjConst &c, ProjectOut o,
-                        cudaStream_t s);
+struct SoAIn {
+  const float *x, *y, *z, *r, *I, *cr, *cg, *cb;
+  const uint16_t *type;
+};
+
+// aos non-null: particle_sim records; otherwise soa.  compact selects the
+// active-only form (the render path) over the full form.
+void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                    ProjectOut o, bool compact, cudaStream_t s);
 // AoS writeback (particle_sim records) in visiting order (perm may be null).
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,
                           const void *type_src, int type_src_kind, const uint32_t *perm,

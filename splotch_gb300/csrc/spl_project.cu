@@ -168,8 +168,13 @@ __device__ __forceinline__ void palette(const ProjConst &c, int t, float v, floa
   b = rgb[3 * idx + 2];
 }
 
-__device__ __forceinline__ void project_one(const ProjConst &c, const PIn &in, int64_t i,
-                                            const ProjectOut &o) {
+struct POut {
+  float4 pos, col;
+  bool active;
+  uint32_t count, key;
+};
+
+__device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, uint32_t *err) {
   const float *m = c.mat;
   const bool fast = !c.exact_fp64;
   bool fell_back = false;
@@ -188,7 +193,7 @@ __device__ __forceinline__ void project_one(const ProjConst &c, const PIn &in, i
   bool active = false;
   const int t = in.type;
   if (t < 0 || t >= c.ptypes) {
-    atomicOr(o.err, 1u);  // type outside [0, ptypes): planck_fail in spirit
+    atomicOr(err, 1u);  // type outside [0, ptypes): planck_fail in spirit
   } else if (!(-z <= c.zmin) && !(-z >= c.zmax)) {
     float xfac2 = c.xfac;
     if (!c.projection) {
@@ -240,53 +245,42 @@ __device__ __forceinline__ void project_one(const ProjConst &c, const PIn &in, i
     const uint32_t fb = __ballot_sync(am, fell_back);
     if (fb && (int)(threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(c.n_fallback, __popc(fb));
   }
-  o.pos[i] = make_float4(x, y, r, z);
-  o.col[i] = make_float4(er, eg, eb, I);
-  o.active[i] = active ? 1 : 0;
-  if (o.count) {
-    uint32_t cnt = 0;
-    if (active) {
-      Tiling g{c.T, c.ncx, c.ncy, c.rcell, c.cmid0};
-      cnt = (uint32_t)for_each_tile(x, y, r, g, [](int, int) {});
-    }
-    o.count[i] = cnt;
+  POut o;
+  o.pos = make_float4(x, y, r, z);
+  o.col = make_float4(er, eg, eb, I);
+  o.active = active;
+  o.count = 0;
+  if (active) {
+    Tiling g{c.T, c.ncx, c.ncy, c.rcell, c.cmid0};
+    o.count = (uint32_t)for_each_tile(x, y, r, g, [](int, int) {});
   }
-  if (o.key) {
-    uint32_t k;
-    switch (c.sort_type) {
-      case 1: k = fkey_asc(z); break;             // zcmp: z ascending
-      case 2: k = ~fkey_asc(er); break;           // vcmp1: e.r descending
-      case 3: k = fkey_asc(er); break;            // vcmp2: e.r ascending
-      default: k = ~fkey_asc(r); break;           // hcmp: r descending
-    }
-    o.key[i] = k;
+  switch (c.sort_type) {
+    case 1: o.key = fkey_asc(z); break;    // zcmp: z ascending
+    case 2: o.key = ~fkey_asc(er); break;  // vcmp1: e.r descending
+    case 3: o.key = fkey_asc(er); break;   // vcmp2: e.r ascending
+    case 4: o.key = ~fkey_asc(r); break;   // hcmp: r descending
+    default: o.key = 0u; break;
   }
+  return o;
 }
 
-__global__ void __launch_bounds__(256) k_project_aos(const uint8_t *__restrict__ aos,
-                                                     int64_t n, ProjConst c, ProjectOut o) {
-  // 4 particles = 144 bytes = 9 aligned float4 per thread group step when the
-  // base is 16-byte aligned; the simple strided form below lets L1 merge the
-  // 36-byte records of a warp into full sectors.
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+struct LoadAoS {
+  const uint8_t *aos;
+  __device__ __forceinline__ PIn operator()(int64_t i) const {
     const float *f = reinterpret_cast<const float *>(aos + i * 36);
     PIn in;
     in.er = __ldg(f + 0); in.eg = __ldg(f + 1); in.eb = __ldg(f + 2);
     in.x = __ldg(f + 3); in.y = __ldg(f + 4); in.z = __ldg(f + 5);
     in.r = __ldg(f + 6); in.I = __ldg(f + 7);
     in.type = __ldg(reinterpret_cast<const unsigned short *>(aos + i * 36 + 32));
-    project_one(c, in, i, o);
+    return in;
   }
-}
+};
 
-__global__ void __launch_bounds__(256) k_project_soa(
-    const float *__restrict__ x, const float *__restrict__ y, const float *__restrict__ z,
-    const float *__restrict__ r, const float *__restrict__ I, const float *__restrict__ cr,
-    const float *__restrict__ cg, const float *__restrict__ cb,
-    const uint16_t *__restrict__ type, int64_t n, ProjConst c, ProjectOut o) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+struct LoadSoA {
+  const float *x, *y, *z, *r, *I, *cr, *cg, *cb;
+  const uint16_t *type;
+  __device__ __forceinline__ PIn operator()(int64_t i) const {
     PIn in;
     in.x = __ldg(x + i); in.y = __ldg(y + i); in.z = __ldg(z + i);
     in.r = __ldg(r + i); in.I = __ldg(I + i);
@@ -294,7 +288,119 @@ __global__ void __launch_bounds__(256) k_project_soa(
     in.eg = cg ? __ldg(cg + i) : 0.f;
     in.eb = cb ? __ldg(cb + i) : 0.f;
     in.type = type ? (int)__ldg(type + i) : 0;
-    project_one(c, in, i, o);
+    return in;
+  }
+};
+
+// Every particle's projected state, indexed by particle (writeback, test hooks,
+// and the full-array depth sort that the reference's in-place sort implies).
+template <class L>
+__global__ void __launch_bounds__(256) k_project_full(L load, int64_t n, ProjConst c,
+                                                      ProjectOut o) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const POut p = project_core(c, load(i), o.err);
+    o.pos[i] = p.pos;
+    o.col[i] = p.col;
+    o.active[i] = p.active ? 1 : 0;
+    if (o.count) o.count[i] = p.count;
+    if (o.key) o.key[i] = p.key;
+  }
+}
+
+// Active particles only, compacted in ascending particle order.  Blocks take
+// 256-particle tiles in launch order from a counter; a block's output offset
+// is the number of active particles in all earlier tiles, found by a
+// decoupled look-back over published per-tile counts (bounded waits).
+constexpr uint32_t CP_SPIN_LIMIT = 1u << 22;
+
+// Warp-parallel decoupled look-back (called by one full warp): publishes this
+// tile's count, then reads 32 predecessors per step until one carries an
+// inclusive prefix, and returns the exclusive prefix.  State word: kind (2 bits:
+// 1 = tile count, 2 = inclusive prefix) | value (62 bits).
+__device__ __forceinline__ unsigned long long lookback_warp(unsigned long long *state,
+                                                            int64_t tile,
+                                                            unsigned long long tot,
+                                                            uint32_t *err) {
+  const int lane = threadIdx.x & 31;
+  volatile unsigned long long *vs = state;
+  constexpr unsigned long long VM = (1ull << 62) - 1ull;
+  if (lane == 0) vs[tile] = ((tile == 0 ? 2ull : 1ull) << 62) | tot;
+  unsigned long long excl = 0;
+  int64_t hi = tile - 1;
+  bool ok = true;
+  while (hi >= 0) {
+    const int64_t t = hi - lane;
+    unsigned long long v = 2ull << 62;  // before tile 0: an inclusive zero
+    if (t >= 0) {
+      uint32_t spins = 0;
+      v = vs[t];
+      while ((v >> 62) == 0) {
+        if (++spins > CP_SPIN_LIMIT) {
+          ok = false;
+          break;
+        }
+        if (spins > 64) __nanosleep(64);
+        v = vs[t];
+      }
+    }
+    const uint32_t inc = __ballot_sync(0xffffffffu, (v >> 62) == 2);
+    unsigned long long val = v & VM;
+    int stop = 32;
+    if (inc) {
+      stop = __ffs(inc) - 1;  // the nearest inclusive prefix
+      if (lane > stop) val = 0;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+    excl += val;
+    if (inc) break;
+    hi -= 32;
+  }
+  if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicOr(err, 2u);
+  if (lane == 0 && tile > 0) vs[tile] = (2ull << 62) | (excl + tot);
+  return excl;
+}
+
+template <class L>
+__global__ void __launch_bounds__(256) k_project_compact(L load, int64_t n, ProjConst c,
+                                                         ProjectOut o) {
+  __shared__ uint32_t s_tile, s_base, s_warp[8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tile = atomicAdd(o.tile_ctr, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const int64_t i = (int64_t)tile * 256 + threadIdx.x;
+  POut p;
+  p.active = false;
+  if (i < n) p = project_core(c, load(i), o.err);
+  const uint32_t bal = __ballot_sync(0xffffffffu, p.active);
+  if (lane == 0) s_warp[w] = __popc(bal);
+  __syncthreads();
+  if (w == 0) {
+    const uint32_t cnt = lane < 8 ? s_warp[lane] : 0u;
+    uint32_t inc = cnt;
+#pragma unroll
+    for (int d = 1; d < 8; d <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+      if (lane >= d) inc += t;
+    }
+    const uint32_t tot = __shfl_sync(0xffffffffu, inc, 7);
+    const unsigned long long excl = lookback_warp(o.state, tile, tot, o.err);
+    if (lane < 8) s_warp[lane] = inc - cnt;
+    if (lane == 0) {
+      s_base = (uint32_t)excl;
+      if (tot) atomicAdd(o.n_act, tot);
+    }
+  }
+  __syncthreads();
+  if (p.active) {
+    const uint32_t k = s_base + s_warp[w] + __popc(bal & ((1u << lane) - 1u));
+    o.pos_c[k] = p.pos;
+    o.col_c[k] = p.col;
+    o.idx_c[k] = (uint32_t)i;
+    o.count_c[k] = p.count;
+    if (o.key_c) o.key_c[k] = p.key;
   }
 }
 
@@ -331,18 +437,27 @@ int grid_for(int64_t n) {
 
 }  // namespace
 
-void launch_project_aos(const void *aos, int64_t n, const ProjConst &c, ProjectOut o,
-                        cudaStream_t s) {
+void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                    ProjectOut o, bool compact, cudaStream_t s) {
   if (n <= 0) return;
-  k_project_aos<<<grid_for(n), 256, 0, s>>>(static_cast<const uint8_t *>(aos), n, c, o);
-}
-
-void launch_project_soa(const float *x, const float *y, const float *z, const float *r,
-                        const float *I, const float *cr, const float *cg, const float *cb,
-                        const uint16_t *type, int64_t n, const ProjConst &c, ProjectOut o,
-                        cudaStream_t s) {
-  if (n <= 0) return;
-  k_project_soa<<<grid_for(n), 256, 0, s>>>(x, y, z, r, I, cr, cg, cb, type, n, c, o);
+  if (compact) {
+    const int64_t nb = (n + 255) / 256;
+    if (aos)
+      k_project_compact<<<(unsigned)nb, 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)},
+                                                      n, c, o);
+    else
+      k_project_compact<<<(unsigned)nb, 256, 0, s>>>(
+          LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
+          n, c, o);
+  } else {
+    if (aos)
+      k_project_full<<<grid_for(n), 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n, c,
+                                                 o);
+    else
+      k_project_full<<<grid_for(n), 256, 0, s>>>(
+          LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
+          n, c, o);
+  }
 }
 
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,

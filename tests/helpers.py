@@ -71,7 +71,8 @@ def assert_parity(g: FrameResult, o: OracleResult, tol: float = IMAGE_TOL) -> di
     bad = np.nonzero((gb != ob).any(axis=1))[0]
     assert bad.size == 0, (f"{bad.size} projected particles differ, first {bad[:5]}: "
                            f"gpu {g.projected[bad[:2]]} oracle {o.projected[bad[:2]]}")
-    want_order = o.order if o.order is not None else np.arange(n, dtype=np.uint32)
+    full = o.order if o.order is not None else np.arange(n, dtype=np.uint32)
+    want_order = full[o.projected["active"][full].astype(bool)]  # active particles, in order
     assert np.array_equal(g.order, want_order), "visiting order (sort permutation) differs"
     assert np.array_equal(g.tile_start, o.tile_start), "tile ranges differ"
     assert np.array_equal(g.entries, o.entries), "tile bin entries differ"
