@@ -194,22 +194,26 @@ def run_reference(args):
     return 0
 
 
-def roofline(stage_ms: dict, n: int, n_entries: int, frags: int, args, pk: dict,
-             a_eq_e: bool) -> tuple[dict, dict]:
-    """Per-stage rooflines; the top-level one is the dominant stage's."""
+def roofline(stage_ms: dict, n: int, n_act: int, n_entries: int, n_tiles: int, frags: int,
+             args, pk: dict, a_eq_e: bool) -> tuple[dict, dict]:
+    """Per-stage rooflines; the top-level one is the dominant stage's.
+    Algorithmic bytes: project reads every particle's SoA fields (x,y,z,r,I,
+    e.r,e.g,e.b: 32 B + type 2 B) and writes the projected record of each
+    active particle (x,y,r,z,rgb,I: 32 B); the depth sort reads and writes one
+    (key, index) pair per active particle (16 B); binning reads x,y,r of each
+    active particle (12 B), writes one 4-byte entry per (particle, tile) and
+    4 B per tile."""
     hbm = pk["hbm_gbs"]
     fp32_peak = 2 * 128 * 152 * pk["sm_max_mhz"] * 1e6 / 1e12  # TFLOP/s, nominal issue
     st = {}
-    # project+colourise: read SoA x,y,z,r,I,e(3),type (34 B), write x,y,r,z + rgb,I
-    # (32 B), active (1), tile count (4), sort key (4 when sorting)
-    proj_bytes = n * (34 + 32 + 1 + 4 + (0 if a_eq_e else 4))
+    proj_bytes = n * 34 + n_act * 32
     st["project"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": proj_bytes,
                      "achieved": proj_bytes / (stage_ms["project_ms"] * 1e-3) / 1e9}
     if not a_eq_e and stage_ms["sort_ms"] > 0:
-        sort_bytes = n * 16  # read key+index once, write once
+        sort_bytes = n_act * 16
         st["sort"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": sort_bytes,
                       "achieved": sort_bytes / (stage_ms["sort_ms"] * 1e-3) / 1e9}
-    bin_bytes = n * 12 + n_entries * 4
+    bin_bytes = n_act * 12 + n_entries * 4 + n_tiles * 4
     st["bin"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": bin_bytes,
                  "achieved": bin_bytes / (stage_ms["bin_ms"] * 1e-3) / 1e9}
     # splat: reference fragments x useful FP32 work per fragment
@@ -322,7 +326,8 @@ def run_gpu(args):
             dist.destroy_process_group()
         return 0
     pk = peaks()
-    top, st = roofline(stages, n, int(last["n_entries"]), frags, args, pk, bool(desc.a_eq_e))
+    top, st = roofline(stages, n, int(last["n_active"]), int(last["n_entries"]),
+                       int(last["n_tiles"]), frags, args, pk, bool(desc.a_eq_e))
     cb = None
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w)
