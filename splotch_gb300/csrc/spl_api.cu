@@ -27,7 +27,8 @@ struct spl_context {
   };
   Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
-      aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate;
+      aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
+      poff;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   // state of the last frame (for the debug getters)
   int64_t n = 0, na = 0, ne = 0, ntiles = 0;
@@ -167,8 +168,7 @@ spl_status project_full(spl_context *c, int64_t n, bool with_key, int *launches)
   po.err = as<uint32_t>(c->small);
   spl::ProjConst pc = c->last_pc;
   pc.n_fallback = nullptr;
-  spl::launch_project(c->last_aos, &c->last_soa, n, pc, po, false, c->stream);
-  if (n > 0) ++*launches;
+  spl::launch_project(c->last_aos, &c->last_soa, n, pc, po, false, c->stream, launches);
   return SPL_OK;
 }
 
@@ -209,7 +209,7 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->tile_start, &c->wide_list, &c->small, &c->pic, &c->pal_x,
                               &c->pal_rgb, &c->aos_out, &c->pal_thr, &c->pal_xff,
                               &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord, &c->pos_c,
-                              &c->col_c, &c->idx_c, &c->pstate};
+                              &c->col_c, &c->idx_c, &c->pstate, &c->poff};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
@@ -311,7 +311,8 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
       (st = ensure(c->idx_c, n * 4)) || (st = ensure(c->count, n * 4)) ||
       (st = ensure(c->off, (n + 1) * 8)) || (st = ensure(c->wide_list, n * 4)) ||
       (st = ensure(c->small, 256)) || (st = ensure(c->tile_start, (ntiles + 1) * 4)) ||
-      (st = ensure(c->pstate, (nprojtiles + 1) * 8)) ||
+      (st = ensure(c->pstate, (nprojtiles * 8 + 1) * 4)) ||
+      (st = ensure(c->poff, (nprojtiles * 8 + 1) * 4)) ||
       (st = ensure(c->pic, (size_t)xres * yres * 3 * 4)) ||
       (st = ensure(c->pal_x, (npal + 1) * 8)) || (st = ensure(c->pal_rgb, (npal + 1) * 12)))
     return st;
@@ -327,7 +328,6 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   uint32_t *d_err = as<uint32_t>(c->small);
   uint32_t *d_wide_n = d_err + 1;
   uint32_t *d_nact = d_err + 3;
-  uint32_t *d_ptile = d_err + 4;
 
   // palettes (a few KB)
   for (int t = 0; t < d->ptypes; ++t) {
@@ -369,7 +369,6 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     pc.pal_invff = as<float2>(c->pal_invff);
   }
   SPL_CK(cudaMemsetAsync(d_err, 0, 32, s));
-  SPL_CK(cudaMemsetAsync(c->pstate.p, 0, (nprojtiles + 1) * 8, s));
   pc.n_fallback = d_err + 2;
 
   cudaEventRecord(c->ev[0], s);
@@ -409,11 +408,11 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   po.count_c = as<uint32_t>(c->count);
   po.key_c = do_sort ? as<uint32_t>(c->key) : nullptr;
   po.n_act = d_nact;
-  po.state = as<unsigned long long>(c->pstate);
-  po.tile_ctr = d_ptile;
+  po.flags = as<uint32_t>(c->pstate);
+  po.word_off = as<uint32_t>(c->poff);
+  po.scan_scratch = c->scratch.p;
   po.err = d_err;
-  spl::launch_project(aos_dev, &soa, n, pc, po, true, s);
-  if (n > 0) ++launches;
+  spl::launch_project(aos_dev, &soa, n, pc, po, true, s, &launches);
   uint32_t nact_h = 0;
   SPL_CK(cudaMemcpyAsync(&nact_h, d_nact, 4, cudaMemcpyDeviceToHost, s));
   cudaEventRecord(c->ev[2], s);

@@ -190,9 +190,10 @@ struct ProjectOut {
   uint32_t *idx_c;    // particle index of each active particle
   uint32_t *count_c;
   uint32_t *key_c;    // may be null
-  uint32_t *n_act;    // number of active particles (zeroed by the caller)
-  unsigned long long *state;  // one word per 256-particle tile, zeroed
-  uint32_t *tile_ctr;         // zeroed
+  uint32_t *n_act;       // number of active particles
+  uint32_t *flags;       // activity bits, (n+31)/32 words
+  uint32_t *word_off;    // exclusive scan of the words' popcounts
+  void *scan_scratch;    // scan_scratch_bytes((n+31)/32)
   uint32_t *err;    // device error word
 };
 
@@ -204,7 +205,12 @@ struct SoAIn {
 // aos non-null: particle_sim records; otherwise soa.  compact selects the
 // active-only form (the render path) over the full form.
 void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
-                    ProjectOut o, bool compact, cudaStream_t s);
+                    ProjectOut o, bool compact, cudaStream_t s, int *launches);
+
+// Exclusive scan of popcount(words[i]) into out (nwords entries); the total
+// goes to *total.
+void scan_popc(const uint32_t *words, int64_t nwords, uint32_t *out, uint32_t *total,
+               void *scratch, cudaStream_t s, int *launches);
 // AoS writeback (particle_sim records) in visiting order (perm may be null).
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,
                           const void *type_src, int type_src_kind, const uint32_t *perm,

@@ -174,12 +174,15 @@ struct POut {
   uint32_t count, key;
 };
 
-__device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, uint32_t *err) {
+// Geometry of particle_project (splotch_host.cc:118-176): camera transform,
+// z cut, perspective, radius and intensity scaling, footprint test.  Returns
+// `active`; x,y,z,r,I hold what the reference leaves in the particle.
+__device__ __forceinline__ bool project_geom(const ProjConst &c, const PIn &in, float &x,
+                                             float &y, float &z, float &r, float &I,
+                                             bool &fell_back, uint32_t *err) {
   const float *m = c.mat;
   const bool fast = !c.exact_fp64;
-  bool fell_back = false;
   // TRANSFORM::TransPoint (kernel/transform.cxx:212-219), double in the reference
-  float x, y, z;
   if (!(fast && transpoint_fast(m, in.x, in.y, in.z, x) &&
         transpoint_fast(m + 4, in.x, in.y, in.z, y) &&
         transpoint_fast(m + 8, in.x, in.y, in.z, z))) {
@@ -188,40 +191,51 @@ __device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, 
     y = transpoint_fp64(m + 4, in.x, in.y, in.z);
     z = transpoint_fp64(m + 8, in.x, in.y, in.z);
   }
-  float r = in.r, I = in.I;
-  float er = in.er, eg = in.eg, eb = in.eb;
-  bool active = false;
+  r = in.r;
+  I = in.I;
   const int t = in.type;
   if (t < 0 || t >= c.ptypes) {
     atomicOr(err, 1u);  // type outside [0, ptypes): planck_fail in spirit
-  } else if (!(-z <= c.zmin) && !(-z >= c.zmax)) {
-    float xfac2 = c.xfac;
-    if (!c.projection) {
-      x = fadd(c.res2, fmul(x, xfac2));
-      y = fadd(fadd(c.res2, c.ycorr), fmul(y, xfac2));
-    } else {
-      xfac2 = fdiv(-c.res2, fmul(c.fovfct, z));
-      const float px = fmul(x, xfac2), py = fmul(y, xfac2);
-      // res2 + xshift + x*xfac2 in double, stored to float (splotch_host.cc:134-135)
-      if (!(fast && shift_fast(c.xsum_ff, px, x) && shift_fast(c.ysum_ff, py, y))) {
-        fell_back = fell_back || fast;
-        x = __double2float_rn(dadd(c.xsum, (double)px));
-        y = __double2float_rn(dadd(c.ysum, (double)py));
-      }
+    return false;
+  }
+  if (-z <= c.zmin || -z >= c.zmax) return false;
+  float xfac2 = c.xfac;
+  if (!c.projection) {
+    x = fadd(c.res2, fmul(x, xfac2));
+    y = fadd(fadd(c.res2, c.ycorr), fmul(y, xfac2));
+  } else {
+    xfac2 = fdiv(-c.res2, fmul(c.fovfct, z));
+    const float px = fmul(x, xfac2), py = fmul(y, xfac2);
+    // res2 + xshift + x*xfac2 in double, stored to float (splotch_host.cc:134-135)
+    if (!(fast && shift_fast(c.xsum_ff, px, x) && shift_fast(c.ysum_ff, py, y))) {
+      fell_back = fell_back || fast;
+      x = __double2float_rn(dadd(c.xsum, (double)px));
+      y = __double2float_rn(dadd(c.ysum, (double)py));
     }
-    I = fmul(I, fdiv(c.half_bfak, r));
-    r = fmul(r, 2.f);
-    r = fmul(r, fmul(xfac2, c.smooth[t]));
-    const float rcorr = fdiv(fsqrt(fadd(fmul(r, r), c.minrad2)), r);
-    r = fmul(r, rcorr);
-    I = fdiv(I, rcorr);
-    const float rfacr = fmul(0.75f, r);
-    int minx = f2i(fadd(fsub(x, rfacr), 1.f));
-    int maxx = f2i(fadd(fadd(x, rfacr), 1.f));
-    int miny = f2i(fadd(fsub(y, rfacr), 1.f));
-    int maxy = f2i(fadd(fadd(y, rfacr), 1.f));
-    active = !(minx >= c.xres) && !(maxx <= 0) && max(minx, 0) < min(maxx, c.xres) &&
-             !(miny >= c.yres) && !(maxy <= 0) && max(miny, 0) < min(maxy, c.yres);
+  }
+  I = fmul(I, fdiv(c.half_bfak, r));
+  r = fmul(r, 2.f);
+  r = fmul(r, fmul(xfac2, c.smooth[t]));
+  const float rcorr = fdiv(fsqrt(fadd(fmul(r, r), c.minrad2)), r);
+  r = fmul(r, rcorr);
+  I = fdiv(I, rcorr);
+  const float rfacr = fmul(0.75f, r);
+  const int minx = f2i(fadd(fsub(x, rfacr), 1.f));
+  const int maxx = f2i(fadd(fadd(x, rfacr), 1.f));
+  const int miny = f2i(fadd(fsub(y, rfacr), 1.f));
+  const int maxy = f2i(fadd(fadd(y, rfacr), 1.f));
+  return !(minx >= c.xres) && !(maxx <= 0) && max(minx, 0) < min(maxx, c.xres) &&
+         !(miny >= c.yres) && !(maxy <= 0) && max(miny, 0) < min(maxy, c.yres);
+}
+
+__device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, uint32_t *err) {
+  const bool fast = !c.exact_fp64;
+  bool fell_back = false;
+  float x, y, z, r, I;
+  float er = in.er, eg = in.eg, eb = in.eb;
+  const int t = in.type;
+  const bool active = project_geom(c, in, x, y, z, r, I, fell_back, err);
+  {
     if (active) {  // particle_colorize (splotch_host.cc:276-282)
       if (!c.colvec[t]) {
         float pr, pg, pb;
@@ -308,99 +322,72 @@ __global__ void __launch_bounds__(256) k_project_full(L load, int64_t n, ProjCon
   }
 }
 
-// Active particles only, compacted in ascending particle order.  Blocks take
-// 256-particle tiles in launch order from a counter; a block's output offset
-// is the number of active particles in all earlier tiles, found by a
-// decoupled look-back over published per-tile counts (bounded waits).
-constexpr uint32_t CP_SPIN_LIMIT = 1u << 22;
-
-// Warp-parallel decoupled look-back (called by one full warp): publishes this
-// tile's count, then reads 32 predecessors per step until one carries an
-// inclusive prefix, and returns the exclusive prefix.  State word: kind (2 bits:
-// 1 = tile count, 2 = inclusive prefix) | value (62 bits).
-__device__ __forceinline__ unsigned long long lookback_warp(unsigned long long *state,
-                                                            int64_t tile,
-                                                            unsigned long long tot,
-                                                            uint32_t *err) {
+// Active particles only, compacted in ascending particle order, in three
+// deterministic kernels (no inter-block waits):
+//   k_project_flags  : activity of every particle, one bit each, 32 per word
+//   (scan)           : exclusive scan of the words' population counts
+//   k_project_dense  : each block expands its words into a dense list of
+//                      active particles, projects and colourises them with
+//                      all lanes busy, and writes the compact records
+template <class L>
+__global__ void __launch_bounds__(256) k_project_flags(L load, int64_t n, ProjConst c,
+                                                       uint32_t *__restrict__ flags,
+                                                       uint32_t *err) {
   const int lane = threadIdx.x & 31;
-  volatile unsigned long long *vs = state;
-  constexpr unsigned long long VM = (1ull << 62) - 1ull;
-  if (lane == 0) vs[tile] = ((tile == 0 ? 2ull : 1ull) << 62) | tot;
-  unsigned long long excl = 0;
-  int64_t hi = tile - 1;
-  bool ok = true;
-  while (hi >= 0) {
-    const int64_t t = hi - lane;
-    unsigned long long v = 2ull << 62;  // before tile 0: an inclusive zero
-    if (t >= 0) {
-      uint32_t spins = 0;
-      v = vs[t];
-      while ((v >> 62) == 0) {
-        if (++spins > CP_SPIN_LIMIT) {
-          ok = false;
-          break;
-        }
-        if (spins > 64) __nanosleep(64);
-        v = vs[t];
-      }
+  const int64_t nwords = (n + 31) / 32;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nwords;
+       w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t i = w * 32 + lane;
+    bool active = false;
+    if (i < n) {
+      const PIn in = load(i);
+      float x, y, z, r, I;
+      bool fb = false;
+      active = project_geom(c, in, x, y, z, r, I, fb, err);
     }
-    const uint32_t inc = __ballot_sync(0xffffffffu, (v >> 62) == 2);
-    unsigned long long val = v & VM;
-    int stop = 32;
-    if (inc) {
-      stop = __ffs(inc) - 1;  // the nearest inclusive prefix
-      if (lane > stop) val = 0;
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
-    excl += val;
-    if (inc) break;
-    hi -= 32;
+    const uint32_t bits = __ballot_sync(0xffffffffu, active);
+    if (lane == 0) flags[w] = bits;
   }
-  if (!__all_sync(0xffffffffu, ok) && lane == 0) atomicOr(err, 2u);
-  if (lane == 0 && tile > 0) vs[tile] = (2ull << 62) | (excl + tot);
-  return excl;
 }
 
+constexpr int DW = 64;  // flag words per dense block (2048 particles)
+
 template <class L>
-__global__ void __launch_bounds__(256) k_project_compact(L load, int64_t n, ProjConst c,
-                                                         ProjectOut o) {
-  __shared__ uint32_t s_tile, s_base, s_warp[8];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (threadIdx.x == 0) s_tile = atomicAdd(o.tile_ctr, 1u);
+__global__ void __launch_bounds__(256) k_project_dense(L load, int64_t n, ProjConst c,
+                                                       const uint32_t *__restrict__ flags,
+                                                       const uint32_t *__restrict__ word_off,
+                                                       ProjectOut o) {
+  __shared__ uint32_t s_list[DW * 32];
+  __shared__ uint32_t s_cnt[DW];
+  const int64_t nwords = (n + 31) / 32;
+  const int64_t w0 = (int64_t)blockIdx.x * DW;
+  const int nw = (int)min((int64_t)DW, nwords - w0);
+  uint32_t f = 0;
+  if ((int)threadIdx.x < nw) f = __ldg(flags + w0 + threadIdx.x);
+  if (threadIdx.x < DW) s_cnt[threadIdx.x] = __popc(f);
   __syncthreads();
-  const uint32_t tile = s_tile;
-  const int64_t i = (int64_t)tile * 256 + threadIdx.x;
-  POut p;
-  p.active = false;
-  if (i < n) p = project_core(c, load(i), o.err);
-  const uint32_t bal = __ballot_sync(0xffffffffu, p.active);
-  if (lane == 0) s_warp[w] = __popc(bal);
-  __syncthreads();
-  if (w == 0) {
-    const uint32_t cnt = lane < 8 ? s_warp[lane] : 0u;
-    uint32_t inc = cnt;
-#pragma unroll
-    for (int d = 1; d < 8; d <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
-      if (lane >= d) inc += t;
-    }
-    const uint32_t tot = __shfl_sync(0xffffffffu, inc, 7);
-    const unsigned long long excl = lookback_warp(o.state, tile, tot, o.err);
-    if (lane < 8) s_warp[lane] = inc - cnt;
-    if (lane == 0) {
-      s_base = (uint32_t)excl;
-      if (tot) atomicAdd(o.n_act, tot);
+  if ((int)threadIdx.x < nw) {  // expand word t's set bits at its local offset
+    uint32_t pos = __ldg(word_off + w0 + threadIdx.x) - __ldg(word_off + w0);
+    const int64_t ibase = (w0 + threadIdx.x) * 32;
+    while (f) {
+      const int b = __ffs(f) - 1;
+      f &= f - 1;
+      s_list[pos++] = (uint32_t)(ibase + b);
     }
   }
+  uint32_t nloc = 0;
+  for (int k = 0; k < nw; ++k) nloc += s_cnt[k];
   __syncthreads();
-  if (p.active) {
-    const uint32_t k = s_base + s_warp[w] + __popc(bal & ((1u << lane) - 1u));
-    o.pos_c[k] = p.pos;
-    o.col_c[k] = p.col;
-    o.idx_c[k] = (uint32_t)i;
-    o.count_c[k] = p.count;
-    if (o.key_c) o.key_c[k] = p.key;
+  const uint32_t base = nw > 0 ? __ldg(word_off + w0) : 0u;
+  for (uint32_t k = threadIdx.x; k < nloc; k += blockDim.x) {
+    const uint32_t i = s_list[k];
+    const POut p = project_core(c, load(i), o.err);
+    const uint32_t dst = base + k;
+    o.pos_c[dst] = p.pos;
+    o.col_c[dst] = p.col;
+    o.idx_c[dst] = i;
+    o.count_c[dst] = p.count;
+    if (o.key_c) o.key_c[dst] = p.key;
   }
 }
 
@@ -438,25 +425,34 @@ int grid_for(int64_t n) {
 }  // namespace
 
 void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
-                    ProjectOut o, bool compact, cudaStream_t s) {
-  if (n <= 0) return;
+                    ProjectOut o, bool compact, cudaStream_t s, int *launches) {
+  if (n <= 0) {
+    if (compact) cudaMemsetAsync(o.n_act, 0, 4, s);
+    return;
+  }
+  const LoadAoS la{static_cast<const uint8_t *>(aos)};
+  const LoadSoA ls{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type};
   if (compact) {
-    const int64_t nb = (n + 255) / 256;
-    if (aos)
-      k_project_compact<<<(unsigned)nb, 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)},
-                                                      n, c, o);
-    else
-      k_project_compact<<<(unsigned)nb, 256, 0, s>>>(
-          LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
-          n, c, o);
+    const int64_t nwords = (n + 31) / 32;
+    int fb = (int)((nwords * 32 + 255) / 256);
+    if (fb > 152 * 16) fb = 152 * 16;
+    const unsigned db = (unsigned)((nwords + DW - 1) / DW);
+    if (aos) {
+      k_project_flags<<<fb, 256, 0, s>>>(la, n, c, o.flags, o.err);
+      scan_popc(o.flags, nwords, o.word_off, o.n_act, o.scan_scratch, s, launches);
+      k_project_dense<<<db, 256, 0, s>>>(la, n, c, o.flags, o.word_off, o);
+    } else {
+      k_project_flags<<<fb, 256, 0, s>>>(ls, n, c, o.flags, o.err);
+      scan_popc(o.flags, nwords, o.word_off, o.n_act, o.scan_scratch, s, launches);
+      k_project_dense<<<db, 256, 0, s>>>(ls, n, c, o.flags, o.word_off, o);
+    }
+    if (launches) *launches += 2;
   } else {
     if (aos)
-      k_project_full<<<grid_for(n), 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n, c,
-                                                 o);
+      k_project_full<<<grid_for(n), 256, 0, s>>>(la, n, c, o);
     else
-      k_project_full<<<grid_for(n), 256, 0, s>>>(
-          LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
-          n, c, o);
+      k_project_full<<<grid_for(n), 256, 0, s>>>(ls, n, c, o);
+    if (launches) *launches += 1;
   }
 }
 

@@ -337,6 +337,10 @@ struct LoadU32 {
   const uint32_t *p;
   __device__ __forceinline__ uint32_t operator()(int64_t i) const { return __ldg(p + i); }
 };
+struct LoadPopc {
+  const uint32_t *w;
+  __device__ __forceinline__ uint32_t operator()(int64_t i) const { return __popc(__ldg(w + i)); }
+};
 struct LoadCountOrdered {
   const uint32_t *count;
   const uint32_t *order;
@@ -430,6 +434,11 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
 
 size_t scan_scratch_bytes(int64_t n) {
   return (size_t)((n + SC_TILE - 1) / SC_TILE + 64) * sizeof(uint64_t);
+}
+
+void scan_popc(const uint32_t *words, int64_t nwords, uint32_t *out, uint32_t *total,
+               void *scratch, cudaStream_t s, int *launches) {
+  exclusive_scan<uint32_t>(LoadPopc{words}, nwords, out, total, scratch, s, launches);
 }
 
 void scan_counts(const uint32_t *count, const uint32_t *order, int64_t n, uint64_t *off,
