@@ -1,0 +1,86 @@
+"""Generate the golden fixtures from the reference's own compiled code.
+
+Runs where the reference sources are available: builds oracle/_ref with
+oracle/build_ref.sh, runs the reference's particle_project + particle_colorize,
+render_new and host_rendering on small seeded inputs, and stores inputs and
+outputs under tests/golden/*.npz.  The CPU tests pin the oracle restatement to
+these files; the GPU tests compare the CUDA path with them.
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle  # noqa: E402
+from splotch_gb300 import RenderContext, synth  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def cases():
+    yield "additive", synth.plain_additive(n=3000, xres=96, yres=80, tile=16)
+    yield "absorption", synth.plain_absorption(n_gas=2400, n_star=600, xres=96, yres=54,
+                                               tile=16, order="btf")
+    w = synth.plain_additive(n=2500, xres=72, yres=90, tile=12, seed=7)
+    w.params.params.update({"projection": "F", "zmin": "185.0", "zmax": "232.5",
+                            "minrad_pix": "2.5", "smooth_factor0": "1.7",
+                            "brightness0": "0.6", "fov": "38.0"})
+    w.rc.b_brightness = 1.3
+    yield "variants_orthographic", w
+    w = synth.plain_absorption(n_gas=2000, n_star=500, xres=80, yres=80, tile=10, seed=9)
+    w.rc.campos = np.array([620.0, 430.0, -180.0])
+    w.rc.centerpos = np.array([600.0, 420.0, -170.0])
+    w.rc.lookat = np.array([250.0, 240.0, 260.0])
+    w.rc.sky = np.array([0.1, 1.0, 0.2])
+    w.params.params.update({"gray_absorption": "0.35", "brightness1": "2.0"})
+    yield "tilted_camera_center", w
+
+
+def main() -> int:
+    if not oracle.build_ref():
+        print("reference sources not available; fixtures unchanged")
+        return 1
+    refs = {"simd": oracle.Ref(scalar=False), "scalar": oracle.Ref(scalar=True)}
+    port = oracle.Port()
+    for name, w in cases():
+        prm = dict(w.params.params)
+        rc: RenderContext = w.rc
+        xres, yres = int(prm["xres"]), int(prm.get("yres", prm["xres"]))
+        T = int(float(prm["tile_size_cpu"]))
+        a_eq_e = prm.get("a_eq_e", "T") in ("T", "True", "true")
+        gray = float(prm.get("gray_absorption", 0.2))
+        out = {"particles_in": w.particles.view(np.uint8).copy()}
+        proj = w.particles.copy()
+        refs["simd"].project_colorize(prm, rc, proj)
+        out["projected"] = proj.view(np.uint8).copy()
+        perm = port.sort_perm(proj, int(prm.get("sort_type", 1))) if not a_eq_e else None
+        ordered = proj[perm].copy() if perm is not None else proj.copy()
+        if perm is not None:
+            out["stable_perm"] = perm
+        for br, ref in refs.items():
+            out[f"render_new_{br}"] = ref.render_new(ordered.copy(), xres, yres, a_eq_e, gray, T)
+            out[f"host_rendering_{br}"] = ref.host_rendering(prm, rc, w.particles.copy())
+        pic64, frags = port.render_fp64(proj, perm, xres, yres, T, a_eq_e, gray)
+        out["render_fp64"] = pic64
+        out["fragments"] = np.array(frags)
+        meta = {"params": prm, "campos": list(rc.campos), "centerpos": list(rc.centerpos),
+                "lookat": list(rc.lookat), "sky": list(rc.sky), "b_brightness": rc.b_brightness,
+                "palettes": [None if p is None else {"x": p.x.tolist(), "rgb": p.rgb.tolist()}
+                             for p in rc.amap]}
+        out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(OUT / f"{name}.npz", **out)
+        print(f"{name}: {len(w.particles)} particles, {int(proj['active'].sum())} active, "
+              f"{frags} fragments")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
