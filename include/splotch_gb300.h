@@ -167,6 +167,37 @@ spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
 #define SPL_DEBUG_RADIX_REDUCE_SCAN 2
 spl_status spl_debug_set_options(spl_context *ctx, int flags);
 
+/* ---- depth sort without allocation ------------------------------------ */
+/* No counterpart in the reference, which sorts the particle array on the host
+   with std::sort (splotch/splotch_host.cc:289-321).
+
+   Stable LSD radix sort of n (key, value) uint32 pairs in device memory,
+   ascending in the low key_bits bits of the key; equal keys keep their input
+   order.  It is the sort spl_render applies to the active particles' depth
+   keys, with all of its scratch in one fixed array inside the library, so the
+   call allocates nothing: for callers that must not allocate device memory
+   while they run (a render loop whose memory is all reserved up front, a
+   process whose device memory belongs to another allocator, code under a
+   fixed device-memory budget).  spl_render grows its buffers on demand and
+   does not suit them.
+
+   keys_in   device, 16-byte aligned, n keys
+   vals_in   device, n values; NULL sorts the indices 0..n-1
+   keys_out, vals_out  device, n entries each, overlapping neither input
+   key_bits  1..32
+   stream    cudaStream_t as void*, NULL = legacy default stream
+   The call only enqueues work on the stream.  n > SPL_NOALLOC_MAX_PAIRS
+   returns SPL_ERR_CAPACITY before anything is launched.  The scratch array
+   (about 19 MB per device) is shared by all calls on a device: calls that may
+   run at the same time, on different streams or host threads, race and
+   corrupt each other's results; serialise them.  The first call on a device
+   (n == 0 is enough) looks up the array's address with that device current;
+   make it before any stream capture begins. */
+#define SPL_NOALLOC_MAX_PAIRS (1 << 21)
+spl_status spl_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *vals_in,
+                                  uint32_t *keys_out, uint32_t *vals_out, int64_t n,
+                                  int key_bits, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

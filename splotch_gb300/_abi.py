@@ -26,8 +26,9 @@ EXPORTED = [
     "spl_last_error_string", "spl_version", "spl_frame_desc_defaults", "spl_camera_setup",
     "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
     "spl_debug_get_bins", "spl_debug_count_fragments", "spl_debug_set_options",
-    "spl_splat_config_count", "spl_splat_config_valid",
+    "spl_splat_config_count", "spl_splat_config_valid", "spl_sort_pairs_noalloc",
 ]
+SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
 
 
@@ -114,6 +115,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_debug_set_options": (C.c_int, [vp, C.c_int]),
         "spl_splat_config_count": (C.c_int, []),
         "spl_splat_config_valid": (C.c_int, [C.c_int, C.c_int]),
+        "spl_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, i64, C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

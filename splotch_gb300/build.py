@@ -19,7 +19,8 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsplgpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["spl_api.cu", "spl_project.cu", "spl_sort.cu", "spl_bin.cu", "spl_splat.cu"]
+CU_SOURCES = ["spl_api.cu", "spl_project.cu", "spl_sort.cu", "spl_bin.cu", "spl_splat.cu",
+              "spl_noalloc.cu"]
 CPP_SOURCES = ["spl_camera.cpp"]
 
 

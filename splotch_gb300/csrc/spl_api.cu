@@ -174,6 +174,8 @@ spl_status project_full(spl_context *c, int64_t n, bool with_key, int *launches)
 
 }  // namespace
 
+void spl::set_last_error(const char *msg) { g_err = msg; }
+
 extern "C" {
 
 const char *spl_last_error_string(void) { return g_err.c_str(); }

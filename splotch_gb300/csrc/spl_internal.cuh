@@ -230,6 +230,9 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
                      int bit0, int bit1, bool keys_needed, void *scratch, cudaStream_t s,
                      int *launches, uint32_t *err, bool onesweep);
 
+// Message returned by spl_last_error_string() on this host thread.
+void set_last_error(const char *msg);
+
 // Exclusive scan of count[order[s]] (order may be null) into off (n+1 slots;
 // off[n] = total).
 size_t scan_scratch_bytes(int64_t n);
