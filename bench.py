@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--order", default="ftb", choices=["ftb", "btf"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fwd-bwd", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="particle-count multiplier (profiling runs use a smaller frame)")
     return ap.parse_args()
@@ -237,6 +238,76 @@ def roofline(stage_ms: dict, n: int, n_act: int, n_entries: int, n_tiles: int, f
     return top, st
 
 
+def fwd_bwd(args, local: int) -> dict:
+    """Forward vs forward+backward on the differentiable-render workload: 4M
+    particles of the halo mixture, 1024x1024, additive and ordered absorption.
+    One step = render + dL/dpic of L = sum((pic - target)^2) + backward with
+    respect to I, colour, position, hsml and the camera position; inputs and
+    outputs resident in HBM, CUDA events on the render stream."""
+    import torch
+
+    import splotch_gb300 as sg
+    from splotch_gb300 import _abi, synth
+
+    dev = f"cuda:{local}"
+    out = {}
+    n = int(4_000_000 * min(args.scale, 1.0))
+    for mode in ("additive", "absorption"):
+        w = synth.differentiable(n=n, mode=mode, xres=1024, tile=args.tile, order=args.order)
+        r = sg.Renderer(local)
+        stream = torch.cuda.Stream(device=dev)
+        r.set_stream(stream.cuda_stream)
+        keep: list = []
+        desc = sg.frame_desc(w.params, w.rc, keep)
+        soa_t = {k: torch.from_numpy(v).to(dev) for k, v in
+                 synth.soa_from_aos(w.notes["target"]).items()}
+        soa = {k: torch.from_numpy(v).to(dev) for k, v in synth.soa_from_aos(w.particles).items()}
+        target = torch.zeros((desc.xres, desc.yres, 3), dtype=torch.float32, device=dev)
+        pic = torch.zeros_like(target)
+        r.render_soa(desc, soa_t, target)
+        grads = {f: torch.zeros(n, dtype=torch.float32, device=dev) for f in _abi.GRAD_FIELDS}
+
+        def step(backward: bool):
+            r.render_soa(desc, soa, pic)
+            if backward:
+                with torch.cuda.stream(stream):
+                    gpic = 2.0 * (pic - target)
+                r.backward(gpic, grads, device=True)
+
+        res = {}
+        for name, bw in (("fwd", False), ("fwd_bwd", True)):
+            r.set_differentiable(bw)  # the plain forward keeps nothing extra
+            for _ in range(args.warmup):
+                step(bw)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            fwd_total = bwd_total = 0.0
+            e0.record(stream)
+            for _ in range(args.steps):
+                step(bw)
+                s = r.stats()
+                fwd_total += s["total_ms"]
+                bwd_total += s["bwd_total_ms"] if bw else 0.0
+            e1.record(stream)
+            torch.cuda.synchronize()
+            res[name + "_ms"] = e0.elapsed_time(e1) / args.steps
+            res[name + "_render_call_ms"] = fwd_total / args.steps
+            if bw:
+                res["backward_call_ms"] = bwd_total / args.steps
+        st = r.stats()
+        res["ratio_fwd_bwd_over_fwd"] = res["fwd_bwd_ms"] / res["fwd_ms"]
+        res["fwd_bwd_mparticles_per_s"] = n / (res["fwd_bwd_ms"] * 1e-3) / 1e6
+        res["fwd_bwd_frames_per_s"] = 1e3 / res["fwd_bwd_ms"]
+        res["bwd_splat_ms"] = st["bwd_splat_ms"]
+        res["bwd_project_ms"] = st["bwd_project_ms"]
+        res["splat_ms"] = st["splat_ms"]
+        res["particles"] = n
+        res["active"] = int(st["n_active"])
+        out[mode] = res
+        r.close()
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -331,6 +402,7 @@ def run_gpu(args):
     cb = None
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w)
+    fb = None if args.no_fwd_bwd else fwd_bwd(args, local)
     line = {"metric": METRIC, "value": world * n / (ms * 1e-3) / 1e6, "unit": "Mparticles/s",
             "frames_per_s": world * 1e3 / ms, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -338,7 +410,7 @@ def run_gpu(args):
             "data": "synthetic (seeded halo mixture; no snapshot available)", "config": cfg,
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "roofline": top,
             "stages": st, "fragments": frags, "bin_entries": int(last["n_entries"]),
-            "cpu_baseline": cb}
+            "cpu_baseline": cb, "fwd_bwd": fb}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

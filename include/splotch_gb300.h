@@ -114,6 +114,8 @@ typedef struct {
   int kernel_launches; /* kernels launched by the call */
   int64_t n_fallback;  /* particles projected through the exact FP64 fallback */
   int64_t n_wide;      /* particles binned by the wide (many-tile) path */
+  /* last spl_render_backward: adjoint splat, chain rule, whole call */
+  float bwd_splat_ms, bwd_project_ms, bwd_total_ms;
 } spl_stats;
 
 /* ---- context ---------------------------------------------------------- */
@@ -166,6 +168,84 @@ spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
 #define SPL_DEBUG_EXACT_FP64 1
 #define SPL_DEBUG_RADIX_REDUCE_SCAN 2
 spl_status spl_debug_set_options(spl_context *ctx, int flags);
+
+/* ---- gradients ---------------------------------------------------------- */
+/* Per-particle gradient arrays (n floats each, by particle index, in
+   memspace; NULL = not wanted) and the camera-position gradient.  Colour:
+   for palette types d/d(colour value) lands in cr (cg, cb stay 0); for
+   color_is_vector types cr, cg, cb get d/d(r, g, b).  x, y, z are world
+   positions, r is the smoothing length (hsml) as read. */
+typedef struct {
+  int memspace; /* SPL_MEM_* */
+  float *I, *cr, *cg, *cb, *x, *y, *z, *r;
+  double campos[3]; /* out: d/dcampos (centerpos, lookat, sky held) */
+} spl_grads;
+
+/* No counterpart in the reference, which has no derivative of its renderer.
+   Gradients of a scalar loss L with respect to the inputs of the last frame
+   spl_render drew on ctx, given grad_pic = dL/dpic (the image's layout).
+   Coverage, tile lists and order are held at the forward's decisions (their
+   derivative is zero almost everywhere).  Needs that frame's inputs and, for
+   a device image, its output unchanged, and a forward without writeback.
+   Absorption frames are differentiated front to back from the stored final
+   image (no per-particle intermediates are kept). */
+spl_status spl_render_backward(spl_context *ctx, const spl_image *grad_pic, spl_grads *g);
+/* Ordered (a_eq_e = false) frames can only be differentiated when they were
+   rendered with this switch on: the forward then also keeps, per pixel, the
+   optical depth it composited and where its front-to-back pass stopped
+   (16 bytes per pixel, a few adds per fragment).  Off by default. */
+spl_status spl_context_set_differentiable(spl_context *ctx, int enable);
+
+/* ---- batched rendering ------------------------------------------------- */
+/* No counterpart in the reference, which renders one frame per
+   host_rendering call.  Many frames -- camera poses, resolutions, additive or
+   ordered modes, particle sets of uneven size -- are rendered by one launch of
+   a captured CUDA graph: projection of every frame, one stable depth sort and
+   one tile binning over all frames' active particles, and persistent splat
+   kernels that take (frame, tile) items from a work queue ordered
+   longest-list-first across all frames.  Buffer sizes come from a measured
+   plan (one plain render of every frame at create); a render whose counts
+   outgrow the plan re-plans and renders again.  Each frame's image equals the
+   image spl_render gives for that frame at the same tile size and launch
+   configuration, bit for bit. */
+typedef struct {
+  int set;              /* index into the particle sets */
+  spl_frame_desc desc;  /* the frame's keys; tile_size and splat_config are the batch's */
+  float *pic;           /* device image, x-major xres*yres*3 floats */
+} spl_batch_frame;
+
+typedef struct {
+  int tile_size;                /* 0: chosen by the autotuner among 8, 16, 32 */
+  int splat_config_additive;    /* -1: chosen by the autotuner */
+  int splat_config_absorption;  /* -1: chosen by the autotuner */
+  float capacity_margin;        /* buffer headroom over the measured counts (1.1);
+                                   below 1 forces a re-plan (test hook) */
+  int use_graph;                /* 1: capture and replay a CUDA graph; 0: launch eagerly */
+} spl_batch_options;
+
+typedef struct {
+  int tile_size, splat_config_additive, splat_config_absorption;
+  int graph;                    /* 1 when renders replay a captured graph */
+  int64_t cap_active, cap_entries, total_tiles;
+  int64_t n_active, n_entries;  /* last render */
+  float render_ms;              /* last spl_batch_render, launch to completion */
+  float tune_ms;                /* autotuning time spent in spl_batch_create */
+  int kernel_launches;          /* kernels per render */
+  int replans;                  /* capacity re-plans so far */
+} spl_batch_info;
+
+typedef struct spl_batch spl_batch;
+
+void spl_batch_options_defaults(spl_batch_options *o);
+/* Sets must be device-resident (AoS or SoA) and stay unchanged while the batch
+   lives; frame palettes are copied at create.  The batch uses its own stream. */
+spl_status spl_batch_create(spl_context *ctx, const spl_particles *sets, int nsets,
+                            const spl_batch_frame *frames, int nframes,
+                            const spl_batch_options *opt, spl_batch **out);
+/* Render every frame into its image; returns once they are complete. */
+spl_status spl_batch_render(spl_batch *b);
+spl_status spl_batch_get_info(const spl_batch *b, spl_batch_info *info);
+spl_status spl_batch_destroy(spl_batch *b);
 
 /* ---- depth sort without allocation ------------------------------------ */
 /* No counterpart in the reference, which sorts the particle array on the host

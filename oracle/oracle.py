@@ -149,6 +149,16 @@ class Port:
             ("spo_host_rendering", i32, [vp, vp, i64, i32, vp]),
             ("spo_splat_adjoint_fp64", i32,
              [vp, vp, i64, i32, i32, i32, i32, C.c_double, vp, vp, vp, vp, vp]),
+            ("spo_model_project_all", i32, [vp, vp, vp, i64, vp]),
+            ("spo_model_vjp_all", i32, [vp, vp, vp, i64, vp, vp, vp]),
+            ("spo_render_frozen_fp64", i64,
+             [vp, vp, vp, i64, i32, i32, i32, i32, C.c_double, vp]),
+            ("spo_render_frozen_vjp_fp64", i32,
+             [vp, vp, vp, i64, i32, i32, i32, i32, C.c_double, vp, vp]),
+            ("spo_grad_fp64", i32, [vp, vp, vp, vp, i64, i32, vp, vp, vp]),
+            ("spo_fd_particles", i32,
+             [vp, vp, vp, vp, i64, i32, vp, vp, i32, C.c_double, vp, vp]),
+            ("spo_fd_campos", i32, [vp, vp, vp, vp, i64, i32, vp, C.c_double, vp]),
         ]:
             f = getattr(lib, name)
             f.restype = res
@@ -222,6 +232,82 @@ class Port:
                                         float(np.float32(gray)), _vp(g), _vp(gx), _vp(gy),
                                         _vp(gr), _vp(ge))
         return gx, gy, gr, ge
+
+    # ---- differentiable FP64 model (checker of the adjoint path) ----------
+    # raw: particle_sim records before projection (world inputs); cov: the same
+    # records after project_colorize (their active flags, positions and radii
+    # fix coverage, bins and order).  Gradient columns: I, e.r, e.g, e.b, x, y,
+    # z, r (hsml).
+
+    GRAD_FIELDS = ("I", "er", "eg", "eb", "x", "y", "z", "r")
+
+    def model_project(self, params: dict, rc, raw, cov) -> np.ndarray:
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        w = np.zeros((len(raw), 6))
+        if self.lib.spo_model_project_all(C.byref(prm), _vp(raw), _vp(cov), len(raw), _vp(w)):
+            raise ValueError("degenerate matrix")
+        return w
+
+    def render_frozen_fp64(self, params: dict, cov, w, order) -> np.ndarray:
+        xres = int(_get(params, "xres", 800))
+        yres = int(_get(params, "yres", xres))
+        T = int(_get(params, "tile_size_cpu", 50.0))
+        a_eq_e = 1 if _get(params, "a_eq_e", True) else 0
+        gray = float(np.float32(_get(params, "gray_absorption", 0.2)))
+        pic = np.zeros((xres, yres, 3))
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        if self.lib.spo_render_frozen_fp64(_vp(cov), _vp(w), _vp(order), len(cov), xres, yres,
+                                           T, a_eq_e, gray, _vp(pic)) < 0:
+            raise RuntimeError("frozen render failed")
+        return pic
+
+    def grad_fp64(self, params: dict, rc, raw, cov, order, gpic):
+        """FP64 adjoint: dL/d(inputs) (n x 8) and dL/dcampos for L = sum(gpic*pic)."""
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        g = np.ascontiguousarray(gpic, dtype=np.float64)
+        grad = np.zeros((len(raw), 8))
+        gc = np.zeros(3)
+        if self.lib.spo_grad_fp64(C.byref(prm), _vp(raw), _vp(cov), _vp(order), len(raw),
+                                  prm.tile_size, _vp(g), _vp(grad), _vp(gc)):
+            raise RuntimeError("oracle gradient failed")
+        return grad, gc
+
+    def model_vjp(self, params: dict, rc, raw, cov, gw):
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        gw = np.ascontiguousarray(gw, dtype=np.float64)
+        grad = np.zeros((len(raw), 8))
+        gc = np.zeros(3)
+        if self.lib.spo_model_vjp_all(C.byref(prm), _vp(raw), _vp(cov), len(raw), _vp(gw),
+                                      _vp(grad), _vp(gc)):
+            raise ValueError("degenerate matrix")
+        return grad, gc
+
+    def fd_particles(self, params: dict, rc, raw, cov, order, target, sel, h: float = 1e-4):
+        """Central differences of sum((pic - target)^2), coverage frozen."""
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        sel = np.ascontiguousarray(sel, dtype=np.int64)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        fd = np.zeros((len(sel), 8))
+        ex = np.zeros((len(sel), 8), dtype=np.uint8)
+        if self.lib.spo_fd_particles(C.byref(prm), _vp(raw), _vp(cov), _vp(order), len(raw),
+                                     prm.tile_size, _vp(t), _vp(sel), len(sel), h, _vp(fd),
+                                     _vp(ex)):
+            raise RuntimeError("oracle finite differences failed")
+        return fd, ex.astype(bool)
+
+    def fd_campos(self, params: dict, rc, raw, cov, order, target, h: float = 1e-4):
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        fd = np.zeros(3)
+        if self.lib.spo_fd_campos(C.byref(prm), _vp(raw), _vp(cov), _vp(order), len(raw),
+                                  prm.tile_size, _vp(t), h, _vp(fd)):
+            raise RuntimeError("oracle finite differences failed")
+        return fd
 
 
 class Ref:

@@ -781,3 +781,521 @@ int spo_host_rendering(const spo_params *prm, spo_particle *p, int64_t n,
                               prm->a_eq_e, prm->gray_absorption, simd_branch, pic);
   return r < 0 ? -4 : 0;
 }
+
+/* ====================================================================== */
+/* Differentiable FP64 model -- the checker of the adjoint (gradient) path.
+   particle_project + particle_colorize (splotch_host.cc:111-153, 270-284) as
+   a smooth double-precision function of one particle's inputs and of the
+   camera position; the splat as a function of (X, Y, R, E) with coverage,
+   tile lists and order held at the reference's float decisions. */
+
+static spo_model_in model_in_of(const spo_particle *p) {
+  spo_model_in q;
+  q.I = p->I; q.e[0] = p->er; q.e[1] = p->eg; q.e[2] = p->eb;
+  q.x = p->x; q.y = p->y; q.z = p->z; q.r = p->r;
+  q.type = p->type;
+  return q;
+}
+
+static void model_colour(const spo_model *m, const spo_model_in *p, double col[3],
+                         double dcol[3], int *seg) {
+  const int t = p->type;
+  *seg = -3;
+  if (m->colvec[t]) {
+    col[0] = p->e[0]; col[1] = p->e[1]; col[2] = p->e[2];
+    dcol[0] = dcol[1] = dcol[2] = 0.0;
+    return;
+  }
+  /* linearMap::getVal_const in double (linear_map.h:71-84), plus its slope */
+  const int n = m->pal_n[t];
+  const double *x = m->pal_x[t];
+  const float *rgb = m->pal_rgb[t];
+  const double v = p->e[0];
+  int idx;
+  if (n == 1 || v <= x[0]) { idx = 0; *seg = -1; goto ends; }
+  if (v >= x[n - 1]) { idx = n - 1; *seg = -2; goto ends; }
+  {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      int mid = lo + (hi - lo) / 2;
+      if (x[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    idx = lo > 0 ? lo - 1 : 0;
+    if (idx > n - 2) idx = n - 2;
+    const double dx = x[idx + 1] - x[idx], frac = (v - x[idx]) / dx;
+    for (int c = 0; c < 3; ++c) {
+      col[c] = rgb[3 * idx + c] * (1. - frac) + rgb[3 * (idx + 1) + c] * frac;
+      dcol[c] = (rgb[3 * (idx + 1) + c] - (double)rgb[3 * idx + c]) / dx;
+    }
+    *seg = idx;
+    return;
+  }
+ends:
+  for (int c = 0; c < 3; ++c) { col[c] = rgb[3 * idx + c]; dcol[c] = 0.0; }
+}
+
+int spo_model_setup(const spo_params *prm, spo_model *m) {
+  spo_camera cam;
+  if (spo_camera_setup(prm, &cam)) return -1;
+  memset(m, 0, sizeof(*m));
+  for (int i = 0; i < 3; ++i) {
+    for (int j = 0; j < 3; ++j) m->A[i][j] = cam.mat[4 * i + j];
+    m->campos[i] = prm->campos[i];
+    m->centerpos[i] = prm->centerpos[i];
+  }
+  m->res2 = cam.res2; m->ycorr = cam.ycorr; m->fovfct = cam.fovfct; m->xfac = cam.xfac;
+  m->projection = prm->projection;
+  m->minrad = prm->minrad_pix;
+  m->bfak = bfak_f();
+  m->h2sigma = h2sigma_f();
+  for (int t = 0; t < prm->ptypes && t < SPO_MAX_TYPES; ++t) {
+    m->smooth[t] = prm->smooth_factor[t];
+    m->bright[t] = (float)(prm->brightness[t] * prm->b_brightness);
+    m->colvec[t] = prm->color_is_vector[t];
+    m->pal_n[t] = prm->pal_n[t];
+    m->pal_x[t] = prm->pal_x[t];
+    m->pal_rgb[t] = prm->pal_rgb[t];
+  }
+  return 0;
+}
+
+typedef struct {
+  double xc, yc, zc, f, r2, R, K, col[3], dcol[3];
+  int seg;
+} model_fwd;
+
+static void model_eval(const spo_model *m, const spo_model_in *p, model_fwd *s, double w[6]) {
+  double d[3] = {p->x - m->campos[0], p->y - m->campos[1], p->z - m->campos[2]};
+  s->xc = m->A[0][0] * d[0] + m->A[0][1] * d[1] + m->A[0][2] * d[2];
+  s->yc = m->A[1][0] * d[0] + m->A[1][1] * d[1] + m->A[1][2] * d[2];
+  s->zc = m->A[2][0] * d[0] + m->A[2][1] * d[1] + m->A[2][2] * d[2];
+  if (m->projection) {
+    double dc[3] = {m->centerpos[0] - m->campos[0], m->centerpos[1] - m->campos[1],
+                    m->centerpos[2] - m->campos[2]};
+    double xs = -m->xfac * (m->A[0][0] * dc[0] + m->A[0][1] * dc[1] + m->A[0][2] * dc[2]);
+    double ys = -m->xfac * (m->A[1][0] * dc[0] + m->A[1][1] * dc[1] + m->A[1][2] * dc[2]);
+    s->f = -m->res2 / (m->fovfct * s->zc);
+    w[0] = m->res2 + xs + s->xc * s->f;
+    w[1] = m->res2 + ys + m->ycorr + s->yc * s->f;
+  } else {
+    s->f = m->xfac;
+    w[0] = m->res2 + s->xc * s->f;
+    w[1] = m->res2 + m->ycorr + s->yc * s->f;
+  }
+  const int t = p->type;
+  s->r2 = 2.0 * p->r * s->f * m->smooth[t];
+  s->R = sqrt(s->r2 * s->r2 + m->minrad * m->minrad);
+  s->K = m->bfak * m->bright[t] * s->f * m->smooth[t] / s->R;
+  model_colour(m, p, s->col, s->dcol, &s->seg);
+  w[2] = s->R;
+  for (int c = 0; c < 3; ++c) w[3 + c] = s->col[c] * p->I * s->K;
+}
+
+void spo_model_project(const spo_model *m, const spo_model_in *p, double w[6]) {
+  model_fwd s;
+  model_eval(m, p, &s, w);
+}
+
+void spo_model_vjp(const spo_model *m, const spo_model_in *p, const double gin[6],
+                   double gout[8], double gcampos[3]) {
+  model_fwd s;
+  double w[6];
+  model_eval(m, p, &s, w);
+  const int t = p->type;
+  const double sm = m->smooth[t];
+  const double gX = gin[0], gY = gin[1], gR = gin[2];
+  double gK = 0.0, gI = 0.0, gcol[3];
+  for (int c = 0; c < 3; ++c) {
+    gK += gin[3 + c] * s.col[c] * p->I;
+    gI += gin[3 + c] * s.col[c] * s.K;
+    gcol[c] = gin[3 + c] * p->I * s.K;
+  }
+  /* K = bfak*bright*f*s/R */
+  const double gRt = gR - gK * s.K / s.R;
+  double gf = gK * s.K / s.f;
+  /* R = sqrt(r2^2 + minrad^2), r2 = 2*h*f*s */
+  const double gr2 = gRt * s.r2 / s.R;
+  const double gh = gr2 * 2.0 * s.f * sm;
+  gf += gr2 * 2.0 * p->r * sm;
+  /* X = res2 (+ xshift) + xc*f */
+  gf += gX * s.xc + gY * s.yc;
+  double gcam[3] = {gX * s.f, gY * s.f, 0.0};
+  if (m->projection) {
+    gcam[2] = gf * (-s.f / s.zc);  /* f = -res2/(fovfct*zc) */
+    for (int j = 0; j < 3; ++j)  /* xshift = -xfac*A0.(centerpos-campos) */
+      gcampos[j] += m->xfac * (gX * m->A[0][j] + gY * m->A[1][j]);
+  }
+  double gp[3];
+  for (int j = 0; j < 3; ++j) {
+    gp[j] = m->A[0][j] * gcam[0] + m->A[1][j] * gcam[1] + m->A[2][j] * gcam[2];
+    gcampos[j] -= gp[j];
+  }
+  gout[0] = gI;
+  if (m->colvec[t]) {
+    gout[1] = gcol[0]; gout[2] = gcol[1]; gout[3] = gcol[2];
+  } else {
+    gout[1] = gcol[0] * s.dcol[0] + gcol[1] * s.dcol[1] + gcol[2] * s.dcol[2];
+    gout[2] = gout[3] = 0.0;
+  }
+  gout[4] = gp[0]; gout[5] = gp[1]; gout[6] = gp[2];
+  gout[7] = gh;
+}
+
+static void model_all(const spo_model *m, const spo_particle *raw, const spo_particle *cov,
+                      int64_t n, double *w) {
+#pragma omp parallel for schedule(static) num_threads(spo_get_threads())
+  for (int64_t i = 0; i < n; ++i) {
+    if (cov[i].active) {
+      const spo_model_in q = model_in_of(&raw[i]);
+      spo_model_project(m, &q, w + 6 * i);
+    } else {
+      memset(w + 6 * i, 0, 6 * sizeof(double));
+    }
+  }
+}
+
+/* one pixel's fragment weight: exp(stp*d^2) with the model's X, Y, R */
+static inline double frag_att(const double *wi, double h2sigma, double px, double py) {
+  const double sigma = h2sigma * wi[2];
+  const double stp = -1.0 / (sigma * sigma);
+  const double dx = px - wi[0], dy = py - wi[1];
+  return exp(stp * (dx * dx + dy * dy));
+}
+
+static inline int covers_pixel(const pcov *c, int x, int y) {
+  if (x < c->minx || x >= c->maxx || y < c->miny || y >= c->maxy) return 0;
+  int lo, hi;
+  float dxsq;
+  column_run(c, x, &lo, &hi, &dxsq);
+  return y >= lo && y < hi;
+}
+
+static inline void frag_apply(int a_eq_e, double gray, const double *E, double att,
+                              double *v) {
+  for (int ch = 0; ch < 3; ++ch) {
+    if (a_eq_e) v[ch] += -E[ch] * att;
+    else v[ch] += expm1(-E[ch] * att) * (v[ch] - E[ch] / (E[ch] + gray));
+  }
+}
+
+int64_t spo_render_frozen_fp64(const spo_particle *cov, const double *w, const uint32_t *order,
+                               int64_t n, int xres, int yres, int T, int a_eq_e, double gray,
+                               double *pic) {
+  bins b;
+  if (make_bins(cov, order, n, xres, yres, T, &b)) return -1;
+  const double h2s = h2sigma_f();
+  const float h2sf = h2sigma_f();
+  int64_t frags = 0;
+#pragma omp parallel num_threads(spo_get_threads()) reduction(+ : frags)
+  {
+    double *lpic = (double *)malloc((size_t)T * T * 3 * sizeof(double));
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t chunk = 0; chunk < b.ntiles; ++chunk) {
+      int ix = (int)(chunk % b.g.ncx), iy = (int)(chunk / b.g.ncx);
+      int x0s = ix * T, y0s = iy * T;
+      int x1 = imin(x0s + T, xres) - x0s, y1 = imin(y0s + T, yres) - y0s;
+      memset(lpic, 0, (size_t)x1 * y1 * 3 * sizeof(double));
+      for (int64_t k = b.start[chunk]; k < b.start[chunk + 1]; ++k) {
+        const uint32_t i = b.ent[k];
+        pcov c;
+        particle_cover(&cov[i], x0s, y0s, x1, y1, h2sf, &c);
+        const double *wi = w + 6 * (size_t)i;
+        for (int x = c.minx; x < c.maxx; ++x) {
+          int lo, hi;
+          float dxsq;
+          column_run(&c, x, &lo, &hi, &dxsq);
+          for (int y = lo; y < hi; ++y) {
+            double att = frag_att(wi, h2s, (double)(x + x0s), (double)(y + y0s));
+            frag_apply(a_eq_e, gray, wi + 3, att, lpic + ((size_t)x * y1 + y) * 3);
+          }
+          if (hi > lo) frags += hi - lo;
+        }
+      }
+      for (int x = 0; x < x1; ++x)
+        memcpy(pic + ((size_t)(x + x0s) * yres + y0s) * 3, lpic + (size_t)x * y1 * 3,
+               (size_t)y1 * 3 * sizeof(double));
+    }
+    free(lpic);
+  }
+  free_bins(&b);
+  return frags;
+}
+
+/* Exact reverse mode of the frozen render: per pixel, replay the ordered list
+   storing every intermediate, then sweep it backwards.  gw (n x 6) receives
+   dL/d(X, Y, R, E.r, E.g, E.b) for L = sum(gpic * pic). */
+int spo_render_frozen_vjp_fp64(const spo_particle *cov, const double *w, const uint32_t *order,
+                               int64_t n, int xres, int yres, int T, int a_eq_e, double gray,
+                               const double *gpic, double *gw) {
+  bins b;
+  if (make_bins(cov, order, n, xres, yres, T, &b)) return -1;
+  const double h2s = h2sigma_f();
+  const float h2sf = h2sigma_f();
+  memset(gw, 0, (size_t)n * 6 * sizeof(double));
+#pragma omp parallel num_threads(spo_get_threads())
+  {
+    int64_t cap = 0;
+    double *att = NULL, *hist = NULL;
+    pcov *cv = NULL;
+#pragma omp for schedule(dynamic, 1)
+    for (int64_t chunk = 0; chunk < b.ntiles; ++chunk) {
+      int ix = (int)(chunk % b.g.ncx), iy = (int)(chunk / b.g.ncx);
+      int x0s = ix * T, y0s = iy * T;
+      int x1 = imin(x0s + T, xres) - x0s, y1 = imin(y0s + T, yres) - y0s;
+      int64_t k0 = b.start[chunk], L = b.start[chunk + 1] - k0;
+      if (L == 0) continue;
+      if (L > cap) {
+        cap = L;
+        free(att); free(hist); free(cv);
+        att = (double *)malloc((size_t)L * sizeof(double));
+        hist = (double *)malloc((size_t)(L + 1) * 3 * sizeof(double));
+        cv = (pcov *)malloc((size_t)L * sizeof(pcov));
+      }
+      for (int64_t k = 0; k < L; ++k)
+        particle_cover(&cov[b.ent[k0 + k]], x0s, y0s, x1, y1, h2sf, &cv[k]);
+      for (int x = 0; x < x1; ++x)
+        for (int y = 0; y < y1; ++y) {
+          const double *G = gpic + ((size_t)(x + x0s) * yres + (y + y0s)) * 3;
+          const double px = x + x0s, py = y + y0s;
+          hist[0] = hist[1] = hist[2] = 0.0;
+          for (int64_t k = 0; k < L; ++k) {
+            const double *wi = w + 6 * (size_t)b.ent[k0 + k];
+            memcpy(hist + 3 * (k + 1), hist + 3 * k, 3 * sizeof(double));
+            att[k] = 0.0;
+            if (!covers_pixel(&cv[k], x, y)) continue;
+            att[k] = frag_att(wi, h2s, px, py);
+            frag_apply(a_eq_e, gray, wi + 3, att[k], hist + 3 * (k + 1));
+          }
+          double lam[3] = {G[0], G[1], G[2]};
+          for (int64_t k = L - 1; k >= 0; --k) {
+            if (!covers_pixel(&cv[k], x, y)) continue;
+            const uint32_t i = b.ent[k0 + k];
+            const double *wi = w + 6 * (size_t)i;
+            const double a = att[k];
+            double ge[3], gatt = 0.0;
+            for (int ch = 0; ch < 3; ++ch) {
+              const double E = wi[3 + ch];
+              if (a_eq_e) {
+                ge[ch] = -lam[ch] * a;
+                gatt += -lam[ch] * E;
+              } else {
+                const double Cp = hist[3 * k + ch], q = E / (E + gray), Tk = exp(-E * a);
+                const double dT = lam[ch] * (Cp - q), dq = lam[ch] * (1.0 - Tk);
+                ge[ch] = dT * (-a * Tk) + dq * gray / ((E + gray) * (E + gray));
+                gatt += dT * (-E * Tk);
+                lam[ch] *= Tk;
+              }
+            }
+            const double sigma = h2s * wi[2], stp = -1.0 / (sigma * sigma);
+            const double dx = px - wi[0], dy = py - wi[1];
+            const double gg[6] = {gatt * a * (-2.0 * stp) * dx, gatt * a * (-2.0 * stp) * dy,
+                                  gatt * a * (dx * dx + dy * dy) * (-2.0 * stp / wi[2]),
+                                  ge[0], ge[1], ge[2]};
+            for (int j = 0; j < 6; ++j) {
+#pragma omp atomic
+              gw[6 * (size_t)i + j] += gg[j];
+            }
+          }
+        }
+    }
+    free(att); free(hist); free(cv);
+  }
+  free_bins(&b);
+  return 0;
+}
+
+int spo_grad_fp64(const spo_params *prm, const spo_particle *raw, const spo_particle *cov,
+                  const uint32_t *order, int64_t n, int T, const double *gpic, double *grad,
+                  double gcampos[3]) {
+  spo_model m;
+  if (spo_model_setup(prm, &m)) return -1;
+  double *w = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  double *gw = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  if (!w || !gw) { free(w); free(gw); return -2; }
+  model_all(&m, raw, cov, n, w);
+  int rc = spo_render_frozen_vjp_fp64(cov, w, order, n, prm->xres, prm->yres, T, prm->a_eq_e,
+                                      (double)prm->gray_absorption, gpic, gw);
+  gcampos[0] = gcampos[1] = gcampos[2] = 0.0;
+  for (int64_t i = 0; i < n && rc == 0; ++i) {
+    if (!cov[i].active) { memset(grad + 8 * i, 0, 8 * sizeof(double)); continue; }
+    const spo_model_in q = model_in_of(&raw[i]);
+    spo_model_vjp(&m, &q, gw + 6 * i, grad + 8 * i, gcampos);
+  }
+  free(w);
+  free(gw);
+  return rc;
+}
+
+/* Central differences of L = sum((pic - target)^2) of the model with frozen
+   coverage.  Per selected particle and input (I, e.r, e.g, e.b, x, y, z, r):
+   only the pixels the particle covers change, and each of them is the affine
+   image of the particle's own update -- C_final = C_i * Tsuffix + Dsuffix
+   (C_i + Dsuffix in additive mode) with C_i computed from the state Cprefix
+   that the earlier list entries leave -- so each evaluation costs one pass
+   over the covered pixels.  excluded[j] = 1 where the +-h pair lands on
+   different palette segments (a kink of the piecewise-linear colour map). */
+int spo_fd_particles(const spo_params *prm, const spo_particle *raw, const spo_particle *cov,
+                     const uint32_t *order, int64_t n, int T, const float *target,
+                     const int64_t *sel, int nsel, double h, double *fd, uint8_t *excluded) {
+  spo_model m;
+  if (spo_model_setup(prm, &m)) return -1;
+  const int xres = prm->xres, yres = prm->yres, a_eq_e = prm->a_eq_e;
+  const double gray = prm->gray_absorption;
+  double *w = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  if (!w) return -2;
+  model_all(&m, raw, cov, n, w);
+  bins b;
+  if (make_bins(cov, order, n, xres, yres, T, &b)) { free(w); return -1; }
+  const double h2s = h2sigma_f();
+  const float h2sf = h2sigma_f();
+  int err = 0;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(spo_get_threads())
+  for (int s = 0; s < nsel; ++s) {
+    const int64_t i = sel[s];
+    memset(fd + 8 * (size_t)s, 0, 8 * sizeof(double));
+    memset(excluded + 8 * (size_t)s, 0, 8);
+    if (i < 0 || i >= n || !cov[i].active) continue;
+    /* pixels covered by i with their prefix state and suffix map */
+    int64_t np = 0, capp = 64;
+    double *px = (double *)malloc((size_t)capp * 14 * sizeof(double));
+    uint32_t ids[4096];
+    int nt = particle_tiles(&cov[i], &b.g, NULL);
+    if (nt > 4096) { err = 1; free(px); continue; }
+    particle_tiles(&cov[i], &b.g, ids);
+    for (int tt = 0; tt < nt; ++tt) {
+      const int64_t chunk = ids[tt];
+      int ix = (int)(chunk % b.g.ncx), iy = (int)(chunk / b.g.ncx);
+      int x0s = ix * T, y0s = iy * T;
+      int x1 = imin(x0s + T, xres) - x0s, y1 = imin(y0s + T, yres) - y0s;
+      int64_t k0 = b.start[chunk], k1 = b.start[chunk + 1], ki = -1;
+      for (int64_t k = k0; k < k1; ++k)
+        if (b.ent[k] == (uint32_t)i) { ki = k; break; }
+      if (ki < 0) continue;
+      pcov ci;
+      particle_cover(&cov[i], x0s, y0s, x1, y1, h2sf, &ci);
+      for (int x = ci.minx; x < ci.maxx; ++x)
+        for (int y = ci.miny; y < ci.maxy; ++y) {
+          if (!covers_pixel(&ci, x, y)) continue;
+          double C[3] = {0, 0, 0}, Tp[3] = {1, 1, 1}, D[3] = {0, 0, 0};
+          const double gx = x + x0s, gy = y + y0s;
+          for (int64_t k = k0; k < k1; ++k) {
+            if (k == ki) continue;
+            const uint32_t j = b.ent[k];
+            pcov cj;
+            particle_cover(&cov[j], x0s, y0s, x1, y1, h2sf, &cj);
+            if (!covers_pixel(&cj, x, y)) continue;
+            const double *wj = w + 6 * (size_t)j;
+            const double att = frag_att(wj, h2s, gx, gy);
+            if (k < ki) {
+              frag_apply(a_eq_e, gray, wj + 3, att, C);
+            } else {
+              for (int ch = 0; ch < 3; ++ch) {
+                const double E = wj[3 + ch];
+                if (a_eq_e) D[ch] += -E * att;
+                else {
+                  const double Tj = exp(-E * att), q = E / (E + gray);
+                  Tp[ch] *= Tj;
+                  D[ch] = D[ch] * Tj + q * (1.0 - Tj);
+                }
+              }
+            }
+          }
+          if (np == capp) {
+            capp *= 2;
+            px = (double *)realloc(px, (size_t)capp * 14 * sizeof(double));
+          }
+          double *r = px + 14 * np++;
+          r[0] = gx; r[1] = gy;
+          const float *tg = target + ((size_t)(x + x0s) * yres + (y + y0s)) * 3;
+          for (int ch = 0; ch < 3; ++ch) {
+            r[2 + ch] = C[ch]; r[5 + ch] = Tp[ch]; r[8 + ch] = D[ch]; r[11 + ch] = tg[ch];
+          }
+        }
+    }
+    for (int j = 0; j < 8; ++j) {
+      double L[2];
+      int segs[2];
+      for (int sg = 0; sg < 2; ++sg) {
+        spo_model_in q = model_in_of(&raw[i]);
+        double *fld[8] = {&q.I, &q.e[0], &q.e[1], &q.e[2], &q.x, &q.y, &q.z, &q.r};
+        *fld[j] += sg ? -h : h;
+        double wq[6];
+        model_fwd st;
+        model_eval(&m, &q, &st, wq);
+        segs[sg] = st.seg;
+        double acc = 0.0;
+        for (int64_t k = 0; k < np; ++k) {
+          const double *r = px + 14 * k;
+          const double att = frag_att(wq, h2s, r[0], r[1]);
+          double Ci[3] = {r[2], r[3], r[4]};
+          frag_apply(a_eq_e, gray, wq + 3, att, Ci);
+          for (int ch = 0; ch < 3; ++ch) {
+            const double Cf = a_eq_e ? Ci[ch] + r[8 + ch] : Ci[ch] * r[5 + ch] + r[8 + ch];
+            const double dlt = Cf - r[11 + ch];
+            acc += dlt * dlt;
+          }
+        }
+        L[sg] = acc;
+      }
+      fd[8 * (size_t)s + j] = (L[0] - L[1]) / (2.0 * h);
+      if (j == 1 && segs[0] != segs[1]) excluded[8 * (size_t)s + j] = 1;
+    }
+    free(px);
+  }
+  free_bins(&b);
+  free(w);
+  return err ? -3 : 0;
+}
+
+/* Central differences of the same loss with respect to the camera position
+   (centerpos, lookat and sky held): two frozen renders per component. */
+int spo_fd_campos(const spo_params *prm, const spo_particle *raw, const spo_particle *cov,
+                  const uint32_t *order, int64_t n, int T, const float *target, double h,
+                  double fd[3]) {
+  const size_t npix = (size_t)prm->xres * prm->yres * 3;
+  double *w = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  double *pp = (double *)malloc(npix * sizeof(double));
+  double *pm = (double *)malloc(npix * sizeof(double));
+  if (!w || !pp || !pm) { free(w); free(pp); free(pm); return -2; }
+  int rc = 0;
+  for (int k = 0; k < 3 && rc == 0; ++k) {
+    for (int sg = 0; sg < 2 && rc == 0; ++sg) {
+      spo_model m;
+      if (spo_model_setup(prm, &m)) { rc = -1; break; }
+      m.campos[k] += sg ? -h : h;
+      model_all(&m, raw, cov, n, w);
+      if (spo_render_frozen_fp64(cov, w, order, n, prm->xres, prm->yres, T, prm->a_eq_e,
+                                 (double)prm->gray_absorption, sg ? pm : pp) < 0)
+        rc = -1;
+    }
+    double acc = 0.0;
+    for (size_t j = 0; j < npix && rc == 0; ++j)
+      acc += (pp[j] - pm[j]) * (pp[j] + pm[j] - 2.0 * (double)target[j]);
+    fd[k] = acc / (2.0 * h);
+  }
+  free(w); free(pp); free(pm);
+  return rc;
+}
+
+/* The model's X, Y, R, E for every active particle (zeros elsewhere). */
+int spo_model_project_all(const spo_params *prm, const spo_particle *raw,
+                          const spo_particle *cov, int64_t n, double *w) {
+  spo_model m;
+  if (spo_model_setup(prm, &m)) return -1;
+  model_all(&m, raw, cov, n, w);
+  return 0;
+}
+
+/* Per-particle chain rule alone: gw (n x 6, d/d(X,Y,R,E)) -> grad (n x 8). */
+int spo_model_vjp_all(const spo_params *prm, const spo_particle *raw, const spo_particle *cov,
+                      int64_t n, const double *gw, double *grad, double gcampos[3]) {
+  spo_model m;
+  if (spo_model_setup(prm, &m)) return -1;
+  gcampos[0] = gcampos[1] = gcampos[2] = 0.0;
+  for (int64_t i = 0; i < n; ++i) {
+    if (!cov[i].active) { memset(grad + 8 * i, 0, 8 * sizeof(double)); continue; }
+    const spo_model_in q = model_in_of(&raw[i]);
+    spo_model_vjp(&m, &q, gw + 6 * i, grad + 8 * i, gcampos);
+  }
+  return 0;
+}

@@ -108,6 +108,68 @@ int spo_splat_adjoint_fp64(const spo_particle *p, const uint32_t *order,
                            double gray, const double *gpic, double *gx,
                            double *gy, double *gr, double *ge);
 
+/* ---- differentiable FP64 model: checker of the adjoint path ------------
+   particle_project + particle_colorize (splotch_host.cc:111-153, 270-284)
+   as a smooth double-precision function of a particle's inputs and of the
+   camera position (centerpos, lookat, sky held); coverage, tile lists and
+   order stay at the reference's float decisions ("frozen").  Loss
+   L = sum over pixels and channels of (pic - target)^2 for the FD routines. */
+typedef struct {
+  double A[3][3]; /* camera rotation: the float TRANSMAT entries */
+  double campos[3], centerpos[3];
+  double res2, ycorr, fovfct, xfac;
+  int projection;
+  double minrad, bfak, h2sigma;
+  double smooth[SPO_MAX_TYPES], bright[SPO_MAX_TYPES]; /* bright*b_brightness */
+  int colvec[SPO_MAX_TYPES];
+  int pal_n[SPO_MAX_TYPES];
+  const double *pal_x[SPO_MAX_TYPES];
+  const float *pal_rgb[SPO_MAX_TYPES];
+} spo_model;
+
+/* One particle's inputs in double: I, colour (palette value in e[0], or
+   RGB), world position, hsml, type. */
+typedef struct {
+  double I, e[3], x, y, z, r;
+  int type;
+} spo_model_in;
+
+int spo_model_setup(const spo_params *prm, spo_model *m);
+/* w = X, Y, R (pixels), E.r, E.g, E.b */
+void spo_model_project(const spo_model *m, const spo_model_in *p, double w[6]);
+/* gin = dL/d(X, Y, R, E); gout = dL/d(I, e.r, e.g, e.b, x, y, z, r);
+   gcampos += dL/dcampos of this particle */
+void spo_model_vjp(const spo_model *m, const spo_model_in *p, const double gin[6],
+                   double gout[8], double gcampos[3]);
+int spo_model_project_all(const spo_params *prm, const spo_particle *raw,
+                          const spo_particle *cov, int64_t n, double *w);
+int spo_model_vjp_all(const spo_params *prm, const spo_particle *raw,
+                      const spo_particle *cov, int64_t n, const double *gw,
+                      double *grad, double gcampos[3]);
+/* Splat with coverage from cov (projected particles) and weights w (n x 6). */
+int64_t spo_render_frozen_fp64(const spo_particle *cov, const double *w,
+                               const uint32_t *order, int64_t n, int xres,
+                               int yres, int T, int a_eq_e, double gray,
+                               double *pic);
+/* Its exact reverse mode: gw = dL/dw for L = sum(gpic * pic). */
+int spo_render_frozen_vjp_fp64(const spo_particle *cov, const double *w,
+                               const uint32_t *order, int64_t n, int xres,
+                               int yres, int T, int a_eq_e, double gray,
+                               const double *gpic, double *gw);
+/* Full FP64 gradient: grad (n x 8, the gout layout) and dL/dcampos. */
+int spo_grad_fp64(const spo_params *prm, const spo_particle *raw,
+                  const spo_particle *cov, const uint32_t *order, int64_t n, int T,
+                  const double *gpic, double *grad, double gcampos[3]);
+/* Central finite differences (step h) of L for selected particles
+   (fd: nsel x 8, excluded: nsel x 8 palette-kink flags) and for campos. */
+int spo_fd_particles(const spo_params *prm, const spo_particle *raw,
+                     const spo_particle *cov, const uint32_t *order, int64_t n,
+                     int T, const float *target, const int64_t *sel, int nsel,
+                     double h, double *fd, uint8_t *excluded);
+int spo_fd_campos(const spo_params *prm, const spo_particle *raw,
+                  const spo_particle *cov, const uint32_t *order, int64_t n,
+                  int T, const float *target, double h, double fd[3]);
+
 #ifdef __cplusplus
 }
 #endif

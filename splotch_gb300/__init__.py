@@ -270,6 +270,7 @@ class Renderer:
         self.ctx = C.c_void_p()
         _abi.check(self.lib.spl_context_create(C.byref(self.ctx), device))
         self.device = device
+        self._last_n = 0
 
     def close(self) -> None:
         if self.ctx:
@@ -299,6 +300,7 @@ class Renderer:
         _abi.check(self.lib.spl_render(self.ctx, C.byref(desc), C.byref(p), C.byref(img),
                                        _abi.SPL_WRITEBACK_FULL if writeback
                                        else _abi.SPL_WRITEBACK_NONE))
+        self._last_n = n
 
     def render_soa(self, desc: _abi.FrameDesc, soa: dict, pic, *, device: bool = True) -> None:
         """Render SoA fields x,y,z,r,I,cr[,cg,cb][,type] (float32 / uint16)."""
@@ -311,11 +313,37 @@ class Renderer:
                          else _abi.SPL_MEM_HOST)
         _abi.check(self.lib.spl_render(self.ctx, C.byref(desc), C.byref(p), C.byref(img),
                                        _abi.SPL_WRITEBACK_NONE))
+        self._last_n = n
 
     def stats(self) -> dict:
         s = _abi.Stats()
         _abi.check(self.lib.spl_get_stats(self.ctx, C.byref(s)))
         return s.as_dict()
+
+    # -- gradients ------------------------------------------------------------
+    def set_differentiable(self, enable: bool = True) -> None:
+        """Ordered frames keep what spl_render_backward needs (per-pixel optical
+        depth and stop position) while this is on."""
+        _abi.check(self.lib.spl_context_set_differentiable(self.ctx, 1 if enable else 0))
+
+    def backward(self, grad_pic, out: dict | None = None, *, device: bool = False) -> dict:
+        """spl_render_backward for the last frame: dL/d(I, cr, cg, cb, x, y, z, r)
+        per particle and dL/dcampos, given grad_pic = dL/dpic.  out maps field
+        names to preallocated float32 arrays (numpy, or device tensors when
+        device=True); by default numpy arrays are allocated."""
+        if out is None:
+            out = {f: np.zeros(self._last_n, np.float32) for f in _abi.GRAD_FIELDS}
+            device = False
+        g = _abi.Grads(memspace=_abi.SPL_MEM_DEVICE if device else _abi.SPL_MEM_HOST)
+        for f in _abi.GRAD_FIELDS:
+            setattr(g, f, _abi.ptr(out.get(f)))
+        dev_img = not isinstance(grad_pic, np.ndarray)
+        img = _abi.Image(pic=_abi.ptr(grad_pic),
+                         memspace=_abi.SPL_MEM_DEVICE if dev_img else _abi.SPL_MEM_HOST)
+        _abi.check(self.lib.spl_render_backward(self.ctx, C.byref(img), C.byref(g)))
+        res = dict(out)
+        res["campos"] = np.array(g.campos[:], dtype=np.float64)
+        return res
 
     # -- test hooks -----------------------------------------------------------
     def projected(self, n: int) -> np.ndarray:
@@ -347,6 +375,62 @@ class Renderer:
         _abi.check(self.lib.spl_debug_get_bins(self.ctx, ts.ctypes.data, ntiles + 1,
                                                ent.ctypes.data, len(ent)))
         return ts, ent[: s["n_entries"]]
+
+
+class Batch:
+    """spl_batch_*: many frames rendered by one captured CUDA graph.
+
+    sets: list of device SoA dicts (x, y, z, r, I, cr[, cg, cb][, type] as
+    tensors); frames: list of (set index, FrameDesc, device image tensor).
+    The descs' palette arrays are copied at create."""
+
+    def __init__(self, renderer: Renderer, sets: list, frames: list, *, tile_size: int = 0,
+                 splat_config_additive: int = -1, splat_config_absorption: int = -1,
+                 capacity_margin: float = 1.1, use_graph: bool = True):
+        self.lib = renderer.lib
+        self._keep = [sets, frames]
+        psets = (_abi.Particles * max(1, len(sets)))()
+        for k, soa in enumerate(sets):
+            p = psets[k]
+            p.n = int(soa["x"].shape[0])
+            p.layout = _abi.SPL_LAYOUT_SOA
+            p.memspace = _abi.SPL_MEM_DEVICE
+            for f in ("x", "y", "z", "r", "I", "cr", "cg", "cb", "type"):
+                setattr(p, f, _abi.ptr(soa.get(f)))
+        pframes = (_abi.BatchFrame * len(frames))()
+        for k, (s, desc, pic) in enumerate(frames):
+            pframes[k].set = int(s)
+            pframes[k].desc = desc
+            pframes[k].pic = _abi.ptr(pic)
+        opt = _abi.BatchOptions()
+        self.lib.spl_batch_options_defaults(C.byref(opt))
+        opt.tile_size = tile_size
+        opt.splat_config_additive = splat_config_additive
+        opt.splat_config_absorption = splat_config_absorption
+        opt.capacity_margin = capacity_margin
+        opt.use_graph = 1 if use_graph else 0
+        self.handle = C.c_void_p()
+        _abi.check(self.lib.spl_batch_create(renderer.ctx, psets, len(sets), pframes,
+                                             len(frames), C.byref(opt), C.byref(self.handle)))
+
+    def render(self) -> None:
+        _abi.check(self.lib.spl_batch_render(self.handle))
+
+    def info(self) -> dict:
+        i = _abi.BatchInfo()
+        _abi.check(self.lib.spl_batch_get_info(self.handle, C.byref(i)))
+        return i.as_dict()
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.spl_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 _default_renderer: Renderer | None = None

@@ -27,6 +27,8 @@ EXPORTED = [
     "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
     "spl_debug_get_bins", "spl_debug_count_fragments", "spl_debug_set_options",
     "spl_splat_config_count", "spl_splat_config_valid", "spl_sort_pairs_noalloc",
+    "spl_render_backward", "spl_context_set_differentiable", "spl_batch_options_defaults",
+    "spl_batch_create", "spl_batch_render", "spl_batch_get_info", "spl_batch_destroy",
 ]
 SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
@@ -70,7 +72,39 @@ class Stats(C.Structure):
                 ("bin_ms", C.c_float), ("splat_ms", C.c_float), ("d2h_ms", C.c_float),
                 ("total_ms", C.c_float), ("n_active", C.c_int64), ("n_entries", C.c_int64),
                 ("n_tiles", C.c_int64), ("kernel_launches", C.c_int),
-                ("n_fallback", C.c_int64), ("n_wide", C.c_int64)]
+                ("n_fallback", C.c_int64), ("n_wide", C.c_int64),
+                ("bwd_splat_ms", C.c_float), ("bwd_project_ms", C.c_float),
+                ("bwd_total_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+GRAD_FIELDS = ("I", "cr", "cg", "cb", "x", "y", "z", "r")
+
+
+class Grads(C.Structure):
+    _fields_ = [("memspace", C.c_int)] + [(f, C.c_void_p) for f in GRAD_FIELDS] + [
+        ("campos", C.c_double * 3)]
+
+
+class BatchFrame(C.Structure):
+    _fields_ = [("set", C.c_int), ("desc", FrameDesc), ("pic", C.c_void_p)]
+
+
+class BatchOptions(C.Structure):
+    _fields_ = [("tile_size", C.c_int), ("splat_config_additive", C.c_int),
+                ("splat_config_absorption", C.c_int), ("capacity_margin", C.c_float),
+                ("use_graph", C.c_int)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("tile_size", C.c_int), ("splat_config_additive", C.c_int),
+                ("splat_config_absorption", C.c_int), ("graph", C.c_int),
+                ("cap_active", C.c_int64), ("cap_entries", C.c_int64),
+                ("total_tiles", C.c_int64), ("n_active", C.c_int64), ("n_entries", C.c_int64),
+                ("render_ms", C.c_float), ("tune_ms", C.c_float), ("kernel_launches", C.c_int),
+                ("replans", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -116,6 +150,14 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_splat_config_count": (C.c_int, []),
         "spl_splat_config_valid": (C.c_int, [C.c_int, C.c_int]),
         "spl_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, i64, C.c_int, vp]),
+        "spl_render_backward": (C.c_int, [vp, C.POINTER(Image), C.POINTER(Grads)]),
+        "spl_context_set_differentiable": (C.c_int, [vp, C.c_int]),
+        "spl_batch_options_defaults": (None, [C.POINTER(BatchOptions)]),
+        "spl_batch_create": (C.c_int, [vp, vp, C.c_int, vp, C.c_int,
+                                       C.POINTER(BatchOptions), C.POINTER(vp)]),
+        "spl_batch_render": (C.c_int, [vp]),
+        "spl_batch_get_info": (C.c_int, [vp, C.POINTER(BatchInfo)]),
+        "spl_batch_destroy": (C.c_int, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

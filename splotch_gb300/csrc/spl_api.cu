@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/splotch_gb300.h"
+#include "spl_host.h"
 #include "spl_internal.cuh"
 
 struct spl_context {
@@ -28,8 +29,9 @@ struct spl_context {
   Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
-      poff;
+      poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux;
   int debug_flags = 0;  // SPL_DEBUG_* bits
+  bool differentiable = false;  // ordered forwards keep SplatArgs::aux
   // state of the last frame (for the debug getters)
   int64_t n = 0, na = 0, ne = 0, ntiles = 0;
   bool has_order = false, writeback_done = false;
@@ -146,12 +148,6 @@ float greatest_float_not_above(double v) {  // greatest float f with f <= v
   return f;
 }
 
-int bits_for(int64_t v) {  // bits needed to represent 0..v-1
-  int b = 0;
-  while (b < 32 && ((int64_t)1 << b) < v) ++b;
-  return b;
-}
-
 // Every particle's projected state (indexed by particle) from the last
 // frame's inputs and constants: the writeback and the projection test hook.
 spl_status project_full(spl_context *c, int64_t n, bool with_key, int *launches) {
@@ -175,6 +171,97 @@ spl_status project_full(spl_context *c, int64_t n, bool with_key, int *launches)
 }  // namespace
 
 void spl::set_last_error(const char *msg) { g_err = msg; }
+
+spl_status spl::host_fail(spl_status code, const std::string &msg) { return fail(code, msg); }
+
+spl_status spl::validate_frame(const spl_frame_desc *d, const spl_particles *p,
+                               const spl_image *o) {
+  return validate(d, p, o);
+}
+
+int spl::context_device(const spl_context *c) { return c->device; }
+
+int spl::bits_for(int64_t v) {
+  int b = 0;
+  while (b < 32 && ((int64_t)1 << b) < v) ++b;
+  return b;
+}
+
+spl_status spl::frame_setup(const spl_frame_desc *d, int T, bool exact_fp64, FrameSetup &fs) {
+  spl_camera cam;
+  if (spl_camera_setup(d, &cam))
+    return fail(SPL_ERR_INVALID, "degenerate matrix in TRANSMAT::Inverse()");
+  const int xres = d->xres, yres = d->yres;
+  ProjConst &pc = fs.pc;
+  std::memset(&pc, 0, sizeof(pc));
+  std::memcpy(pc.mat, cam.mat, sizeof(pc.mat));
+  pc.res2 = cam.res2;
+  pc.ycorr = cam.ycorr;
+  pc.fovfct = cam.fovfct;
+  pc.xfac = cam.xfac;
+  pc.xsum = (double)cam.res2 + cam.xshift;
+  pc.ysum = (double)cam.res2 + cam.yshift + (double)cam.ycorr;
+  {
+    const float2 xs = split_ff(pc.xsum), ys = split_ff(pc.ysum);
+    pc.xsum_ff = ff{xs.x, xs.y};
+    pc.ysum_ff = ff{ys.x, ys.y};
+  }
+  pc.exact_fp64 = exact_fp64 ? 1 : 0;
+  pc.zmin = d->zmin > 0.f ? d->zmin : 0.f;
+  pc.zmax = d->zmax;
+  pc.minrad2 = d->minrad_pix * d->minrad_pix;
+  const float bfak = (float)(0.5 * std::pow(3.141592653589793238462643383279502884197, -5. / 6.));
+  pc.half_bfak = 0.5f * bfak;
+  pc.xres = xres;
+  pc.yres = yres;
+  pc.projection = d->projection ? 1 : 0;
+  pc.ptypes = d->ptypes;
+  int npal = 0;
+  for (int t = 0; t < d->ptypes; ++t) {
+    pc.smooth[t] = d->smooth_factor[t];
+    pc.bright[t] = d->brightness[t] * d->b_brightness;
+    pc.colvec[t] = d->color_is_vector[t] ? 1 : 0;
+    pc.pal_off[t] = npal;
+    pc.pal_n[t] = d->color_is_vector[t] ? 0 : d->pal_n[t];
+    npal += pc.pal_n[t];
+  }
+  Tiling &g = fs.g;
+  g.T = T;
+  g.ncx = (xres + T - 1) / T;
+  g.ncy = (yres + T - 1) / T;
+  g.rcell = std::sqrt(2.f) * (T * 0.5f - 0.5f);
+  g.cmid0 = 0.5f * (T - 1);
+  pc.T = g.T;
+  pc.ncx = g.ncx;
+  pc.ncy = g.ncy;
+  pc.rcell = g.rcell;
+  pc.cmid0 = g.cmid0;
+  fs.do_sort = !d->a_eq_e && d->sort_type != 0;
+  pc.sort_type = fs.do_sort ? d->sort_type : 0;
+  fs.ntiles = (int64_t)g.ncx * g.ncy;
+  if (fs.ntiles >= 0xffffffffLL) return fail(SPL_ERR_INVALID, "too many tiles");
+  fs.npal = npal;
+  fs.pal_x.assign(npal + 1, 0.0);
+  fs.pal_rgb.assign(3 * (size_t)(npal + 1), 0.f);
+  fs.thr.assign(npal + 1, 0.f);
+  fs.xff.assign(npal + 1, make_float2(0.f, 0.f));
+  fs.invff.assign(npal + 1, make_float2(0.f, 0.f));
+  for (int t = 0; t < d->ptypes; ++t) {
+    const int nk = pc.pal_n[t], o = pc.pal_off[t];
+    if (!nk) continue;
+    const double *x = d->pal_x[t];
+    for (int k = 0; k < nk; ++k) {
+      fs.pal_x[o + k] = x[k];
+      for (int ch = 0; ch < 3; ++ch) fs.pal_rgb[3 * (o + k) + ch] = d->pal_rgb[t][3 * k + ch];
+      fs.thr[o + k] = least_float_above(x[k]);
+      fs.xff[o + k] = split_ff(x[k]);
+      fs.invff[o + k] = k + 1 < nk ? split_ff(1.0 / (x[k + 1] - x[k])) : make_float2(0.f, 0.f);
+    }
+    pc.pal_lo_f[t] = greatest_float_not_above(x[0]);
+    pc.pal_hi_f[t] = least_float_not_below(x[nk - 1]);
+  }
+  return SPL_OK;
+}
 
 extern "C" {
 
@@ -211,10 +298,13 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->tile_start, &c->wide_list, &c->small, &c->pic, &c->pal_x,
                               &c->pal_rgb, &c->aos_out, &c->pal_thr, &c->pal_xff,
                               &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord, &c->pos_c,
-                              &c->col_c, &c->idx_c, &c->pstate, &c->poff};
+                              &c->col_c, &c->idx_c, &c->pstate, &c->poff, &c->gpic,
+                              &c->gpos_c, &c->gcol_c, &c->camsum, &c->aux};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
+    if (b.p) cudaFree(b.p);
+  for (auto &b : c->gout)
     if (b.p) cudaFree(b.p);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -251,59 +341,15 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   const int xres = d->xres, yres = d->yres, T = d->tile_size;
   int launches = 0;
 
-  spl_camera cam;
-  if (spl_camera_setup(d, &cam)) return fail(SPL_ERR_INVALID, "degenerate matrix in TRANSMAT::Inverse()");
-
   // ---- frame constants ---------------------------------------------------
-  spl::ProjConst pc;
-  std::memset(&pc, 0, sizeof(pc));
-  std::memcpy(pc.mat, cam.mat, sizeof(pc.mat));
-  pc.res2 = cam.res2;
-  pc.ycorr = cam.ycorr;
-  pc.fovfct = cam.fovfct;
-  pc.xfac = cam.xfac;
-  pc.xsum = (double)cam.res2 + cam.xshift;
-  pc.ysum = (double)cam.res2 + cam.yshift + (double)cam.ycorr;
-  {
-    const float2 xs = split_ff(pc.xsum), ys = split_ff(pc.ysum);
-    pc.xsum_ff = spl::ff{xs.x, xs.y};
-    pc.ysum_ff = spl::ff{ys.x, ys.y};
-  }
-  pc.exact_fp64 = (c->debug_flags & 1) ? 1 : 0;
+  spl::FrameSetup fs;
+  if ((st = spl::frame_setup(d, T, (c->debug_flags & 1) != 0, fs))) return st;
+  spl::ProjConst pc = fs.pc;
+  const spl::Tiling g = fs.g;
   const bool onesweep = (c->debug_flags & 2) == 0;
-  pc.zmin = d->zmin > 0.f ? d->zmin : 0.f;
-  pc.zmax = d->zmax;
-  pc.minrad2 = d->minrad_pix * d->minrad_pix;
-  const float bfak = (float)(0.5 * std::pow(3.141592653589793238462643383279502884197, -5. / 6.));
-  pc.half_bfak = 0.5f * bfak;
-  pc.xres = xres;
-  pc.yres = yres;
-  pc.projection = d->projection ? 1 : 0;
-  pc.ptypes = d->ptypes;
-  int npal = 0;
-  for (int t = 0; t < d->ptypes; ++t) {
-    pc.smooth[t] = d->smooth_factor[t];
-    pc.bright[t] = d->brightness[t] * d->b_brightness;
-    pc.colvec[t] = d->color_is_vector[t] ? 1 : 0;
-    pc.pal_off[t] = npal;
-    pc.pal_n[t] = d->color_is_vector[t] ? 0 : d->pal_n[t];
-    npal += pc.pal_n[t];
-  }
-  spl::Tiling g;
-  g.T = T;
-  g.ncx = (xres + T - 1) / T;
-  g.ncy = (yres + T - 1) / T;
-  g.rcell = std::sqrt(2.f) * (T * 0.5f - 0.5f);
-  g.cmid0 = 0.5f * (T - 1);
-  pc.T = g.T;
-  pc.ncx = g.ncx;
-  pc.ncy = g.ncy;
-  pc.rcell = g.rcell;
-  pc.cmid0 = g.cmid0;
-  const bool do_sort = !d->a_eq_e && d->sort_type != 0;
-  pc.sort_type = do_sort ? d->sort_type : 0;
-  const int64_t ntiles = (int64_t)g.ncx * g.ncy;
-  if (ntiles >= 0xffffffffLL) return fail(SPL_ERR_INVALID, "too many tiles");
+  const int npal = fs.npal;
+  const bool do_sort = fs.do_sort;
+  const int64_t ntiles = fs.ntiles;
 
   // ---- buffers -------------------------------------------------------------
   // compact (active-only) arrays are sized for n: the active count is known
@@ -331,45 +377,25 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   uint32_t *d_wide_n = d_err + 1;
   uint32_t *d_nact = d_err + 3;
 
-  // palettes (a few KB)
-  for (int t = 0; t < d->ptypes; ++t) {
-    if (!pc.pal_n[t]) continue;
-    SPL_CK(cudaMemcpyAsync(as<double>(c->pal_x) + pc.pal_off[t], d->pal_x[t], pc.pal_n[t] * 8,
-                           cudaMemcpyHostToDevice, s));
-    SPL_CK(cudaMemcpyAsync(as<float>(c->pal_rgb) + 3 * pc.pal_off[t], d->pal_rgb[t],
-                           pc.pal_n[t] * 12, cudaMemcpyHostToDevice, s));
-  }
+  // palettes (a few KB): exact knots and the float-float tables of the fast
+  // colourisation path
+  if ((st = ensure(c->pal_thr, (npal + 1) * 4)) || (st = ensure(c->pal_xff, (npal + 1) * 8)) ||
+      (st = ensure(c->pal_invff, (npal + 1) * 8)))
+    return st;
+  SPL_CK(cudaMemcpyAsync(c->pal_x.p, fs.pal_x.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_rgb.p, fs.pal_rgb.data(), (npal + 1) * 12, cudaMemcpyHostToDevice,
+                         s));
+  SPL_CK(cudaMemcpyAsync(c->pal_thr.p, fs.thr.data(), (npal + 1) * 4, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_xff.p, fs.xff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_invff.p, fs.invff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice,
+                         s));
+  // the host tables live in fs: wait for the copies before anything else
+  SPL_CK(cudaStreamSynchronize(s));
   pc.pal_x = as<double>(c->pal_x);
   pc.pal_rgb = as<float>(c->pal_rgb);
-  // float-float palette tables for the fast colourisation path
-  {
-    std::vector<float> thr(npal + 1);
-    std::vector<float2> xff(npal + 1), invff(npal + 1);
-    for (int t = 0; t < d->ptypes; ++t) {
-      const int nk = pc.pal_n[t], o = pc.pal_off[t];
-      if (!nk) continue;
-      const double *x = d->pal_x[t];
-      for (int k = 0; k < nk; ++k) {
-        thr[o + k] = least_float_above(x[k]);
-        xff[o + k] = split_ff(x[k]);
-        invff[o + k] = k + 1 < nk ? split_ff(1.0 / (x[k + 1] - x[k])) : make_float2(0.f, 0.f);
-      }
-      pc.pal_lo_f[t] = greatest_float_not_above(x[0]);
-      pc.pal_hi_f[t] = least_float_not_below(x[nk - 1]);
-    }
-    if ((st = ensure(c->pal_thr, (npal + 1) * 4)) || (st = ensure(c->pal_xff, (npal + 1) * 8)) ||
-        (st = ensure(c->pal_invff, (npal + 1) * 8)))
-      return st;
-    SPL_CK(cudaMemcpyAsync(c->pal_thr.p, thr.data(), (npal + 1) * 4, cudaMemcpyHostToDevice, s));
-    SPL_CK(cudaMemcpyAsync(c->pal_xff.p, xff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
-    SPL_CK(cudaMemcpyAsync(c->pal_invff.p, invff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice,
-                           s));
-    // the host vectors die at scope end: wait for the copies
-    SPL_CK(cudaStreamSynchronize(s));
-    pc.pal_thr = as<float>(c->pal_thr);
-    pc.pal_xff = as<float2>(c->pal_xff);
-    pc.pal_invff = as<float2>(c->pal_invff);
-  }
+  pc.pal_thr = as<float>(c->pal_thr);
+  pc.pal_xff = as<float2>(c->pal_xff);
+  pc.pal_invff = as<float2>(c->pal_invff);
   SPL_CK(cudaMemsetAsync(d_err, 0, 32, s));
   pc.n_fallback = d_err + 2;
 
@@ -414,6 +440,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   po.word_off = as<uint32_t>(c->poff);
   po.scan_scratch = c->scratch.p;
   po.err = d_err;
+  po.cap_c = (uint32_t)n;  // compact arrays hold every particle
   spl::launch_project(aos_dev, &soa, n, pc, po, true, s, &launches);
   uint32_t nact_h = 0;
   SPL_CK(cudaMemcpyAsync(&nact_h, d_nact, 4, cudaMemcpyDeviceToHost, s));
@@ -459,7 +486,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
                      as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->wide_list),
                      d_wide_n, s);
     launches += 2;
-    const int tb = bits_for(ntiles);
+    const int tb = spl::bits_for(ntiles);
     if (tb > 0) {
       spl::radix_sort_pairs(as<uint32_t>(c->tkey), as<uint32_t>(c->tval),
                             as<uint32_t>(c->tkey2), as<uint32_t>(c->tval2),
@@ -504,6 +531,11 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   sa.ftb_eps = d->ftb_epsilon;
   sa.config = d->splat_config;
   sa.pic = out->memspace == SPL_MEM_DEVICE ? out->pic : as<float>(c->pic);
+  sa.aux = nullptr;
+  if (c->differentiable && !d->a_eq_e) {
+    if ((st = ensure(c->aux, (size_t)xres * yres * 16))) return st;
+    sa.aux = as<float4>(c->aux);
+  }
   launches += spl::launch_splat(sa, s);
   SPL_CK(cudaGetLastError());
   c->last_splat = sa;
@@ -570,6 +602,110 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   S.n_tiles = ntiles;
   S.kernel_launches = launches;
   S.n_active = na;
+  return SPL_OK;
+}
+
+spl_status spl_context_set_differentiable(spl_context *c, int enable) {
+  if (!c) return fail(SPL_ERR_INVALID, "null ctx");
+  c->differentiable = enable != 0;
+  return SPL_OK;
+}
+
+spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g) {
+  if (!c || !gp || !g || !gp->pic) return fail(SPL_ERR_INVALID, "null argument");
+  if (c->last_T <= 0)
+    return fail(SPL_ERR_INVALID, "spl_render_backward: no frame was rendered on this context");
+  if (c->writeback_done)
+    return fail(SPL_ERR_UNSUPPORTED,
+                "spl_render_backward: the last frame wrote its particles back; render it "
+                "with writeback none to differentiate it");
+  if ((gp->memspace != SPL_MEM_HOST && gp->memspace != SPL_MEM_DEVICE) ||
+      (g->memspace != SPL_MEM_HOST && g->memspace != SPL_MEM_DEVICE))
+    return fail(SPL_ERR_INVALID, "spl_render_backward: bad memspace");
+  if (!c->last_splat.a_eq_e && !c->last_splat.aux)
+    return fail(SPL_ERR_INVALID,
+                "spl_render_backward: the ordered frame was rendered without "
+                "spl_context_set_differentiable(ctx, 1)");
+  SPL_CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const int64_t n = c->n, na = c->na;
+  const spl::SplatArgs &f = c->last_splat;
+  const size_t npix = (size_t)f.xres * f.yres * 3;
+  spl_status st;
+  float *outs[8] = {g->I, g->cr, g->cg, g->cb, g->x, g->y, g->z, g->r};
+  float *dev[8];
+  for (int k = 0; k < 8; ++k) {
+    dev[k] = nullptr;
+    if (!outs[k]) continue;
+    if (g->memspace == SPL_MEM_DEVICE) {
+      dev[k] = outs[k];
+    } else {
+      if ((st = ensure(c->gout[k], n * 4))) return st;
+      dev[k] = as<float>(c->gout[k]);
+    }
+  }
+  if ((st = ensure(c->gpos_c, na * 16)) || (st = ensure(c->gcol_c, na * 16)) ||
+      (st = ensure(c->camsum, 5 * 8)))
+    return st;
+  const float *gpic_d = gp->pic;
+  cudaEventRecord(c->ev[0], s);
+  if (gp->memspace == SPL_MEM_HOST) {
+    if ((st = ensure(c->gpic, npix * 4))) return st;
+    SPL_CK(cudaMemcpyAsync(c->gpic.p, gp->pic, npix * 4, cudaMemcpyHostToDevice, s));
+    gpic_d = as<float>(c->gpic);
+  }
+  SPL_CK(cudaMemsetAsync(c->camsum.p, 0, 5 * 8, s));
+  for (int k = 0; k < 8; ++k)
+    if (dev[k] && n > 0) SPL_CK(cudaMemsetAsync(dev[k], 0, n * 4, s));
+  cudaEventRecord(c->ev[1], s);
+  if (na > 0) {
+    SPL_CK(cudaMemsetAsync(c->gpos_c.p, 0, na * 16, s));
+    SPL_CK(cudaMemsetAsync(c->gcol_c.p, 0, na * 16, s));
+    spl::AdjArgs aa;
+    aa.f = f;
+    aa.gpic = gpic_d;
+    aa.gpos = as<float4>(c->gpos_c);
+    aa.gcol = as<float4>(c->gcol_c);
+    spl::launch_splat_adjoint(aa, s);
+  }
+  cudaEventRecord(c->ev[2], s);
+  spl::ProjAdjArgs pa;
+  pa.c = c->last_pc;
+  pa.aos = c->last_aos;
+  pa.soa = c->last_soa;
+  pa.pos_c = as<float4>(c->pos_c);
+  pa.idx_c = as<uint32_t>(c->idx_c);
+  pa.gpos = as<float4>(c->gpos_c);
+  pa.gcol = as<float4>(c->gcol_c);
+  pa.na = na;
+  pa.h2sigma = f.h2sigma;
+  pa.gI = dev[0]; pa.gcr = dev[1]; pa.gcg = dev[2]; pa.gcb = dev[3];
+  pa.gx = dev[4]; pa.gy = dev[5]; pa.gz = dev[6]; pa.gr = dev[7];
+  pa.cam_sums = as<double>(c->camsum);
+  spl::launch_project_adjoint(pa, s);
+  SPL_CK(cudaGetLastError());
+  cudaEventRecord(c->ev[3], s);
+  if (g->memspace == SPL_MEM_HOST)
+    for (int k = 0; k < 8; ++k)
+      if (dev[k] && n > 0)
+        SPL_CK(cudaMemcpyAsync(outs[k], dev[k], n * 4, cudaMemcpyDeviceToHost, s));
+  double cs[5];
+  SPL_CK(cudaMemcpyAsync(cs, c->camsum.p, 5 * 8, cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(c->ev[4], s);
+  SPL_CK(cudaStreamSynchronize(s));
+  SPL_CK(cudaGetLastError());
+  // campos: cam = A*(p - campos) and, in perspective, xshift/yshift =
+  // -xfac*A[0|1]*(centerpos - campos)
+  const float *m = c->last_pc.mat;
+  for (int j = 0; j < 3; ++j) {
+    double v = -(m[j] * cs[0] + m[4 + j] * cs[1] + m[8 + j] * cs[2]);
+    if (c->last_pc.projection) v += (double)c->last_pc.xfac * (m[j] * cs[3] + m[4 + j] * cs[4]);
+    g->campos[j] = v;
+  }
+  spl_stats &S = c->stats;
+  cudaEventElapsedTime(&S.bwd_splat_ms, c->ev[1], c->ev[2]);
+  cudaEventElapsedTime(&S.bwd_project_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&S.bwd_total_ms, c->ev[0], c->ev[4]);
   return SPL_OK;
 }
 

@@ -1,0 +1,870 @@
+// spl_batch.cu -- batched rendering: many frames (camera poses, resolutions,
+// additive or ordered modes, particle sets of uneven size) in one launch of a
+// captured CUDA graph.
+//
+// Per render, with no host round trip between stages:
+//   per frame   : activity flags of the frame's particle set (projection test)
+//   all frames  : one popcount scan -> every frame's active particles get
+//                 consecutive global record numbers, frame after frame
+//   per frame   : dense projection + colourisation into the shared records
+//   all frames  : stable depth sort by key, then stable sort by frame id
+//                 (visiting order: frame-major, each frame in its own order);
+//                 tile counts in that order, one scan, one emission of
+//                 (global tile id, record) pairs, one stable sort by tile id;
+//                 tile ranges; work queue = every (frame, tile) item, additive
+//                 frames first, each class longest list first
+//   splat       : one persistent kernel per class (additive / ordered) that
+//                 takes items from the queue; each item renders one tile of
+//                 one frame straight into that frame's image.
+// Sizes that depend on the data (active records, bin entries) are capacities
+// taken from a measured plan; the arrays past the live counts hold sentinel
+// keys that sort last, and a render whose counts outgrow the plan sets a
+// status bit, re-plans from new measurements and renders again.
+//
+// The autotuner picks the tile size and a launch configuration per class by
+// timing the pipeline (tile sizes 8, 16, 32) and the persistent splat (every
+// configuration that covers the tile size) on the batch itself.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "spl_host.h"
+
+namespace spl {
+namespace {
+
+struct FrameTile {
+  Tiling g;
+  uint32_t tile_base;
+};
+
+constexpr int kWide = 64;  // tiles above which a record goes to the warp path
+
+__global__ void k_frame_bounds(const uint32_t *__restrict__ word_off,
+                               const uint32_t *__restrict__ wbase, int nf, int64_t nwords,
+                               const uint32_t *__restrict__ total,
+                               uint32_t *__restrict__ actv_start) {
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f <= nf; f += gridDim.x * blockDim.x)
+    actv_start[f] = (f == nf || (int64_t)wbase[f] >= nwords) ? *total : word_off[wbase[f]];
+}
+
+// Frame of every live record (binary search over the frames' record starts);
+// sentinels past the live count: key all ones, frame nf, no tiles.
+__global__ void k_batch_records(const uint32_t *__restrict__ actv_start, int nf, uint32_t cap,
+                                uint32_t *__restrict__ key, uint32_t *__restrict__ count,
+                                uint32_t *__restrict__ frame, uint32_t *status) {
+  const uint32_t live = actv_start[nf];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && live > cap) atomicOr(status, 1u);
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < cap;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    if (r < live) {
+      int lo = 0, hi = nf;  // last f with actv_start[f] <= r
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (actv_start[mid] <= (uint32_t)r) lo = mid; else hi = mid;
+      }
+      frame[r] = (uint32_t)lo;
+    } else {
+      frame[r] = (uint32_t)nf;
+      key[r] = 0xffffffffu;
+      count[r] = 0u;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) k_emit_batch_narrow(
+    const float4 *__restrict__ pos, const uint32_t *__restrict__ count,
+    const uint32_t *__restrict__ order, const uint64_t *__restrict__ off, int64_t n,
+    const uint32_t *__restrict__ frame, const FrameTile *__restrict__ ft, uint64_t cap,
+    uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval, uint32_t *__restrict__ wide_list,
+    uint32_t *__restrict__ wide_n, uint32_t *status) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = __ldg(count + s);
+    if (c == 0) continue;
+    const uint64_t o = __ldg(off + s);
+    if (o + c > cap) {
+      // over capacity: this render is redone after a re-plan; the slots it
+      // would have used below the capacity become sentinels (sorted last,
+      // never read as entries)
+      atomicOr(status, 2u);
+      for (uint64_t p = o; p < cap && p < o + c; ++p) {
+        tkey[p] = 0xffffffffu;
+        tval[p] = 0u;
+      }
+      continue;
+    }
+    if (c > (uint32_t)kWide) {
+      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+      continue;
+    }
+    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
+    const FrameTile t = ft[__ldg(frame + i)];
+    const float4 p = __ldg(pos + i);
+    for_each_tile(p.x, p.y, p.z, t.g, [&](int tile, int j) {
+      tkey[o + j] = t.tile_base + (uint32_t)tile;
+      tval[o + j] = i;
+    });
+  }
+}
+
+// One warp per wide record: lane l takes tile rows miny + l, +32, ...
+__global__ void __launch_bounds__(256) k_emit_batch_wide(
+    const float4 *__restrict__ pos, const uint32_t *__restrict__ order,
+    const uint64_t *__restrict__ off, const uint32_t *__restrict__ wide_list,
+    const uint32_t *__restrict__ wide_n, const uint32_t *__restrict__ frame,
+    const FrameTile *__restrict__ ft, uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int64_t nw = *wide_n;
+  for (int64_t w = warp0; w < nw; w += nwarps) {
+    const uint32_t s = wide_list[w];
+    const uint32_t i = order ? __ldg(order + s) : s;
+    const FrameTile t = ft[__ldg(frame + i)];
+    const Tiling &g = t.g;
+    const uint64_t o = __ldg(off + s);
+    const float4 p = __ldg(pos + i);
+    const int T = g.T;
+    const float rfacr = fmul(0.75f, p.z);
+    const int minx = max(0, f2i(fadd(fsub(p.x, rfacr), 1.f)) / T);
+    const int maxx = min(g.ncx - 1, f2i(fadd(p.x, rfacr)) / T);
+    const int miny = max(0, f2i(fadd(fsub(p.y, rfacr), 1.f)) / T);
+    const int maxy = min(g.ncy - 1, f2i(fadd(p.y, rfacr)) / T);
+    const float rs = fadd(g.rcell, rfacr);
+    const float sumsq = fmul(rs, rs);
+    uint64_t base = o;
+    for (int iy0 = miny; iy0 <= maxy; iy0 += 32) {
+      const int iy = iy0 + lane;
+      int rc = 0;
+      float dy2 = 0.f;
+      if (iy <= maxy) {
+        const float dy = fsub(p.y, fadd(g.cmid0, (float)(iy * T)));
+        dy2 = fmul(dy, dy);
+        for (int ix = minx; ix <= maxx; ++ix) {
+          const float dx = fsub(p.x, fadd(g.cmid0, (float)(ix * T)));
+          if (fadd(fmul(dx, dx), dy2) < sumsq) ++rc;
+        }
+      }
+      int incl = rc;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += v;
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      uint64_t slot = base + (uint64_t)(incl - rc);
+      if (iy <= maxy && rc > 0) {
+        for (int ix = minx; ix <= maxx; ++ix) {
+          const float dx = fsub(p.x, fadd(g.cmid0, (float)(ix * T)));
+          if (fadd(fmul(dx, dx), dy2) < sumsq) {
+            tkey[slot] = t.tile_base + (uint32_t)(iy * g.ncx + ix);
+            tval[slot] = i;
+            ++slot;
+          }
+        }
+      }
+      base += (uint64_t)total;
+    }
+  }
+}
+
+__global__ void k_fill_tail(uint32_t *__restrict__ key, const uint64_t *__restrict__ live,
+                            uint64_t cap) {
+  const uint64_t from = min(*live, cap);
+  for (uint64_t p = from + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < cap;
+       p += (uint64_t)gridDim.x * blockDim.x)
+    key[p] = 0xffffffffu;
+}
+
+// tile_start[t] = first sorted position whose key is >= t; sentinel keys
+// (past every real tile) count as ntiles.
+__global__ void k_tile_ranges_clamped(const uint32_t *__restrict__ key, int64_t ne,
+                                      int64_t ntiles, uint32_t *__restrict__ tile_start) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= ne;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t kprev = p > 0 ? min((int64_t)key[p - 1], ntiles) : -1;
+    const int64_t kcur = p < ne ? min((int64_t)key[p], ntiles) : ntiles;
+    for (int64_t t = kprev + 1; t <= kcur; ++t) tile_start[t] = (uint32_t)p;
+  }
+}
+
+// Queue key: class (0 additive, 1 ordered) above an inverted 8-bit log of the
+// list length, so one ascending sort gives each class longest-first.
+__global__ void k_tile_cost_class(const uint32_t *__restrict__ tile_start, int64_t ntiles,
+                                  const uint32_t *__restrict__ frame_of_tile,
+                                  const uint8_t *__restrict__ frame_ordered,
+                                  uint32_t *__restrict__ key) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t cnt = tile_start[t + 1] - tile_start[t];
+    const int lg = (int)(8.f * __log2f((float)cnt + 1.f));
+    key[t] = ((uint32_t)frame_ordered[frame_of_tile[t]] << 8) | (255u - (uint32_t)min(lg, 255));
+  }
+}
+
+int grid_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 16) b = 152 * 16;
+  return (int)(b > 0 ? b : 1);
+}
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+}  // namespace spl
+
+using spl::DevBuf;
+
+struct spl_batch {
+  spl_context *ctx = nullptr;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<spl_particles> sets;
+  std::vector<spl_batch_frame> frames;  // descs point at the palette copies below
+  std::vector<std::vector<double>> pal_x_copy;
+  std::vector<std::vector<float>> pal_rgb_copy;
+  spl_batch_options opt{};
+  int T = 16, cfg_add = 0, cfg_abs = 2;
+  // plan
+  std::vector<spl::FrameSetup> fs;
+  std::vector<spl::ProjConst> pc;      // device palette pointers filled in
+  std::vector<uint32_t> wbase;         // activity-word base per frame (+ total)
+  std::vector<uint32_t> tbase;         // global tile base per frame (+ total)
+  int64_t nwords = 0, ntiles = 0, n_add_tiles = 0, cap_a = 0, cap_e = 0;
+  bool any_ordered = false;
+  int frame_bits = 1, tile_bits = 1;
+  std::vector<DevBuf *> owned;
+  DevBuf pal_x, pal_rgb, pal_thr, pal_xff, pal_invff;
+  DevBuf flags, word_off, d_wbase, d_tbase, actv_start;
+  DevBuf pos_c, col_c, idx_c, count_c, key_c, frame_c;
+  DevBuf ktmp, vtmp, kout, perm1, fkey, perm, count_seq, off, wide_list, radix_scr;
+  DevBuf tkey, tval, tkey2, tval2, tkey_s, tval_s;
+  DevBuf tile_start, tcost, tcost_s, work, work_tmp, frame_of_tile, frame_ord, ft, splat_args;
+  DevBuf status;  // [0] overflow bits, [1] wide count, [2],[3] queue counters,
+                  // [4] error word, [5] live records, [6..7] spare
+  uint32_t *h_status = nullptr;  // pinned copy of the first 8 status words
+  uint64_t *h_entries = nullptr; // pinned copy of the live entry count
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int launches = 0;
+  spl_batch_info info{};
+};
+
+namespace {
+
+spl_status fail(spl_status code, const std::string &msg) { return spl::host_fail(code, msg); }
+
+#define BCK(call)                                                                       \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess) {                                                            \
+      cudaGetLastError();                                                               \
+      return fail(SPL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    }                                                                                   \
+  } while (0)
+
+spl_status dev_alloc(spl_batch *b, DevBuf &d, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  if (d.bytes >= bytes) return SPL_OK;
+  if (d.p) cudaFree(d.p);
+  d.p = nullptr;
+  d.bytes = 0;
+  cudaError_t e = cudaMalloc(&d.p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SPL_ERR_ALLOC, "batch: cudaMalloc(" + std::to_string(bytes) + "): " +
+                                   cudaGetErrorString(e));
+  }
+  d.bytes = bytes;
+  if (std::find(b->owned.begin(), b->owned.end(), &d) == b->owned.end()) b->owned.push_back(&d);
+  return SPL_OK;
+}
+
+template <typename T>
+T *as(DevBuf &d) {
+  return static_cast<T *>(d.p);
+}
+
+void drop_graph(spl_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+const void *set_aos(const spl_particles &p) {
+  return p.layout == SPL_LAYOUT_AOS ? p.aos : nullptr;
+}
+
+spl::SoAIn set_soa(const spl_particles &p) {
+  return spl::SoAIn{p.x, p.y, p.z, p.r, p.I, p.cr, p.cg, p.cb, p.type};
+}
+
+// Measured sizes at tile size T: one plain render of every frame on the
+// context (its image lands in the frame's buffer and is redrawn by the batch).
+spl_status measure(spl_batch *b, int T, int64_t &acts, int64_t &ents) {
+  acts = ents = 0;
+  for (const auto &fr : b->frames) {
+    spl_frame_desc d = fr.desc;
+    d.tile_size = T;
+    d.splat_config = -1;
+    spl_image img{fr.pic, SPL_MEM_DEVICE};
+    spl_status st = spl_render(b->ctx, &d, &b->sets[fr.set], &img, SPL_WRITEBACK_NONE);
+    if (st) return st;
+    spl_stats s;
+    spl_get_stats(b->ctx, &s);
+    acts += s.n_active;
+    ents += s.n_entries;
+  }
+  return SPL_OK;
+}
+
+// Buffers, per-frame constants and the static tables for tile size T and the
+// given capacities.
+spl_status plan(spl_batch *b, int T, int64_t cap_a, int64_t cap_e) {
+  drop_graph(b);
+  const int nf = (int)b->frames.size();
+  b->T = T;
+  b->fs.assign(nf, spl::FrameSetup());
+  b->pc.assign(nf, spl::ProjConst());
+  b->wbase.assign(nf + 1, 0);
+  b->tbase.assign(nf + 1, 0);
+  int64_t npal = 0, words = 0, tiles = 0, add_tiles = 0;
+  b->any_ordered = false;
+  std::vector<uint8_t> ordered(nf, 0);
+  spl_status st;
+  for (int f = 0; f < nf; ++f) {
+    const spl_batch_frame &fr = b->frames[f];
+    if ((st = spl::frame_setup(&fr.desc, T, false, b->fs[f]))) return st;
+    b->wbase[f] = (uint32_t)words;
+    b->tbase[f] = (uint32_t)tiles;
+    words += (b->sets[fr.set].n + 31) / 32;
+    tiles += b->fs[f].ntiles;
+    npal += b->fs[f].npal + 1;
+    ordered[f] = fr.desc.a_eq_e ? 0 : 1;
+    if (fr.desc.a_eq_e) add_tiles += b->fs[f].ntiles;
+    if (b->fs[f].do_sort) b->any_ordered = true;
+  }
+  if (tiles >= 0x7fffffffLL || words >= 0xffffffffLL || cap_a >= 0xffffffffLL ||
+      cap_e >= 0xffffffffLL)
+    return fail(SPL_ERR_CAPACITY, "batch: more than 2^31 tiles or 2^32 records/entries");
+  b->wbase[nf] = (uint32_t)words;
+  b->tbase[nf] = (uint32_t)tiles;
+  b->nwords = words;
+  b->ntiles = tiles;
+  b->n_add_tiles = add_tiles;
+  b->cap_a = std::max<int64_t>(cap_a, 1);
+  b->cap_e = std::max<int64_t>(cap_e, 1);
+  b->frame_bits = spl::bits_for(nf + 1);
+  b->tile_bits = spl::bits_for(tiles + 1);
+  const int64_t A = b->cap_a, E = b->cap_e;
+
+  // ---- buffers -------------------------------------------------------------
+  size_t scan_b = spl::scan_scratch_bytes(std::max<int64_t>(words, A + 1));
+  size_t radix_b = std::max(spl::radix_scratch_bytes(A), spl::radix_scratch_bytes(E));
+  radix_b = std::max(radix_b, spl::radix_scratch_bytes(tiles));
+  radix_b = std::max(radix_b, scan_b);
+  if ((st = dev_alloc(b, b->pal_x, npal * 8)) || (st = dev_alloc(b, b->pal_rgb, npal * 12)) ||
+      (st = dev_alloc(b, b->pal_thr, npal * 4)) || (st = dev_alloc(b, b->pal_xff, npal * 8)) ||
+      (st = dev_alloc(b, b->pal_invff, npal * 8)) ||
+      (st = dev_alloc(b, b->flags, words * 4)) || (st = dev_alloc(b, b->word_off, words * 4)) ||
+      (st = dev_alloc(b, b->d_wbase, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->d_tbase, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->actv_start, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->pos_c, A * 16)) || (st = dev_alloc(b, b->col_c, A * 16)) ||
+      (st = dev_alloc(b, b->idx_c, A * 4)) || (st = dev_alloc(b, b->count_c, A * 4)) ||
+      (st = dev_alloc(b, b->key_c, A * 4)) || (st = dev_alloc(b, b->frame_c, A * 4)) ||
+      (st = dev_alloc(b, b->ktmp, A * 4)) || (st = dev_alloc(b, b->vtmp, A * 4)) ||
+      (st = dev_alloc(b, b->kout, A * 4)) || (st = dev_alloc(b, b->perm1, A * 4)) ||
+      (st = dev_alloc(b, b->fkey, A * 4)) || (st = dev_alloc(b, b->perm, A * 4)) ||
+      (st = dev_alloc(b, b->count_seq, A * 4)) || (st = dev_alloc(b, b->off, (A + 1) * 8)) ||
+      (st = dev_alloc(b, b->wide_list, A * 4)) || (st = dev_alloc(b, b->radix_scr, radix_b)) ||
+      (st = dev_alloc(b, b->tkey, E * 4)) || (st = dev_alloc(b, b->tval, E * 4)) ||
+      (st = dev_alloc(b, b->tkey2, E * 4)) || (st = dev_alloc(b, b->tval2, E * 4)) ||
+      (st = dev_alloc(b, b->tkey_s, E * 4)) || (st = dev_alloc(b, b->tval_s, E * 4)) ||
+      (st = dev_alloc(b, b->tile_start, (tiles + 1) * 4)) ||
+      (st = dev_alloc(b, b->tcost, tiles * 4)) || (st = dev_alloc(b, b->tcost_s, tiles * 4)) ||
+      (st = dev_alloc(b, b->work, tiles * 4)) || (st = dev_alloc(b, b->work_tmp, tiles * 4)) ||
+      (st = dev_alloc(b, b->frame_of_tile, tiles * 4)) ||
+      (st = dev_alloc(b, b->frame_ord, nf)) ||
+      (st = dev_alloc(b, b->ft, nf * sizeof(spl::FrameTile))) ||
+      (st = dev_alloc(b, b->splat_args, nf * sizeof(spl::SplatArgs))) ||
+      (st = dev_alloc(b, b->status, 64)))
+    return st;
+
+  // ---- static tables ---------------------------------------------------------
+  std::vector<double> px;
+  std::vector<float> prgb, pthr;
+  std::vector<float2> pxff, pinvff;
+  std::vector<uint32_t> fot((size_t)tiles);
+  std::vector<spl::FrameTile> fts(nf);
+  std::vector<spl::SplatArgs> sas(nf);
+  const float h2sigma =
+      (float)(0.5 * std::pow(3.141592653589793238462643383279502884197, -1. / 6.));
+  for (int f = 0; f < nf; ++f) {
+    const spl::FrameSetup &s = b->fs[f];
+    const size_t o = px.size();
+    px.insert(px.end(), s.pal_x.begin(), s.pal_x.end());
+    prgb.insert(prgb.end(), s.pal_rgb.begin(), s.pal_rgb.end());
+    pthr.insert(pthr.end(), s.thr.begin(), s.thr.end());
+    pxff.insert(pxff.end(), s.xff.begin(), s.xff.end());
+    pinvff.insert(pinvff.end(), s.invff.begin(), s.invff.end());
+    spl::ProjConst c = s.pc;
+    c.pal_x = as<double>(b->pal_x) + o;
+    c.pal_rgb = as<float>(b->pal_rgb) + 3 * o;
+    c.pal_thr = as<float>(b->pal_thr) + o;
+    c.pal_xff = as<float2>(b->pal_xff) + o;
+    c.pal_invff = as<float2>(b->pal_invff) + o;
+    c.n_fallback = nullptr;
+    b->pc[f] = c;
+    for (int64_t t = 0; t < s.ntiles; ++t) fot[b->tbase[f] + t] = (uint32_t)f;
+    fts[f].g = s.g;
+    fts[f].tile_base = b->tbase[f];
+    const spl_frame_desc &d = b->frames[f].desc;
+    spl::SplatArgs &a = sas[f];
+    std::memset(&a, 0, sizeof(a));
+    a.pos = as<float4>(b->pos_c);
+    a.col = as<float4>(b->col_c);
+    a.entries = as<uint32_t>(b->tval_s);
+    a.tile_start = as<uint32_t>(b->tile_start) + b->tbase[f];
+    a.tile_order = nullptr;
+    a.T = T;
+    a.ncx = s.g.ncx;
+    a.ncy = s.g.ncy;
+    a.xres = d.xres;
+    a.yres = d.yres;
+    a.gray = d.gray_absorption;
+    a.h2sigma = h2sigma;
+    a.a_eq_e = d.a_eq_e ? 1 : 0;
+    a.order_mode = d.order_mode;
+    a.ftb_eps = d.ftb_epsilon;
+    a.config = -1;
+    a.pic = b->frames[f].pic;
+  }
+  cudaStream_t s = b->stream;
+  BCK(cudaMemcpyAsync(b->pal_x.p, px.data(), px.size() * 8, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->pal_rgb.p, prgb.data(), prgb.size() * 4, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->pal_thr.p, pthr.data(), pthr.size() * 4, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->pal_xff.p, pxff.data(), pxff.size() * 8, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->pal_invff.p, pinvff.data(), pinvff.size() * 8, cudaMemcpyHostToDevice,
+                      s));
+  BCK(cudaMemcpyAsync(b->d_wbase.p, b->wbase.data(), (nf + 1) * 4, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->d_tbase.p, b->tbase.data(), (nf + 1) * 4, cudaMemcpyHostToDevice, s));
+  if (tiles)
+    BCK(cudaMemcpyAsync(b->frame_of_tile.p, fot.data(), tiles * 4, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->frame_ord.p, ordered.data(), nf, cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->ft.p, fts.data(), nf * sizeof(spl::FrameTile), cudaMemcpyHostToDevice,
+                      s));
+  BCK(cudaMemcpyAsync(b->splat_args.p, sas.data(), nf * sizeof(spl::SplatArgs),
+                      cudaMemcpyHostToDevice, s));
+  BCK(cudaStreamSynchronize(s));
+  b->info.cap_active = b->cap_a;
+  b->info.cap_entries = b->cap_e;
+  b->info.total_tiles = tiles;
+  b->info.tile_size = T;
+  return SPL_OK;
+}
+
+// The work queue of one class: 0 additive frames (the first n_add_tiles
+// items), 1 ordered frames (the rest); counter in status word 2 + cls.
+spl::BatchSplatArgs queue_args(spl_batch *b, int cls) {
+  spl::BatchSplatArgs q;
+  q.frames = as<spl::SplatArgs>(b->splat_args);
+  q.tile_base = as<uint32_t>(b->d_tbase);
+  q.frame_of_tile = as<uint32_t>(b->frame_of_tile);
+  q.work = as<uint32_t>(b->work);
+  q.T = b->T;
+  q.work_begin = cls == 0 ? 0u : (uint32_t)b->n_add_tiles;
+  q.nwork = cls == 0 ? (uint32_t)b->n_add_tiles : (uint32_t)(b->ntiles - b->n_add_tiles);
+  q.counter = as<uint32_t>(b->status) + 2 + cls;
+  return q;
+}
+
+// Every kernel of one batch render, in stream order (eager or under capture).
+// splat_class: -1 both queues, 0 additive only, 1 ordered only, 2 none.
+spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
+  const int nf = (int)b->frames.size();
+  int launches = 0;
+  uint32_t *status = as<uint32_t>(b->status);
+  uint32_t *err = status + 4;
+  const uint32_t capA = (uint32_t)b->cap_a;
+  const uint64_t capE = (uint64_t)b->cap_e;
+  BCK(cudaMemsetAsync(status, 0, 64, s));
+  // ---- projection: flags per frame, one scan, dense per frame -------------------
+  spl::ProjectOut po;
+  std::memset(&po, 0, sizeof(po));
+  po.pos_c = as<float4>(b->pos_c);
+  po.col_c = as<float4>(b->col_c);
+  po.idx_c = as<uint32_t>(b->idx_c);
+  po.count_c = as<uint32_t>(b->count_c);
+  po.key_c = as<uint32_t>(b->key_c);
+  po.cap_c = capA;
+  po.err = err;
+  for (int f = 0; f < nf; ++f) {
+    const spl_particles &p = b->sets[b->frames[f].set];
+    const spl::SoAIn soa = set_soa(p);
+    po.flags = as<uint32_t>(b->flags) + b->wbase[f];
+    spl::launch_project_flags(set_aos(p), &soa, p.n, b->pc[f], po, s);
+    if (p.n > 0) ++launches;
+  }
+  spl::scan_popc(as<uint32_t>(b->flags), b->nwords, as<uint32_t>(b->word_off), status + 5,
+                 b->radix_scr.p, s, &launches);
+  spl::k_frame_bounds<<<1, 256, 0, s>>>(as<uint32_t>(b->word_off), as<uint32_t>(b->d_wbase), nf,
+                                        b->nwords, status + 5, as<uint32_t>(b->actv_start));
+  ++launches;
+  for (int f = 0; f < nf; ++f) {
+    const spl_particles &p = b->sets[b->frames[f].set];
+    const spl::SoAIn soa = set_soa(p);
+    po.flags = as<uint32_t>(b->flags) + b->wbase[f];
+    po.word_off = as<uint32_t>(b->word_off) + b->wbase[f];
+    spl::launch_project_dense(set_aos(p), &soa, p.n, b->pc[f], po, s);
+    if (p.n > 0) ++launches;
+  }
+  spl::k_batch_records<<<spl::grid_for(capA), 256, 0, s>>>(
+      as<uint32_t>(b->actv_start), nf, capA, as<uint32_t>(b->key_c), as<uint32_t>(b->count_c),
+      as<uint32_t>(b->frame_c), status);
+  ++launches;
+  // ---- visiting order: stable by depth key, then stable by frame ---------------------
+  const uint32_t *order = nullptr;
+  if (b->any_ordered) {
+    spl::radix_sort_pairs(as<uint32_t>(b->key_c), nullptr, as<uint32_t>(b->ktmp),
+                          as<uint32_t>(b->vtmp), as<uint32_t>(b->kout), as<uint32_t>(b->perm1),
+                          capA, 0, 32, false, b->radix_scr.p, s, &launches, err, true);
+    spl::launch_gather_u32(as<uint32_t>(b->frame_c), as<uint32_t>(b->perm1), capA,
+                           as<uint32_t>(b->fkey), s);
+    ++launches;
+    spl::radix_sort_pairs(as<uint32_t>(b->fkey), as<uint32_t>(b->perm1), as<uint32_t>(b->ktmp),
+                          as<uint32_t>(b->vtmp), as<uint32_t>(b->kout), as<uint32_t>(b->perm),
+                          capA, 0, b->frame_bits, false, b->radix_scr.p, s, &launches, err, true);
+    order = as<uint32_t>(b->perm);
+  }
+  // ---- binning over all frames ------------------------------------------------------
+  const uint32_t *count_seq = as<uint32_t>(b->count_c);
+  if (order) {
+    spl::launch_gather_u32(as<uint32_t>(b->count_c), order, capA, as<uint32_t>(b->count_seq), s);
+    ++launches;
+    count_seq = as<uint32_t>(b->count_seq);
+  }
+  uint64_t *off = as<uint64_t>(b->off);
+  spl::scan_counts(count_seq, nullptr, capA, off, b->radix_scr.p, s, &launches);
+  spl::k_emit_batch_narrow<<<spl::grid_for(capA), 256, 0, s>>>(
+      as<float4>(b->pos_c), count_seq, order, off, capA, as<uint32_t>(b->frame_c),
+      as<spl::FrameTile>(b->ft), capE, as<uint32_t>(b->tkey), as<uint32_t>(b->tval),
+      as<uint32_t>(b->wide_list), status + 1, status);
+  spl::k_emit_batch_wide<<<152 * 4, 256, 0, s>>>(
+      as<float4>(b->pos_c), order, off, as<uint32_t>(b->wide_list), status + 1,
+      as<uint32_t>(b->frame_c), as<spl::FrameTile>(b->ft), as<uint32_t>(b->tkey),
+      as<uint32_t>(b->tval));
+  spl::k_fill_tail<<<spl::grid_for(capE), 256, 0, s>>>(as<uint32_t>(b->tkey), off + capA, capE);
+  launches += 3;
+  spl::radix_sort_pairs(as<uint32_t>(b->tkey), as<uint32_t>(b->tval), as<uint32_t>(b->tkey2),
+                        as<uint32_t>(b->tval2), as<uint32_t>(b->tkey_s), as<uint32_t>(b->tval_s),
+                        (int64_t)capE, 0, b->tile_bits, true, b->radix_scr.p, s, &launches, err,
+                        true);
+  spl::k_tile_ranges_clamped<<<spl::grid_for((int64_t)capE + 1), 256, 0, s>>>(
+      as<uint32_t>(b->tkey_s), (int64_t)capE, b->ntiles, as<uint32_t>(b->tile_start));
+  spl::k_tile_cost_class<<<spl::grid_for(b->ntiles), 256, 0, s>>>(
+      as<uint32_t>(b->tile_start), b->ntiles, as<uint32_t>(b->frame_of_tile),
+      as<uint8_t>(b->frame_ord), as<uint32_t>(b->tcost));
+  launches += 2;
+  spl::radix_sort_pairs(as<uint32_t>(b->tcost), nullptr, as<uint32_t>(b->tcost_s),
+                        as<uint32_t>(b->work_tmp), as<uint32_t>(b->tcost_s),
+                        as<uint32_t>(b->work), b->ntiles, 0, 9, false, b->radix_scr.p, s,
+                        &launches, err, true);
+  // ---- splat: one persistent launch per class ---------------------------------------------
+  if (splat_class == -1 || splat_class == 0)
+    launches += spl::launch_splat_queue(queue_args(b, 0), b->cfg_add, s);
+  if (splat_class == -1 || splat_class == 1)
+    launches += spl::launch_splat_queue(queue_args(b, 1), b->cfg_abs, s);
+  BCK(cudaMemcpyAsync(b->h_status, status, 32, cudaMemcpyDeviceToHost, s));
+  BCK(cudaMemcpyAsync(b->h_entries, off + capA, 8, cudaMemcpyDeviceToHost, s));
+  b->launches = launches;
+  return SPL_OK;
+}
+
+spl_status capture(spl_batch *b) {
+  drop_graph(b);
+  cudaStream_t s = b->stream;
+  BCK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  spl_status st = enqueue(b, s);
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(s, &g);
+  if (st) {
+    if (g) cudaGraphDestroy(g);
+    return st;
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SPL_ERR_CUDA, std::string("batch: graph capture failed: ") + cudaGetErrorString(e));
+  }
+  e = cudaGraphInstantiate(&b->exec, g, 0);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaGraphDestroy(g);
+    return fail(SPL_ERR_CUDA, std::string("batch: graph instantiation failed: ") +
+                                  cudaGetErrorString(e));
+  }
+  b->graph = g;
+  return SPL_OK;
+}
+
+// One render (graph or eager), waiting for completion; returns the status
+// words through the pinned copies.
+spl_status run_once(spl_batch *b, float *ms) {
+  cudaStream_t s = b->stream;
+  BCK(cudaEventRecord(b->ev0, s));
+  if (b->exec) {
+    BCK(cudaGraphLaunch(b->exec, s));
+  } else {
+    spl_status st = enqueue(b, s);
+    if (st) return st;
+  }
+  BCK(cudaEventRecord(b->ev1, s));
+  BCK(cudaStreamSynchronize(s));
+  BCK(cudaGetLastError());
+  if (ms) cudaEventElapsedTime(ms, b->ev0, b->ev1);
+  return SPL_OK;
+}
+
+spl_status check_status(spl_batch *b, bool &overflow) {
+  const uint32_t *h = b->h_status;
+  overflow = (h[0] & 3u) != 0 || (h[4] & 8u) != 0;
+  if (h[4] & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
+  if (h[4] & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
+  return SPL_OK;
+}
+
+int64_t with_margin(int64_t v, float margin) {
+  return (int64_t)std::ceil((double)v * (double)margin) + 1024;
+}
+
+spl_status build(spl_batch *b, int T) {
+  int64_t acts, ents;
+  spl_status st;
+  if ((st = measure(b, T, acts, ents))) return st;
+  return plan(b, T, with_margin(acts, b->opt.capacity_margin),
+              with_margin(ents, b->opt.capacity_margin));
+}
+
+// Autotuner: for each tile size, the fastest splat configuration per class
+// (persistent launch timed alone on this batch's bins), then the fastest tile
+// size by timing the whole pipeline.
+spl_status autotune(spl_batch *b) {
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<int> sizes;
+  if (b->opt.tile_size > 0) sizes.push_back(b->opt.tile_size);
+  else sizes = {8, 16, 32};
+  bool has_add = false, has_ord = false;
+  for (const auto &fr : b->frames) (fr.desc.a_eq_e ? has_add : has_ord) = true;
+  float best_ms = 1e30f;
+  int best_T = sizes[0], best_add = 0, best_abs = 0;
+  spl_status st;
+  for (int T : sizes) {
+    if ((st = build(b, T))) return st;
+    int cands[8], nc = 0;
+    for (int c = 0; c < spl::splat_config_count(); ++c)
+      if (spl::splat_config_valid(c, T)) cands[nc++] = c;
+    if (nc == 0) continue;
+    // bins of this tile size once; then each class's splat timed alone per
+    // configuration (second of two launches)
+    if ((st = enqueue(b, b->stream, 2))) return st;
+    BCK(cudaStreamSynchronize(b->stream));
+    bool overflow = false;
+    if ((st = check_status(b, overflow))) return st;
+    for (int cls = 0; cls < 2; ++cls) {
+      const bool present = cls == 0 ? has_add : has_ord;
+      const int fixed = cls == 0 ? b->opt.splat_config_additive : b->opt.splat_config_absorption;
+      const bool is_fixed = fixed >= 0 && spl::splat_config_valid(fixed, T);
+      int pick = is_fixed ? fixed : spl::splat_default_config(T, cls == 0);
+      if (present && !is_fixed) {
+        float bms = 1e30f;
+        for (int k = 0; k < nc; ++k) {
+          float ms = 0.f;
+          for (int rep = 0; rep < 2; ++rep) {
+            BCK(cudaMemsetAsync(as<uint32_t>(b->status) + 2 + cls, 0, 4, b->stream));
+            BCK(cudaEventRecord(b->ev0, b->stream));
+            spl::launch_splat_queue(queue_args(b, cls), cands[k], b->stream);
+            BCK(cudaEventRecord(b->ev1, b->stream));
+            BCK(cudaStreamSynchronize(b->stream));
+            BCK(cudaGetLastError());
+            cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+          }
+          if (ms < bms) {
+            bms = ms;
+            pick = cands[k];
+          }
+        }
+      }
+      (cls == 0 ? b->cfg_add : b->cfg_abs) = pick;
+    }
+    float tot = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      if ((st = run_once(b, &tot))) return st;
+    }
+    if ((st = check_status(b, overflow))) return st;
+    if (tot < best_ms && !overflow) {
+      best_ms = tot;
+      best_T = T;
+      best_add = b->cfg_add;
+      best_abs = b->cfg_abs;
+    }
+  }
+  b->cfg_add = best_add;
+  b->cfg_abs = best_abs;
+  if (b->T != best_T || sizes.size() > 1) {
+    if ((st = build(b, best_T))) return st;
+  }
+  b->info.tune_ms = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() -
+                                                             t0).count();
+  return SPL_OK;
+}
+
+void free_batch(spl_batch *b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  for (DevBuf *d : b->owned)
+    if (d->p) cudaFree(d->p);
+  if (b->h_status) cudaFreeHost(b->h_status);
+  if (b->h_entries) cudaFreeHost(b->h_entries);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+void spl_batch_options_defaults(spl_batch_options *o) {
+  if (!o) return;
+  o->tile_size = 0;
+  o->splat_config_additive = -1;
+  o->splat_config_absorption = -1;
+  o->capacity_margin = 1.1f;
+  o->use_graph = 1;
+}
+
+spl_status spl_batch_create(spl_context *ctx, const spl_particles *sets, int nsets,
+                            const spl_batch_frame *frames, int nframes,
+                            const spl_batch_options *opt, spl_batch **out) {
+  if (!ctx || !out || (nsets > 0 && !sets) || nframes < 1 || !frames)
+    return fail(SPL_ERR_INVALID, "batch: null argument or no frames");
+  *out = nullptr;
+  spl_batch_options o;
+  spl_batch_options_defaults(&o);
+  if (opt) o = *opt;
+  if (o.tile_size < 0 || o.tile_size > 64 || !(o.capacity_margin > 0.f))
+    return fail(SPL_ERR_INVALID, "batch: bad options");
+  for (int k = 0; k < nsets; ++k) {
+    const spl_particles &p = sets[k];
+    if (p.memspace != SPL_MEM_DEVICE)
+      return fail(SPL_ERR_UNSUPPORTED, "batch: particle sets must be device-resident");
+  }
+  for (int f = 0; f < nframes; ++f) {
+    const spl_batch_frame &fr = frames[f];
+    if (fr.set < 0 || fr.set >= nsets)
+      return fail(SPL_ERR_INVALID, "batch: frame " + std::to_string(f) + " names no set");
+    spl_image img{fr.pic, SPL_MEM_DEVICE};
+    spl_frame_desc d = fr.desc;
+    d.tile_size = o.tile_size > 0 ? o.tile_size : 16;
+    spl_status st = spl::validate_frame(&d, &sets[fr.set], &img);
+    if (st) return st;
+  }
+  spl_batch *b = new spl_batch();
+  b->ctx = ctx;
+  b->device = spl::context_device(ctx);
+  b->sets.assign(sets, sets + nsets);
+  b->frames.assign(frames, frames + nframes);
+  b->opt = o;
+  cudaSetDevice(b->device);
+  spl_status st = SPL_OK;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+      cudaMallocHost((void **)&b->h_status, 64) != cudaSuccess ||
+      cudaMallocHost((void **)&b->h_entries, 8) != cudaSuccess) {
+    cudaGetLastError();
+    free_batch(b);
+    return fail(SPL_ERR_CUDA, "batch: stream, event or pinned-memory creation failed");
+  }
+  // private copies of the frames' palettes: re-plans read them after create
+  b->pal_x_copy.reserve((size_t)nframes * SPL_MAX_TYPES);
+  b->pal_rgb_copy.reserve((size_t)nframes * SPL_MAX_TYPES);
+  for (auto &fr : b->frames) {
+    for (int t = 0; t < fr.desc.ptypes; ++t) {
+      if (fr.desc.color_is_vector[t] || fr.desc.pal_n[t] < 1) continue;
+      const int nk = fr.desc.pal_n[t];
+      b->pal_x_copy.emplace_back(fr.desc.pal_x[t], fr.desc.pal_x[t] + nk);
+      b->pal_rgb_copy.emplace_back(fr.desc.pal_rgb[t], fr.desc.pal_rgb[t] + 3 * nk);
+      fr.desc.pal_x[t] = b->pal_x_copy.back().data();
+      fr.desc.pal_rgb[t] = b->pal_rgb_copy.back().data();
+    }
+  }
+  if ((st = autotune(b))) {
+    free_batch(b);
+    return st;
+  }
+  b->info.splat_config_additive = b->cfg_add;
+  b->info.splat_config_absorption = b->cfg_abs;
+  if (o.use_graph && (st = capture(b))) {
+    free_batch(b);
+    return st;
+  }
+  b->info.graph = b->exec ? 1 : 0;
+  b->info.replans = 0;
+  *out = b;
+  return SPL_OK;
+}
+
+spl_status spl_batch_render(spl_batch *b) {
+  if (!b) return fail(SPL_ERR_INVALID, "null batch");
+  BCK(cudaSetDevice(b->device));
+  spl_status st;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    float ms = 0.f;
+    if ((st = run_once(b, &ms))) return st;
+    bool overflow = false;
+    if ((st = check_status(b, overflow))) return st;
+    b->info.render_ms = ms;
+    b->info.n_active = b->h_status[5];
+    b->info.n_entries = (int64_t)*b->h_entries;
+    b->info.kernel_launches = b->launches;
+    if (!overflow) return SPL_OK;
+    // counts outgrew the plan: measure again with a margin of at least 1.1
+    b->opt.capacity_margin = std::max(b->opt.capacity_margin, 1.1f);
+    ++b->info.replans;
+    if ((st = build(b, b->T))) return st;
+    if (b->opt.use_graph && (st = capture(b))) return st;
+  }
+  return fail(SPL_ERR_CAPACITY, "batch: capacities still exceeded after re-planning");
+}
+
+spl_status spl_batch_get_info(const spl_batch *b, spl_batch_info *info) {
+  if (!b || !info) return fail(SPL_ERR_INVALID, "null argument");
+  *info = b->info;
+  info->tile_size = b->T;
+  info->splat_config_additive = b->cfg_add;
+  info->splat_config_absorption = b->cfg_abs;
+  info->graph = b->exec ? 1 : 0;
+  info->cap_active = b->cap_a;
+  info->cap_entries = b->cap_e;
+  info->total_tiles = b->ntiles;
+  return SPL_OK;
+}
+
+spl_status spl_batch_destroy(spl_batch *b) {
+  free_batch(b);
+  return SPL_OK;
+}
+
+}  // extern "C"

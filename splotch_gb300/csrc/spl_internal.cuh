@@ -190,6 +190,8 @@ struct ProjectOut {
   uint32_t *idx_c;    // particle index of each active particle
   uint32_t *count_c;
   uint32_t *key_c;    // may be null
+  uint32_t cap_c;        // capacity of the compact arrays: records at or beyond
+                         // it are dropped and bit 3 (8) of *err is set
   uint32_t *n_act;       // number of active particles
   uint32_t *flags;       // activity bits, (n+31)/32 words
   uint32_t *word_off;    // exclusive scan of the words' popcounts
@@ -206,6 +208,14 @@ struct SoAIn {
 // active-only form (the render path) over the full form.
 void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
                     ProjectOut o, bool compact, cudaStream_t s, int *launches);
+// The two passes of the compact form on their own (the batch runs the
+// popcount scan once over every frame's activity words): o.flags and
+// o.word_off point at this frame's words, o.pos_c etc. at the arrays shared
+// by all frames (records land at the scanned global positions).
+void launch_project_flags(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                          const ProjectOut &o, cudaStream_t s);
+void launch_project_dense(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                          const ProjectOut &o, cudaStream_t s);
 
 // Exclusive scan of popcount(words[i]) into out (nwords entries); the total
 // goes to *total.
@@ -271,11 +281,60 @@ struct SplatArgs {
   float ftb_eps;
   int config;                  // launch configuration (-1: default for T)
   float *pic;                  // device, x-major xres*yres*3
+  // ordered frames kept for the adjoint (null: not kept): per pixel, x-major,
+  // the optical depth sum(E*att) over the fragments composited (rgb) and, in
+  // w (as uint bits), the tile-list position below which nothing was
+  // composited (front-to-back early stop; 0 when the whole list was used)
+  float4 *aux;
 };
 int launch_splat(const SplatArgs &a, cudaStream_t s);
 int splat_config_count();
 bool splat_config_valid(int cfg, int T);
 int splat_default_config(int T, bool additive);
 void launch_count_fragments(const SplatArgs &a, unsigned long long *total, cudaStream_t s);
+
+// Persistent splat over a (frame, tile) work queue: item i of this launch is
+// global tile work[work_begin + i]; its frame f = frame_of_tile[tile] and its
+// local tile = tile - tile_base[f]; frames[f] holds the frame's arguments with
+// tile_start pointing at the frame's slice of the global tile ranges.  One
+// launch configuration (cfg) and tile size T for every item of the launch.
+struct BatchSplatArgs {
+  const SplatArgs *frames;
+  const uint32_t *tile_base;
+  const uint32_t *frame_of_tile;
+  const uint32_t *work;
+  uint32_t work_begin, nwork;
+  uint32_t *counter;  // zero before the launch
+  int T;
+};
+int launch_splat_queue(const BatchSplatArgs &q, int cfg, cudaStream_t s);
+
+// Adjoint of the splat: per active particle, sums of dL/dE (gcol.xyz) and of
+// gatt*att*(dx, dy, dx^2+dy^2) (gpos.xyz), accumulated with atomics (zero them
+// first).  f is the forward's argument set, f.pic its final image.
+struct AdjArgs {
+  SplatArgs f;
+  const float *gpic;  // dL/dpic, x-major
+  float4 *gpos;
+  float4 *gcol;
+};
+int launch_splat_adjoint(const AdjArgs &a, cudaStream_t s);
+
+// Chain rule from the splat sums to the inputs (written by particle index;
+// inactive particles are not touched) and block sums for the camera
+// position: cam_sums = sum d/d(xc, yc, zc), sum dL/dX, sum dL/dY (zero it).
+struct ProjAdjArgs {
+  ProjConst c;
+  const void *aos;  // particle_sim records, or null: soa
+  SoAIn soa;
+  const float4 *pos_c;
+  const uint32_t *idx_c;
+  const float4 *gpos, *gcol;
+  int64_t na;
+  float h2sigma;
+  float *gI, *gcr, *gcg, *gcb, *gx, *gy, *gz, *gr;
+  double *cam_sums;
+};
+int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s);
 
 }  // namespace spl

@@ -383,6 +383,10 @@ __global__ void __launch_bounds__(256) k_project_dense(L load, int64_t n, ProjCo
     const uint32_t i = s_list[k];
     const POut p = project_core(c, load(i), o.err);
     const uint32_t dst = base + k;
+    if (dst >= o.cap_c) {
+      atomicOr(o.err, 8u);
+      continue;
+    }
     o.pos_c[dst] = p.pos;
     o.col_c[dst] = p.col;
     o.idx_c[dst] = i;
@@ -454,6 +458,35 @@ void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjCons
       k_project_full<<<grid_for(n), 256, 0, s>>>(ls, n, c, o);
     if (launches) *launches += 1;
   }
+}
+
+void launch_project_flags(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                          const ProjectOut &o, cudaStream_t s) {
+  if (n <= 0) return;
+  const int64_t nwords = (n + 31) / 32;
+  int fb = (int)((nwords * 32 + 255) / 256);
+  if (fb > 152 * 16) fb = 152 * 16;
+  if (aos)
+    k_project_flags<<<fb, 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n, c,
+                                       o.flags, o.err);
+  else
+    k_project_flags<<<fb, 256, 0, s>>>(
+        LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
+        n, c, o.flags, o.err);
+}
+
+void launch_project_dense(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                          const ProjectOut &o, cudaStream_t s) {
+  if (n <= 0) return;
+  const int64_t nwords = (n + 31) / 32;
+  const unsigned db = (unsigned)((nwords + DW - 1) / DW);
+  if (aos)
+    k_project_dense<<<db, 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n, c, o.flags,
+                                       o.word_off, o);
+  else
+    k_project_dense<<<db, 256, 0, s>>>(
+        LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
+        n, c, o.flags, o.word_off, o);
 }
 
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,

@@ -49,15 +49,19 @@ size_t smem_bytes(int T) {
   return sizeof(Smem<B>) + (size_t)B * T * 2;
 }
 
-template <int NT, int WX, int WY, int B, bool ADD, bool FTB>
-__global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
+// One tile of one frame, by the whole CTA (shared by the per-frame launch and
+// the persistent batch kernel).
+// AUX (ordered frames only): also accumulate each pixel's optical depth and
+// record where the warp stopped, for the adjoint (SplatArgs::aux).
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false>
+__device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
+                                           uint8_t *smem_raw) {
   constexpr int K = WX * WY;
-  extern __shared__ __align__(16) uint8_t smem_raw[];
+  static_assert(!(AUX && ADD), "optical depth is kept for ordered frames only");
   Smem<B> &S = *reinterpret_cast<Smem<B> *>(smem_raw);
   uint16_t *srun = reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem<B>));
 
   const int T = a.T;
-  const int tile = a.tile_order ? (int)__ldg(a.tile_order + blockIdx.x) : (int)blockIdx.x;
   const int ix = tile % a.ncx, iy = tile / a.ncx;
   const int x0s = ix * T, y0s = iy * T;
   const int tw = min(x0s + T, a.xres) - x0s;
@@ -76,6 +80,8 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
   int pxi[K], pyi[K];
   bool valid[K];
   float acc[K][3], tr[K][3];
+  float od[AUX ? K : 1][3];  // optical depth (AUX)
+  uint32_t stop = 0;         // list position below which this warp composited nothing
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int x = wbx0 + (k % WX) * IW + (lane & 7);
@@ -87,6 +93,7 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
     pyf[k] = (float)y;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
+      if (AUX) od[AUX ? k : 0][c] = 0.f;
       acc[k][c] = 0.f;
       tr[k][c] = 1.f;
     }
@@ -184,17 +191,29 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
                   acc[k][1] = fmaf(-e.y, att, acc[k][1]);
                   acc[k][2] = fmaf(-e.z, att, acc[k][2]);
                 } else if (!FTB) {
-                  const float m0 = expm1_neg(-e.x * att);
-                  const float m1 = expm1_neg(-e.y * att);
-                  const float m2 = expm1_neg(-e.z * att);
+                  const float u0 = e.x * att, u1 = e.y * att, u2 = e.z * att;
+                  if (AUX) {
+                    od[AUX ? k : 0][0] += u0;
+                    od[AUX ? k : 0][1] += u1;
+                    od[AUX ? k : 0][2] += u2;
+                  }
+                  const float m0 = expm1_neg(-u0);
+                  const float m1 = expm1_neg(-u1);
+                  const float m2 = expm1_neg(-u2);
                   acc[k][0] = fmaf(m0, acc[k][0] - e.w, acc[k][0]);
                   acc[k][1] = fmaf(m1, acc[k][1] - q2.x, acc[k][1]);
                   acc[k][2] = fmaf(m2, acc[k][2] - q2.y, acc[k][2]);
                 } else {
                   // w = Tr*(1-T) = -Tr*expm1(-e*att); C += w*q; Tr -= w
-                  const float w0 = -tr[k][0] * expm1_neg(-e.x * att);
-                  const float w1 = -tr[k][1] * expm1_neg(-e.y * att);
-                  const float w2 = -tr[k][2] * expm1_neg(-e.z * att);
+                  const float u0 = e.x * att, u1 = e.y * att, u2 = e.z * att;
+                  if (AUX) {
+                    od[AUX ? k : 0][0] += u0;
+                    od[AUX ? k : 0][1] += u1;
+                    od[AUX ? k : 0][2] += u2;
+                  }
+                  const float w0 = -tr[k][0] * expm1_neg(-u0);
+                  const float w1 = -tr[k][1] * expm1_neg(-u1);
+                  const float w2 = -tr[k][2] * expm1_neg(-u2);
                   acc[k][0] = fmaf(w0, e.w, acc[k][0]);
                   acc[k][1] = fmaf(w1, q2.x, acc[k][1]);
                   acc[k][2] = fmaf(w2, q2.y, acc[k][2]);
@@ -215,6 +234,7 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
             mine_done = mine_done && tr[k][0] < a.ftb_eps && tr[k][1] < a.ftb_eps &&
                         tr[k][2] < a.ftb_eps;
         warp_done = __all_sync(0xffffffffu, mine_done);
+        if (AUX && warp_done) stop = (uint32_t)bi * B;
       }
     }
     if (FTB) {
@@ -232,7 +252,45 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
       o[0] = acc[k][0];
       o[1] = acc[k][1];
       o[2] = acc[k][2];
+      if (AUX)
+        a.aux[(size_t)(x0s + pxi[k]) * a.yres + (y0s + pyi[k])] =
+            make_float4(od[AUX ? k : 0][0], od[AUX ? k : 0][1], od[AUX ? k : 0][2],
+                        __uint_as_float(stop));
     }
+  }
+}
+
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX>
+__global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  const int tile = a.tile_order ? (int)__ldg(a.tile_order + blockIdx.x) : (int)blockIdx.x;
+  splat_tile<NT, WX, WY, B, ADD, FTB, AUX>(a, tile, smem_raw);
+}
+
+// Persistent splat over a queue of (frame, tile) items: each CTA takes the
+// next item from an atomic counter until the queue is empty.  The queue is in
+// longest-list-first order across all frames; every frame's own arguments
+// (image, tiling, mode, tile-range slice) come from a per-frame table.
+template <int NT, int WX, int WY, int B>
+__global__ void __launch_bounds__(NT) k_splat_queue(BatchSplatArgs q) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  __shared__ uint32_t s_item;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(q.counter, 1u);
+    __syncthreads();
+    const uint32_t item = s_item;
+    if (item >= q.nwork) break;
+    const uint32_t gt = __ldg(q.work + q.work_begin + item);
+    const uint32_t f = __ldg(q.frame_of_tile + gt);
+    const SplatArgs a = q.frames[f];
+    const int tile = (int)(gt - q.tile_base[f]);
+    if (a.a_eq_e)
+      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw);
+    else if (a.order_mode == 1)
+      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw);
+    else
+      splat_tile<NT, WX, WY, B, false, false>(a, tile, smem_raw);
+    __syncthreads();  // s_item and the staging buffers are reused
   }
 }
 
@@ -269,23 +327,25 @@ __global__ void __launch_bounds__(256) k_count_fragments(SplatArgs a,
   if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(total, cnt);
 }
 
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX>
+void launch_one(const SplatArgs &a, size_t sm, cudaStream_t s) {
+  auto k = k_splat<NT, WX, WY, B, ADD, FTB, AUX>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<a.ncx * a.ncy, NT, sm, s>>>(a);
+}
+
 template <int NT, int WX, int WY, int B>
 int launch_cfg(const SplatArgs &a, cudaStream_t s) {
-  const int ntiles = a.ncx * a.ncy;
   const size_t sm = smem_bytes<B>(a.T);
-  if (a.a_eq_e) {
-    auto k = k_splat<NT, WX, WY, B, true, false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<ntiles, NT, sm, s>>>(a);
-  } else if (a.order_mode == 1) {
-    auto k = k_splat<NT, WX, WY, B, false, true>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<ntiles, NT, sm, s>>>(a);
-  } else {
-    auto k = k_splat<NT, WX, WY, B, false, false>;
-    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<ntiles, NT, sm, s>>>(a);
-  }
+  const bool aux = a.aux != nullptr;
+  if (a.a_eq_e)
+    launch_one<NT, WX, WY, B, true, false, false>(a, sm, s);
+  else if (a.order_mode == 1)
+    aux ? launch_one<NT, WX, WY, B, false, true, true>(a, sm, s)
+        : launch_one<NT, WX, WY, B, false, true, false>(a, sm, s);
+  else
+    aux ? launch_one<NT, WX, WY, B, false, false, true>(a, sm, s)
+        : launch_one<NT, WX, WY, B, false, false, false>(a, sm, s);
   return 1;
 }
 
@@ -339,6 +399,38 @@ int launch_splat(const SplatArgs &a, cudaStream_t s) {
     case 2: return launch_cfg<128, 2, 1, 128>(a, s);
     case 3: return launch_cfg<256, 2, 2, 256>(a, s);
     default: return launch_cfg<256, 4, 4, 256>(a, s);
+  }
+}
+
+namespace {
+
+template <int NT, int WX, int WY, int B>
+int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
+  const size_t sm = smem_bytes<B>(q.T);
+  auto k = k_splat_queue<NT, WX, WY, B>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  int per_sm = 0, dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, NT, sm);
+  if (per_sm < 1) per_sm = 1;
+  int grid = nsm * per_sm;
+  if ((uint32_t)grid > q.nwork) grid = (int)q.nwork;
+  if (grid < 1) return 0;
+  k<<<grid, NT, sm, s>>>(q);
+  return 1;
+}
+
+}  // namespace
+
+int launch_splat_queue(const BatchSplatArgs &q, int cfg, cudaStream_t s) {
+  if (q.nwork == 0) return 0;
+  switch (cfg) {
+    case 0: return launch_queue_cfg<256, 1, 1, 256>(q, s);
+    case 1: return launch_queue_cfg<64, 2, 2, 128>(q, s);
+    case 2: return launch_queue_cfg<128, 2, 1, 128>(q, s);
+    case 3: return launch_queue_cfg<256, 2, 2, 256>(q, s);
+    default: return launch_queue_cfg<256, 4, 4, 256>(q, s);
   }
 }
 

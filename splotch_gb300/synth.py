@@ -105,6 +105,97 @@ def plain_absorption(n_gas: int = 40_000_000, n_star: int = 10_000_000, seed: in
                     _rc((250, 250, -50), (250, 250, 250), [five_stop_palette(), None]))
 
 
+def differentiable(n: int = 4_000_000, mode: str = "additive", seed: int = 3, xres: int = 1024,
+                   yres: int | None = None, tile: int = 16, order: str = "ftb") -> Workload:
+    """Differentiable render: halo mixture in [0,100]^3, hsml ~ lognormal(ln 0.3, 0.5),
+    I ~ lognormal(0,1); three quarters of the particles take a colour value U[0,1]
+    through the 256-entry blue->white palette (type 0), one quarter a per-particle
+    RGB U[0,1]^3 (type 1, colour vector).  Camera (50,50,250) -> (50,50,50), fov 30.
+    notes["target"] holds the target particle set: I scaled by lognormal(0,0.2)
+    noise and positions moved by N(0, 0.1*hsml)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = np.zeros(n, dtype=PARTICLE_DTYPE)
+    pos = halo_positions(rng, n, 100.0)
+    p["x"], p["y"], p["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
+    p["r"] = rng.lognormal(np.log(0.3), 0.5, n).astype(np.float32)
+    p["I"] = rng.lognormal(0.0, 1.0, n).astype(np.float32)
+    nv = n // 4
+    p["type"][n - nv:] = 1
+    p["er"] = rng.uniform(0.0, 1.0, n).astype(np.float32)
+    rgb = rng.uniform(0.0, 1.0, (nv, 2)).astype(np.float32)
+    p["eg"][n - nv:], p["eb"][n - nv:] = rgb[:, 0], rgb[:, 1]
+    t = p.copy()
+    t["I"] = (p["I"] * rng.lognormal(0.0, 0.2, n)).astype(np.float32)
+    for ax in ("x", "y", "z"):
+        t[ax] = (p[ax] + rng.standard_normal(n) * 0.1 * p["r"]).astype(np.float32)
+    yres = xres if yres is None else yres
+    additive = mode == "additive"
+    params = ParamFile({"xres": xres, "yres": yres, "fov": 30.0, "a_eq_e": additive,
+                        "sort_type": 1, "gray_absorption": 0.2, "ptypes": 2,
+                        "color_is_vector0": False, "color_is_vector1": True,
+                        "brightness0": 1.0, "brightness1": 1.0, "tile_size_cpu": tile,
+                        "gpu_order": order})
+    return Workload(f"differentiable_{mode}", p, params,
+                    _rc((50, 50, 250), (50, 50, 50), [blue_white_palette(), None]),
+                    notes={"target": t})
+
+
+BATCH_RESOLUTIONS = ((512, 512), (1024, 1024), (1920, 1080), (2048, 2048))
+
+
+@dataclass
+class BatchWorkload:
+    sets: list            # particle_sim arrays, one per set
+    frames: list          # (set index, ParamFile, RenderContext)
+    notes: dict = field(default_factory=dict)
+
+
+def batched(n_sets: int = 8, poses: int = 12, seed: int = 2, scale: float = 1.0,
+            tile: int = 16, order: str = "ftb",
+            resolutions=BATCH_RESOLUTIONS) -> BatchWorkload:
+    """Batched rendering: n_sets particle sets with N log-uniform in [1M, 32M]
+    (times scale), alternating additive / ordered absorption, each from the halo
+    mixture in [0,100]^3 (hsml ~ lognormal(ln 0.3, 0.5), I ~ lognormal(0,1);
+    three quarters colour value through a palette -- blue->white for additive
+    sets, 5-stop for ordered ones --, one quarter per-particle RGB), and
+    `poses` camera poses per set on a circular orbit of radius 2L = 200 in the
+    xz plane around the box centre, looking at the centre (sky +y), fov
+    U[30, 60] degrees, resolution drawn from `resolutions`."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    L = 100.0
+    centre = np.array([L / 2, L / 2, L / 2])
+    sets, frames = [], []
+    for s in range(n_sets):
+        n = max(1, int(round(np.exp(rng.uniform(np.log(1e6), np.log(32e6))) * scale)))
+        additive = s % 2 == 0
+        prng = np.random.Generator(np.random.PCG64(seed * 1000 + s))
+        p = np.zeros(n, dtype=PARTICLE_DTYPE)
+        pos = halo_positions(prng, n, L)
+        p["x"], p["y"], p["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
+        p["r"] = prng.lognormal(np.log(0.3), 0.5, n).astype(np.float32)
+        p["I"] = prng.lognormal(0.0, 1.0, n).astype(np.float32)
+        nv = n // 4
+        p["type"][n - nv:] = 1
+        p["er"] = prng.uniform(0.0, 1.0, n).astype(np.float32)
+        rgb = prng.uniform(0.0, 1.0, (nv, 2)).astype(np.float32)
+        p["eg"][n - nv:], p["eb"][n - nv:] = rgb[:, 0], rgb[:, 1]
+        sets.append(p)
+        pal = blue_white_palette() if additive else five_stop_palette()
+        phase = rng.uniform(0.0, 2 * np.pi)
+        for k in range(poses):
+            a = phase + 2 * np.pi * k / poses
+            campos = centre + 2 * L * np.array([np.sin(a), 0.0, np.cos(a)])
+            xres, yres = resolutions[int(rng.integers(0, len(resolutions)))]
+            fov = float(rng.uniform(30.0, 60.0))
+            params = ParamFile({"xres": xres, "yres": yres, "fov": fov, "a_eq_e": additive,
+                                "sort_type": 1, "gray_absorption": 0.2, "ptypes": 2,
+                                "color_is_vector0": False, "color_is_vector1": True,
+                                "brightness0": 1.0, "brightness1": 1.0, "tile_size_cpu": tile,
+                                "gpu_order": order})
+            frames.append((s, params, _rc(campos, centre, [pal, None])))
+    return BatchWorkload(sets, frames, notes={"particles": sum(len(p) for p in sets)})
+
+
 def soa_from_aos(p: np.ndarray) -> dict:
     """Split a particle_sim array into the SoA fields the C ABI takes."""
     return {"x": np.ascontiguousarray(p["x"]), "y": np.ascontiguousarray(p["y"]),
