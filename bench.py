@@ -54,6 +54,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fwd-bwd", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-scale", type=float, default=1.0,
+                    help="particle-count multiplier of the batched workload")
+    ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="particle-count multiplier (profiling runs use a smaller frame)")
     return ap.parse_args()
@@ -308,6 +312,83 @@ def fwd_bwd(args, local: int) -> dict:
     return out
 
 
+def batched(args, local: int) -> dict:
+    """Batched rendering vs the plain per-frame path on the same frames: 8
+    particle sets (N log-uniform in [1M, 32M] x batch_scale, alternating
+    additive / ordered), 12 orbit poses each, resolutions from {512^2, 1024^2,
+    1920x1080, 2048^2} -> 96 frames.  Plain: one spl_render call per frame
+    (tile 16, default launch configurations); batched: one spl_batch_render
+    (captured graph, autotuned).  Inputs and images resident in HBM; CUDA events
+    on each path's stream; frames/s = 96 / time of one whole pass."""
+    import torch
+
+    import splotch_gb300 as sg
+    from splotch_gb300 import synth
+
+    dev = f"cuda:{local}"
+    bw = synth.batched(scale=args.batch_scale, tile=16, order=args.order)
+    sets = [{k: torch.from_numpy(v).to(dev) for k, v in synth.soa_from_aos(p).items()}
+            for p in bw.sets]
+    keep: list = []
+    frames = []
+    for s, params, rc in bw.frames:
+        desc = sg.frame_desc(params, rc, keep)
+        frames.append((s, desc, torch.zeros((desc.xres, desc.yres, 3), dtype=torch.float32,
+                                            device=dev)))
+    torch.cuda.synchronize()
+    r = sg.Renderer(local)
+    stream = torch.cuda.Stream(device=dev)
+    r.set_stream(stream.cuda_stream)
+    nf = len(frames)
+    pf_total = sum(len(bw.sets[s]) for s, _, _ in frames)
+    out = {"frames": nf, "sets": len(bw.sets), "particles": bw.notes["particles"],
+           "particle_frames": pf_total,
+           "pixels": int(sum(d.xres * d.yres for _, d, _ in frames))}
+
+    def plain_pass():
+        for s, desc, pic in frames:
+            r.render_soa(desc, sets[s], pic)
+
+    for _ in range(max(1, args.warmup // 2)):
+        plain_pass()
+    torch.cuda.synchronize()
+    reps = max(1, args.batch_steps)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        plain_pass()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1) / reps
+
+    t0 = time.perf_counter()
+    b = sg.Batch(r, sets, frames)
+    create_s = time.perf_counter() - t0
+    for _ in range(max(1, args.warmup // 2)):
+        b.render()
+    ts = []
+    for _ in range(reps):
+        t1 = time.perf_counter()
+        b.render()
+        ts.append(time.perf_counter() - t1)
+    info = b.info()
+    batch_ms = statistics.median(ts) * 1e3
+    out.update({"plain_ms": plain_ms, "plain_frames_per_s": nf / (plain_ms * 1e-3),
+                "batched_ms": batch_ms, "batched_device_ms": info["render_ms"],
+                "batched_frames_per_s": nf / (batch_ms * 1e-3),
+                "batched_mparticle_frames_per_s": pf_total / (batch_ms * 1e-3) / 1e6,
+                "speedup_frames_per_s": plain_ms / batch_ms,
+                "tile_size": info["tile_size"],
+                "splat_config_additive": info["splat_config_additive"],
+                "splat_config_absorption": info["splat_config_absorption"],
+                "graph": info["graph"], "create_s": create_s, "tune_ms": info["tune_ms"],
+                "kernel_launches_per_render": info["kernel_launches"],
+                "active_records": info["n_active"], "bin_entries": info["n_entries"]})
+    b.close()
+    r.close()
+    return out
+
+
 def run_gpu(args):
     import torch
 
@@ -403,6 +484,7 @@ def run_gpu(args):
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w)
     fb = None if args.no_fwd_bwd else fwd_bwd(args, local)
+    bt = None if args.no_batched else batched(args, local)
     line = {"metric": METRIC, "value": world * n / (ms * 1e-3) / 1e6, "unit": "Mparticles/s",
             "frames_per_s": world * 1e3 / ms, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -410,7 +492,7 @@ def run_gpu(args):
             "data": "synthetic (seeded halo mixture; no snapshot available)", "config": cfg,
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "roofline": top,
             "stages": st, "fragments": frags, "bin_entries": int(last["n_entries"]),
-            "cpu_baseline": cb, "fwd_bwd": fb}
+            "cpu_baseline": cb, "fwd_bwd": fb, "batched": bt}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
