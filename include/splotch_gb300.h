@@ -196,6 +196,31 @@ spl_status spl_render_backward(spl_context *ctx, const spl_image *grad_pic, spl_
    (16 bytes per pixel, a few adds per fragment).  Off by default. */
 spl_status spl_context_set_differentiable(spl_context *ctx, int enable);
 
+/* ---- after host_rendering: post-processing and image output ------------ */
+/* What splotch/splotch.cc:272-323 does with the image once host_rendering has
+   returned, on the device. */
+typedef struct {
+  int a_eq_e;        /* additive frame: pic = -expm1(pic) with exptable<float32>(-20) */
+  double gamma;      /* colour_adjust (splotchutils.cc:230-250): pic_gamma (1) */
+  double brightness; /* pic_brightness (0) */
+  double contrast;   /* pic_contrast (1) */
+  int colorbar;      /* add_colorbar (splotchutils.cc:35-58): colorbar (F) */
+} spl_post_desc;
+void spl_post_desc_defaults(spl_post_desc *p);
+/* In place on an x-major image (host or device) of d->xres x d->yres; the
+   colour bars use d's palettes and types. */
+spl_status spl_postprocess(spl_context *ctx, const spl_frame_desc *d, const spl_post_desc *p,
+                           spl_image *img);
+/* LS_Image's file bytes (cxxsupport/ls_image.cc:178-314) for pictype 0 (TGA),
+   2 (PPM) or 3 (run-length TGA): Colour8 conversion and the x-major to row
+   transpose on the device.  *len = full length; at most cap bytes are stored
+   (out may be NULL to query the length). */
+spl_status spl_image_encode(spl_context *ctx, const spl_image *img, int xres, int yres,
+                            int pictype, uint8_t *out, int64_t cap, int64_t *len);
+/* The same bytes written to path (splotch.cc:299-323). */
+spl_status spl_write_image(spl_context *ctx, const spl_image *img, int xres, int yres,
+                           int pictype, const char *path);
+
 /* ---- batched rendering ------------------------------------------------- */
 /* No counterpart in the reference, which renders one frame per
    host_rendering call.  Many frames -- camera poses, resolutions, additive or

@@ -22,7 +22,7 @@ mkdir -p "$OUT"
 SRCS=(splotch/splotch_host.cc splotch/splotchutils.cc splotch/new_renderer.cc
       kernel/transform.cxx cxxsupport/paramfile.cc cxxsupport/error_handling.cc
       cxxsupport/string_utils.cc cxxsupport/mpi_support.cc cxxsupport/walltimer.cc
-      cxxsupport/announce.cc cxxsupport/ls_image.cc)
+      cxxsupport/announce.cc cxxsupport/ls_image.cc splotch/scenemaker.cc)
 CXXFLAGS=(-O2 -std=c++11 -fopenmp -ffp-contract=off -fPIC -w
           -I"$REF" -I"$REF/cxxsupport" -I"$REF/c_utils")
 
@@ -39,9 +39,10 @@ build_variant() {  # $1 = output name, $2.. = extra flags
   gcc -O2 -fPIC -ffp-contract=off "$@" -I"$REF/c_utils" -c "$REF/c_utils/walltime_c.c" \
       -o "$obj/walltime_c.o" & pids+=($!)
   g++ "${CXXFLAGS[@]}" "$@" -c "$HERE/ref_harness.cc" -o "$obj/ref_harness.o" & pids+=($!)
+  g++ "${CXXFLAGS[@]}" "$@" -c "$HERE/ref_stubs.cc" -o "$obj/ref_stubs.o" & pids+=($!)
   for p in "${pids[@]}"; do wait "$p"; done
-  g++ -shared -fopenmp -o "$OUT/$name.so" "${objs[@]}" "$obj/walltime_c.o" \
-      "$obj/ref_harness.o"
+  g++ -shared -fopenmp -Wl,--no-undefined -o "$OUT/$name.so" "${objs[@]}" \
+      "$obj/walltime_c.o" "$obj/ref_harness.o" "$obj/ref_stubs.o"
 }
 
 build_variant libsplotch_ref

@@ -75,6 +75,45 @@ class SpoCamera(C.Structure):
                 ("yshift", C.c_double)]
 
 
+class SpoNormParams(C.Structure):
+    _fields_ = [("ptypes", C.c_int)] + [
+        (k, C.c_int * MAXT) for k in ("intensity_log", "color_log", "color_asinh",
+                                       "color_is_vector", "has_intensity_min",
+                                       "has_intensity_max", "has_color_min", "has_color_max")] + [
+        (k, C.c_float * MAXT) for k in ("intensity_min", "intensity_max", "color_min",
+                                         "color_max")]
+
+
+class SpoNormOut(C.Structure):
+    _fields_ = [(k, C.c_double * MAXT) for k in ("range_min", "range_max", "clamp_min",
+                                                  "clamp_max", "intensity_min", "intensity_max",
+                                                  "size_min", "size_max")]
+
+
+def norm_params(params: dict) -> SpoNormParams:
+    """The keys particle_normalize reads (scenemaker.cc:44-55, 222-232)."""
+    p = SpoNormParams()
+    p.ptypes = _get(params, "ptypes", 1)
+    for t in range(p.ptypes):
+        p.intensity_log[t] = 1 if _get(params, f"intensity_log{t}", False) else 0
+        p.color_log[t] = 1 if _get(params, f"color_log{t}", False) else 0
+        p.color_asinh[t] = 1 if _get(params, f"color_asinh{t}", False) else 0
+        p.color_is_vector[t] = 1 if _get(params, f"color_is_vector{t}", False) else 0
+        for key, has, val in (("intensity_min", "has_intensity_min", "intensity_min"),
+                              ("intensity_max", "has_intensity_max", "intensity_max"),
+                              ("color_min", "has_color_min", "color_min"),
+                              ("color_max", "has_color_max", "color_max")):
+            if f"{key}{t}" in params:
+                getattr(p, has)[t] = 1
+                getattr(p, val)[t] = float(np.float32(_get(params, f"{key}{t}", 0.0)))
+    return p
+
+
+class SpoPost(C.Structure):
+    _fields_ = [("a_eq_e", C.c_int), ("gamma", C.c_double), ("brightness", C.c_double),
+                ("contrast", C.c_double), ("colorbar", C.c_int)]
+
+
 def _get(params: dict, key: str, default):
     """paramfile::find semantics on a plain dict of strings (no insertion)."""
     if key not in params:
@@ -159,6 +198,9 @@ class Port:
             ("spo_fd_particles", i32,
              [vp, vp, vp, vp, i64, i32, vp, vp, i32, C.c_double, vp, vp]),
             ("spo_fd_campos", i32, [vp, vp, vp, vp, i64, i32, vp, C.c_double, vp]),
+            ("spo_postprocess", i32, [vp, vp, vp, i32, i32]),
+            ("spo_image_bytes", i64, [vp, i32, i32, i32, vp, i64]),
+            ("spo_particle_normalize", i32, [vp, vp, i64, vp]),
         ]:
             f = getattr(lib, name)
             f.restype = res
@@ -232,6 +274,37 @@ class Port:
                                         float(np.float32(gray)), _vp(g), _vp(gx), _vp(gy),
                                         _vp(gr), _vp(ge))
         return gx, gy, gr, ge
+
+    # ---- after host_rendering: post-processing and image output -------------
+    def postprocess(self, params: dict, rc, pic: np.ndarray, a_eq_e: bool) -> np.ndarray:
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        post = SpoPost(a_eq_e=int(a_eq_e), gamma=_get(params, "pic_gamma", 1.0),
+                       brightness=_get(params, "pic_brightness", 0.0),
+                       contrast=_get(params, "pic_contrast", 1.0),
+                       colorbar=1 if _get(params, "colorbar", False) else 0)
+        out = np.ascontiguousarray(pic, np.float32).copy()
+        self.lib.spo_postprocess(C.byref(prm), C.byref(post), _vp(out), out.shape[0],
+                                 out.shape[1])
+        return out
+
+    def particle_normalize(self, params: dict, p: np.ndarray) -> dict:
+        """In place on particle_sim records; returns the per-type ranges it
+        leaves in the paramfile (range_min/max, clamp_min/max) and more."""
+        np_ = norm_params(params)
+        out = SpoNormOut()
+        if self.lib.spo_particle_normalize(C.byref(np_), _vp(p), len(p), C.byref(out)):
+            raise ValueError("particle type outside [0, ptypes)")
+        return {k: list(getattr(out, k)[:np_.ptypes]) for k, _ in SpoNormOut._fields_}
+
+    def image_bytes(self, pic: np.ndarray, pictype: int) -> bytes:
+        p = np.ascontiguousarray(pic, np.float32)
+        n = self.lib.spo_image_bytes(_vp(p), p.shape[0], p.shape[1], pictype, None, 0)
+        if n < 0:
+            raise ValueError("No valid image file type given ...")
+        buf = np.zeros(n, np.uint8)
+        self.lib.spo_image_bytes(_vp(p), p.shape[0], p.shape[1], pictype, _vp(buf), n)
+        return buf.tobytes()
 
     # ---- differentiable FP64 model (checker of the adjoint path) ----------
     # raw: particle_sim records before projection (world inputs); cov: the same
@@ -331,6 +404,12 @@ class Ref:
         lib.ref_host_rendering.restype = i32
         lib.ref_host_rendering.argtypes = [vp, vp, i32, vp, i64, vp, vp, vp, vp, i32, vp, vp, vp,
                                            f32, i32, i32, vp]
+        lib.ref_postprocess.restype = i32
+        lib.ref_postprocess.argtypes = [vp, vp, i32, vp, i32, i32, i32, i32, vp, vp, vp]
+        lib.ref_write_image.restype = i32
+        lib.ref_write_image.argtypes = [vp, i32, i32, i32, C.c_char_p]
+        lib.ref_particle_normalize.restype = i32
+        lib.ref_particle_normalize.argtypes = [vp, vp, i32, vp, i64, i32, vp]
         self.lib = lib
         self.simd = bool(lib.ref_simd_branch())
 
@@ -396,6 +475,35 @@ class Ref:
                                        n, xs, rgbs, float(rc.b_brightness), xres, yres, _vp(pic)):
             raise RuntimeError("reference host_rendering failed")
         return pic
+
+    def postprocess(self, params: dict, rc, pic: np.ndarray, a_eq_e: bool) -> np.ndarray:
+        """splotch.cc:272-291 on a copy of the x-major image."""
+        ka, va, nkv = self._kv(params)
+        nt = int(params.get("ptypes", 1))
+        n, xs, rgbs, keep = self._pals(rc, nt)
+        out = np.ascontiguousarray(pic, np.float32).copy()
+        if self.lib.ref_postprocess(ka, va, nkv, _vp(out), out.shape[0], out.shape[1],
+                                    int(a_eq_e), nt, n, xs, rgbs):
+            raise RuntimeError("reference post-processing failed")
+        return out
+
+    def particle_normalize(self, params: dict, p: np.ndarray) -> dict:
+        """sceneMaker::particle_normalize in place; the range/clamp keys it sets."""
+        ka, va, nkv = self._kv(params)
+        nt = int(params.get("ptypes", 1))
+        out = np.zeros((nt, 4))
+        if self.lib.ref_particle_normalize(ka, va, nkv, _vp(p), len(p), nt, _vp(out)):
+            raise RuntimeError("reference particle_normalize failed")
+        return {"range_min": list(out[:, 0]), "range_max": list(out[:, 1]),
+                "clamp_min": list(out[:, 2]), "clamp_max": list(out[:, 3])}
+
+    def image_bytes(self, pic: np.ndarray, pictype: int, tmpdir) -> bytes:
+        """The file LS_Image writes (splotch.cc:295-323)."""
+        path = str(Path(tmpdir) / f"ref_image_{pictype}")
+        p = np.ascontiguousarray(pic, np.float32)
+        if self.lib.ref_write_image(_vp(p), p.shape[0], p.shape[1], pictype, path.encode()):
+            raise RuntimeError("reference image output failed")
+        return Path(path).read_bytes()
 
 
 def rel_linf(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-6) -> float:

@@ -7,10 +7,13 @@
 // same seeded inputs as the CUDA path, to pin the oracle restatement and to
 // make golden fixtures.  Nothing in the product links it.
 #include <algorithm>
+#include <cstdlib>
 #include <map>
 #include <string>
 #include <vector>
 
+#include "cxxsupport/ls_image.h"
+#include "splotch/scenemaker.h"
 #include "splotch/splotch_host.h"
 #include "splotch/splotchutils.h"
 
@@ -23,6 +26,21 @@ void render_new(particle_sim *p, int npart, arr2<COLOUR> &pic, bool a_eq_e,
 }  // namespace host_funct
 
 static_assert(sizeof(particle_sim) == 36, "particle_sim must be 36 bytes");
+
+// sceneMaker::particle_normalize (splotch/scenemaker.cc:40-296) is private: its
+// address is taken through an explicit template instantiation, where access
+// checking does not apply ([temp.explicit]).
+namespace {
+struct NormalizeTag {
+  typedef void (sceneMaker::*type)(std::vector<particle_sim> &, bool) const;
+  friend type member(NormalizeTag);
+};
+template <typename Tag, typename Tag::type M>
+struct Expose {
+  friend typename Tag::type member(Tag) { return M; }
+};
+template struct Expose<NormalizeTag, &sceneMaker::particle_normalize>;
+}  // namespace
 
 namespace {
 
@@ -142,6 +160,94 @@ int ref_host_rendering(const char *const *keys, const char *const *vals, int nkv
     host_rendering(params, v, rc);
     std::copy(v.begin(), v.end(), p);
     pic_out(rc.pic, pic);
+    return 0;
+  } catch (...) {
+    return -1;
+  }
+}
+
+// The master's post-processing of splotch/splotch.cc:272-291 on an x-major
+// image, in place: pic = -expm1(pic) with exptable<float32>(-20) when a_eq_e,
+// then colour_adjust, then add_colorbar when the colorbar key is set.
+int ref_postprocess(const char *const *keys, const char *const *vals, int nkv, float *pic,
+                    int xres, int yres, int a_eq_e, int ntypes, const int *pal_n,
+                    const double *const *pal_x, const float *const *pal_rgb) {
+  try {
+    paramfile params = make_params(keys, vals, nkv);
+    render_context rc;
+    make_amap(rc.amap, ntypes, pal_n, pal_x, pal_rgb);
+    rc.xres = xres;
+    rc.yres = yres;
+    rc.pic.alloc(xres, yres);
+    for (int x = 0; x < xres; ++x)
+      for (int y = 0; y < yres; ++y) {
+        const float *s = pic + ((size_t)x * yres + y) * 3;
+        rc.pic[x][y] = COLOUR(s[0], s[1], s[2]);
+      }
+    exptable<float32> xexp(-20.0);
+    if (a_eq_e)
+      for (int ix = 0; ix < rc.xres; ix++)
+        for (int iy = 0; iy < rc.yres; iy++) {
+          rc.pic[ix][iy].r = -xexp.expm1(rc.pic[ix][iy].r);
+          rc.pic[ix][iy].g = -xexp.expm1(rc.pic[ix][iy].g);
+          rc.pic[ix][iy].b = -xexp.expm1(rc.pic[ix][iy].b);
+        }
+    colour_adjust(params, rc);
+    if (params.find<bool>("colorbar", false)) add_colorbar(params, rc.pic, rc.amap);
+    pic_out(rc.pic, pic);
+    return 0;
+  } catch (...) {
+    return -1;
+  }
+}
+
+// sceneMaker::particle_normalize on particle_sim records, in place.  out
+// receives, per type, the values it leaves in the paramfile: range_min,
+// range_max, clamp_min, clamp_max (4 doubles per type).
+int ref_particle_normalize(const char *const *keys, const char *const *vals, int nkv,
+                           void *particles, long n, int ntypes, double *out) {
+  try {
+    paramfile params = make_params(keys, vals, nkv);
+    if (!params.param_present("outfile")) params.setParam("outfile", std::string("ref"));
+    sceneMaker sm(params);
+    particle_sim *p = static_cast<particle_sim *>(particles);
+    std::vector<particle_sim> v(p, p + n);
+    (sm.*member(NormalizeTag()))(v, false);
+    std::copy(v.begin(), v.end(), p);
+    // read back as text: the values may be infinite, which stringToData<double>
+    // does not parse
+    auto num = [&](const std::string &k) {
+      return std::strtod(params.find<std::string>(k).c_str(), nullptr);
+    };
+    for (int t = 0; t < ntypes; ++t) {
+      const std::string s = dataToString(t);
+      out[4 * t + 0] = num("range_min" + s);
+      out[4 * t + 1] = num("range_max" + s);
+      out[4 * t + 2] = num("clamp_min" + s);
+      out[4 * t + 3] = num("clamp_max" + s);
+    }
+    return 0;
+  } catch (...) {
+    return -1;
+  }
+}
+
+// The output step of splotch/splotch.cc:295-323: LS_Image from an x-major
+// image, written as pictype 0 (TGA), 2 (PPM) or 3 (run-length TGA).
+int ref_write_image(const float *pic, int xres, int yres, int pictype, const char *path) {
+  try {
+    LS_Image img(xres, yres);
+    for (int i = 0; i < xres; ++i)
+      for (int j = 0; j < yres; ++j) {
+        const float *s = pic + ((size_t)i * yres + j) * 3;
+        img.put_pixel(i, j, Colour(s[0], s[1], s[2]));
+      }
+    switch (pictype) {
+      case 0: img.write_TGA(path); break;
+      case 2: img.write_PPM(path); break;
+      case 3: img.write_TGA_rle(path); break;
+      default: return -2;
+    }
     return 0;
   } catch (...) {
     return -1;

@@ -15,6 +15,7 @@
 #include <float.h>
 #include <limits.h>
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -1296,6 +1297,214 @@ int spo_model_vjp_all(const spo_params *prm, const spo_particle *raw, const spo_
     if (!cov[i].active) { memset(grad + 8 * i, 0, 8 * sizeof(double)); continue; }
     const spo_model_in q = model_in_of(&raw[i]);
     spo_model_vjp(&m, &q, gw + 6 * i, grad + 8 * i, gcampos);
+  }
+  return 0;
+}
+
+/* ====================================================================== */
+/* Post-processing and image output after host_rendering
+   (splotch/splotch.cc:272-323). */
+
+/* pic = -expm1(pic) with exptable<float32>(-20) when a_eq_e
+   (splotch.cc:272-281); colour_adjust (splotchutils.cc:230-250); add_colorbar
+   (splotchutils.cc:35-58).  Colour-bar rows that would fall below row 0 (more
+   than yres/10 palette types) are skipped. */
+int spo_postprocess(const spo_params *prm, const spo_post *post, float *pic, int xres,
+                    int yres) {
+  const size_t nv = (size_t)xres * yres * 3;
+  if (post->a_eq_e) {
+    exptab t;
+    exptab_init(&t, -20.f);
+    for (size_t k = 0; k < nv; ++k) pic[k] = -exptab_expm1(&t, pic[k]);
+  }
+  const double g = post->gamma, h = post->brightness, c = post->contrast;
+  if (g != 1.0 || h != 0.0 || c != 1.0)
+    for (size_t k = 0; k < nv; ++k) pic[k] = (float)(c * pow((double)pic[k], g) + h);
+  if (post->colorbar) {
+    int offset = 0;
+    for (int t = 0; t < prm->ptypes && t < SPO_MAX_TYPES; ++t) {
+      if (prm->color_is_vector[t]) continue;
+      for (int x = 0; x < xres; ++x) {
+        float e[3];
+        palette_lookup(prm->pal_n[t], prm->pal_x[t], prm->pal_rgb[t], x / (double)xres, e);
+        for (int y = 0; y < 10; ++y) {
+          const int row = yres - offset - 1 - y;
+          if (row < 0) continue;
+          float *o = pic + ((size_t)x * yres + row) * 3;
+          o[0] = e[0]; o[1] = e[1]; o[2] = e[2];
+        }
+      }
+      offset += 10;
+    }
+  }
+  return 0;
+}
+
+/* Colour8 (cxxsupport/ls_image.h:65-75) */
+static inline uint8_t to8(float v) {
+  int i = f2i(v * 256);
+  return (uint8_t)(i < 0 ? 0 : (i > 255 ? 255 : i));
+}
+
+static void put(uint8_t *out, int64_t cap, int64_t *len, uint8_t v) {
+  if (*len < cap) out[*len] = v;
+  ++*len;
+}
+
+/* The bytes LS_Image writes (cxxsupport/ls_image.cc:178-314) for pictype 0
+   (TGA), 2 (PPM) or 3 (run-length TGA).  Returns the length (bytes beyond cap
+   are counted, not stored); -1 for another pictype. */
+int64_t spo_image_bytes(const float *pic, int xres, int yres, int pictype, uint8_t *out,
+                        int64_t cap) {
+  int64_t len = 0;
+  if (pictype == 0 || pictype == 3) {
+    const uint8_t hdr[18] = {0, 0, (uint8_t)(pictype == 0 ? 2 : 10), 0, 0, 0, 0, 0, 0, 0, 0,
+                             0, (uint8_t)(xres % 256), (uint8_t)(xres / 256),
+                             (uint8_t)(yres % 256), (uint8_t)(yres / 256), 24, 32};
+    for (int k = 0; k < 18; ++k) put(out, cap, &len, hdr[k]);
+  } else if (pictype == 2) {
+    char hdr[64];
+    int n = snprintf(hdr, sizeof hdr, "P6\n%d\n%d\n255\n", xres, yres);
+    for (int k = 0; k < n; ++k) put(out, cap, &len, (uint8_t)hdr[k]);
+  } else {
+    return -1;
+  }
+  uint8_t *row = (uint8_t *)malloc((size_t)xres * 3 + 3);
+  for (int j = 0; j < yres; ++j) {
+    for (int i = 0; i < xres; ++i) {
+      const float *s = pic + ((size_t)i * yres + j) * 3;
+      row[3 * i] = to8(s[0]); row[3 * i + 1] = to8(s[1]); row[3 * i + 2] = to8(s[2]);
+    }
+    if (pictype != 3) {
+      for (int i = 0; i < xres; ++i) {
+        const uint8_t *p = row + 3 * i;
+        if (pictype == 0) { put(out, cap, &len, p[2]); put(out, cap, &len, p[1]); put(out, cap, &len, p[0]); }
+        else { put(out, cap, &len, p[0]); put(out, cap, &len, p[1]); put(out, cap, &len, p[2]); }
+      }
+      continue;
+    }
+    /* run-length encoding of one row (ls_image.cc:206-286): runs of equal
+       pixels and of pairwise-different pixels, each cut into chunks of 128 */
+#define SAME(a, b) (row[3 * (a)] == row[3 * (b)] && row[3 * (a) + 1] == row[3 * (b) + 1] && \
+                    row[3 * (a) + 2] == row[3 * (b) + 2])
+    int xs = 0;
+    while (xs < xres) {
+      int xe;
+      int equal;
+      if (xs == xres - 1) { xe = xres; equal = 0; }
+      else if (SAME(xs + 1, xs)) {
+        xe = xs + 2;
+        while (xe < xres && SAME(xe, xs)) ++xe;
+        equal = 1;
+      } else {
+        xe = xs + 2;
+        while (xe < xres && !SAME(xe, xe - 1)) ++xe;
+        equal = 0;
+      }
+      for (int cb = xs; cb < xe; cb += 128) {
+        const int csz = (xe - cb) < 128 ? (xe - cb) : 128;
+        if (equal) {
+          put(out, cap, &len, (uint8_t)(csz - 1 + 128));
+          put(out, cap, &len, row[3 * xs + 2]); put(out, cap, &len, row[3 * xs + 1]);
+          put(out, cap, &len, row[3 * xs]);
+        } else {
+          put(out, cap, &len, (uint8_t)(csz - 1));
+          for (int k = cb; k < cb + csz; ++k) {
+            put(out, cap, &len, row[3 * k + 2]); put(out, cap, &len, row[3 * k + 1]);
+            put(out, cap, &len, row[3 * k]);
+          }
+        }
+      }
+      xs = xe;
+    }
+#undef SAME
+  }
+  free(row);
+  return len;
+}
+
+/* ====================================================================== */
+/* sceneMaker::particle_normalize, host branch (splotch/scenemaker.cc:40-296),
+   with Normalizer (splotch/splotchutils.h:139-172) and my_asinh
+   (splotch/splotchutils.cc:31-32). */
+
+typedef struct { float minv, maxv; } spo_normalizer;
+
+static inline void nz_collect(spo_normalizer *z, float v) {
+  /* std::min(minv, v) / std::max(maxv, v): a NaN v leaves both unchanged */
+  z->minv = (v < z->minv) ? v : z->minv;
+  z->maxv = (z->maxv < v) ? v : z->maxv;
+}
+
+static inline float nz_clamp(const spo_normalizer *z, float v) {
+  if (z->maxv == z->minv) return 1.f;
+  float lo = (v < z->maxv) ? v : z->maxv;  /* min(maxv, v) */
+  lo = (z->minv < lo) ? lo : z->minv;      /* max(minv, .) */
+  return (lo - z->minv) / (z->maxv - z->minv);
+}
+
+static inline float my_asinh_f(float v) {
+  const double d = v;
+  return (float)log(d + sqrt(1. + d * d));
+}
+
+int spo_particle_normalize(const spo_norm_params *np, spo_particle *p, int64_t n,
+                           spo_norm_out *out) {
+  const int nt = np->ptypes;
+  if (nt < 1 || nt > SPO_MAX_TYPES) return -1;
+  spo_normalizer in[SPO_MAX_TYPES], cn[SPO_MAX_TYPES], rn[SPO_MAX_TYPES];
+  for (int t = 0; t < nt; ++t) {
+    in[t].minv = cn[t].minv = rn[t].minv = 1e37f;
+    in[t].maxv = cn[t].maxv = rn[t].maxv = -1e37f;
+  }
+  for (int64_t m = 0; m < n; ++m) {
+    spo_particle *q = &p[m];
+    const int t = q->type;
+    if (t < 0 || t >= nt) return -2;
+    nz_collect(&rn[t], q->r);
+    if (np->intensity_log[t]) {
+      if (q->I > 0) { q->I = log10f(q->I); nz_collect(&in[t], q->I); }
+      else q->I = -38;
+    } else {
+      nz_collect(&in[t], q->I);
+    }
+    if (np->color_log[t]) {
+      if (q->er > 0) { q->er = log10f(q->er); nz_collect(&cn[t], q->er); }
+      else q->er = -38;
+    } else {
+      if (np->color_asinh[t]) q->er = my_asinh_f(q->er);
+      nz_collect(&cn[t], q->er);
+    }
+    if (np->color_is_vector[t]) {
+      if (np->color_log[t]) { q->eg = log10f(q->eg); q->eb = log10f(q->eb); }
+      if (np->color_asinh[t]) { q->eg = my_asinh_f(q->eg); q->eb = my_asinh_f(q->eb); }
+      nz_collect(&cn[t], q->eg);
+      nz_collect(&cn[t], q->eb);
+    }
+  }
+  for (int t = 0; t < nt; ++t) {
+    out->range_min[t] = cn[t].minv;
+    out->range_max[t] = cn[t].maxv;
+    if (np->has_intensity_min[t]) in[t].minv = np->intensity_min[t];
+    if (np->has_intensity_max[t]) in[t].maxv = np->intensity_max[t];
+    if (np->has_color_min[t]) cn[t].minv = np->color_min[t];
+    if (np->has_color_max[t]) cn[t].maxv = np->color_max[t];
+    out->clamp_min[t] = cn[t].minv;
+    out->clamp_max[t] = cn[t].maxv;
+    out->intensity_min[t] = in[t].minv;
+    out->intensity_max[t] = in[t].maxv;
+    out->size_min[t] = rn[t].minv;
+    out->size_max[t] = rn[t].maxv;
+  }
+  for (int64_t m = 0; m < n; ++m) {
+    spo_particle *q = &p[m];
+    const int t = q->type;
+    q->I = nz_clamp(&in[t], q->I);
+    q->er = nz_clamp(&cn[t], q->er);
+    if (np->color_is_vector[t]) {
+      q->eg = nz_clamp(&cn[t], q->eg);
+      q->eb = nz_clamp(&cn[t], q->eb);
+    }
   }
   return 0;
 }

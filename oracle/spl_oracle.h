@@ -170,6 +170,46 @@ int spo_fd_campos(const spo_params *prm, const spo_particle *raw,
                   const spo_particle *cov, const uint32_t *order, int64_t n,
                   int T, const float *target, double h, double fd[3]);
 
+/* ---- after host_rendering: post-processing and image output -------------
+   splotch/splotch.cc:272-323, splotchutils.cc:35-58,230-250,
+   cxxsupport/ls_image.cc:178-314. */
+typedef struct {
+  int a_eq_e;        /* pic = -expm1(pic) with exptable<float32>(-20) */
+  double gamma, brightness, contrast; /* pic_gamma, pic_brightness, pic_contrast */
+  int colorbar;
+} spo_post;
+/* in place on an x-major image; palettes and types from prm */
+int spo_postprocess(const spo_params *prm, const spo_post *post, float *pic, int xres,
+                    int yres);
+/* the file bytes of pictype 0 (TGA), 2 (PPM), 3 (run-length TGA) */
+int64_t spo_image_bytes(const float *pic, int xres, int yres, int pictype, uint8_t *out,
+                        int64_t cap);
+
+/* ---- before host_rendering: sceneMaker::particle_normalize ---------------
+   splotch/scenemaker.cc:40-296 (host branch): per type optional log10 of I,
+   log10 or asinh of the colour, min/max of size, intensity and colour,
+   optional intensity_min/max and color_min/max overrides, then
+   Normalizer::normAndClamp of I and colour. */
+typedef struct {
+  int ptypes;
+  int intensity_log[SPO_MAX_TYPES], color_log[SPO_MAX_TYPES];
+  int color_asinh[SPO_MAX_TYPES], color_is_vector[SPO_MAX_TYPES];
+  int has_intensity_min[SPO_MAX_TYPES], has_intensity_max[SPO_MAX_TYPES];
+  int has_color_min[SPO_MAX_TYPES], has_color_max[SPO_MAX_TYPES];
+  float intensity_min[SPO_MAX_TYPES], intensity_max[SPO_MAX_TYPES];
+  float color_min[SPO_MAX_TYPES], color_max[SPO_MAX_TYPES];
+} spo_norm_params;
+typedef struct {
+  /* range_*: colour range of the data (the range_min/max keys it sets);
+     clamp_*: the colour range used, after overrides (clamp_min/max keys) */
+  double range_min[SPO_MAX_TYPES], range_max[SPO_MAX_TYPES];
+  double clamp_min[SPO_MAX_TYPES], clamp_max[SPO_MAX_TYPES];
+  double intensity_min[SPO_MAX_TYPES], intensity_max[SPO_MAX_TYPES];
+  double size_min[SPO_MAX_TYPES], size_max[SPO_MAX_TYPES];
+} spo_norm_out;
+int spo_particle_normalize(const spo_norm_params *np, spo_particle *p, int64_t n,
+                           spo_norm_out *out);
+
 #ifdef __cplusplus
 }
 #endif

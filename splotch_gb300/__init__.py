@@ -377,6 +377,76 @@ class Renderer:
         return ts, ent[: s["n_entries"]]
 
 
+def _renderer() -> "Renderer":
+    global _default_renderer
+    if _default_renderer is None:
+        _default_renderer = Renderer()
+    return _default_renderer
+
+
+def post_desc(params: ParamFile, a_eq_e: bool | None = None) -> _abi.PostDesc:
+    """The keys of splotch.cc:272-291 (a_eq_e, pic_gamma, pic_brightness,
+    pic_contrast, colorbar) with the reference's defaults."""
+    p = _abi.PostDesc()
+    _abi.load().spl_post_desc_defaults(C.byref(p))
+    p.a_eq_e = 1 if (params.find("a_eq_e", True) if a_eq_e is None else a_eq_e) else 0
+    p.gamma = params.find("pic_gamma", 1.0)
+    p.brightness = params.find("pic_brightness", 0.0)
+    p.contrast = params.find("pic_contrast", 1.0)
+    p.colorbar = 1 if params.find("colorbar", False) else 0
+    return p
+
+
+def postprocess(params: ParamFile, rc: RenderContext, renderer: Renderer | None = None,
+                pic=None) -> None:
+    """The master's post-processing after host_rendering (splotch.cc:272-291),
+    in place on rc.pic (or on pic: a numpy array or a device tensor)."""
+    r = renderer or _renderer()
+    keep: list = []
+    desc = frame_desc(params, rc, keep)
+    target = rc.pic if pic is None else pic
+    dev = not isinstance(target, np.ndarray)
+    img = _abi.Image(pic=_abi.ptr(target), memspace=_abi.SPL_MEM_DEVICE if dev
+                     else _abi.SPL_MEM_HOST)
+    _abi.check(r.lib.spl_postprocess(r.ctx, C.byref(desc), C.byref(post_desc(params)),
+                                     C.byref(img)))
+
+
+PICTYPES = {0: ".tga", 2: ".ppm", 3: ".tga"}
+
+
+def encode_image(pic, pictype: int = 0, renderer: Renderer | None = None) -> bytes:
+    """The bytes of LS_Image's file for pictype 0 (TGA), 2 (PPM), 3 (RLE TGA)."""
+    r = renderer or _renderer()
+    dev = not isinstance(pic, np.ndarray)
+    xres, yres = int(pic.shape[0]), int(pic.shape[1])
+    img = _abi.Image(pic=_abi.ptr(pic), memspace=_abi.SPL_MEM_DEVICE if dev
+                     else _abi.SPL_MEM_HOST)
+    n = C.c_int64()
+    _abi.check(r.lib.spl_image_encode(r.ctx, C.byref(img), xres, yres, pictype, None, 0,
+                                      C.byref(n)))
+    buf = np.zeros(n.value, np.uint8)
+    _abi.check(r.lib.spl_image_encode(r.ctx, C.byref(img), xres, yres, pictype,
+                                      buf.ctypes.data, n.value, C.byref(n)))
+    return buf.tobytes()
+
+
+def write_image(params: ParamFile, rc: RenderContext, outfile: str,
+                renderer: Renderer | None = None) -> str:
+    """splotch.cc:295-323: write rc.pic as outfile + .tga/.ppm by pictype."""
+    pictype = params.find("pictype", 0)
+    if pictype == 1:
+        raise _abi.SplotchError(_abi.SPL_ERR_UNSUPPORTED, "ASCII PPM no longer supported")
+    if pictype not in PICTYPES:
+        raise _abi.SplotchError(_abi.SPL_ERR_INVALID, "No valid image file type given ...")
+    r = renderer or _renderer()
+    path = outfile + PICTYPES[pictype]
+    img = _abi.Image(pic=_abi.ptr(rc.pic), memspace=_abi.SPL_MEM_HOST)
+    _abi.check(r.lib.spl_write_image(r.ctx, C.byref(img), rc.pic.shape[0], rc.pic.shape[1],
+                                     pictype, path.encode()))
+    return path
+
+
 class Batch:
     """spl_batch_*: many frames rendered by one captured CUDA graph.
 

@@ -29,6 +29,7 @@ EXPORTED = [
     "spl_splat_config_count", "spl_splat_config_valid", "spl_sort_pairs_noalloc",
     "spl_render_backward", "spl_context_set_differentiable", "spl_batch_options_defaults",
     "spl_batch_create", "spl_batch_render", "spl_batch_get_info", "spl_batch_destroy",
+    "spl_post_desc_defaults", "spl_postprocess", "spl_image_encode", "spl_write_image",
 ]
 SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
@@ -86,6 +87,11 @@ GRAD_FIELDS = ("I", "cr", "cg", "cb", "x", "y", "z", "r")
 class Grads(C.Structure):
     _fields_ = [("memspace", C.c_int)] + [(f, C.c_void_p) for f in GRAD_FIELDS] + [
         ("campos", C.c_double * 3)]
+
+
+class PostDesc(C.Structure):
+    _fields_ = [("a_eq_e", C.c_int), ("gamma", C.c_double), ("brightness", C.c_double),
+                ("contrast", C.c_double), ("colorbar", C.c_int)]
 
 
 class BatchFrame(C.Structure):
@@ -158,6 +164,13 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_batch_render": (C.c_int, [vp]),
         "spl_batch_get_info": (C.c_int, [vp, C.POINTER(BatchInfo)]),
         "spl_batch_destroy": (C.c_int, [vp]),
+        "spl_post_desc_defaults": (None, [C.POINTER(PostDesc)]),
+        "spl_postprocess": (C.c_int, [vp, C.POINTER(FrameDesc), C.POINTER(PostDesc),
+                                      C.POINTER(Image)]),
+        "spl_image_encode": (C.c_int, [vp, C.POINTER(Image), C.c_int, C.c_int, C.c_int, vp,
+                                       i64, C.POINTER(i64)]),
+        "spl_write_image": (C.c_int, [vp, C.POINTER(Image), C.c_int, C.c_int, C.c_int,
+                                      C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -8,6 +8,7 @@
 //
 // All device memory is owned by the context and grows on demand; a frame that
 // fits the current capacity allocates nothing.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -29,7 +30,7 @@ struct spl_context {
   Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
-      poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux;
+      poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
   // state of the last frame (for the debug getters)
@@ -299,7 +300,8 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->pal_rgb, &c->aos_out, &c->pal_thr, &c->pal_xff,
                               &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord, &c->pos_c,
                               &c->col_c, &c->idx_c, &c->pstate, &c->poff, &c->gpic,
-                              &c->gpos_c, &c->gcol_c, &c->camsum, &c->aux};
+                              &c->gpos_c, &c->gcol_c, &c->camsum, &c->aux, &c->post_tab,
+                              &c->post_bar, &c->post_img, &c->post_bytes};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
@@ -706,6 +708,217 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
   cudaEventElapsedTime(&S.bwd_splat_ms, c->ev[1], c->ev[2]);
   cudaEventElapsedTime(&S.bwd_project_ms, c->ev[2], c->ev[3]);
   cudaEventElapsedTime(&S.bwd_total_ms, c->ev[0], c->ev[4]);
+  return SPL_OK;
+}
+
+// ---- post-processing and image output ---------------------------------------
+
+void spl_post_desc_defaults(spl_post_desc *p) {
+  if (!p) return;
+  p->a_eq_e = 0;
+  p->gamma = 1.0;
+  p->brightness = 0.0;
+  p->contrast = 1.0;
+  p->colorbar = 0;
+}
+
+namespace {
+
+// linearMap<COLOUR>::getVal_const (cxxsupport/linear_map.h:71-84) on the host:
+// lower_bound in double, interpolated per channel in double, rounded to float
+// per term, summed in float.
+void palette_host(int n, const double *x, const float *rgb, double v, float out[3]) {
+  int idx;
+  if (n == 1 || v <= x[0]) {
+    idx = 0;
+  } else if (v >= x[n - 1]) {
+    idx = n - 1;
+  } else {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = lo + (hi - lo) / 2;
+      if (x[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    idx = lo > 0 ? lo - 1 : 0;
+    if (idx > n - 2) idx = n - 2;
+    const double frac = (v - x[idx]) / (x[idx + 1] - x[idx]);
+    for (int c = 0; c < 3; ++c) {
+      const float a = (float)(rgb[3 * idx + c] * (1. - frac));
+      const float b = (float)(rgb[3 * (idx + 1) + c] * frac);
+      out[c] = a + b;
+    }
+    return;
+  }
+  for (int c = 0; c < 3; ++c) out[c] = rgb[3 * idx + c];
+}
+
+}  // namespace
+
+spl_status spl_postprocess(spl_context *c, const spl_frame_desc *d, const spl_post_desc *p,
+                           spl_image *img) {
+  if (!c || !d || !p || !img || !img->pic) return fail(SPL_ERR_INVALID, "null argument");
+  if (d->xres <= 0 || d->yres <= 0) return fail(SPL_ERR_INVALID, "xres/yres out of range");
+  SPL_CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const int xres = d->xres, yres = d->yres;
+  const size_t nf = (size_t)xres * yres * 3;
+  spl_status st;
+  float *pic = img->pic;
+  if (img->memspace == SPL_MEM_HOST) {
+    if ((st = ensure(c->post_img, nf * 4))) return st;
+    SPL_CK(cudaMemcpyAsync(c->post_img.p, img->pic, nf * 4, cudaMemcpyHostToDevice, s));
+    pic = as<float>(c->post_img);
+  }
+  const bool adjust = p->gamma != 1.0 || p->brightness != 0.0 || p->contrast != 1.0;
+  std::vector<float> tabs(2048);
+  float expfac = 0.f, taylor = 0.f;
+  if (p->a_eq_e) {
+    spl::exptable_tables(-20.f, tabs.data(), tabs.data() + 1024, &expfac, &taylor);
+    if ((st = ensure(c->post_tab, 2048 * 4))) return st;
+    SPL_CK(cudaMemcpyAsync(c->post_tab.p, tabs.data(), 2048 * 4, cudaMemcpyHostToDevice, s));
+  }
+  spl::launch_post(pic, (int64_t)nf, p->a_eq_e != 0, adjust, expfac, taylor,
+                   as<float>(c->post_tab), as<float>(c->post_tab) + 1024, p->gamma,
+                   p->brightness, p->contrast, s);
+  std::vector<float> bars;
+  std::vector<int> rows;
+  if (p->colorbar) {
+    int offset = 0;
+    for (int t = 0; t < d->ptypes && t < SPL_MAX_TYPES; ++t) {
+      if (d->color_is_vector[t]) continue;  // "adding no color bar for type t"
+      if (d->pal_n[t] < 1 || !d->pal_x[t] || !d->pal_rgb[t])
+        return fail(SPL_ERR_INVALID, "trying to access an empty map");
+      const size_t o = bars.size();
+      bars.resize(o + (size_t)xres * 3);
+      for (int x = 0; x < xres; ++x)
+        palette_host(d->pal_n[t], d->pal_x[t], d->pal_rgb[t], x / (double)xres,
+                     bars.data() + o + 3 * (size_t)x);
+      rows.push_back(yres - offset - 1);
+      offset += 10;
+    }
+    if (!rows.empty()) {
+      const size_t nb = bars.size() * 4, nr = rows.size() * 4;
+      if ((st = ensure(c->post_bar, nb + nr + 16))) return st;
+      SPL_CK(cudaMemcpyAsync(c->post_bar.p, bars.data(), nb, cudaMemcpyHostToDevice, s));
+      int *drows = reinterpret_cast<int *>(static_cast<uint8_t *>(c->post_bar.p) + nb);
+      SPL_CK(cudaMemcpyAsync(drows, rows.data(), nr, cudaMemcpyHostToDevice, s));
+      spl::launch_colorbar(pic, xres, yres, as<float>(c->post_bar), drows, (int)rows.size(), s);
+    }
+  }
+  if (img->memspace == SPL_MEM_HOST)
+    SPL_CK(cudaMemcpyAsync(img->pic, pic, nf * 4, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));  // the host tables above die here
+  SPL_CK(cudaGetLastError());
+  return SPL_OK;
+}
+
+namespace {
+
+// One row of the run-length TGA body (cxxsupport/ls_image.cc:206-286): runs of
+// equal pixels and of pairwise-different pixels, each cut into chunks of 128.
+void rle_row(const uint8_t *bgr, int xres, std::vector<uint8_t> &buf) {
+  auto same = [&](int a, int b) {
+    return bgr[3 * a] == bgr[3 * b] && bgr[3 * a + 1] == bgr[3 * b + 1] &&
+           bgr[3 * a + 2] == bgr[3 * b + 2];
+  };
+  int xs = 0;
+  while (xs < xres) {
+    int xe;
+    bool equal;
+    if (xs == xres - 1) {
+      xe = xres;
+      equal = false;
+    } else if (same(xs + 1, xs)) {
+      xe = xs + 2;
+      while (xe < xres && same(xe, xs)) ++xe;
+      equal = true;
+    } else {
+      xe = xs + 2;
+      while (xe < xres && !same(xe, xe - 1)) ++xe;
+      equal = false;
+    }
+    for (int cb = xs; cb < xe; cb += 128) {
+      const int csz = std::min(xe - cb, 128);
+      if (equal) {
+        buf.push_back((uint8_t)(csz - 1 + 128));
+        buf.insert(buf.end(), bgr + 3 * xs, bgr + 3 * xs + 3);
+      } else {
+        buf.push_back((uint8_t)(csz - 1));
+        buf.insert(buf.end(), bgr + 3 * cb, bgr + 3 * (cb + csz));
+      }
+    }
+    xs = xe;
+  }
+}
+
+spl_status encode_image(spl_context *c, const spl_image *img, int xres, int yres, int pictype,
+                        std::vector<uint8_t> &file) {
+  if (!img || !img->pic) return fail(SPL_ERR_INVALID, "null image");
+  if (xres <= 0 || yres <= 0) return fail(SPL_ERR_INVALID, "xres/yres out of range");
+  if (pictype == 1) return fail(SPL_ERR_UNSUPPORTED, "ASCII PPM no longer supported");
+  if (pictype != 0 && pictype != 2 && pictype != 3)
+    return fail(SPL_ERR_INVALID, "No valid image file type given ...");
+  SPL_CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  const size_t np = (size_t)xres * yres;
+  spl_status st;
+  const float *pic = img->pic;
+  if (img->memspace == SPL_MEM_HOST) {
+    if ((st = ensure(c->post_img, np * 12))) return st;
+    SPL_CK(cudaMemcpyAsync(c->post_img.p, img->pic, np * 12, cudaMemcpyHostToDevice, s));
+    pic = as<float>(c->post_img);
+  }
+  if ((st = ensure(c->post_bytes, np * 3))) return st;
+  spl::launch_encode(pic, xres, yres, pictype != 2, as<uint8_t>(c->post_bytes), s);
+  std::vector<uint8_t> body(np * 3);
+  SPL_CK(cudaMemcpyAsync(body.data(), c->post_bytes.p, np * 3, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));
+  SPL_CK(cudaGetLastError());
+  file.clear();
+  if (pictype == 2) {
+    char hdr[64];
+    const int n = std::snprintf(hdr, sizeof hdr, "P6\n%d\n%d\n255\n", xres, yres);
+    file.insert(file.end(), hdr, hdr + n);
+    file.insert(file.end(), body.begin(), body.end());
+    return SPL_OK;
+  }
+  const uint8_t hdr[18] = {0, 0, (uint8_t)(pictype == 0 ? 2 : 10), 0, 0, 0, 0, 0, 0, 0, 0, 0,
+                           (uint8_t)(xres % 256), (uint8_t)(xres / 256),
+                           (uint8_t)(yres % 256), (uint8_t)(yres / 256), 24, 32};
+  file.insert(file.end(), hdr, hdr + 18);
+  if (pictype == 0) {
+    file.insert(file.end(), body.begin(), body.end());
+  } else {
+    for (int y = 0; y < yres; ++y) rle_row(body.data() + (size_t)y * xres * 3, xres, file);
+  }
+  return SPL_OK;
+}
+
+}  // namespace
+
+spl_status spl_image_encode(spl_context *c, const spl_image *img, int xres, int yres,
+                            int pictype, uint8_t *out, int64_t cap, int64_t *len) {
+  if (!c || !len) return fail(SPL_ERR_INVALID, "null argument");
+  std::vector<uint8_t> file;
+  spl_status st = encode_image(c, img, xres, yres, pictype, file);
+  if (st) return st;
+  *len = (int64_t)file.size();
+  if (out && cap > 0) std::memcpy(out, file.data(), std::min<size_t>((size_t)cap, file.size()));
+  return SPL_OK;
+}
+
+spl_status spl_write_image(spl_context *c, const spl_image *img, int xres, int yres,
+                           int pictype, const char *path) {
+  if (!c || !path) return fail(SPL_ERR_INVALID, "null argument");
+  std::vector<uint8_t> file;
+  spl_status st = encode_image(c, img, xres, yres, pictype, file);
+  if (st) return st;
+  FILE *f = std::fopen(path, "wb");
+  if (!f) return fail(SPL_ERR_INVALID, std::string("could not create file '") + path + "'");
+  const size_t w = std::fwrite(file.data(), 1, file.size(), f);
+  const int cl = std::fclose(f);
+  if (w != file.size() || cl != 0)
+    return fail(SPL_ERR_INVALID, std::string("error writing output file '") + path + "'");
   return SPL_OK;
 }
 

@@ -243,6 +243,21 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
 // Message returned by spl_last_error_string() on this host thread.
 void set_last_error(const char *msg);
 
+// Post-processing and output (spl_post.cu).  exptable_tables builds the two
+// 1024-entry tables, expfac and taylorlimit of exptable<float32>(maxexp) on the
+// host; launch_post applies -expm1 and/or colour_adjust to nfloats floats;
+// launch_colorbar writes 10 rows ending at rows[k] (top) with colours[k]
+// (xres rgb each); launch_encode writes Colour8 rows (row-major, BGR if bgr).
+void exptable_tables(float maxexp, float *tab1, float *tab2, float *expfac,
+                     float *taylorlimit);
+void launch_post(float *pic, int64_t nfloats, bool do_expm1, bool do_adjust, float expfac,
+                 float taylorlimit, const float *tab1, const float *tab2, double gamma,
+                 double bright, double contrast, cudaStream_t s);
+void launch_colorbar(float *pic, int xres, int yres, const float *colours, const int *rows,
+                     int nbars, cudaStream_t s);
+void launch_encode(const float *pic, int xres, int yres, bool bgr, uint8_t *out,
+                   cudaStream_t s);
+
 // Exclusive scan of count[order[s]] (order may be null) into off (n+1 slots;
 // off[n] = total).
 size_t scan_scratch_bytes(int64_t n);

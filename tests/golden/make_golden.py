@@ -79,7 +79,56 @@ def main() -> int:
         np.savez_compressed(OUT / f"{name}.npz", **out)
         print(f"{name}: {len(w.particles)} particles, {int(proj['active'].sum())} active, "
               f"{frags} fragments")
+    post_cases(refs["simd"])
     return 0
+
+
+POST_VARIANTS = {
+    "plain": {},
+    "adjusted": {"pic_gamma": "0.8", "pic_brightness": "0.05", "pic_contrast": "1.3",
+                 "colorbar": "T"},
+}
+
+
+def post_cases(ref) -> None:
+    """splotch.cc:272-323 after host_rendering: -expm1 (additive frames),
+    colour_adjust, colour bar, and the TGA / PPM / run-length TGA bytes of the
+    result, from the reference's own code on the host_rendering images above."""
+    import tempfile
+
+    for name in ("additive", "absorption"):
+        g = np.load(OUT / f"{name}.npz")
+        meta = json.loads(bytes(g["meta"]).decode())
+        prm = dict(meta["params"])
+        a_eq_e = prm.get("a_eq_e", "T") in ("T", "True", "true")
+        pic = g["host_rendering_simd"].astype(np.float32)
+        if a_eq_e:  # a few pre-exp values across the whole exptable range
+            rng = np.random.default_rng(11)
+            pic[:3] = rng.uniform(-25.0, 0.0, pic[:3].shape).astype(np.float32)
+            pic[3:5] = rng.uniform(-0.005, 0.0, pic[3:5].shape).astype(np.float32)
+        rc = _rc_from_meta(meta)
+        out = {"pic_in": pic, "meta": g["meta"]}
+        with tempfile.TemporaryDirectory() as d:
+            for var, extra in POST_VARIANTS.items():
+                q = dict(prm)
+                q.update(extra)
+                res = ref.postprocess(q, rc, pic, a_eq_e)
+                out[f"post_{var}"] = res
+                for pt in (0, 2, 3):
+                    out[f"bytes_{var}_{pt}"] = np.frombuffer(ref.image_bytes(res, pt, d),
+                                                             dtype=np.uint8)
+        np.savez_compressed(OUT / f"post_{name}.npz", **out)
+        print(f"post_{name}: {pic.shape[0]}x{pic.shape[1]}")
+
+
+def _rc_from_meta(meta) -> RenderContext:
+    from splotch_gb300 import Palette
+
+    pals = [None if p is None else Palette(np.array(p["x"]), np.array(p["rgb"], np.float32))
+            for p in meta["palettes"]]
+    return RenderContext(campos=np.array(meta["campos"]), centerpos=np.array(meta["centerpos"]),
+                         lookat=np.array(meta["lookat"]), sky=np.array(meta["sky"]), amap=pals,
+                         b_brightness=meta["b_brightness"])
 
 
 if __name__ == "__main__":
