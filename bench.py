@@ -58,6 +58,11 @@ def parse():
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="particle-count multiplier of the batched workload")
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--only", default="all", choices=["all", "fwd_bwd", "batched", "large"],
+                    help="run one section alone (profiling; 'large' runs only this way)")
+    ap.add_argument("--large-scale", type=float, default=1.0)
+    ap.add_argument("--large-steps", type=int, default=2)
+    ap.add_argument("--fwd-bwd-particles", type=int, default=4_000_000)
     ap.add_argument("--scale", type=float, default=1.0,
                     help="particle-count multiplier (profiling runs use a smaller frame)")
     return ap.parse_args()
@@ -255,7 +260,7 @@ def fwd_bwd(args, local: int) -> dict:
 
     dev = f"cuda:{local}"
     out = {}
-    n = int(4_000_000 * min(args.scale, 1.0))
+    n = int(args.fwd_bwd_particles * min(args.scale, 1.0))
     for mode in ("additive", "absorption"):
         w = synth.differentiable(n=n, mode=mode, xres=1024, tile=args.tile, order=args.order)
         r = sg.Renderer(local)
@@ -309,6 +314,68 @@ def fwd_bwd(args, local: int) -> dict:
         res["active"] = int(st["n_active"])
         out[mode] = res
         r.close()
+    return out
+
+
+def large(args, local: int) -> dict:
+    """Large render, forward+backward (opt-in, --only large): 400M particles x
+    large_scale, ordered absorption, per-particle RGB, Pareto hsml, 4096^2.
+    One step = render + dL/dpic + backward, all resident in HBM."""
+    import torch
+
+    import splotch_gb300 as sg
+    from splotch_gb300 import _abi, synth
+
+    dev = f"cuda:{local}"
+    n = int(400_000_000 * args.large_scale)
+    t0 = time.perf_counter()
+    w = synth.large(n=n, tile=args.tile, order=args.order)
+    gen_s = time.perf_counter() - t0
+    r = sg.Renderer(local)
+    stream = torch.cuda.Stream(device=dev)
+    r.set_stream(stream.cuda_stream)
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    soa = {}
+    for k, v in synth.soa_from_aos(w.particles).items():
+        soa[k] = torch.from_numpy(v).to(dev)
+    del w
+    pic = torch.zeros((desc.xres, desc.yres, 3), dtype=torch.float32, device=dev)
+    grads = {f: torch.zeros(n, dtype=torch.float32, device=dev) for f in _abi.GRAD_FIELDS}
+    out = {"particles": n, "image": [desc.xres, desc.yres], "generate_s": gen_s}
+    for name, bw in (("fwd", False), ("fwd_bwd", True)):
+        r.set_differentiable(bw)
+        for _ in range(max(1, args.warmup // 3)):
+            r.render_soa(desc, soa, pic)
+            if bw:
+                with torch.cuda.stream(stream):
+                    gpic = 2.0 * pic
+                r.backward(gpic, grads, device=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, args.large_steps)
+        e0.record(stream)
+        for _ in range(steps):
+            r.render_soa(desc, soa, pic)
+            if bw:
+                with torch.cuda.stream(stream):
+                    gpic = 2.0 * pic
+                r.backward(gpic, grads, device=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name + "_ms"] = e0.elapsed_time(e1) / steps
+        st = r.stats()
+        out[name + "_stages"] = {k: st[k] for k in ("project_ms", "sort_ms", "bin_ms",
+                                                    "splat_ms", "bwd_splat_ms",
+                                                    "bwd_project_ms")}
+    st = r.stats()
+    out.update({"active": int(st["n_active"]), "bin_entries": int(st["n_entries"]),
+                "wide_particles": int(st["n_wide"]),
+                "ratio_fwd_bwd_over_fwd": out["fwd_bwd_ms"] / out["fwd_ms"],
+                "fwd_mparticles_per_s": n / (out["fwd_ms"] * 1e-3) / 1e6,
+                "fwd_bwd_mparticles_per_s": n / (out["fwd_bwd_ms"] * 1e-3) / 1e6,
+                "device_memory_peak_gb": torch.cuda.max_memory_allocated(dev) / 1e9})
+    r.close()
     return out
 
 
@@ -404,6 +471,12 @@ def run_gpu(args):
 
     import splotch_gb300 as sg
     from splotch_gb300 import synth
+
+    if args.only != "all":  # one section alone (profiling runs); prints its own line
+        torch.cuda.set_device(local)
+        res = {"fwd_bwd": fwd_bwd, "batched": batched, "large": large}[args.only](args, local)
+        print(json.dumps({"section": args.only, "result": res}), flush=True)
+        return 0
 
     w, cfg = make_workload(args, seed_offset=rank * 1000)
     cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"

@@ -196,6 +196,34 @@ spl_status spl_render_backward(spl_context *ctx, const spl_image *grad_pic, spl_
    (16 bytes per pixel, a few adds per fragment).  Off by default. */
 spl_status spl_context_set_differentiable(spl_context *ctx, int enable);
 
+/* ---- before host_rendering: particle normalisation --------------------- */
+/* sceneMaker::particle_normalize (splotch/scenemaker.cc:40-296, host branch)
+   on the device: per type, optional log10 of I (intensity_log{t}) and of the
+   colour (color_log{t}) or asinh of the colour (color_asinh{t}); the ranges of
+   size, intensity and colour; intensity_min/max{t} and color_min/max{t}
+   overrides; then every I and colour mapped to [0,1] by Normalizer::
+   normAndClamp.  The particles (AoS or SoA, host or device) change in place;
+   log10f/log come from CUDA's math library (an ulp from the host's). */
+typedef struct {
+  int ptypes;
+  int intensity_log[SPL_MAX_TYPES], color_log[SPL_MAX_TYPES];
+  int color_asinh[SPL_MAX_TYPES], color_is_vector[SPL_MAX_TYPES];
+  int has_intensity_min[SPL_MAX_TYPES], has_intensity_max[SPL_MAX_TYPES];
+  int has_color_min[SPL_MAX_TYPES], has_color_max[SPL_MAX_TYPES];
+  float intensity_min[SPL_MAX_TYPES], intensity_max[SPL_MAX_TYPES];
+  float color_min[SPL_MAX_TYPES], color_max[SPL_MAX_TYPES];
+} spl_normalize_desc;
+typedef struct {
+  /* range_*: colour range of the data (the range_min/max{t} keys the
+     reference sets); clamp_*: the colour range applied (clamp_min/max{t}) */
+  float range_min[SPL_MAX_TYPES], range_max[SPL_MAX_TYPES];
+  float clamp_min[SPL_MAX_TYPES], clamp_max[SPL_MAX_TYPES];
+  float intensity_min[SPL_MAX_TYPES], intensity_max[SPL_MAX_TYPES];
+  float size_min[SPL_MAX_TYPES], size_max[SPL_MAX_TYPES];
+} spl_normalize_result;
+spl_status spl_particle_normalize(spl_context *ctx, const spl_normalize_desc *d,
+                                  spl_particles *p, spl_normalize_result *res);
+
 /* ---- after host_rendering: post-processing and image output ------------ */
 /* What splotch/splotch.cc:272-323 does with the image once host_rendering has
    returned, on the device. */

@@ -384,6 +384,37 @@ def _renderer() -> "Renderer":
     return _default_renderer
 
 
+def particle_normalize(params: ParamFile, particles, renderer: Renderer | None = None, *,
+                       device: bool = False) -> dict:
+    """sceneMaker::particle_normalize (splotch/scenemaker.cc:40-296), in place
+    on a particle_sim array (numpy, or a device uint8 tensor of n*36 bytes when
+    device=True).  Like the reference it records the colour range of the data
+    and the range applied as the range_min/max{t} and clamp_min/max{t} keys."""
+    r = renderer or _renderer()
+    d = _abi.NormalizeDesc()
+    d.ptypes = params.find("ptypes", 1)
+    for t in range(d.ptypes):
+        d.intensity_log[t] = 1 if params.find(f"intensity_log{t}", False) else 0
+        d.color_log[t] = 1 if params.find(f"color_log{t}", False) else 0
+        d.color_asinh[t] = 1 if params.find(f"color_asinh{t}", False) else 0
+        d.color_is_vector[t] = 1 if params.find(f"color_is_vector{t}", False) else 0
+        for key in ("intensity_min", "intensity_max", "color_min", "color_max"):
+            if params.param_present(f"{key}{t}"):
+                getattr(d, "has_" + key)[t] = 1
+                getattr(d, key)[t] = params.find(f"{key}{t}", 0.0)
+    n = len(particles) if isinstance(particles, np.ndarray) else particles.numel() // 36
+    p = _abi.Particles(n=n, layout=_abi.SPL_LAYOUT_AOS,
+                       memspace=_abi.SPL_MEM_DEVICE if device else _abi.SPL_MEM_HOST,
+                       aos=_abi.ptr(particles))
+    res = _abi.NormalizeResult()
+    _abi.check(r.lib.spl_particle_normalize(r.ctx, C.byref(d), C.byref(p), C.byref(res)))
+    out = {k: [float(v) for v in getattr(res, k)[:d.ptypes]] for k, _ in res._fields_}
+    for t in range(d.ptypes):
+        for key in ("range_min", "range_max", "clamp_min", "clamp_max"):
+            params.set_param(f"{key}{t}", out[key][t])
+    return out
+
+
 def post_desc(params: ParamFile, a_eq_e: bool | None = None) -> _abi.PostDesc:
     """The keys of splotch.cc:272-291 (a_eq_e, pic_gamma, pic_brightness,
     pic_contrast, colorbar) with the reference's defaults."""

@@ -30,6 +30,7 @@ EXPORTED = [
     "spl_render_backward", "spl_context_set_differentiable", "spl_batch_options_defaults",
     "spl_batch_create", "spl_batch_render", "spl_batch_get_info", "spl_batch_destroy",
     "spl_post_desc_defaults", "spl_postprocess", "spl_image_encode", "spl_write_image",
+    "spl_particle_normalize",
 ]
 SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
@@ -87,6 +88,21 @@ GRAD_FIELDS = ("I", "cr", "cg", "cb", "x", "y", "z", "r")
 class Grads(C.Structure):
     _fields_ = [("memspace", C.c_int)] + [(f, C.c_void_p) for f in GRAD_FIELDS] + [
         ("campos", C.c_double * 3)]
+
+
+class NormalizeDesc(C.Structure):
+    _fields_ = [("ptypes", C.c_int)] + [
+        (k, C.c_int * SPL_MAX_TYPES) for k in (
+            "intensity_log", "color_log", "color_asinh", "color_is_vector",
+            "has_intensity_min", "has_intensity_max", "has_color_min", "has_color_max")] + [
+        (k, C.c_float * SPL_MAX_TYPES) for k in (
+            "intensity_min", "intensity_max", "color_min", "color_max")]
+
+
+class NormalizeResult(C.Structure):
+    _fields_ = [(k, C.c_float * SPL_MAX_TYPES) for k in (
+        "range_min", "range_max", "clamp_min", "clamp_max", "intensity_min", "intensity_max",
+        "size_min", "size_max")]
 
 
 class PostDesc(C.Structure):
@@ -164,6 +180,8 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_batch_render": (C.c_int, [vp]),
         "spl_batch_get_info": (C.c_int, [vp, C.POINTER(BatchInfo)]),
         "spl_batch_destroy": (C.c_int, [vp]),
+        "spl_particle_normalize": (C.c_int, [vp, C.POINTER(NormalizeDesc), C.POINTER(Particles),
+                                             C.POINTER(NormalizeResult)]),
         "spl_post_desc_defaults": (None, [C.POINTER(PostDesc)]),
         "spl_postprocess": (C.c_int, [vp, C.POINTER(FrameDesc), C.POINTER(PostDesc),
                                       C.POINTER(Image)]),

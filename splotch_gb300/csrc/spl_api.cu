@@ -711,6 +711,122 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
   return SPL_OK;
 }
 
+// ---- particle normalisation ---------------------------------------------------
+
+spl_status spl_particle_normalize(spl_context *c, const spl_normalize_desc *d,
+                                  spl_particles *p, spl_normalize_result *res) {
+  if (!c || !d || !p || !res) return fail(SPL_ERR_INVALID, "null argument");
+  if (d->ptypes < 1 || d->ptypes > SPL_MAX_TYPES)
+    return fail(SPL_ERR_INVALID, "ptypes must be in [1,8]");
+  const int64_t n = p->n;
+  if (n < 0 || n > 0xffffffffLL) return fail(SPL_ERR_INVALID, "particle count out of range");
+  bool any_vec = false;
+  for (int t = 0; t < d->ptypes; ++t) any_vec = any_vec || d->color_is_vector[t];
+  if (p->layout == SPL_LAYOUT_SOA) {
+    if (n > 0 && (!p->r || !p->I || !p->cr || (any_vec && (!p->cg || !p->cb))))
+      return fail(SPL_ERR_INVALID, "null SoA pointer");
+  } else if (p->layout != SPL_LAYOUT_AOS || (n > 0 && !p->aos)) {
+    return fail(SPL_ERR_INVALID, "bad particle view");
+  }
+  SPL_CK(cudaSetDevice(c->device));
+  cudaStream_t s = c->stream;
+  spl_status st;
+  spl::NormView v{};
+  // device view of the particles (host inputs are staged and copied back); the
+  // view's fields are declared read-only for rendering, normalisation writes
+  // them in place
+  float *soa_host[5] = {const_cast<float *>(p->I), const_cast<float *>(p->cr),
+                        const_cast<float *>(p->cg), const_cast<float *>(p->cb),
+                        const_cast<float *>(p->r)};
+  if (p->layout == SPL_LAYOUT_AOS) {
+    if (p->memspace == SPL_MEM_HOST) {
+      if ((st = ensure(c->aos_in, n * 36))) return st;
+      SPL_CK(cudaMemcpyAsync(c->aos_in.p, p->aos, n * 36, cudaMemcpyHostToDevice, s));
+      v.aos = c->aos_in.p;
+    } else {
+      v.aos = p->aos;
+    }
+  } else if (p->memspace == SPL_MEM_HOST) {
+    float **dst[5] = {&v.I, &v.cr, &v.cg, &v.cb, const_cast<float **>(&v.r)};
+    for (int k = 0; k < 5; ++k) {
+      if (!soa_host[k]) continue;
+      if ((st = ensure(c->soa_in[k], n * 4))) return st;
+      SPL_CK(cudaMemcpyAsync(c->soa_in[k].p, soa_host[k], n * 4, cudaMemcpyHostToDevice, s));
+      *dst[k] = as<float>(c->soa_in[k]);
+    }
+    if (p->type) {
+      if ((st = ensure(c->soa_in[8], n * 2))) return st;
+      SPL_CK(cudaMemcpyAsync(c->soa_in[8].p, p->type, n * 2, cudaMemcpyHostToDevice, s));
+      v.type = as<uint16_t>(c->soa_in[8]);
+    }
+  } else {
+    v.I = soa_host[0];
+    v.cr = soa_host[1];
+    v.cg = soa_host[2];
+    v.cb = soa_host[3];
+    v.r = p->r;
+    v.type = p->type;
+  }
+  spl::NormConst nc{};
+  nc.ptypes = d->ptypes;
+  for (int t = 0; t < d->ptypes; ++t) {
+    nc.intensity_log[t] = d->intensity_log[t] != 0;
+    nc.color_log[t] = d->color_log[t] != 0;
+    nc.color_asinh[t] = d->color_asinh[t] != 0;
+    nc.color_is_vector[t] = d->color_is_vector[t] != 0;
+  }
+  // pass 1: transforms and per-type ranges
+  int h_stats[SPL_MAXT * 6];
+  spl::norm_stats_init(h_stats);
+  if ((st = ensure(c->small, 256)) || (st = ensure(c->post_tab, sizeof h_stats))) return st;
+  uint32_t *d_err = as<uint32_t>(c->small);
+  SPL_CK(cudaMemsetAsync(d_err, 0, 4, s));
+  SPL_CK(cudaMemcpyAsync(c->post_tab.p, h_stats, sizeof h_stats, cudaMemcpyHostToDevice, s));
+  spl::launch_norm_collect(v, n, nc, as<int>(c->post_tab), d_err, s);
+  uint32_t err = 0;
+  SPL_CK(cudaMemcpyAsync(h_stats, c->post_tab.p, sizeof h_stats, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));
+  if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
+  // overrides (scenemaker.cc:222-232) and pass 2: normAndClamp
+  spl::NormRanges rg{};
+  for (int t = 0; t < d->ptypes; ++t) {
+    const int *st6 = h_stats + 6 * t;
+    res->size_min[t] = spl::norm_stat_value(st6[0]);
+    res->size_max[t] = spl::norm_stat_value(st6[1]);
+    float imin = spl::norm_stat_value(st6[2]), imax = spl::norm_stat_value(st6[3]);
+    float cmin = spl::norm_stat_value(st6[4]), cmax = spl::norm_stat_value(st6[5]);
+    res->range_min[t] = cmin;
+    res->range_max[t] = cmax;
+    if (d->has_intensity_min[t]) imin = d->intensity_min[t];
+    if (d->has_intensity_max[t]) imax = d->intensity_max[t];
+    if (d->has_color_min[t]) cmin = d->color_min[t];
+    if (d->has_color_max[t]) cmax = d->color_max[t];
+    res->clamp_min[t] = cmin;
+    res->clamp_max[t] = cmax;
+    res->intensity_min[t] = imin;
+    res->intensity_max[t] = imax;
+    rg.imin[t] = imin;
+    rg.imax[t] = imax;
+    rg.cmin[t] = cmin;
+    rg.cmax[t] = cmax;
+  }
+  spl::launch_norm_clamp(v, n, nc, rg, s);
+  if (p->memspace == SPL_MEM_HOST && n > 0) {
+    if (p->layout == SPL_LAYOUT_AOS) {
+      SPL_CK(cudaMemcpyAsync(p->aos, v.aos, n * 36, cudaMemcpyDeviceToHost, s));
+    } else {
+      float *dev[4] = {v.I, v.cr, v.cg, v.cb};
+      for (int k = 0; k < 4; ++k)
+        if (soa_host[k] && dev[k])
+          SPL_CK(cudaMemcpyAsync(soa_host[k], dev[k], n * 4, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  SPL_CK(cudaStreamSynchronize(s));
+  SPL_CK(cudaGetLastError());
+  return SPL_OK;
+}
+
 // ---- post-processing and image output ---------------------------------------
 
 void spl_post_desc_defaults(spl_post_desc *p) {

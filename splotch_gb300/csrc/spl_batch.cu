@@ -43,36 +43,53 @@ struct FrameTile {
 
 constexpr int kWide = 64;  // tiles above which a record goes to the warp path
 
+// Record start of each frame of one class (rows j0 .. j0+m-1 of the projection
+// order, word bases wbase relative to the class's first word; word_off is the
+// class's own exclusive scan) and the class's live count at [m].
 __global__ void k_frame_bounds(const uint32_t *__restrict__ word_off,
-                               const uint32_t *__restrict__ wbase, int nf, int64_t nwords,
-                               const uint32_t *__restrict__ total,
+                               const uint32_t *__restrict__ wbase, int j0, int m,
+                               int64_t nwords, const uint32_t *__restrict__ total,
                                uint32_t *__restrict__ actv_start) {
-  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f <= nf; f += gridDim.x * blockDim.x)
-    actv_start[f] = (f == nf || (int64_t)wbase[f] >= nwords) ? *total : word_off[wbase[f]];
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= m; k += gridDim.x * blockDim.x) {
+    const int64_t w = k < m ? (int64_t)wbase[j0 + k] : nwords;
+    actv_start[k] = (k == m || w >= nwords) ? *total : word_off[w];
+  }
 }
 
-// Frame of every live record (binary search over the frames' record starts);
-// sentinels past the live count: key all ones, frame nf, no tiles.
-__global__ void k_batch_records(const uint32_t *__restrict__ actv_start, int nf, uint32_t cap,
+// Frame of every live record of one class segment (binary search over the
+// class's record starts, frame ids from fmap); sentinels past the live count:
+// key all ones, frame nf, no tiles.
+__global__ void k_batch_records(const uint32_t *__restrict__ actv_start, int m,
+                                const uint32_t *__restrict__ fmap, int nf, uint32_t cap,
                                 uint32_t *__restrict__ key, uint32_t *__restrict__ count,
                                 uint32_t *__restrict__ frame, uint32_t *status) {
-  const uint32_t live = actv_start[nf];
+  const uint32_t live = actv_start[m];
   if (blockIdx.x == 0 && threadIdx.x == 0 && live > cap) atomicOr(status, 1u);
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < cap;
        r += (int64_t)gridDim.x * blockDim.x) {
     if (r < live) {
-      int lo = 0, hi = nf;  // last f with actv_start[f] <= r
+      int lo = 0, hi = m;  // last k with actv_start[k] <= r
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
         if (actv_start[mid] <= (uint32_t)r) lo = mid; else hi = mid;
       }
-      frame[r] = (uint32_t)lo;
+      frame[r] = fmap[lo];
     } else {
       frame[r] = (uint32_t)nf;
       key[r] = 0xffffffffu;
       count[r] = 0u;
     }
   }
+}
+
+// Visiting order of all records: additive records in place, then the ordered
+// segment in its sorted order.
+__global__ void k_compose_order(const uint32_t *__restrict__ perm_ord, uint32_t cap_add,
+                                uint32_t cap_ord, uint32_t *__restrict__ order) {
+  const int64_t total = (int64_t)cap_add + cap_ord;
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < total;
+       s += (int64_t)gridDim.x * blockDim.x)
+    order[s] = s < cap_add ? (uint32_t)s : cap_add + perm_ord[s - cap_add];
 }
 
 __global__ void __launch_bounds__(256) k_emit_batch_narrow(
@@ -232,23 +249,29 @@ struct spl_batch {
   std::vector<std::vector<float>> pal_rgb_copy;
   spl_batch_options opt{};
   int T = 16, cfg_add = 0, cfg_abs = 2;
-  // plan
+  // plan.  Projection order: additive frames, then ordered ones; records of
+  // the two classes live in separate segments, [0, cap_add) and
+  // [cap_add, cap_add + cap_ord), so that only ordered records are sorted.
   std::vector<spl::FrameSetup> fs;
   std::vector<spl::ProjConst> pc;      // device palette pointers filled in
-  std::vector<uint32_t> wbase;         // activity-word base per frame (+ total)
+  std::vector<int> proj;               // projection order -> frame
+  int n_add_frames = 0;
+  std::vector<uint32_t> wbase;         // activity-word base per projection row,
+                                       // relative to its class's first word
   std::vector<uint32_t> tbase;         // global tile base per frame (+ total)
-  int64_t nwords = 0, ntiles = 0, n_add_tiles = 0, cap_a = 0, cap_e = 0;
-  bool any_ordered = false;
+  int64_t nwords = 0, nw_add = 0, ntiles = 0, n_add_tiles = 0;
+  int64_t cap_add = 0, cap_ord = 0, cap_a = 0, cap_e = 0;
+  uint32_t fblocks = 0, dblocks = 0;
   int frame_bits = 1, tile_bits = 1;
   std::vector<DevBuf *> owned;
   DevBuf pal_x, pal_rgb, pal_thr, pal_xff, pal_invff;
-  DevBuf flags, word_off, d_wbase, d_tbase, actv_start;
+  DevBuf flags, word_off, d_wbase, d_tbase, ftab, actv_add, actv_ord, fmap_add, fmap_ord;
   DevBuf pos_c, col_c, idx_c, count_c, key_c, frame_c;
-  DevBuf ktmp, vtmp, kout, perm1, fkey, perm, count_seq, off, wide_list, radix_scr;
+  DevBuf ktmp, vtmp, kout, perm1, fkey, perm, order, count_seq, off, wide_list, radix_scr;
   DevBuf tkey, tval, tkey2, tval2, tkey_s, tval_s;
   DevBuf tile_start, tcost, tcost_s, work, work_tmp, frame_of_tile, frame_ord, ft, splat_args;
   DevBuf status;  // [0] overflow bits, [1] wide count, [2],[3] queue counters,
-                  // [4] error word, [5] live records, [6..7] spare
+                  // [4] error word, [5] live additive records, [6] live ordered
   uint32_t *h_status = nullptr;  // pinned copy of the first 8 status words
   uint64_t *h_entries = nullptr; // pinned copy of the live entry count
   cudaGraph_t graph = nullptr;
@@ -310,8 +333,8 @@ spl::SoAIn set_soa(const spl_particles &p) {
 
 // Measured sizes at tile size T: one plain render of every frame on the
 // context (its image lands in the frame's buffer and is redrawn by the batch).
-spl_status measure(spl_batch *b, int T, int64_t &acts, int64_t &ents) {
-  acts = ents = 0;
+spl_status measure(spl_batch *b, int T, int64_t &acts_add, int64_t &acts_ord, int64_t &ents) {
+  acts_add = acts_ord = ents = 0;
   for (const auto &fr : b->frames) {
     spl_frame_desc d = fr.desc;
     d.tile_size = T;
@@ -321,7 +344,7 @@ spl_status measure(spl_batch *b, int T, int64_t &acts, int64_t &ents) {
     if (st) return st;
     spl_stats s;
     spl_get_stats(b->ctx, &s);
-    acts += s.n_active;
+    (fr.desc.a_eq_e ? acts_add : acts_ord) += s.n_active;
     ents += s.n_entries;
   }
   return SPL_OK;
@@ -329,43 +352,64 @@ spl_status measure(spl_batch *b, int T, int64_t &acts, int64_t &ents) {
 
 // Buffers, per-frame constants and the static tables for tile size T and the
 // given capacities.
-spl_status plan(spl_batch *b, int T, int64_t cap_a, int64_t cap_e) {
+spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t cap_e) {
   drop_graph(b);
   const int nf = (int)b->frames.size();
   b->T = T;
   b->fs.assign(nf, spl::FrameSetup());
   b->pc.assign(nf, spl::ProjConst());
-  b->wbase.assign(nf + 1, 0);
   b->tbase.assign(nf + 1, 0);
-  int64_t npal = 0, words = 0, tiles = 0, add_tiles = 0;
-  b->any_ordered = false;
+  int64_t npal = 0, tiles = 0, add_tiles = 0;
   std::vector<uint8_t> ordered(nf, 0);
   spl_status st;
+  b->proj.clear();
   for (int f = 0; f < nf; ++f) {
     const spl_batch_frame &fr = b->frames[f];
     if ((st = spl::frame_setup(&fr.desc, T, false, b->fs[f]))) return st;
-    b->wbase[f] = (uint32_t)words;
     b->tbase[f] = (uint32_t)tiles;
-    words += (b->sets[fr.set].n + 31) / 32;
     tiles += b->fs[f].ntiles;
     npal += b->fs[f].npal + 1;
     ordered[f] = fr.desc.a_eq_e ? 0 : 1;
-    if (fr.desc.a_eq_e) add_tiles += b->fs[f].ntiles;
-    if (b->fs[f].do_sort) b->any_ordered = true;
+    if (fr.desc.a_eq_e) {
+      add_tiles += b->fs[f].ntiles;
+      b->proj.push_back(f);
+    }
   }
-  if (tiles >= 0x7fffffffLL || words >= 0xffffffffLL || cap_a >= 0xffffffffLL ||
-      cap_e >= 0xffffffffLL)
+  b->n_add_frames = (int)b->proj.size();
+  for (int f = 0; f < nf; ++f)
+    if (ordered[f]) b->proj.push_back(f);
+  // activity words in projection order, based per class
+  b->wbase.assign(nf + 1, 0);
+  int64_t words = 0, nw_add = 0, fblocks = 0, dblocks = 0;
+  std::vector<uint32_t> fb0(nf), db0(nf);
+  for (int j = 0; j < nf; ++j) {
+    if (j == b->n_add_frames) nw_add = words;
+    b->wbase[j] = (uint32_t)(words - (j >= b->n_add_frames ? nw_add : 0));
+    const int64_t w = (b->sets[b->frames[b->proj[j]].set].n + 31) / 32;
+    fb0[j] = (uint32_t)fblocks;
+    db0[j] = (uint32_t)dblocks;
+    fblocks += (w + spl::kFlagWordsPerBlock - 1) / spl::kFlagWordsPerBlock;
+    dblocks += (w + spl::kDenseWordsPerBlock - 1) / spl::kDenseWordsPerBlock;
+    words += w;
+  }
+  if (b->n_add_frames == nf) nw_add = words;
+  if (tiles >= 0x7fffffffLL || words >= 0xffffffffLL || cap_add + cap_ord >= 0xffffffffLL ||
+      cap_e >= 0xffffffffLL || fblocks >= 0x7fffffffLL)
     return fail(SPL_ERR_CAPACITY, "batch: more than 2^31 tiles or 2^32 records/entries");
-  b->wbase[nf] = (uint32_t)words;
   b->tbase[nf] = (uint32_t)tiles;
   b->nwords = words;
+  b->nw_add = nw_add;
+  b->fblocks = (uint32_t)fblocks;
+  b->dblocks = (uint32_t)dblocks;
   b->ntiles = tiles;
   b->n_add_tiles = add_tiles;
-  b->cap_a = std::max<int64_t>(cap_a, 1);
+  b->cap_add = cap_add;
+  b->cap_ord = cap_ord;
+  b->cap_a = std::max<int64_t>(cap_add + cap_ord, 1);
   b->cap_e = std::max<int64_t>(cap_e, 1);
   b->frame_bits = spl::bits_for(nf + 1);
   b->tile_bits = spl::bits_for(tiles + 1);
-  const int64_t A = b->cap_a, E = b->cap_e;
+  const int64_t A = b->cap_a, E = b->cap_e, O = std::max<int64_t>(cap_ord, 1);
 
   // ---- buffers -------------------------------------------------------------
   size_t scan_b = spl::scan_scratch_bytes(std::max<int64_t>(words, A + 1));
@@ -378,13 +422,18 @@ spl_status plan(spl_batch *b, int T, int64_t cap_a, int64_t cap_e) {
       (st = dev_alloc(b, b->flags, words * 4)) || (st = dev_alloc(b, b->word_off, words * 4)) ||
       (st = dev_alloc(b, b->d_wbase, (nf + 1) * 4)) ||
       (st = dev_alloc(b, b->d_tbase, (nf + 1) * 4)) ||
-      (st = dev_alloc(b, b->actv_start, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->ftab, nf * sizeof(spl::FrameProj))) ||
+      (st = dev_alloc(b, b->actv_add, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->actv_ord, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->fmap_add, (nf + 1) * 4)) ||
+      (st = dev_alloc(b, b->fmap_ord, (nf + 1) * 4)) ||
       (st = dev_alloc(b, b->pos_c, A * 16)) || (st = dev_alloc(b, b->col_c, A * 16)) ||
       (st = dev_alloc(b, b->idx_c, A * 4)) || (st = dev_alloc(b, b->count_c, A * 4)) ||
       (st = dev_alloc(b, b->key_c, A * 4)) || (st = dev_alloc(b, b->frame_c, A * 4)) ||
-      (st = dev_alloc(b, b->ktmp, A * 4)) || (st = dev_alloc(b, b->vtmp, A * 4)) ||
-      (st = dev_alloc(b, b->kout, A * 4)) || (st = dev_alloc(b, b->perm1, A * 4)) ||
-      (st = dev_alloc(b, b->fkey, A * 4)) || (st = dev_alloc(b, b->perm, A * 4)) ||
+      (st = dev_alloc(b, b->ktmp, O * 4)) || (st = dev_alloc(b, b->vtmp, O * 4)) ||
+      (st = dev_alloc(b, b->kout, O * 4)) || (st = dev_alloc(b, b->perm1, O * 4)) ||
+      (st = dev_alloc(b, b->fkey, O * 4)) || (st = dev_alloc(b, b->perm, O * 4)) ||
+      (st = dev_alloc(b, b->order, A * 4)) ||
       (st = dev_alloc(b, b->count_seq, A * 4)) || (st = dev_alloc(b, b->off, (A + 1) * 8)) ||
       (st = dev_alloc(b, b->wide_list, A * 4)) || (st = dev_alloc(b, b->radix_scr, radix_b)) ||
       (st = dev_alloc(b, b->tkey, E * 4)) || (st = dev_alloc(b, b->tval, E * 4)) ||
@@ -449,7 +498,43 @@ spl_status plan(spl_batch *b, int T, int64_t cap_a, int64_t cap_e) {
     a.config = -1;
     a.pic = b->frames[f].pic;
   }
+  // projection table (projection order) and the frame ids of each class
+  std::vector<spl::FrameProj> ftab(nf);
+  std::vector<uint32_t> fmap_add, fmap_ord;
+  for (int j = 0; j < nf; ++j) {
+    const int f = b->proj[j];
+    const bool add = j < b->n_add_frames;
+    const spl_particles &p = b->sets[b->frames[f].set];
+    spl::FrameProj &t = ftab[j];
+    std::memset(&t, 0, sizeof(t));
+    t.c = b->pc[f];
+    t.aos = set_aos(p);
+    t.soa = set_soa(p);
+    t.n = p.n;
+    const int64_t seg = add ? 0 : b->cap_add;          // first record of the class
+    const int64_t w = b->wbase[j] + (add ? 0 : nw_add);  // first word, absolute
+    t.o.flags = as<uint32_t>(b->flags) + w;
+    t.o.word_off = as<uint32_t>(b->word_off) + w;
+    t.o.pos_c = as<float4>(b->pos_c) + seg;
+    t.o.col_c = as<float4>(b->col_c) + seg;
+    t.o.idx_c = as<uint32_t>(b->idx_c) + seg;
+    t.o.count_c = as<uint32_t>(b->count_c) + seg;
+    t.o.key_c = as<uint32_t>(b->key_c) + seg;
+    t.o.cap_c = (uint32_t)(add ? b->cap_add : b->cap_ord);
+    t.o.err = as<uint32_t>(b->status) + 4;
+    t.fblock0 = fb0[j];
+    t.dblock0 = db0[j];
+    (add ? fmap_add : fmap_ord).push_back((uint32_t)f);
+  }
+  fmap_add.push_back(0);
+  fmap_ord.push_back(0);
   cudaStream_t s = b->stream;
+  BCK(cudaMemcpyAsync(b->ftab.p, ftab.data(), nf * sizeof(spl::FrameProj),
+                      cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->fmap_add.p, fmap_add.data(), fmap_add.size() * 4,
+                      cudaMemcpyHostToDevice, s));
+  BCK(cudaMemcpyAsync(b->fmap_ord.p, fmap_ord.data(), fmap_ord.size() * 4,
+                      cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->pal_x.p, px.data(), px.size() * 8, cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->pal_rgb.p, prgb.data(), prgb.size() * 4, cudaMemcpyHostToDevice, s));
   BCK(cudaMemcpyAsync(b->pal_thr.p, pthr.data(), pthr.size() * 4, cudaMemcpyHostToDevice, s));
@@ -498,53 +583,60 @@ spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
   const uint32_t capA = (uint32_t)b->cap_a;
   const uint64_t capE = (uint64_t)b->cap_e;
   BCK(cudaMemsetAsync(status, 0, 64, s));
-  // ---- projection: flags per frame, one scan, dense per frame -------------------
-  spl::ProjectOut po;
-  std::memset(&po, 0, sizeof(po));
-  po.pos_c = as<float4>(b->pos_c);
-  po.col_c = as<float4>(b->col_c);
-  po.idx_c = as<uint32_t>(b->idx_c);
-  po.count_c = as<uint32_t>(b->count_c);
-  po.key_c = as<uint32_t>(b->key_c);
-  po.cap_c = capA;
-  po.err = err;
-  for (int f = 0; f < nf; ++f) {
-    const spl_particles &p = b->sets[b->frames[f].set];
-    const spl::SoAIn soa = set_soa(p);
-    po.flags = as<uint32_t>(b->flags) + b->wbase[f];
-    spl::launch_project_flags(set_aos(p), &soa, p.n, b->pc[f], po, s);
-    if (p.n > 0) ++launches;
-  }
-  spl::scan_popc(as<uint32_t>(b->flags), b->nwords, as<uint32_t>(b->word_off), status + 5,
-                 b->radix_scr.p, s, &launches);
-  spl::k_frame_bounds<<<1, 256, 0, s>>>(as<uint32_t>(b->word_off), as<uint32_t>(b->d_wbase), nf,
-                                        b->nwords, status + 5, as<uint32_t>(b->actv_start));
+  // ---- projection: one flags launch, one scan per class, one dense launch -------
+  const int n_add = b->n_add_frames, n_ord = nf - n_add;
+  const int64_t nw_ord = b->nwords - b->nw_add;
+  const spl::FrameProj *tab = as<spl::FrameProj>(b->ftab);
+  spl::launch_project_flags_multi(tab, nf, b->fblocks, s);
   ++launches;
-  for (int f = 0; f < nf; ++f) {
-    const spl_particles &p = b->sets[b->frames[f].set];
-    const spl::SoAIn soa = set_soa(p);
-    po.flags = as<uint32_t>(b->flags) + b->wbase[f];
-    po.word_off = as<uint32_t>(b->word_off) + b->wbase[f];
-    spl::launch_project_dense(set_aos(p), &soa, p.n, b->pc[f], po, s);
-    if (p.n > 0) ++launches;
+  uint32_t *flags = as<uint32_t>(b->flags), *woff = as<uint32_t>(b->word_off);
+  if (n_add > 0) {
+    spl::scan_popc(flags, b->nw_add, woff, status + 5, b->radix_scr.p, s, &launches);
+    spl::k_frame_bounds<<<1, 256, 0, s>>>(woff, as<uint32_t>(b->d_wbase), 0, n_add, b->nw_add,
+                                          status + 5, as<uint32_t>(b->actv_add));
+    ++launches;
   }
-  spl::k_batch_records<<<spl::grid_for(capA), 256, 0, s>>>(
-      as<uint32_t>(b->actv_start), nf, capA, as<uint32_t>(b->key_c), as<uint32_t>(b->count_c),
-      as<uint32_t>(b->frame_c), status);
+  if (n_ord > 0) {
+    spl::scan_popc(flags + b->nw_add, nw_ord, woff + b->nw_add, status + 6, b->radix_scr.p, s,
+                   &launches);
+    spl::k_frame_bounds<<<1, 256, 0, s>>>(woff + b->nw_add, as<uint32_t>(b->d_wbase), n_add,
+                                          n_ord, nw_ord, status + 6, as<uint32_t>(b->actv_ord));
+    ++launches;
+  }
+  spl::launch_project_dense_multi(tab, nf, b->dblocks, s);
   ++launches;
-  // ---- visiting order: stable by depth key, then stable by frame ---------------------
+  if (n_add > 0 && b->cap_add > 0) {
+    spl::k_batch_records<<<spl::grid_for(b->cap_add), 256, 0, s>>>(
+        as<uint32_t>(b->actv_add), n_add, as<uint32_t>(b->fmap_add), nf, (uint32_t)b->cap_add,
+        as<uint32_t>(b->key_c), as<uint32_t>(b->count_c), as<uint32_t>(b->frame_c), status);
+    ++launches;
+  }
+  const int64_t seg = b->cap_add;
+  if (n_ord > 0 && b->cap_ord > 0) {
+    spl::k_batch_records<<<spl::grid_for(b->cap_ord), 256, 0, s>>>(
+        as<uint32_t>(b->actv_ord), n_ord, as<uint32_t>(b->fmap_ord), nf, (uint32_t)b->cap_ord,
+        as<uint32_t>(b->key_c) + seg, as<uint32_t>(b->count_c) + seg,
+        as<uint32_t>(b->frame_c) + seg, status);
+    ++launches;
+  }
+  // ---- visiting order: additive records as they are; the ordered segment
+  //      stable by depth key, then stable by frame ------------------------------------
   const uint32_t *order = nullptr;
-  if (b->any_ordered) {
-    spl::radix_sort_pairs(as<uint32_t>(b->key_c), nullptr, as<uint32_t>(b->ktmp),
+  if (n_ord > 0 && b->cap_ord > 0) {
+    const int64_t O = b->cap_ord;
+    spl::radix_sort_pairs(as<uint32_t>(b->key_c) + seg, nullptr, as<uint32_t>(b->ktmp),
                           as<uint32_t>(b->vtmp), as<uint32_t>(b->kout), as<uint32_t>(b->perm1),
-                          capA, 0, 32, false, b->radix_scr.p, s, &launches, err, true);
-    spl::launch_gather_u32(as<uint32_t>(b->frame_c), as<uint32_t>(b->perm1), capA,
+                          O, 0, 32, false, b->radix_scr.p, s, &launches, err, true);
+    spl::launch_gather_u32(as<uint32_t>(b->frame_c) + seg, as<uint32_t>(b->perm1), O,
                            as<uint32_t>(b->fkey), s);
     ++launches;
     spl::radix_sort_pairs(as<uint32_t>(b->fkey), as<uint32_t>(b->perm1), as<uint32_t>(b->ktmp),
                           as<uint32_t>(b->vtmp), as<uint32_t>(b->kout), as<uint32_t>(b->perm),
-                          capA, 0, b->frame_bits, false, b->radix_scr.p, s, &launches, err, true);
-    order = as<uint32_t>(b->perm);
+                          O, 0, b->frame_bits, false, b->radix_scr.p, s, &launches, err, true);
+    spl::k_compose_order<<<spl::grid_for(capA), 256, 0, s>>>(
+        as<uint32_t>(b->perm), (uint32_t)seg, (uint32_t)O, as<uint32_t>(b->order));
+    ++launches;
+    order = as<uint32_t>(b->order);
   }
   // ---- binning over all frames ------------------------------------------------------
   const uint32_t *count_seq = as<uint32_t>(b->count_c);
@@ -647,11 +739,12 @@ int64_t with_margin(int64_t v, float margin) {
 }
 
 spl_status build(spl_batch *b, int T) {
-  int64_t acts, ents;
+  int64_t acts_add, acts_ord, ents;
   spl_status st;
-  if ((st = measure(b, T, acts, ents))) return st;
-  return plan(b, T, with_margin(acts, b->opt.capacity_margin),
-              with_margin(ents, b->opt.capacity_margin));
+  if ((st = measure(b, T, acts_add, acts_ord, ents))) return st;
+  const float m = b->opt.capacity_margin;
+  return plan(b, T, acts_add ? with_margin(acts_add, m) : 0,
+              acts_ord ? with_margin(acts_ord, m) : 0, with_margin(ents, m));
 }
 
 // Autotuner: for each tile size, the fastest splat configuration per class
@@ -836,7 +929,7 @@ spl_status spl_batch_render(spl_batch *b) {
     bool overflow = false;
     if ((st = check_status(b, overflow))) return st;
     b->info.render_ms = ms;
-    b->info.n_active = b->h_status[5];
+    b->info.n_active = (int64_t)b->h_status[5] + b->h_status[6];
     b->info.n_entries = (int64_t)*b->h_entries;
     b->info.kernel_launches = b->launches;
     if (!overflow) return SPL_OK;

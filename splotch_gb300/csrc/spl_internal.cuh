@@ -50,6 +50,66 @@ __device__ __forceinline__ float expm1_neg(float x) {
 }
 
 // ---------------------------------------------------------------------------
+// Packed float pairs: two FP32 values in one 64-bit register pair, operated on
+// by the .f32x2 forms of add/sub/mul/fma (sm_100 and later).  Each lane of a
+// pair is rounded exactly as the scalar instruction would round it, so a
+// packed computation gives the scalar computation's bits; it takes half the
+// issue slots.
+struct F2 {
+  unsigned long long v;
+};
+
+__device__ __forceinline__ F2 f2(float lo, float hi) {
+  F2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ F2 f2(float x) { return f2(x, x); }
+__device__ __forceinline__ float f2lo(F2 a) {
+  float lo;
+  asm("{\n .reg .f32 t;\n mov.b64 {%0, t}, %1;\n}" : "=f"(lo) : "l"(a.v));
+  return lo;
+}
+__device__ __forceinline__ float f2hi(F2 a) {
+  float hi;
+  asm("{\n .reg .f32 t;\n mov.b64 {t, %0}, %1;\n}" : "=f"(hi) : "l"(a.v));
+  return hi;
+}
+__device__ __forceinline__ F2 add2(F2 a, F2 b) {
+  F2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 sub2(F2 a, F2 b) {
+  F2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 mul2(F2 a, F2 b) {
+  F2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+  F2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return r;
+}
+
+// expm1(-u) for u >= 0 on a pair, lane for lane the value of expm1_neg(-u):
+// the same Taylor polynomial (its coefficients negated with u) below 0.05 and
+// ex2(-u*log2e)-1 above.
+__device__ __forceinline__ F2 expm1_neg2(F2 u) {
+  F2 p = fma2(u, f2(1.f / 24.f), f2(-1.f / 6.f));
+  p = fma2(p, u, f2(0.5f));
+  p = fma2(p, u, f2(-1.f));
+  p = mul2(p, u);
+  const F2 a = mul2(u, f2(-kLog2e));
+  const F2 t = add2(f2(ex2(f2lo(a)), ex2(f2hi(a))), f2(-1.f));
+  return f2(f2lo(u) < 0.05f ? f2lo(p) : f2lo(t), f2hi(u) < 0.05f ? f2hi(p) : f2hi(t));
+}
+
+// ---------------------------------------------------------------------------
 // Float-float ("double-float") arithmetic for reproducing double results.
 // GB300's FP64 rate is a small fraction of its FP32 rate, so the reference's
 // double-precision steps (transform, screen shift, palette interpolation) are
@@ -217,6 +277,24 @@ void launch_project_flags(const void *aos, const SoAIn *soa, int64_t n, const Pr
 void launch_project_dense(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
                           const ProjectOut &o, cudaStream_t s);
 
+// Both passes for many frames in one launch each: a device table of frames
+// (ascending fblock0 / dblock0), each with its constants, inputs and outputs
+// (flags / word_off at the frame's words; pos_c etc. at its record segment,
+// cap_c that segment's capacity).  A flags block covers kFlagWordsPerBlock
+// activity words, a dense block kDenseWordsPerBlock.
+constexpr int kFlagWordsPerBlock = 8;
+constexpr int kDenseWordsPerBlock = 64;
+struct FrameProj {
+  ProjConst c;
+  const void *aos;  // particle_sim records, or null: soa
+  SoAIn soa;
+  int64_t n;
+  ProjectOut o;
+  uint32_t fblock0, dblock0;
+};
+void launch_project_flags_multi(const FrameProj *tab, int nf, uint32_t nblocks, cudaStream_t s);
+void launch_project_dense_multi(const FrameProj *tab, int nf, uint32_t nblocks, cudaStream_t s);
+
 // Exclusive scan of popcount(words[i]) into out (nwords entries); the total
 // goes to *total.
 void scan_popc(const uint32_t *words, int64_t nwords, uint32_t *out, uint32_t *total,
@@ -257,6 +335,31 @@ void launch_colorbar(float *pic, int xres, int yres, const float *colours, const
                      int nbars, cudaStream_t s);
 void launch_encode(const float *pic, int xres, int yres, bool bgr, uint8_t *out,
                    cudaStream_t s);
+
+// particle_normalize (spl_normalize.cu).  Particles as particle_sim records
+// (aos) or SoA arrays, in place.  stats: SPL_MAXT x 6 ints (per type: size,
+// intensity, colour min/max as order-preserving ints), set by norm_stats_init
+// before launch_norm_collect; norm_stat_value turns one back into a float.
+struct NormConst {
+  int ptypes;
+  int intensity_log[SPL_MAXT], color_log[SPL_MAXT], color_asinh[SPL_MAXT];
+  int color_is_vector[SPL_MAXT];
+};
+struct NormRanges {
+  float imin[SPL_MAXT], imax[SPL_MAXT], cmin[SPL_MAXT], cmax[SPL_MAXT];
+};
+struct NormView {
+  void *aos;
+  float *I, *cr, *cg, *cb;
+  const float *r;
+  const uint16_t *type;
+};
+void norm_stats_init(int *h_stats);
+float norm_stat_value(int i);
+void launch_norm_collect(const NormView &v, int64_t n, const NormConst &c, int *stats,
+                         uint32_t *err, cudaStream_t s);
+void launch_norm_clamp(const NormView &v, int64_t n, const NormConst &c, const NormRanges &r,
+                       cudaStream_t s);
 
 // Exclusive scan of count[order[s]] (order may be null) into off (n+1 slots;
 // off[n] = total).

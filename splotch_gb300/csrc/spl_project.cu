@@ -329,6 +329,23 @@ __global__ void __launch_bounds__(256) k_project_full(L load, int64_t n, ProjCon
 //   k_project_dense  : each block expands its words into a dense list of
 //                      active particles, projects and colourises them with
 //                      all lanes busy, and writes the compact records
+// One warp: the activity bits of word w (particles 32w .. 32w+31).
+template <class L>
+__device__ __forceinline__ void flags_word(const L &load, int64_t n, const ProjConst &c,
+                                           uint32_t *__restrict__ flags, uint32_t *err,
+                                           int64_t w, int lane) {
+  const int64_t i = w * 32 + lane;
+  bool active = false;
+  if (i < n) {
+    const PIn in = load(i);
+    float x, y, z, r, I;
+    bool fb = false;
+    active = project_geom(c, in, x, y, z, r, I, fb, err);
+  }
+  const uint32_t bits = __ballot_sync(0xffffffffu, active);
+  if (lane == 0) flags[w] = bits;
+}
+
 template <class L>
 __global__ void __launch_bounds__(256) k_project_flags(L load, int64_t n, ProjConst c,
                                                        uint32_t *__restrict__ flags,
@@ -336,21 +353,18 @@ __global__ void __launch_bounds__(256) k_project_flags(L load, int64_t n, ProjCo
   const int lane = threadIdx.x & 31;
   const int64_t nwords = (n + 31) / 32;
   for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nwords;
-       w += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const int64_t i = w * 32 + lane;
-    bool active = false;
-    if (i < n) {
-      const PIn in = load(i);
-      float x, y, z, r, I;
-      bool fb = false;
-      active = project_geom(c, in, x, y, z, r, I, fb, err);
-    }
-    const uint32_t bits = __ballot_sync(0xffffffffu, active);
-    if (lane == 0) flags[w] = bits;
-  }
+       w += ((int64_t)gridDim.x * blockDim.x) >> 5)
+    flags_word(load, n, c, flags, err, w, lane);
 }
 
-constexpr int DW = 64;  // flag words per dense block (2048 particles)
+constexpr int DW = kDenseWordsPerBlock;  // flag words per dense block (2048 particles)
+
+template <class L>
+__device__ __forceinline__ void dense_block(const L &load, int64_t n, const ProjConst &c,
+                                            const uint32_t *__restrict__ flags,
+                                            const uint32_t *__restrict__ word_off,
+                                            const ProjectOut &o, int64_t w0,
+                                            uint32_t *s_list, uint32_t *s_cnt);
 
 template <class L>
 __global__ void __launch_bounds__(256) k_project_dense(L load, int64_t n, ProjConst c,
@@ -359,8 +373,18 @@ __global__ void __launch_bounds__(256) k_project_dense(L load, int64_t n, ProjCo
                                                        ProjectOut o) {
   __shared__ uint32_t s_list[DW * 32];
   __shared__ uint32_t s_cnt[DW];
+  dense_block(load, n, c, flags, word_off, o, (int64_t)blockIdx.x * DW, s_list, s_cnt);
+}
+
+// One block: the active particles of words [w0, w0 + DW), expanded into a
+// dense list in shared memory, projected and colourised with all lanes busy.
+template <class L>
+__device__ __forceinline__ void dense_block(const L &load, int64_t n, const ProjConst &c,
+                                            const uint32_t *__restrict__ flags,
+                                            const uint32_t *__restrict__ word_off,
+                                            const ProjectOut &o, int64_t w0,
+                                            uint32_t *s_list, uint32_t *s_cnt) {
   const int64_t nwords = (n + 31) / 32;
-  const int64_t w0 = (int64_t)blockIdx.x * DW;
   const int nw = (int)min((int64_t)DW, nwords - w0);
   uint32_t f = 0;
   if ((int)threadIdx.x < nw) f = __ldg(flags + w0 + threadIdx.x);
@@ -393,6 +417,49 @@ __global__ void __launch_bounds__(256) k_project_dense(L load, int64_t n, ProjCo
     o.count_c[dst] = p.count;
     if (o.key_c) o.key_c[dst] = p.key;
   }
+}
+
+// ---- many frames in one launch (batched rendering) ---------------------------
+// Each block belongs to one frame of the table: the frame whose first block
+// (fblock0 / dblock0, ascending in table order) is the last one <= blockIdx.x.
+__device__ __forceinline__ int table_row(const FrameProj *tab, int nf, uint32_t b, bool dense) {
+  int lo = 0, hi = nf;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if ((dense ? tab[mid].dblock0 : tab[mid].fblock0) <= b) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) k_project_flags_multi(const FrameProj *__restrict__ tab,
+                                                             int nf) {
+  const FrameProj &fp = tab[table_row(tab, nf, blockIdx.x, false)];
+  const int64_t nwords = (fp.n + 31) / 32;
+  const int64_t w = (int64_t)(blockIdx.x - fp.fblock0) * kFlagWordsPerBlock + (threadIdx.x >> 5);
+  if (w >= nwords) return;  // whole warps
+  const int lane = threadIdx.x & 31;
+  if (fp.aos)
+    flags_word(LoadAoS{static_cast<const uint8_t *>(fp.aos)}, fp.n, fp.c, fp.o.flags, fp.o.err,
+               w, lane);
+  else
+    flags_word(LoadSoA{fp.soa.x, fp.soa.y, fp.soa.z, fp.soa.r, fp.soa.I, fp.soa.cr, fp.soa.cg,
+                       fp.soa.cb, fp.soa.type},
+               fp.n, fp.c, fp.o.flags, fp.o.err, w, lane);
+}
+
+__global__ void __launch_bounds__(256) k_project_dense_multi(const FrameProj *__restrict__ tab,
+                                                             int nf) {
+  __shared__ uint32_t s_list[DW * 32];
+  __shared__ uint32_t s_cnt[DW];
+  const FrameProj &fp = tab[table_row(tab, nf, blockIdx.x, true)];
+  const int64_t w0 = (int64_t)(blockIdx.x - fp.dblock0) * DW;
+  if (fp.aos)
+    dense_block(LoadAoS{static_cast<const uint8_t *>(fp.aos)}, fp.n, fp.c, fp.o.flags,
+                fp.o.word_off, fp.o, w0, s_list, s_cnt);
+  else
+    dense_block(LoadSoA{fp.soa.x, fp.soa.y, fp.soa.z, fp.soa.r, fp.soa.I, fp.soa.cr, fp.soa.cg,
+                        fp.soa.cb, fp.soa.type},
+                fp.n, fp.c, fp.o.flags, fp.o.word_off, fp.o, w0, s_list, s_cnt);
 }
 
 // particle_sim writeback: e, x, y, z, r, I, type, active (36 bytes).
@@ -487,6 +554,16 @@ void launch_project_dense(const void *aos, const SoAIn *soa, int64_t n, const Pr
     k_project_dense<<<db, 256, 0, s>>>(
         LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},
         n, c, o.flags, o.word_off, o);
+}
+
+void launch_project_flags_multi(const FrameProj *tab, int nf, uint32_t nblocks,
+                                cudaStream_t s) {
+  if (nf > 0 && nblocks > 0) k_project_flags_multi<<<nblocks, 256, 0, s>>>(tab, nf);
+}
+
+void launch_project_dense_multi(const FrameProj *tab, int nf, uint32_t nblocks,
+                                cudaStream_t s) {
+  if (nf > 0 && nblocks > 0) k_project_dense_multi<<<nblocks, 256, 0, s>>>(tab, nf);
 }
 
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,

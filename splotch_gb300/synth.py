@@ -140,6 +140,39 @@ def differentiable(n: int = 4_000_000, mode: str = "additive", seed: int = 3, xr
                     notes={"target": t})
 
 
+def large(n: int = 400_000_000, seed: int = 4, xres: int = 4096, tile: int = 16,
+          order: str = "ftb", chunk: int = 25_000_000) -> Workload:
+    """Large render, forward+backward: halo mixture in [0,1000]^3, ordered
+    absorption, per-particle RGB U[0,1]^3 (colour vector), I ~ lognormal(0,1),
+    hsml ~ Pareto(alpha=1.5, x_min=0.1) clipped so that no particle's pixel
+    radius exceeds a quarter of the image width at its depth.  Camera
+    (500,500,2500) -> (500,500,500), fov 30, xres x xres: ~3.8 pixels per unit
+    at the box centre, so about 0.1% of the particles (hsml > ~10) cover more
+    than 10^4 pixels.  Generated in chunks to bound host memory."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    p = np.zeros(n, dtype=PARTICLE_DTYPE)
+    res2 = 0.5 * xres
+    fovfct = np.tan(np.radians(30.0) / 2)
+    for lo in range(0, n, chunk):
+        m = min(chunk, n - lo)
+        pos = halo_positions(rng, m, 1000.0)
+        s = p[lo:lo + m]
+        s["x"], s["y"], s["z"] = pos[:, 0], pos[:, 1], pos[:, 2]
+        h = 0.1 * (1.0 - rng.uniform(0.0, 1.0, m)) ** (-1.0 / 1.5)  # Pareto(1.5, 0.1)
+        depth = np.maximum(2500.0 - pos[:, 2].astype(np.float64), 1.0)
+        hmax = (xres / 4) * fovfct * depth / (2.0 * res2)  # R = 2 h res2/(fovfct depth)
+        s["r"] = np.minimum(h, hmax).astype(np.float32)
+        s["I"] = rng.lognormal(0.0, 1.0, m).astype(np.float32)
+        rgb = rng.uniform(0.0, 1.0, (m, 3)).astype(np.float32)
+        s["er"], s["eg"], s["eb"] = rgb[:, 0], rgb[:, 1], rgb[:, 2]
+    params = ParamFile({"xres": xres, "yres": xres, "fov": 30.0, "a_eq_e": False,
+                        "sort_type": 1, "gray_absorption": 0.2, "ptypes": 1,
+                        "color_is_vector0": True, "brightness0": 1.0, "tile_size_cpu": tile,
+                        "gpu_order": order})
+    return Workload("large", p, params, _rc((500, 500, 2500), (500, 500, 500), [None]),
+                    notes={"hsml": "Pareto(1.5, 0.1), pixel radius <= xres/4"})
+
+
 BATCH_RESOLUTIONS = ((512, 512), (1024, 1024), (1920, 1080), (2048, 2048))
 
 

@@ -80,7 +80,45 @@ def main() -> int:
         print(f"{name}: {len(w.particles)} particles, {int(proj['active'].sum())} active, "
               f"{frags} fragments")
     post_cases(refs["simd"])
+    norm_cases(refs["simd"])
     return 0
+
+
+NORM_VARIANTS = {
+    "plain": {},
+    "logs": {"intensity_log0": "T", "intensity_log1": "T", "color_log0": "T"},
+    "asinh_overrides": {"color_asinh0": "T", "color_asinh1": "T", "intensity_min0": "-1.5",
+                        "color_max1": "0.8"},
+    "vector_log": {"color_log1": "T", "color_min0": "0.25", "intensity_max1": "2.0"},
+}
+
+
+def norm_inputs():
+    """A two-type set with zero / negative values where the logs must skip them."""
+    w = synth.plain_absorption(n_gas=6000, n_star=2000, xres=96, yres=54, tile=16, seed=5)
+    p = w.particles.copy()
+    p["I"][::97] = 0.0
+    p["er"][::89] = -0.5
+    p["eg"][-50:] = 0.0
+    return dict(w.params.params), p
+
+
+def norm_cases(ref) -> None:
+    """sceneMaker::particle_normalize (scenemaker.cc:40-296) from the reference's
+    own code: normalised particles and the range/clamp keys it sets."""
+    base, p = norm_inputs()
+    out = {"particles_in": p.view(np.uint8).copy()}
+    for var, extra in NORM_VARIANTS.items():
+        prm = dict(base)
+        prm.update(extra)
+        q = p.copy()
+        res = ref.particle_normalize(prm, q)
+        out[f"particles_{var}"] = q.view(np.uint8).copy()
+        out[f"ranges_{var}"] = np.array([res[k] for k in ("range_min", "range_max",
+                                                          "clamp_min", "clamp_max")])
+        out[f"params_{var}"] = np.frombuffer(json.dumps(prm).encode(), dtype=np.uint8)
+    np.savez_compressed(OUT / "norm_absorption.npz", **out)
+    print("norm_absorption:", len(p), "particles")
 
 
 POST_VARIANTS = {

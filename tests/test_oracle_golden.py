@@ -15,7 +15,8 @@ from oracle.oracle import PARTICLE_DTYPE, rel_linf
 from splotch_gb300 import Palette, RenderContext
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-CASES = sorted(p.stem for p in GOLDEN.glob("*.npz") if not p.stem.startswith("post_"))
+CASES = sorted(p.stem for p in GOLDEN.glob("*.npz")
+               if not p.stem.startswith(("post_", "norm_")))
 X86 = platform.machine() in ("x86_64", "AMD64")
 
 
