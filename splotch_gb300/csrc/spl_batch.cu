@@ -2,14 +2,21 @@
 // additive or ordered modes, particle sets of uneven size) in one launch of a
 // captured CUDA graph.
 //
-// Per render, with no host round trip between stages:
-//   per frame   : activity flags of the frame's particle set (projection test)
-//   all frames  : one popcount scan -> every frame's active particles get
-//                 consecutive global record numbers, frame after frame
-//   per frame   : dense projection + colourisation into the shared records
-//   all frames  : stable depth sort by key, then stable sort by frame id
-//                 (visiting order: frame-major, each frame in its own order);
-//                 tile counts in that order, one scan, one emission of
+// Per render, with no host round trip between stages (frames are kept
+// additive first, then ordered):
+//   all frames  : one activity-flag launch over every frame's particle set
+//                 (projection test; a per-frame table of projection constants
+//                 and inputs)
+//   per class   : one popcount scan over the class's flag words -> the class's
+//                 active particles get consecutive record numbers, frame after
+//                 frame, in the class's own segment (additive [0, cap_add),
+//                 ordered [cap_add, cap_add + cap_ord)); record starts per frame
+//   all frames  : one dense projection + colourisation launch into the records
+//   ordered     : stable depth sort of the ordered segment by key, then stable
+//                 sort by frame id (each frame in its own order, frame-major);
+//                 additive records keep their record order, as a per-frame
+//                 additive render does
+//   all frames  : tile counts in visiting order, one scan, one emission of
 //                 (global tile id, record) pairs, one stable sort by tile id;
 //                 tile ranges; work queue = every (frame, tile) item, additive
 //                 frames first, each class longest list first

@@ -15,6 +15,11 @@
 // bounding box and walks only the hits, in list order (or reverse list order
 // front-to-back).
 //
+// A lane's pixels are processed in pairs (items 2p and 2p+1, side by side) with
+// packed .f32x2 arithmetic: the pair's three channels take three packed
+// operations per step where two pixels took six.  A pixel of the pair that the
+// particle does not cover gets weight 0, which leaves its state unchanged.
+//
 // Coverage is decided exactly as the reference decides it (tile-local
 // coordinates, truncating int conversion, the column run
 // y in [int(py-dy+1), int(py+dy+1)) with dy = sqrt(r^2 - dx^2)), in
@@ -36,17 +41,27 @@ namespace {
 
 constexpr int IW = 8, IH = 4;  // item: 8 columns x 4 rows, one pixel per lane
 
+// Staged particles, one entry per list slot.  Each value a pixel pair shares
+// is held twice, so one 128-bit load gives packed (F2) operands.
 template <int B>
 struct Smem {
-  float4 p0[B];  // posx, posy, stp*log2e, bbox bits
-  float4 e[B];   // e.r, e.g, e.b, q.r
-  float2 q[B];   // q.g, q.b
-  // followed by uint16_t run[B*T]: column runs lo | hi<<8
+  float4 pxy[B];   // posx, posx, posy, posy (tile-local)
+  float4 es[B];    // e0, e0, stp*log2e, stp*log2e (e negated when additive)
+  float4 e12[B];   // e1, e1, e2, e2                (negated when additive)
+  float4 q01[B];   // q0, q0, q1, q1 (q = e/(e+grayabsorb), negated front-to-back)
+  float2 q2[B];    // q2, q2
+  uint32_t bb[B];  // clipped bounding box minx | maxx<<8 | miny<<16 | maxy<<24
+  // followed by uint16_t run[B][run_stride(T)]: per column the covered rows
+  // lo | (hi-lo)<<8, zero outside the bounding box
 };
+
+// Run-table row length: T rounded up to whole 8-pixel items, so that every
+// column an item can address lies in the row and rows stay 16-byte aligned.
+__host__ __device__ constexpr int run_stride(int T) { return (T + 7) & ~7; }
 
 template <int B>
 size_t smem_bytes(int T) {
-  return sizeof(Smem<B>) + (size_t)B * T * 2;
+  return sizeof(Smem<B>) + (size_t)B * run_stride(T) * 2;
 }
 
 // One tile of one frame, by the whole CTA (shared by the per-frame launch and
@@ -57,11 +72,14 @@ template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false>
 __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
                                            uint8_t *smem_raw) {
   constexpr int K = WX * WY;
+  constexpr int NP = (K + 1) / 2;  // pixel pairs per lane: items (2p, 2p+1)
   static_assert(!(AUX && ADD), "optical depth is kept for ordered frames only");
+  static_assert(K == 1 || WX % 2 == 0, "the items of a pair share one row");
   Smem<B> &S = *reinterpret_cast<Smem<B> *>(smem_raw);
   uint16_t *srun = reinterpret_cast<uint16_t *>(smem_raw + sizeof(Smem<B>));
 
   const int T = a.T;
+  const int RS = run_stride(T);
   const int ix = tile % a.ncx, iy = tile / a.ncx;
   const int x0s = ix * T, y0s = iy * T;
   const int tw = min(x0s + T, a.xres) - x0s;
@@ -76,26 +94,32 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
   const int wbx0 = wx * WX * IW, wby0 = wy * WY * IH;  // warp box, tile-local
   const int wbx1 = min(wbx0 + WX * IW, tw), wby1 = min(wby0 + WY * IH, th);
 
-  float pxf[K], pyf[K];
-  int pxi[K], pyi[K];
-  bool valid[K];
-  float acc[K][3], tr[K][3];
-  float od[AUX ? K : 1][3];  // optical depth (AUX)
-  uint32_t stop = 0;         // list position below which this warp composited nothing
+  // Pixel (k) of this lane: run-table column and row; a pixel outside the
+  // tile reads column 0 with row 255, which no run contains.
+  int col[K], row[K];
+  F2 px2[NP], py2[NP];                   // pixel coordinates of each pair
+  F2 acc[NP][3], tr[NP][3];              // per channel: (pixel 2p, pixel 2p+1)
+  F2 od[AUX ? NP : 1][3];                // optical depth (AUX)
+  uint32_t stop = 0;  // list position below which this warp composited nothing
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int x = wbx0 + (k % WX) * IW + (lane & 7);
     const int y = wby0 + (k / WX) * IH + (lane >> 3);
-    valid[k] = warp_has_pixels && x < tw && y < th;
-    pxi[k] = x;
-    pyi[k] = y;
-    pxf[k] = (float)x;
-    pyf[k] = (float)y;
+    const bool valid = warp_has_pixels && x < tw && y < th;
+    col[k] = valid ? x : 0;
+    row[k] = valid ? y : 255;
+  }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int x = wbx0 + ((2 * p) % WX) * IW + (lane & 7);
+    const int y = wby0 + ((2 * p) / WX) * IH + (lane >> 3);
+    px2[p] = f2((float)x, (float)(x + IW));
+    py2[p] = f2((float)y);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      if (AUX) od[AUX ? k : 0][c] = 0.f;
-      acc[k][c] = 0.f;
-      tr[k][c] = 1.f;
+      if (AUX) od[AUX ? p : 0][c] = f2(0.f);
+      acc[p][c] = f2(0.f);
+      tr[p][c] = f2(1.f);
     }
   }
 
@@ -110,7 +134,6 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
     for (int slot = threadIdx.x; slot < B; slot += NT) {
       const uint32_t jj = start + (uint32_t)bi * B + slot;
       uint32_t bb = 0;
-      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f);
       if (jj < end) {
         const uint32_t idx = __ldg(a.entries + jj);
         const float4 p = __ldg(a.pos + idx);
@@ -127,28 +150,36 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
         if (minx < maxx && miny < maxy) {
           bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((uint32_t)miny << 16) |
                ((uint32_t)maxy << 24);
-          uint16_t *run = srun + slot * T;
+          uint16_t *run = srun + slot * RS;
+          uint4 *row16 = reinterpret_cast<uint4 *>(run);
+          for (int i = 0; i < RS / 8; ++i) row16[i] = make_uint4(0u, 0u, 0u, 0u);
           for (int x = minx; x < maxx; ++x) {  // splotch_host.cc:603-606
             const float dx = fsub((float)x, posx);
             const float dxsq = fmul(dx, dx);
             const float dy = fsqrt(fsub(radsq, dxsq));
             const int lo = max(miny, f2i(fadd(fsub(posy, dy), 1.f)));
-            int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
-            if (hi < lo) hi = lo;
-            run[x] = (uint16_t)(lo | (hi << 8));
+            const int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
+            run[x] = (uint16_t)(lo | (max(hi - lo, 0) << 8));
           }
         }
-        p0 = make_float4(posx, posy, stp * kLog2e, 0.f);
+        const float s2 = stp * kLog2e;
+        S.pxy[slot] = make_float4(posx, posx, posy, posy);
         if (ADD) {
-          S.e[slot] = make_float4(c.x, c.y, c.z, 0.f);
+          S.es[slot] = make_float4(-c.x, -c.x, s2, s2);
+          S.e12[slot] = make_float4(-c.y, -c.y, -c.z, -c.z);
         } else {
           // q = e/(e+grayabsorb), splotch_host.cc:626-628
-          S.e[slot] = make_float4(c.x, c.y, c.z, fdiv(c.x, fadd(c.x, a.gray)));
-          S.q[slot] = make_float2(fdiv(c.y, fadd(c.y, a.gray)), fdiv(c.z, fadd(c.z, a.gray)));
+          const float sq = FTB ? -1.f : 1.f;
+          const float q0 = sq * fdiv(c.x, fadd(c.x, a.gray));
+          const float q1 = sq * fdiv(c.y, fadd(c.y, a.gray));
+          const float q2 = sq * fdiv(c.z, fadd(c.z, a.gray));
+          S.es[slot] = make_float4(c.x, c.x, s2, s2);
+          S.e12[slot] = make_float4(c.y, c.y, c.z, c.z);
+          S.q01[slot] = make_float4(q0, q0, q1, q1);
+          S.q2[slot] = make_float2(q2, q2);
         }
       }
-      p0.w = __uint_as_float(bb);
-      S.p0[slot] = p0;
+      S.bb[slot] = bb;
     }
     __syncthreads();
     // ---- accumulate ---------------------------------------------------------
@@ -156,7 +187,7 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
 #pragma unroll 1
       for (int cc = 0; cc < B / 32; ++cc) {
         const int ch = FTB ? B / 32 - 1 - cc : cc;
-        const uint32_t bbl = __float_as_uint(S.p0[ch * 32 + lane].w);
+        const uint32_t bbl = S.bb[ch * 32 + lane];
         const int mnx = bbl & 255, mxx = (bbl >> 8) & 255;
         const int mny = (bbl >> 16) & 255, mxy = bbl >> 24;
         const bool hit = (mnx < mxx) && (mnx < wbx1) && (mxx > wbx0) && (mny < wby1) &&
@@ -166,60 +197,60 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
           const int bit = FTB ? 31 - __clz(mask) : __ffs(mask) - 1;
           mask &= ~(1u << bit);
           const int j = ch * 32 + bit;
-          const float4 p0 = S.p0[j];
-          const uint32_t bbj = __float_as_uint(p0.w);
-          const int jmnx = bbj & 255, jmxx = (bbj >> 8) & 255;
-          const int jmny = (bbj >> 16) & 255, jmxy = bbj >> 24;
-          const float4 e = S.e[j];
+          const float4 pxy = S.pxy[j];
+          const float4 es = S.es[j];
+          const float4 e12 = S.e12[j];
+          float4 q01 = make_float4(0.f, 0.f, 0.f, 0.f);
           float2 q2 = make_float2(0.f, 0.f);
-          if (!ADD) q2 = S.q[j];
-          const uint16_t *run = srun + j * T;
+          if (!ADD) {
+            q01 = S.q01[j];
+            q2 = S.q2[j];
+          }
+          uint32_t bbj = 0;
+          if (NP > 1) bbj = S.bb[j];
+          const uint16_t *run = srun + j * RS;
 #pragma unroll
-          for (int k = 0; k < K; ++k) {
-            const int ix0 = wbx0 + (k % WX) * IW, iy0 = wby0 + (k / WX) * IH;
-            if (jmnx < ix0 + IW && jmxx > ix0 && jmny < iy0 + IH && jmxy > iy0) {  // uniform
-              bool in = valid[k] && pxi[k] >= jmnx && pxi[k] < jmxx;
-              if (in) {
-                const uint32_t rr = run[pxi[k]];
-                in = pyi[k] >= (int)(rr & 255) && pyi[k] < (int)(rr >> 8);
-              }
-              if (in) {
-                const float dx = pxf[k] - p0.x, dy = pyf[k] - p0.y;
-                const float att = ex2(p0.z * fmaf(dy, dy, dx * dx));
+          for (int p = 0; p < NP; ++p) {
+            if (NP > 1) {  // does the particle's box reach this pair's 16x4 pixels (uniform)?
+              const int ix0 = wbx0 + ((2 * p) % WX) * IW, iy0 = wby0 + ((2 * p) / WX) * IH;
+              const int jmnx = bbj & 255, jmxx = (bbj >> 8) & 255;
+              const int jmny = (bbj >> 16) & 255, jmxy = bbj >> 24;
+              if (!(jmnx < ix0 + 2 * IW && jmxx > ix0 && jmny < iy0 + IH && jmxy > iy0))
+                continue;
+            }
+            // exact coverage: the pixel's row inside its column's run
+            const uint32_t r0 = run[col[2 * p]];
+            const bool in0 = (uint32_t)(row[2 * p] - (int)(r0 & 255)) < (r0 >> 8);
+            bool in1 = false;
+            if (2 * p + 1 < K) {
+              const uint32_t r1 = run[col[2 * p + 1]];
+              in1 = (uint32_t)(row[2 * p + 1] - (int)(r1 & 255)) < (r1 >> 8);
+            }
+            if (in0 || in1) {
+              // a pixel the particle does not cover gets att = 0: its update is
+              // the identity in every mode
+              const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
+              const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
+              const F2 arg = mul2(f2(es.z, es.w), fma2(dy, dy, mul2(dx, dx)));
+              const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
+              const F2 e[3] = {f2(es.x, es.y), f2(e12.x, e12.y), f2(e12.z, e12.w)};
+              const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
                 if (ADD) {
-                  acc[k][0] = fmaf(-e.x, att, acc[k][0]);
-                  acc[k][1] = fmaf(-e.y, att, acc[k][1]);
-                  acc[k][2] = fmaf(-e.z, att, acc[k][2]);
-                } else if (!FTB) {
-                  const float u0 = e.x * att, u1 = e.y * att, u2 = e.z * att;
-                  if (AUX) {
-                    od[AUX ? k : 0][0] += u0;
-                    od[AUX ? k : 0][1] += u1;
-                    od[AUX ? k : 0][2] += u2;
-                  }
-                  const float m0 = expm1_neg(-u0);
-                  const float m1 = expm1_neg(-u1);
-                  const float m2 = expm1_neg(-u2);
-                  acc[k][0] = fmaf(m0, acc[k][0] - e.w, acc[k][0]);
-                  acc[k][1] = fmaf(m1, acc[k][1] - q2.x, acc[k][1]);
-                  acc[k][2] = fmaf(m2, acc[k][2] - q2.y, acc[k][2]);
+                  acc[p][c] = fma2(e[c], att, acc[p][c]);  // e negated
                 } else {
-                  // w = Tr*(1-T) = -Tr*expm1(-e*att); C += w*q; Tr -= w
-                  const float u0 = e.x * att, u1 = e.y * att, u2 = e.z * att;
-                  if (AUX) {
-                    od[AUX ? k : 0][0] += u0;
-                    od[AUX ? k : 0][1] += u1;
-                    od[AUX ? k : 0][2] += u2;
+                  const F2 u = mul2(e[c], att);
+                  if (AUX) od[AUX ? p : 0][c] = add2(od[AUX ? p : 0][c], u);
+                  const F2 m = expm1_neg2(u);
+                  if (!FTB) {
+                    acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
+                  } else {
+                    // -w = Tr*expm1(-e*att); C += w*q (q negated); Tr -= w
+                    const F2 nw = mul2(tr[p][c], m);
+                    acc[p][c] = fma2(nw, q[c], acc[p][c]);
+                    tr[p][c] = add2(tr[p][c], nw);
                   }
-                  const float w0 = -tr[k][0] * expm1_neg(-u0);
-                  const float w1 = -tr[k][1] * expm1_neg(-u1);
-                  const float w2 = -tr[k][2] * expm1_neg(-u2);
-                  acc[k][0] = fmaf(w0, e.w, acc[k][0]);
-                  acc[k][1] = fmaf(w1, q2.x, acc[k][1]);
-                  acc[k][2] = fmaf(w2, q2.y, acc[k][2]);
-                  tr[k][0] -= w0;
-                  tr[k][1] -= w1;
-                  tr[k][2] -= w2;
                 }
               }
             }
@@ -229,10 +260,15 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
       if (FTB) {
         bool mine_done = true;
 #pragma unroll
-        for (int k = 0; k < K; ++k)
-          if (valid[k])
-            mine_done = mine_done && tr[k][0] < a.ftb_eps && tr[k][1] < a.ftb_eps &&
-                        tr[k][2] < a.ftb_eps;
+        for (int k = 0; k < K; ++k) {
+          if (row[k] != 255) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float t = (k & 1) ? f2hi(tr[k / 2][c]) : f2lo(tr[k / 2][c]);
+              mine_done = mine_done && t < a.ftb_eps;
+            }
+          }
+        }
         warp_done = __all_sync(0xffffffffu, mine_done);
         if (AUX && warp_done) stop = (uint32_t)bi * B;
       }
@@ -247,15 +283,19 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
   // ---- write the tile (pic is x-major: pixel (x,y) at (x*yres + y)*3) ----
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    if (valid[k]) {
-      float *o = a.pic + ((size_t)(x0s + pxi[k]) * a.yres + (y0s + pyi[k])) * 3;
-      o[0] = acc[k][0];
-      o[1] = acc[k][1];
-      o[2] = acc[k][2];
-      if (AUX)
-        a.aux[(size_t)(x0s + pxi[k]) * a.yres + (y0s + pyi[k])] =
-            make_float4(od[AUX ? k : 0][0], od[AUX ? k : 0][1], od[AUX ? k : 0][2],
-                        __uint_as_float(stop));
+    if (row[k] != 255) {
+      const size_t pix = (size_t)(x0s + col[k]) * a.yres + (y0s + row[k]);
+      float v[3], d[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[c] = (k & 1) ? f2hi(acc[k / 2][c]) : f2lo(acc[k / 2][c]);
+        if (AUX) d[c] = (k & 1) ? f2hi(od[AUX ? k / 2 : 0][c]) : f2lo(od[AUX ? k / 2 : 0][c]);
+      }
+      float *o = a.pic + pix * 3;
+      o[0] = v[0];
+      o[1] = v[1];
+      o[2] = v[2];
+      if (AUX) a.aux[pix] = make_float4(d[0], d[1], d[2], __uint_as_float(stop));
     }
   }
 }
