@@ -30,7 +30,8 @@ struct spl_context {
   Buf aos_in, soa_in[9], pos, col, active, count, key, perm, ktmp, vtmp, off, scratch, tkey,
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
-      poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes;
+      poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes,
+      seg_cnt, seg_off;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
   // state of the last frame (for the debug getters)
@@ -647,7 +648,9 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
     }
   }
   if ((st = ensure(c->gpos_c, na * 16)) || (st = ensure(c->gcol_c, na * 16)) ||
-      (st = ensure(c->camsum, 5 * 8)))
+      (st = ensure(c->camsum, 5 * 8)) || (st = ensure(c->seg_cnt, c->ntiles * 4 + 4)) ||
+      (st = ensure(c->seg_off, (c->ntiles + 1) * 8)) ||
+      (st = ensure(c->scratch, spl::scan_scratch_bytes(c->ntiles + 1))))
     return st;
   const float *gpic_d = gp->pic;
   cudaEventRecord(c->ev[0], s);
@@ -668,6 +671,10 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
     aa.gpic = gpic_d;
     aa.gpos = as<float4>(c->gpos_c);
     aa.gcol = as<float4>(c->gcol_c);
+    aa.n_entries = c->ne;
+    aa.seg_cnt = as<uint32_t>(c->seg_cnt);
+    aa.seg_off = as<uint64_t>(c->seg_off);
+    aa.scan_scratch = c->scratch.p;
     spl::launch_splat_adjoint(aa, s);
   }
   cudaEventRecord(c->ev[2], s);

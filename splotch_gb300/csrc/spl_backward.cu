@@ -32,28 +32,28 @@
 //     r2 = 2*h*f*s,  X = res2 (+xshift) + xc*f,  f = -res2/(fovfct*zc) or xfac,
 //     (xc, yc, zc) = A*(p - campos)
 //   and block sums of dL/d(xc, yc, zc) and dL/d(X, Y) for the camera position.
-#include "spl_internal.cuh"
+#include <algorithm>
+
+#include "spl_tile.cuh"
 
 namespace spl {
 
 namespace {
 
-constexpr int IW = 8, IH = 4;
-
 template <int B>
 struct AdjSmem {
-  float4 p0[B];   // posx, posy, stp*log2e, bbox bits
-  float4 e[B];    // E.r, E.g, E.b, q.r
-  float2 q[B];    // q.g, q.b
-  float4 wq[B];   // dq/dE per channel: gray/(E+gray)^2
-  float acc[6][B];
-  uint32_t idx[B];
-  // followed by uint16_t run[B*T]
+  Stage<B> st;
+  float4 nw01[B];       // -dq/dE doubled: -w0, -w0, -w1, -w1 (w = gray/(E+gray)^2)
+  float2 nw2[B];        // -w2, -w2
+  uint32_t idx[B];      // particle index of each slot
+  float acc[6][B + 4];  // the batch's per-particle sums; the row pad puts one
+                        // particle's six sums in six different banks
+  // followed by uint16_t run[B][run_stride(T)]
 };
 
 template <int B>
 size_t adj_smem_bytes(int T) {
-  return sizeof(AdjSmem<B>) + (size_t)B * T * 2;
+  return sizeof(AdjSmem<B>) + (size_t)B * run_stride(T) * 2;
 }
 
 // Warp sum of six values in eight shuffles (reduce-scatter): afterwards lane l
@@ -80,16 +80,46 @@ __device__ __forceinline__ float warp_sum6(const float v[6], int lane, int &j, b
   return c;
 }
 
+// Segments of each tile's list for the adjoint: ceil(len / seg_len), 0 for an
+// empty tile.
+__global__ void k_adj_seg_count(const uint32_t *__restrict__ tile_start, int64_t ntiles,
+                                uint32_t seg_len, uint32_t *__restrict__ cnt) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t len = tile_start[t + 1] - tile_start[t];
+    cnt[t] = len == 0 ? 0u : 1u + (len - 1u) / seg_len;
+  }
+}
+
+// One CTA per segment of a tile's list (segments numbered in tile order,
+// AdjArgs::seg_off); the forward's pixel layout: 8x4 items, WX x WY items per
+// warp, pixels processed in pairs (items 2p, 2p+1) with packed arithmetic.
 template <int NT, int WX, int WY, int B, bool ADD>
 __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
   constexpr int K = WX * WY;
+  constexpr int NP = (K + 1) / 2;
+  constexpr int NO = ADD ? 1 : NP;  // ordered-only state
+  static_assert(K == 1 || WX % 2 == 0, "the items of a pair share one row");
   extern __shared__ __align__(16) uint8_t smem_raw[];
   AdjSmem<B> &S = *reinterpret_cast<AdjSmem<B> *>(smem_raw);
+  Stage<B> &St = S.st;
   uint16_t *srun = reinterpret_cast<uint16_t *>(smem_raw + sizeof(AdjSmem<B>));
   const SplatArgs &f = a.f;
+  const int T = f.T, RS = run_stride(T);
 
-  const int T = f.T;
-  const int tile = f.tile_order ? (int)__ldg(f.tile_order + blockIdx.x) : (int)blockIdx.x;
+  // ---- work item: segment blockIdx.x -> (tile, list range) ----------------
+  const uint64_t item = blockIdx.x;
+  if (item >= a.seg_off[a.ntiles]) return;
+  int o = 0, ohi = (int)a.ntiles;  // seg_off[o] <= item < seg_off[ohi]
+  while (ohi - o > 1) {
+    const int mid = (o + ohi) >> 1;
+    if (a.seg_off[mid] <= item) o = mid; else ohi = mid;
+  }
+  const int tile = f.tile_order ? (int)__ldg(f.tile_order + o) : o;
+  const uint32_t tile_end = f.tile_start[tile + 1];
+  const uint32_t start = f.tile_start[tile] + (uint32_t)(item - a.seg_off[o]) * a.seg_len;
+  const uint32_t end = (uint32_t)min((uint64_t)tile_end, (uint64_t)start + a.seg_len);
+
   const int ix = tile % f.ncx, iy = tile / f.ncx;
   const int x0s = ix * T, y0s = iy * T;
   const int tw = min(x0s + T, f.xres) - x0s;
@@ -103,44 +133,59 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
   const int wbx0 = wx * WX * IW, wby0 = wy * WY * IH;
   const int wbx1 = min(wbx0 + WX * IW, tw), wby1 = min(wby0 + WY * IH, th);
 
-  float pxf[K], pyf[K];
-  int pxi[K], pyi[K];
-  bool valid[K];
   // g: dL/dpic; od: the forward's optical depth; sb: optical depth behind
-  // and at the current particle; bg: composite contribution behind it
-  float g[K][3], od[K][3], sb[K][3], bg[K][3];
+  // and at the current particle; nbg: minus the composite behind it
+  int col[K], row[K];
+  F2 px2[NP], py2[NP];
+  F2 g[NP][3], od[NO][3], sb[NO][3], nbg[NO][3];
   uint32_t mystop = 0xffffffffu;
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     const int x = wbx0 + (k % WX) * IW + (lane & 7);
     const int y = wby0 + (k / WX) * IH + (lane >> 3);
-    valid[k] = warp_has_pixels && x < tw && y < th;
-    pxi[k] = x;
-    pyi[k] = y;
-    pxf[k] = (float)x;
-    pyf[k] = (float)y;
-    const size_t pix = (size_t)(x0s + x) * f.yres + (y0s + y);
-    float4 ax = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (!ADD && valid[k]) {
-      ax = __ldg(f.aux + pix);
-      mystop = min(mystop, __float_as_uint(ax.w));
+    const bool valid = warp_has_pixels && x < tw && y < th;
+    col[k] = valid ? x : 0;
+    row[k] = valid ? y : 255;
+  }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int x = wbx0 + ((2 * p) % WX) * IW + (lane & 7);
+    const int y = wby0 + ((2 * p) / WX) * IH + (lane >> 3);
+    px2[p] = f2((float)x, (float)(x + IW));
+    py2[p] = f2((float)y);
+    float gv[2][3], ov[2][3];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = 2 * p + h;
+      const bool valid = k < K && row[k < K ? k : 0] != 255;
+      const size_t pix = (size_t)(x0s + x + h * IW) * f.yres + (y0s + y);
+      float4 ax = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (!ADD && valid) {
+        ax = __ldg(f.aux + pix);
+        mystop = min(mystop, __float_as_uint(ax.w));
+      }
+      ov[h][0] = ax.x;
+      ov[h][1] = ax.y;
+      ov[h][2] = ax.z;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gv[h][c] = valid ? __ldg(a.gpic + pix * 3 + c) : 0.f;
     }
-    od[k][0] = ax.x;
-    od[k][1] = ax.y;
-    od[k][2] = ax.z;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      g[k][c] = valid[k] ? __ldg(a.gpic + pix * 3 + c) : 0.f;
-      sb[k][c] = 0.f;
-      bg[k][c] = 0.f;
+      g[p][c] = f2(gv[0][c], gv[1][c]);
+      if (!ADD) {
+        od[ADD ? 0 : p][c] = f2(ov[0][c], ov[1][c]);
+        sb[ADD ? 0 : p][c] = f2(0.f);
+        nbg[ADD ? 0 : p][c] = f2(0.f);
+      }
     }
   }
 
-  const uint32_t start = f.tile_start[tile], end = f.tile_start[tile + 1];
   const int nbatch = (int)((end - start + B - 1) / B);
   // Ordered frames: the forward composited, per warp, list positions
   // [stop, end) (a multiple of B); walk exactly those, in list order (back to
-  // front).  Additive frames: the whole list.
+  // front).  An ordered tile is one segment.  Additive frames: the whole
+  // segment.
   __shared__ uint32_t s_first;
   uint32_t wstop = 0;
   if (!ADD) {
@@ -157,47 +202,17 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
     // ---- stage B particles (as the forward, plus dq/dE and the index) ----
 #pragma unroll 1
     for (int slot = threadIdx.x; slot < B; slot += NT) {
-      const uint32_t jj = start + (uint32_t)bi * B + slot;
-      uint32_t bb = 0, idx = 0xffffffffu;
-      float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (jj < end) {
-        idx = __ldg(f.entries + jj);
-        const float4 p = __ldg(f.pos + idx);
-        const float4 c = __ldg(f.col + idx);
-        const float rfacr = fmul(p.z, 0.75f);
-        const float posx = fsub(p.x, (float)x0s), posy = fsub(p.y, (float)y0s);
-        const int minx = max(f2i(fadd(fsub(posx, rfacr), 1.f)), 0);
-        const int maxx = min(f2i(fadd(fadd(posx, rfacr), 1.f)), tw);
-        const int miny = max(f2i(fadd(fsub(posy, rfacr), 1.f)), 0);
-        const int maxy = min(f2i(fadd(fadd(posy, rfacr), 1.f)), th);
-        const float radsq = fmul(rfacr, rfacr);
-        const float sigma = fmul(f.h2sigma, p.z);
-        const float stp = fdiv(-1.f, fmul(sigma, sigma));
-        if (minx < maxx && miny < maxy) {
-          bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((uint32_t)miny << 16) |
-               ((uint32_t)maxy << 24);
-          uint16_t *run = srun + slot * T;
-          for (int x = minx; x < maxx; ++x) {
-            const float dx = fsub((float)x, posx);
-            const float dy = fsqrt(fsub(radsq, fmul(dx, dx)));
-            const int lo = max(miny, f2i(fadd(fsub(posy, dy), 1.f)));
-            int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
-            if (hi < lo) hi = lo;
-            run[x] = (uint16_t)(lo | (hi << 8));
-          }
-        }
-        p0 = make_float4(posx, posy, stp * kLog2e, 0.f);
-        if (ADD) {
-          S.e[slot] = make_float4(c.x, c.y, c.z, 0.f);
-        } else {
-          const float d0 = fadd(c.x, f.gray), d1 = fadd(c.y, f.gray), d2 = fadd(c.z, f.gray);
-          S.e[slot] = make_float4(c.x, c.y, c.z, fdiv(c.x, d0));
-          S.q[slot] = make_float2(fdiv(c.y, d1), fdiv(c.z, d2));
-          S.wq[slot] = make_float4(f.gray / (d0 * d0), f.gray / (d1 * d1), f.gray / (d2 * d2), 0.f);
-        }
+      float4 c;
+      const uint32_t idx = stage_entry<B, ADD, false>(St, srun, RS, slot, f,
+                                                      start + (uint32_t)bi * B + slot, end, x0s,
+                                                      y0s, tw, th, &c);
+      if (!ADD && idx != 0xffffffffu) {
+        const float d0 = fadd(c.x, f.gray), d1 = fadd(c.y, f.gray), d2 = fadd(c.z, f.gray);
+        const float w0 = -(f.gray / (d0 * d0)), w1 = -(f.gray / (d1 * d1));
+        const float w2 = -(f.gray / (d2 * d2));
+        S.nw01[slot] = make_float4(w0, w0, w1, w1);
+        S.nw2[slot] = make_float2(w2, w2);
       }
-      p0.w = __uint_as_float(bb);
-      S.p0[slot] = p0;
       S.idx[slot] = idx;
 #pragma unroll
       for (int j = 0; j < 6; ++j) S.acc[j][slot] = 0.f;
@@ -207,81 +222,91 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
     if (!warp_idle && (ADD || (uint32_t)bi * B >= wstop)) {
 #pragma unroll 1
       for (int ch = 0; ch < B / 32; ++ch) {
-        const uint32_t bbl = __float_as_uint(S.p0[ch * 32 + lane].w);
-        const int mnx = bbl & 255, mxx = (bbl >> 8) & 255;
-        const int mny = (bbl >> 16) & 255, mxy = bbl >> 24;
-        const bool hit = (mnx < mxx) && (mnx < wbx1) && (mxx > wbx0) && (mny < wby1) &&
-                         (mxy > wby0);
+        const bool hit = box_meets_warp(St.bb[ch * 32 + lane], wbx0, wbx1, wby0, wby1);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
           const int bit = __ffs(mask) - 1;
           mask &= ~(1u << bit);
           const int j = ch * 32 + bit;
-          const float4 p0 = S.p0[j];
-          const uint32_t bbj = __float_as_uint(p0.w);
-          const int jmnx = bbj & 255, jmxx = (bbj >> 8) & 255;
-          const int jmny = (bbj >> 16) & 255, jmxy = bbj >> 24;
-          const float4 e = S.e[j];
-          float2 q2 = make_float2(0.f, 0.f);
-          float4 wq = make_float4(0.f, 0.f, 0.f, 0.f);
+          const float4 pxy = St.pxy[j];
+          const float4 es = St.es[j];
+          const float4 e12 = St.e12[j];
+          float4 q01 = make_float4(0.f, 0.f, 0.f, 0.f), nw01 = q01;
+          float2 q2 = make_float2(0.f, 0.f), nw2 = q2;
           if (!ADD) {
-            q2 = S.q[j];
-            wq = S.wq[j];
+            q01 = St.q01[j];
+            q2 = St.q2[j];
+            nw01 = S.nw01[j];
+            nw2 = S.nw2[j];
           }
-          const uint16_t *run = srun + j * T;
-          float sm[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          uint32_t bbj = 0;
+          if (NP > 1) bbj = St.bb[j];
+          const uint16_t *run = srun + j * RS;
+          F2 sm[6];
+#pragma unroll
+          for (int i = 0; i < 6; ++i) sm[i] = f2(0.f);
           bool any = false;
 #pragma unroll
-          for (int k = 0; k < K; ++k) {
-            const int ix0 = wbx0 + (k % WX) * IW, iy0 = wby0 + (k / WX) * IH;
-            if (jmnx < ix0 + IW && jmxx > ix0 && jmny < iy0 + IH && jmxy > iy0) {  // uniform
-              bool in = valid[k] && pxi[k] >= jmnx && pxi[k] < jmxx;
-              if (in) {
-                const uint32_t rr = run[pxi[k]];
-                in = pyi[k] >= (int)(rr & 255) && pyi[k] < (int)(rr >> 8);
-              }
-              if (in) {
-                any = true;
-                const float dx = pxf[k] - p0.x, dy = pyf[k] - p0.y;
-                const float d2 = fmaf(dy, dy, dx * dx);
-                const float att = ex2(p0.z * d2);
-                float gatt;
-                if (ADD) {
-                  sm[0] = fmaf(-g[k][0], att, sm[0]);
-                  sm[1] = fmaf(-g[k][1], att, sm[1]);
-                  sm[2] = fmaf(-g[k][2], att, sm[2]);
-                  gatt = -fmaf(g[k][0], e.x, fmaf(g[k][1], e.y, g[k][2] * e.z));
-                } else {
-                  const float E[3] = {e.x, e.y, e.z}, Q[3] = {e.w, q2.x, q2.y};
-                  const float W[3] = {wq.x, wq.y, wq.z};
-                  gatt = 0.f;
+          for (int p = 0; p < NP; ++p) {
+            if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
+                                          wby0 + ((2 * p) / WX) * IH))
+              continue;
+            const bool in0 = covered(run, col[2 * p], row[2 * p]);
+            const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
+            if (!(in0 || in1)) continue;
+            any = true;
+            // an uncovered pixel of the pair gets att = 0 (and g = 0 outside
+            // the tile): its terms vanish
+            const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
+            const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
+            const F2 d2 = fma2(dy, dy, mul2(dx, dx));
+            const F2 arg = mul2(f2(es.z, es.w), d2);
+            const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
+            const F2 e[3] = {f2(es.x, es.y), f2(e12.x, e12.y), f2(e12.z, e12.w)};
+            F2 gatt;
+            if (ADD) {
+              // pic = -sum E*att (e staged negated): dL/dE_c = -sum g_c*att
+              // (negated at the reduction), gatt = -g.E
 #pragma unroll
-                  for (int c = 0; c < 3; ++c) {
-                    // u as the forward forms it; transmittance in front of the
-                    // particle from the stored optical depth, Tr = exp(-(od - sb))
-                    const float u = E[c] * att;
-                    sb[k][c] += u;
-                    const float trm = ex2((sb[k][c] - od[k][c]) * kLog2e);
-                    const float wt = -trm * expm1_neg(-u);  // Tr - Tr'
-                    const float trn = trm - wt;            // Tr' = Tr*T
-                    // dC/du = q*Tr' - B, dC/dq = Tr - Tr'  (B: composite behind)
-                    const float ga = g[k][c] * fmaf(Q[c], trn, -bg[k][c]);
-                    sm[c] = fmaf(ga, att, fmaf(g[k][c] * wt, W[c], sm[c]));
-                    gatt = fmaf(ga, E[c], gatt);
-                    bg[k][c] = fmaf(wt, Q[c], bg[k][c]);
-                  }
-                }
-                const float ga2 = gatt * att;
-                sm[3] = fmaf(ga2, dx, sm[3]);
-                sm[4] = fmaf(ga2, dy, sm[4]);
-                sm[5] = fmaf(ga2, d2, sm[5]);
+              for (int c = 0; c < 3; ++c) sm[c] = fma2(g[p][c], att, sm[c]);
+              gatt = fma2(g[p][0], e[0], fma2(g[p][1], e[1], mul2(g[p][2], e[2])));
+            } else {
+              const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
+              const F2 nw[3] = {f2(nw01.x, nw01.y), f2(nw01.z, nw01.w), f2(nw2.x, nw2.y)};
+              gatt = f2(0.f);
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                F2 &sbc = sb[ADD ? 0 : p][c], &nbgc = nbg[ADD ? 0 : p][c];
+                // u as the forward forms it; transmittance in front of the
+                // particle from the stored optical depth, Tr = exp(-(od - sb))
+                const F2 u = mul2(e[c], att);
+                sbc = add2(sbc, u);
+                const F2 ta = mul2(sub2(sbc, od[ADD ? 0 : p][c]), f2(kLog2e));
+                const F2 trm = f2(ex2(f2lo(ta)), ex2(f2hi(ta)));
+                const F2 nwt = mul2(trm, expm1_neg2(u));  // -(Tr - Tr')
+                const F2 trn = add2(trm, nwt);            // Tr' = Tr*T
+                // dC/du = q*Tr' - B, dC/dq = Tr - Tr'  (B: composite behind)
+                const F2 ga = mul2(g[p][c], fma2(q[c], trn, nbgc));
+                sm[c] = fma2(ga, att, fma2(mul2(g[p][c], nwt), nw[c], sm[c]));
+                gatt = fma2(ga, e[c], gatt);
+                nbgc = fma2(nwt, q[c], nbgc);
               }
             }
+            const F2 ga2 = mul2(gatt, att);
+            sm[3] = fma2(ga2, dx, sm[3]);
+            sm[4] = fma2(ga2, dy, sm[4]);
+            sm[5] = fma2(ga2, d2, sm[5]);
           }
           if (__any_sync(0xffffffffu, any)) {
+            float v[6];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) {
+              v[i] = f2lo(sm[i]) + f2hi(sm[i]);
+              if (ADD && i < 3) v[i] = -v[i];
+            }
             int jj;
             bool ok;
-            const float tot = warp_sum6(sm, lane, jj, ok);
+            const float tot = warp_sum6(v, lane, jj, ok);
             if ((lane & 3) == 0 && ok) atomicAdd(&S.acc[jj][j], tot);
           }
         }
@@ -302,17 +327,16 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
 }
 
 template <int NT, int WX, int WY, int B>
-void launch_adj_cfg(const AdjArgs &a, cudaStream_t s) {
-  const int ntiles = a.f.ncx * a.f.ncy;
+void launch_adj_cfg(const AdjArgs &a, uint32_t grid, cudaStream_t s) {
   const size_t sm = adj_smem_bytes<B>(a.f.T);
   if (a.f.a_eq_e) {
     auto k = k_splat_adj<NT, WX, WY, B, true>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<ntiles, NT, sm, s>>>(a);
+    k<<<grid, NT, sm, s>>>(a);
   } else {
     auto k = k_splat_adj<NT, WX, WY, B, false>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k<<<ntiles, NT, sm, s>>>(a);
+    k<<<grid, NT, sm, s>>>(a);
   }
 }
 
@@ -467,19 +491,51 @@ __global__ void __launch_bounds__(256) k_project_adj(ProjAdjArgs a) {
 
 }  // namespace
 
-int launch_splat_adjoint(const AdjArgs &a, cudaStream_t s) {
-  if (a.f.ncx * a.f.ncy <= 0) return 0;
-  const int cfg = a.f.config >= 0 && splat_config_valid(a.f.config, a.f.T)
-                      ? a.f.config
-                      : splat_default_config(a.f.T, a.f.a_eq_e != 0);
-  switch (cfg) {
-    case 0: launch_adj_cfg<256, 1, 1, 256>(a, s); break;
-    case 1: launch_adj_cfg<64, 2, 2, 128>(a, s); break;
-    case 2: launch_adj_cfg<128, 2, 1, 128>(a, s); break;
-    case 3: launch_adj_cfg<256, 2, 2, 256>(a, s); break;
-    default: launch_adj_cfg<256, 4, 4, 256>(a, s); break;
+int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
+  const int64_t ntiles = (int64_t)a0.f.ncx * a0.f.ncy;
+  if (ntiles <= 0) return 0;
+  AdjArgs a = a0;
+  const bool add = a.f.a_eq_e != 0;
+  const int T = a.f.T;
+  const int fwd_cfg = a.f.config >= 0 && splat_config_valid(a.f.config, T)
+                          ? a.f.config
+                          : splat_default_config(T, add);
+  // The ordered adjoint walks the forward's warps (it reads where each warp
+  // stopped); the additive one takes its own layout, four warps of 16x4
+  // pixels, which shares each hit's reduction among 64 pixels.
+  const int cfg = add && splat_config_valid(2, T) ? 2 : fwd_cfg;
+  const uint32_t B = (cfg == 1 || cfg == 2) ? 128u : 256u;
+  // Additive tiles: segments of about 1/16 of an SM's share of the frame's
+  // entries (at least four batches), so that the heaviest tiles spread over
+  // many SMs; ordered tiles stay whole.
+  uint32_t seg_len = 0xffffffffu;
+  if (add) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t per = (a.n_entries + (int64_t)nsm * 16 - 1) / ((int64_t)nsm * 16);
+    int64_t L = (per + B - 1) / B * B;
+    if (L < 4 * (int64_t)B) L = 4 * (int64_t)B;
+    if (L > 0x40000000) L = 0x40000000;
+    seg_len = (uint32_t)L;
   }
-  return 1;
+  a.ntiles = ntiles;
+  a.seg_len = seg_len;
+  int launches = 1;
+  int cb = (int)std::min<int64_t>((ntiles + 255) / 256, 152 * 8);
+  k_adj_seg_count<<<cb, 256, 0, s>>>(a.f.tile_start, ntiles, seg_len, a.seg_cnt);
+  scan_counts(a.seg_cnt, a.f.tile_order, ntiles, a.seg_off, a.scan_scratch, s, &launches);
+  // segments <= sum over tiles of (len / seg_len + 1)
+  const int64_t grid64 = ntiles + (add ? a.n_entries / seg_len + 1 : 0);
+  const uint32_t grid = (uint32_t)std::min<int64_t>(grid64, 0x7fffffff);
+  switch (cfg) {
+    case 0: launch_adj_cfg<256, 1, 1, 256>(a, grid, s); break;
+    case 1: launch_adj_cfg<64, 2, 2, 128>(a, grid, s); break;
+    case 2: launch_adj_cfg<128, 2, 1, 128>(a, grid, s); break;
+    case 3: launch_adj_cfg<256, 2, 2, 256>(a, grid, s); break;
+    default: launch_adj_cfg<256, 4, 4, 256>(a, grid, s); break;
+  }
+  return launches + 1;
 }
 
 int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s) {

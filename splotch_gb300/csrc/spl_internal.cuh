@@ -430,11 +430,22 @@ int launch_splat_queue(const BatchSplatArgs &q, int cfg, cudaStream_t s);
 // Adjoint of the splat: per active particle, sums of dL/dE (gcol.xyz) and of
 // gatt*att*(dx, dy, dx^2+dy^2) (gpos.xyz), accumulated with atomics (zero them
 // first).  f is the forward's argument set, f.pic its final image.
+// The adjoint runs one CTA per segment of a tile's list: additive tiles are
+// cut into segments of seg_len entries (their per-particle sums do not depend
+// on list order), ordered tiles are one segment each.  seg_cnt (ntiles) and
+// seg_off (ntiles + 1) are scratch for the launch; scan_scratch holds
+// scan_scratch_bytes(ntiles + 1) bytes.
 struct AdjArgs {
   SplatArgs f;
   const float *gpic;  // dL/dpic, x-major
   float4 *gpos;
   float4 *gcol;
+  int64_t n_entries;  // bin entries of the frame
+  uint32_t *seg_cnt;
+  uint64_t *seg_off;  // exclusive scan of segments per tile, in tile order
+  void *scan_scratch;
+  int64_t ntiles;     // set by the launch
+  uint32_t seg_len;   // set by the launch
 };
 int launch_splat_adjoint(const AdjArgs &a, cudaStream_t s);
 

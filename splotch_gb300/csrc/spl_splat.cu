@@ -33,31 +33,14 @@
 // accumulates C += Tr*q*(1-T), Tr *= T -- the same sum term by term -- and stops
 // a warp once every pixel's transmittance in all channels is below epsilon,
 // and the tile once every warp has stopped.
-#include "spl_internal.cuh"
+#include "spl_tile.cuh"
 
 namespace spl {
 
 namespace {
 
-constexpr int IW = 8, IH = 4;  // item: 8 columns x 4 rows, one pixel per lane
-
-// Staged particles, one entry per list slot.  Each value a pixel pair shares
-// is held twice, so one 128-bit load gives packed (F2) operands.
 template <int B>
-struct Smem {
-  float4 pxy[B];   // posx, posx, posy, posy (tile-local)
-  float4 es[B];    // e0, e0, stp*log2e, stp*log2e (e negated when additive)
-  float4 e12[B];   // e1, e1, e2, e2                (negated when additive)
-  float4 q01[B];   // q0, q0, q1, q1 (q = e/(e+grayabsorb), negated front-to-back)
-  float2 q2[B];    // q2, q2
-  uint32_t bb[B];  // clipped bounding box minx | maxx<<8 | miny<<16 | maxy<<24
-  // followed by uint16_t run[B][run_stride(T)]: per column the covered rows
-  // lo | (hi-lo)<<8, zero outside the bounding box
-};
-
-// Run-table row length: T rounded up to whole 8-pixel items, so that every
-// column an item can address lies in the row and rows stay 16-byte aligned.
-__host__ __device__ constexpr int run_stride(int T) { return (T + 7) & ~7; }
+using Smem = Stage<B>;  // followed by uint16_t run[B][run_stride(T)]
 
 template <int B>
 size_t smem_bytes(int T) {
@@ -131,67 +114,16 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
     const int bi = FTB ? nbatch - 1 - b : b;
     // ---- stage B particles ------------------------------------------------
 #pragma unroll 1
-    for (int slot = threadIdx.x; slot < B; slot += NT) {
-      const uint32_t jj = start + (uint32_t)bi * B + slot;
-      uint32_t bb = 0;
-      if (jj < end) {
-        const uint32_t idx = __ldg(a.entries + jj);
-        const float4 p = __ldg(a.pos + idx);
-        const float4 c = __ldg(a.col + idx);
-        const float rfacr = fmul(p.z, 0.75f);
-        const float posx = fsub(p.x, (float)x0s), posy = fsub(p.y, (float)y0s);
-        const int minx = max(f2i(fadd(fsub(posx, rfacr), 1.f)), 0);
-        const int maxx = min(f2i(fadd(fadd(posx, rfacr), 1.f)), tw);
-        const int miny = max(f2i(fadd(fsub(posy, rfacr), 1.f)), 0);
-        const int maxy = min(f2i(fadd(fadd(posy, rfacr), 1.f)), th);
-        const float radsq = fmul(rfacr, rfacr);
-        const float sigma = fmul(a.h2sigma, p.z);
-        const float stp = fdiv(-1.f, fmul(sigma, sigma));
-        if (minx < maxx && miny < maxy) {
-          bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((uint32_t)miny << 16) |
-               ((uint32_t)maxy << 24);
-          uint16_t *run = srun + slot * RS;
-          uint4 *row16 = reinterpret_cast<uint4 *>(run);
-          for (int i = 0; i < RS / 8; ++i) row16[i] = make_uint4(0u, 0u, 0u, 0u);
-          for (int x = minx; x < maxx; ++x) {  // splotch_host.cc:603-606
-            const float dx = fsub((float)x, posx);
-            const float dxsq = fmul(dx, dx);
-            const float dy = fsqrt(fsub(radsq, dxsq));
-            const int lo = max(miny, f2i(fadd(fsub(posy, dy), 1.f)));
-            const int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
-            run[x] = (uint16_t)(lo | (max(hi - lo, 0) << 8));
-          }
-        }
-        const float s2 = stp * kLog2e;
-        S.pxy[slot] = make_float4(posx, posx, posy, posy);
-        if (ADD) {
-          S.es[slot] = make_float4(-c.x, -c.x, s2, s2);
-          S.e12[slot] = make_float4(-c.y, -c.y, -c.z, -c.z);
-        } else {
-          // q = e/(e+grayabsorb), splotch_host.cc:626-628
-          const float sq = FTB ? -1.f : 1.f;
-          const float q0 = sq * fdiv(c.x, fadd(c.x, a.gray));
-          const float q1 = sq * fdiv(c.y, fadd(c.y, a.gray));
-          const float q2 = sq * fdiv(c.z, fadd(c.z, a.gray));
-          S.es[slot] = make_float4(c.x, c.x, s2, s2);
-          S.e12[slot] = make_float4(c.y, c.y, c.z, c.z);
-          S.q01[slot] = make_float4(q0, q0, q1, q1);
-          S.q2[slot] = make_float2(q2, q2);
-        }
-      }
-      S.bb[slot] = bb;
-    }
+    for (int slot = threadIdx.x; slot < B; slot += NT)
+      stage_entry<B, ADD, FTB>(S, srun, RS, slot, a, start + (uint32_t)bi * B + slot, end, x0s,
+                               y0s, tw, th);
     __syncthreads();
     // ---- accumulate ---------------------------------------------------------
     if (!warp_done) {
 #pragma unroll 1
       for (int cc = 0; cc < B / 32; ++cc) {
         const int ch = FTB ? B / 32 - 1 - cc : cc;
-        const uint32_t bbl = S.bb[ch * 32 + lane];
-        const int mnx = bbl & 255, mxx = (bbl >> 8) & 255;
-        const int mny = (bbl >> 16) & 255, mxy = bbl >> 24;
-        const bool hit = (mnx < mxx) && (mnx < wbx1) && (mxx > wbx0) && (mny < wby1) &&
-                         (mxy > wby0);
+        const bool hit = box_meets_warp(S.bb[ch * 32 + lane], wbx0, wbx1, wby0, wby1);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {
           const int bit = FTB ? 31 - __clz(mask) : __ffs(mask) - 1;
@@ -211,21 +143,12 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
           const uint16_t *run = srun + j * RS;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
-            if (NP > 1) {  // does the particle's box reach this pair's 16x4 pixels (uniform)?
-              const int ix0 = wbx0 + ((2 * p) % WX) * IW, iy0 = wby0 + ((2 * p) / WX) * IH;
-              const int jmnx = bbj & 255, jmxx = (bbj >> 8) & 255;
-              const int jmny = (bbj >> 16) & 255, jmxy = bbj >> 24;
-              if (!(jmnx < ix0 + 2 * IW && jmxx > ix0 && jmny < iy0 + IH && jmxy > iy0))
-                continue;
-            }
-            // exact coverage: the pixel's row inside its column's run
-            const uint32_t r0 = run[col[2 * p]];
-            const bool in0 = (uint32_t)(row[2 * p] - (int)(r0 & 255)) < (r0 >> 8);
-            bool in1 = false;
-            if (2 * p + 1 < K) {
-              const uint32_t r1 = run[col[2 * p + 1]];
-              in1 = (uint32_t)(row[2 * p + 1] - (int)(r1 & 255)) < (r1 >> 8);
-            }
+            // does the particle's box reach this pair's 16x4 pixels (uniform)?
+            if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
+                                          wby0 + ((2 * p) / WX) * IH))
+              continue;
+            const bool in0 = covered(run, col[2 * p], row[2 * p]);
+            const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
             if (in0 || in1) {
               // a pixel the particle does not cover gets att = 0: its update is
               // the identity in every mode
