@@ -369,12 +369,16 @@ def large(args, local: int) -> dict:
                                                     "splat_ms", "bwd_splat_ms",
                                                     "bwd_project_ms")}
     st = r.stats()
+    free_b, total_b = torch.cuda.mem_get_info(dev)
     out.update({"active": int(st["n_active"]), "bin_entries": int(st["n_entries"]),
                 "wide_particles": int(st["n_wide"]),
                 "ratio_fwd_bwd_over_fwd": out["fwd_bwd_ms"] / out["fwd_ms"],
                 "fwd_mparticles_per_s": n / (out["fwd_ms"] * 1e-3) / 1e6,
                 "fwd_bwd_mparticles_per_s": n / (out["fwd_bwd_ms"] * 1e-3) / 1e6,
-                "device_memory_peak_gb": torch.cuda.max_memory_allocated(dev) / 1e9})
+                # torch tensors (inputs, image, gradients) at their peak, and the
+                # whole device in use with the renderer's buffers still held
+                "torch_memory_peak_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
+                "device_memory_in_use_gb": (total_b - free_b) / 1e9})
     r.close()
     return out
 
