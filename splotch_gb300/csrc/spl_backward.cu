@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
 
   const int nbatch = (int)((end - start + B - 1) / B);
   // Ordered frames: the forward composited, per warp, list positions
-  // [stop, end) (a multiple of 32); walk exactly those, in list order (back to
+  // [stop, end) (a multiple of B); walk exactly those, in list order (back to
   // front).  An ordered tile is one segment.  Additive frames: the whole
   // segment.
   __shared__ uint32_t s_first;
@@ -219,10 +219,9 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
     }
     __syncthreads();
     // ---- per-fragment adjoint ----------------------------------------------
-    if (!warp_idle && (ADD || (uint32_t)bi * B + B > wstop)) {
+    if (!warp_idle && (ADD || (uint32_t)bi * B >= wstop)) {
 #pragma unroll 1
       for (int ch = 0; ch < B / 32; ++ch) {
-        if (!ADD && (uint32_t)bi * B + (uint32_t)ch * 32 < wstop) continue;  // not composited
         const bool hit = box_meets_warp(St.bb[ch * 32 + lane], wbx0, wbx1, wby0, wby1);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
         while (mask) {

@@ -70,7 +70,6 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t *__res
 constexpr int OS_EPOCH_SHIFT = 56, OS_KIND_SHIFT = 54;
 constexpr unsigned long long OS_VALUE_MASK = (1ull << OS_KIND_SHIFT) - 1ull;
 constexpr uint32_t OS_SPIN_LIMIT = 1u << 22;  // bounded wait, then error flag
-constexpr int OS_LB = 8;                      // look-back words read per step
 
 __device__ __forceinline__ unsigned long long os_word(uint32_t epoch, uint32_t kind,
                                                       unsigned long long v) {
@@ -153,38 +152,23 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
         *st = os_word(epoch, 2u, run);
       } else {
         *st = os_word(epoch, 1u, run);
-        // walk back OS_LB words at a time (independent loads in flight); a
-        // word not yet published for this pass restarts the step from it
-        const volatile unsigned long long *vs = state;
         int t = blk - 1;
         uint32_t spins = 0;
-        bool done = false;
-        while (!done && t >= 0) {
-          unsigned long long v[OS_LB];
-#pragma unroll
-          for (int q = 0; q < OS_LB; ++q)
-            v[q] = t - q >= 0 ? vs[(size_t)(t - q) * RS_BINS + d] : os_word(epoch, 2u, 0);
-          int used = OS_LB;
-#pragma unroll
-          for (int q = 0; q < OS_LB; ++q) {
-            if (used < OS_LB || done) continue;
-            const uint32_t kind = (uint32_t)(v[q] >> OS_KIND_SHIFT) & 3u;
-            if ((uint32_t)(v[q] >> OS_EPOCH_SHIFT) != epoch || kind == 0u) {
-              used = q;  // not published yet: wait for it
-              continue;
-            }
-            excl += v[q] & OS_VALUE_MASK;
-            if (kind == 2u) done = true;
-          }
-          if (done) break;
-          t -= used;
-          if (used < OS_LB) {
+        while (t >= 0) {
+          const unsigned long long v =
+              reinterpret_cast<volatile unsigned long long *>(state)[(size_t)t * RS_BINS + d];
+          const uint32_t kind = (uint32_t)(v >> OS_KIND_SHIFT) & 3u;
+          if ((uint32_t)(v >> OS_EPOCH_SHIFT) != epoch || kind == 0u) {
             if (++spins > OS_SPIN_LIMIT) {  // give up: results invalid, host reports it
               atomicOr(err, 2u);
               break;
             }
-            if (spins > 16) __nanosleep(64);
+            if (spins > 64) __nanosleep(64);
+            continue;
           }
+          excl += v & OS_VALUE_MASK;
+          if (kind == 2u) break;
+          --t;
         }
         *st = os_word(epoch, 2u, excl + run);
       }

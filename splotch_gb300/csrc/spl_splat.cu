@@ -50,8 +50,7 @@ size_t smem_bytes(int T) {
 // One tile of one frame, by the whole CTA (shared by the per-frame launch and
 // the persistent batch kernel).
 // AUX (ordered frames only): also accumulate each pixel's optical depth and
-// record where the warp stopped (a multiple of 32 list positions), for the
-// adjoint (SplatArgs::aux).
+// record where the warp stopped, for the adjoint (SplatArgs::aux).
 template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false>
 __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
                                            uint8_t *smem_raw) {
@@ -126,7 +125,6 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
         const int ch = FTB ? B / 32 - 1 - cc : cc;
         const bool hit = box_meets_warp(S.bb[ch * 32 + lane], wbx0, wbx1, wby0, wby1);
         uint32_t mask = __ballot_sync(0xffffffffu, hit);
-        const bool any_hit = mask != 0u;
         while (mask) {
           const int bit = FTB ? 31 - __clz(mask) : __ffs(mask) - 1;
           mask &= ~(1u << bit);
@@ -181,26 +179,21 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
             }
           }
         }
-        // front-to-back: stop the warp after the chunk that made every one of
-        // its pixels opaque (checked only when the chunk composited anything)
-        if (FTB && any_hit) {
-          bool mine_done = true;
+      }
+      if (FTB) {
+        bool mine_done = true;
 #pragma unroll
-          for (int k = 0; k < K; ++k) {
-            if (row[k] != 255) {
+        for (int k = 0; k < K; ++k) {
+          if (row[k] != 255) {
 #pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                const float t = (k & 1) ? f2hi(tr[k / 2][c]) : f2lo(tr[k / 2][c]);
-                mine_done = mine_done && t < a.ftb_eps;
-              }
+            for (int c = 0; c < 3; ++c) {
+              const float t = (k & 1) ? f2hi(tr[k / 2][c]) : f2lo(tr[k / 2][c]);
+              mine_done = mine_done && t < a.ftb_eps;
             }
           }
-          warp_done = __all_sync(0xffffffffu, mine_done);
-          if (warp_done) {
-            if (AUX) stop = (uint32_t)bi * B + (uint32_t)ch * 32;
-            break;
-          }
         }
+        warp_done = __all_sync(0xffffffffu, mine_done);
+        if (AUX && warp_done) stop = (uint32_t)bi * B;
       }
     }
     if (FTB) {
