@@ -99,65 +99,39 @@ __global__ void k_compose_order(const uint32_t *__restrict__ perm_ord, uint32_t 
     order[s] = s < cap_add ? (uint32_t)s : cap_add + perm_ord[s - cap_add];
 }
 
-// Records are taken 256 at a time, as in k_emit_narrow: a group whose entries
-// fit kEmitStage and lie below the capacity is built in shared memory and
-// written out coalesced; any other group writes record by record.
-constexpr int kEmitStage = 2048;
-
 __global__ void __launch_bounds__(256) k_emit_batch_narrow(
     const float4 *__restrict__ pos, const uint32_t *__restrict__ count,
     const uint32_t *__restrict__ order, const uint64_t *__restrict__ off, int64_t n,
     const uint32_t *__restrict__ frame, const FrameTile *__restrict__ ft, uint64_t cap,
     uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval, uint32_t *__restrict__ wide_list,
     uint32_t *__restrict__ wide_n, uint32_t *status) {
-  __shared__ uint32_t s_key[kEmitStage], s_val[kEmitStage];
-  for (int64_t s0 = (int64_t)blockIdx.x * 256; s0 < n; s0 += (int64_t)gridDim.x * 256) {
-    const int64_t s1 = min(s0 + 256, n);
-    const uint64_t base = __ldg(off + s0), lim = __ldg(off + s1);
-    const bool staged = lim - base <= (uint64_t)kEmitStage && lim <= cap;
-    const int64_t s = s0 + threadIdx.x;
-    if (s < n) {
-      const uint32_t c = __ldg(count + s);
-      const uint64_t o = __ldg(off + s);
-      if (c == 0) {
-      } else if (o + c > cap) {
-        // over capacity: this render is redone after a re-plan; the slots it
-        // would have used below the capacity become sentinels (sorted last,
-        // never read as entries)
-        atomicOr(status, 2u);
-        for (uint64_t p = o; p < cap && p < o + c; ++p) {
-          tkey[p] = 0xffffffffu;
-          tval[p] = 0u;
-        }
-      } else if (c > (uint32_t)kWide) {
-        wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
-      } else {
-        const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
-        const FrameTile t = ft[__ldg(frame + i)];
-        const float4 p = __ldg(pos + i);
-        if (staged) {
-          const uint32_t lo = (uint32_t)(o - base);
-          for_each_tile(p.x, p.y, p.z, t.g, [&](int tile, int j) {
-            s_key[lo + j] = t.tile_base + (uint32_t)tile;
-            s_val[lo + j] = i;
-          });
-        } else {
-          for_each_tile(p.x, p.y, p.z, t.g, [&](int tile, int j) {
-            tkey[o + j] = t.tile_base + (uint32_t)tile;
-            tval[o + j] = i;
-          });
-        }
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = __ldg(count + s);
+    if (c == 0) continue;
+    const uint64_t o = __ldg(off + s);
+    if (o + c > cap) {
+      // over capacity: this render is redone after a re-plan; the slots it
+      // would have used below the capacity become sentinels (sorted last,
+      // never read as entries)
+      atomicOr(status, 2u);
+      for (uint64_t p = o; p < cap && p < o + c; ++p) {
+        tkey[p] = 0xffffffffu;
+        tval[p] = 0u;
       }
+      continue;
     }
-    if (staged) {
-      __syncthreads();
-      const uint32_t m = (uint32_t)(lim - base);
-      for (uint32_t k = threadIdx.x; k < m; k += 256) {
-        tkey[base + k] = s_key[k];
-        tval[base + k] = s_val[k];
-      }
+    if (c > (uint32_t)kWide) {
+      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+      continue;
     }
-    __syncthreads();  // the staging buffer is reused by the next group
+    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
+    const FrameTile t = ft[__ldg(frame + i)];
+    const float4 p = __ldg(pos + i);
+    for_each_tile(p.x, p.y, p.z, t.g, [&](int tile, int j) {
+      tkey[o + j] = t.tile_base + (uint32_t)tile;
+      tval[o + j] = i;
+    });
   }
 }
 

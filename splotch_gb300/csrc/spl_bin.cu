@@ -21,13 +21,6 @@ namespace {
 
 constexpr int kWideTiles = 64;
 
-// Records are taken 256 at a time; their entries occupy one contiguous range
-// [off[s0], off[s0 + 256]).  When that range fits kEmitStage entries the block
-// builds it in shared memory and writes it out with consecutive threads
-// (coalesced); otherwise each record writes its own entries.  The slots of
-// records handed to the wide path are written by k_emit_wide afterwards.
-constexpr int kEmitStage = 2048;
-
 __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ pos,
                                                      const uint32_t *__restrict__ count,
                                                      const uint32_t *__restrict__ order,
@@ -37,45 +30,21 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
                                                      uint32_t *__restrict__ tval,
                                                      uint32_t *__restrict__ wide_list,
                                                      uint32_t *__restrict__ wide_n) {
-  __shared__ uint32_t s_key[kEmitStage], s_val[kEmitStage];
-  for (int64_t s0 = (int64_t)blockIdx.x * 256; s0 < n; s0 += (int64_t)gridDim.x * 256) {
-    const int64_t s1 = min(s0 + 256, n);
-    const uint64_t base = __ldg(off + s0), lim = __ldg(off + s1);
-    const bool staged = lim - base <= (uint64_t)kEmitStage;
-    const int64_t s = s0 + threadIdx.x;
-    if (s < n) {
-      const uint32_t c = __ldg(count + s);  // counts are in visiting order
-      if (c > 0) {
-        const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
-        if (c > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
-          wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
-        } else {
-          const uint64_t o = __ldg(off + s);
-          const float4 p = __ldg(pos + i);
-          if (staged) {
-            const uint32_t lo = (uint32_t)(o - base);
-            for_each_tile(p.x, p.y, p.z, g, [&](int tile, int j) {
-              s_key[lo + j] = (uint32_t)tile;
-              s_val[lo + j] = i;
-            });
-          } else {
-            for_each_tile(p.x, p.y, p.z, g, [&](int tile, int j) {
-              tkey[o + j] = (uint32_t)tile;
-              tval[o + j] = i;
-            });
-          }
-        }
-      }
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = __ldg(count + s);  // counts are in visiting order
+    if (c == 0) continue;
+    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
+    if (c > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
+      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+      continue;
     }
-    if (staged) {
-      __syncthreads();
-      const uint32_t m = (uint32_t)(lim - base);
-      for (uint32_t k = threadIdx.x; k < m; k += 256) {
-        tkey[base + k] = s_key[k];
-        tval[base + k] = s_val[k];
-      }
-    }
-    __syncthreads();  // the staging buffer is reused by the next group
+    const uint64_t o = __ldg(off + s);
+    const float4 p = __ldg(pos + i);
+    for_each_tile(p.x, p.y, p.z, g, [&](int tile, int j) {
+      tkey[o + j] = (uint32_t)tile;
+      tval[o + j] = i;
+    });
   }
 }
 
