@@ -115,12 +115,16 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     key[j] = valid ? __ldg(keys_in + idx) : 0xffffffffu;
     val[j] = valid ? (vals_in ? __ldg(vals_in + idx) : (uint32_t)idx) : 0u;
     const uint32_t d = valid ? (key[j] >> shift) & mask : RS_BINS + lane;
+    // the lanes holding digit d: the lowest one claims their slots in the
+    // warp's histogram with one shared atomic and passes the old count on.
+    // Successive items' claims are performed in the warp's issue order, which
+    // keeps item order for equal digits (the stable-order GPU tests against
+    // the oracle's permutation check this).
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
     uint32_t prior = 0;
-    if (valid) prior = whist[w][d];
-    __syncwarp();
-    if (valid && (__ffs(peers) - 1) == lane) whist[w][d] = prior + __popc(peers);
-    __syncwarp();
+    if (valid && lane == leader) prior = atomicAdd(&whist[w][d], (uint32_t)__popc(peers));
+    prior = __shfl_sync(0xffffffffu, prior, leader);
     rank[j] = prior + __popc(peers & lanemask_lt());
   }
   __syncthreads();
