@@ -431,6 +431,15 @@ def batched(args, local: int) -> dict:
     e1.record(stream)
     torch.cuda.synchronize()
     plain_ms = e0.elapsed_time(e1) / reps
+    # one more (untimed) plain pass: each frame's device stage times, summed
+    stage_keys = ("project_ms", "sort_ms", "bin_ms", "splat_ms", "total_ms")
+    plain_stages = dict.fromkeys(stage_keys, 0.0)
+    for s, desc, pic in frames:
+        r.render_soa(desc, sets[s], pic)
+        st = r.stats()
+        for k in stage_keys:
+            plain_stages[k] += float(st[k])
+    out["plain_stage_ms_sum"] = {k: round(v, 3) for k, v in plain_stages.items()}
 
     t0 = time.perf_counter()
     b = sg.Batch(r, sets, frames)
