@@ -20,8 +20,7 @@
 //                 (global tile id, record) pairs, one stable sort by tile id;
 //                 tile ranges; work queue = every (frame, tile) item, additive
 //                 frames first, each class longest list first
-//   splat       : one persistent kernel per class (additive / ordered), or
-//                 one for both when they share a launch configuration, that
+//   splat       : one persistent kernel per class (additive / ordered) that
 //                 takes items from the queue; each item renders one tile of
 //                 one frame straight into that frame's image.
 // Sizes that depend on the data (active records, bin entries) are capacities
@@ -221,14 +220,13 @@ __global__ void k_tile_ranges_clamped(const uint32_t *__restrict__ key, int64_t 
 // list length, so one ascending sort gives each class longest-first.
 __global__ void k_tile_cost_class(const uint32_t *__restrict__ tile_start, int64_t ntiles,
                                   const uint32_t *__restrict__ frame_of_tile,
-                                  const uint8_t *__restrict__ frame_ordered, int by_class,
+                                  const uint8_t *__restrict__ frame_ordered,
                                   uint32_t *__restrict__ key) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles;
        t += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t cnt = tile_start[t + 1] - tile_start[t];
     const int lg = (int)(8.f * __log2f((float)cnt + 1.f));
-    const uint32_t cls = by_class ? (uint32_t)frame_ordered[frame_of_tile[t]] : 0u;
-    key[t] = (cls << 8) | (255u - (uint32_t)min(lg, 255));
+    key[t] = ((uint32_t)frame_ordered[frame_of_tile[t]] << 8) | (255u - (uint32_t)min(lg, 255));
   }
 }
 
@@ -569,7 +567,6 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
 
 // The work queue of one class: 0 additive frames (the first n_add_tiles
 // items), 1 ordered frames (the rest); counter in status word 2 + cls.
-// cls 0: additive items, 1: ordered items, 2: every item (one merged queue).
 spl::BatchSplatArgs queue_args(spl_batch *b, int cls) {
   spl::BatchSplatArgs q;
   q.frames = as<spl::SplatArgs>(b->splat_args);
@@ -577,20 +574,15 @@ spl::BatchSplatArgs queue_args(spl_batch *b, int cls) {
   q.frame_of_tile = as<uint32_t>(b->frame_of_tile);
   q.work = as<uint32_t>(b->work);
   q.T = b->T;
-  q.work_begin = cls == 1 ? (uint32_t)b->n_add_tiles : 0u;
-  q.nwork = cls == 0   ? (uint32_t)b->n_add_tiles
-            : cls == 1 ? (uint32_t)(b->ntiles - b->n_add_tiles)
-                       : (uint32_t)b->ntiles;
-  q.counter = as<uint32_t>(b->status) + 2 + (cls == 1 ? 1 : 0);
+  q.work_begin = cls == 0 ? 0u : (uint32_t)b->n_add_tiles;
+  q.nwork = cls == 0 ? (uint32_t)b->n_add_tiles : (uint32_t)(b->ntiles - b->n_add_tiles);
+  q.counter = as<uint32_t>(b->status) + 2 + cls;
   return q;
 }
 
 // Every kernel of one batch render, in stream order (eager or under capture).
-// splat_class: -1 both classes, 0 additive only, 1 ordered only, 2 none.  With
-// both classes on one launch configuration, one merged queue takes every
-// item longest-list-first, whatever its class.
+// splat_class: -1 both queues, 0 additive only, 1 ordered only, 2 none.
 spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
-  const bool merged = splat_class == -1 && b->cfg_add == b->cfg_abs;
   const int nf = (int)b->frames.size();
   int launches = 0;
   uint32_t *status = as<uint32_t>(b->status);
@@ -680,21 +672,17 @@ spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
       as<uint32_t>(b->tkey_s), (int64_t)capE, b->ntiles, as<uint32_t>(b->tile_start));
   spl::k_tile_cost_class<<<spl::grid_for(b->ntiles), 256, 0, s>>>(
       as<uint32_t>(b->tile_start), b->ntiles, as<uint32_t>(b->frame_of_tile),
-      as<uint8_t>(b->frame_ord), merged ? 0 : 1, as<uint32_t>(b->tcost));
+      as<uint8_t>(b->frame_ord), as<uint32_t>(b->tcost));
   launches += 2;
   spl::radix_sort_pairs(as<uint32_t>(b->tcost), nullptr, as<uint32_t>(b->tcost_s),
                         as<uint32_t>(b->work_tmp), as<uint32_t>(b->tcost_s),
-                        as<uint32_t>(b->work), b->ntiles, 0, merged ? 8 : 9, false,
-                        b->radix_scr.p, s, &launches, err, true);
-  // ---- splat: one persistent launch per class, or one merged ------------------------------
-  if (merged) {
-    launches += spl::launch_splat_queue(queue_args(b, 2), b->cfg_add, s);
-  } else {
-    if (splat_class == -1 || splat_class == 0)
-      launches += spl::launch_splat_queue(queue_args(b, 0), b->cfg_add, s);
-    if (splat_class == -1 || splat_class == 1)
-      launches += spl::launch_splat_queue(queue_args(b, 1), b->cfg_abs, s);
-  }
+                        as<uint32_t>(b->work), b->ntiles, 0, 9, false, b->radix_scr.p, s,
+                        &launches, err, true);
+  // ---- splat: one persistent launch per class ---------------------------------------------
+  if (splat_class == -1 || splat_class == 0)
+    launches += spl::launch_splat_queue(queue_args(b, 0), b->cfg_add, s);
+  if (splat_class == -1 || splat_class == 1)
+    launches += spl::launch_splat_queue(queue_args(b, 1), b->cfg_abs, s);
   BCK(cudaMemcpyAsync(b->h_status, status, 32, cudaMemcpyDeviceToHost, s));
   BCK(cudaMemcpyAsync(b->h_entries, off + capA, 8, cudaMemcpyDeviceToHost, s));
   b->launches = launches;
