@@ -256,6 +256,7 @@ struct spl_batch {
   std::vector<std::vector<float>> pal_rgb_copy;
   spl_batch_options opt{};
   int T = 16, cfg_add = 0, cfg_abs = 2;
+  bool ord_all_ftb = true;  // every ordered frame composites front-to-back
   // plan.  Projection order: additive frames, then ordered ones; records of
   // the two classes live in separate segments, [0, cap_add) and
   // [cap_add, cap_add + cap_ord), so that only ordered records are sorted.
@@ -463,6 +464,7 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
   std::vector<uint32_t> fot((size_t)tiles);
   std::vector<spl::FrameTile> fts(nf);
   std::vector<spl::SplatArgs> sas(nf);
+  b->ord_all_ftb = true;
   const float h2sigma =
       (float)(0.5 * std::pow(3.141592653589793238462643383279502884197, -1. / 6.));
   for (int f = 0; f < nf; ++f) {
@@ -501,6 +503,7 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
     a.h2sigma = h2sigma;
     a.a_eq_e = d.a_eq_e ? 1 : 0;
     a.order_mode = d.order_mode;
+    if (!d.a_eq_e && d.order_mode != 1) b->ord_all_ftb = false;
     a.ftb_eps = d.ftb_epsilon;
     a.config = -1;
     a.pic = b->frames[f].pic;
@@ -577,6 +580,7 @@ spl::BatchSplatArgs queue_args(spl_batch *b, int cls) {
   q.work_begin = cls == 0 ? 0u : (uint32_t)b->n_add_tiles;
   q.nwork = cls == 0 ? (uint32_t)b->n_add_tiles : (uint32_t)(b->ntiles - b->n_add_tiles);
   q.counter = as<uint32_t>(b->status) + 2 + cls;
+  q.mode = cls == 0 ? 0 : (b->ord_all_ftb ? 1 : 2);
   return q;
 }
 

@@ -424,6 +424,10 @@ struct BatchSplatArgs {
   uint32_t work_begin, nwork;
   uint32_t *counter;  // zero before the launch
   int T;
+  // the frames of the queue's items: 0 all additive, 1 all ordered
+  // front-to-back, 2 any (the kernel chooses per item); a single-mode kernel
+  // holds one splat form and fewer registers
+  int mode;
 };
 int launch_splat_queue(const BatchSplatArgs &q, int cfg, cudaStream_t s);
 

@@ -233,21 +233,32 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
 // Persistent splat over a queue of (frame, tile) items: each CTA takes the
 // next item from an atomic counter until the queue is empty.  The queue is in
 // longest-list-first order across all frames; every frame's own arguments
-// (image, tiling, mode, tile-range slice) come from a per-frame table.
-template <int NT, int WX, int WY, int B>
+// (image, tiling, mode, tile-range slice) come from a per-frame table.  MODE
+// 0 / 1: every item is additive / front-to-back (one splat form compiled in);
+// 2: the form is chosen per item.
+template <int NT, int WX, int WY, int B, int MODE>
 __global__ void __launch_bounds__(NT) k_splat_queue(BatchSplatArgs q) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   __shared__ uint32_t s_item;
+  __shared__ SplatArgs s_args;  // the item's frame arguments, read from shared memory
   for (;;) {
-    if (threadIdx.x == 0) s_item = atomicAdd(q.counter, 1u);
+    if (threadIdx.x == 0) {
+      const uint32_t item = atomicAdd(q.counter, 1u);
+      s_item = item;
+      if (item < q.nwork) s_args = q.frames[__ldg(q.frame_of_tile + __ldg(q.work + q.work_begin + item))];
+    }
     __syncthreads();
     const uint32_t item = s_item;
     if (item >= q.nwork) break;
     const uint32_t gt = __ldg(q.work + q.work_begin + item);
     const uint32_t f = __ldg(q.frame_of_tile + gt);
-    const SplatArgs a = q.frames[f];
+    const SplatArgs &a = s_args;
     const int tile = (int)(gt - q.tile_base[f]);
-    if (a.a_eq_e)
+    if (MODE == 0)
+      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw);
+    else if (MODE == 1)
+      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw);
+    else if (a.a_eq_e)
       splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw);
     else if (a.order_mode == 1)
       splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw);
@@ -367,10 +378,10 @@ int launch_splat(const SplatArgs &a, cudaStream_t s) {
 
 namespace {
 
-template <int NT, int WX, int WY, int B>
-int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
+template <int NT, int WX, int WY, int B, int MODE>
+int launch_queue_mode(const BatchSplatArgs &q, cudaStream_t s) {
   const size_t sm = smem_bytes<B>(q.T);
-  auto k = k_splat_queue<NT, WX, WY, B>;
+  auto k = k_splat_queue<NT, WX, WY, B, MODE>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int per_sm = 0, dev = 0, nsm = 0;
   cudaGetDevice(&dev);
@@ -382,6 +393,15 @@ int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
   if (grid < 1) return 0;
   k<<<grid, NT, sm, s>>>(q);
   return 1;
+}
+
+template <int NT, int WX, int WY, int B>
+int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
+  switch (q.mode) {
+    case 0: return launch_queue_mode<NT, WX, WY, B, 0>(q, s);
+    case 1: return launch_queue_mode<NT, WX, WY, B, 1>(q, s);
+    default: return launch_queue_mode<NT, WX, WY, B, 2>(q, s);
+  }
 }
 
 }  // namespace
