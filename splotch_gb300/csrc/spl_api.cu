@@ -240,6 +240,7 @@ spl_status spl::frame_setup(const spl_frame_desc *d, int T, bool exact_fp64, Fra
   pc.cmid0 = g.cmid0;
   fs.do_sort = !d->a_eq_e && d->sort_type != 0;
   pc.sort_type = fs.do_sort ? d->sort_type : 0;
+  pc.pal_cache = nullptr;
   fs.ntiles = (int64_t)g.ncx * g.ncy;
   if (fs.ntiles >= 0xffffffffLL) return fail(SPL_ERR_INVALID, "too many tiles");
   fs.npal = npal;

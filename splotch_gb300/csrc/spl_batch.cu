@@ -4,6 +4,9 @@
 //
 // Per render, with no host round trip between stages (frames are kept
 // additive first, then ordered):
+//   per set     : the palette colour of each particle, when several frames
+//                 share the set and its palettes (it does not depend on the
+//                 camera); their projection reads it instead of interpolating
 //   all frames  : one activity-flag launch over every frame's particle set
 //                 (projection test; a per-frame table of projection constants
 //                 and inputs)
@@ -257,6 +260,10 @@ struct spl_batch {
   spl_batch_options opt{};
   int T = 16, cfg_add = 0, cfg_abs = 2;
   bool ord_all_ftb = true;  // every ordered frame composites front-to-back
+  // palette cache: per set, the frame whose constants colourise the set once
+  // per render for all its frames (-1: not cached), and its offset in pal_cache
+  std::vector<int> cache_frame;
+  std::vector<int64_t> cache_off;
   // plan.  Projection order: additive frames, then ordered ones; records of
   // the two classes live in separate segments, [0, cap_add) and
   // [cap_add, cap_add + cap_ord), so that only ordered records are sorted.
@@ -273,7 +280,7 @@ struct spl_batch {
   int frame_bits = 1, tile_bits = 1;
   std::vector<DevBuf *> owned;
   DevBuf pal_x, pal_rgb, pal_thr, pal_xff, pal_invff;
-  DevBuf flags, word_off, d_wbase, d_tbase, ftab, actv_add, actv_ord, fmap_add, fmap_ord;
+  DevBuf flags, word_off, d_wbase, pal_cache, d_tbase, ftab, actv_add, actv_ord, fmap_add, fmap_ord;
   DevBuf pos_c, col_c, idx_c, count_c, key_c, frame_c;
   DevBuf ktmp, vtmp, kout, perm1, fkey, perm, order, count_seq, off, wide_list, radix_scr;
   DevBuf tkey, tval, tkey2, tval2, tkey_s, tval_s;
@@ -384,6 +391,44 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
     }
   }
   b->n_add_frames = (int)b->proj.size();
+  // palette cache: a set is colourised once per render when it has two or
+  // more frames and they all use the same palettes and colour-vector flags
+  const int ns = (int)b->sets.size();
+  b->cache_frame.assign(ns, -1);
+  b->cache_off.assign(ns, 0);
+  int64_t cache_n = 0;
+  {
+    std::vector<int> nfr(ns, 0);
+    for (int f = 0; f < nf; ++f) {
+      const int si = b->frames[f].set;
+      const spl::FrameSetup &a = b->fs[f];
+      if (nfr[si]++ == 0) {
+        b->cache_frame[si] = f;
+        continue;
+      }
+      const int f0 = b->cache_frame[si];
+      if (f0 < 0) continue;
+      const spl::FrameSetup &z = b->fs[f0];
+      bool same = a.pal_x == z.pal_x && a.pal_rgb == z.pal_rgb && a.pc.ptypes == z.pc.ptypes &&
+                  a.pc.exact_fp64 == z.pc.exact_fp64;
+      for (int t = 0; same && t < a.pc.ptypes; ++t)
+        same = a.pc.colvec[t] == z.pc.colvec[t] && a.pc.pal_off[t] == z.pc.pal_off[t] &&
+               a.pc.pal_n[t] == z.pc.pal_n[t];
+      if (!same) b->cache_frame[si] = -1;
+    }
+    for (int si = 0; si < ns; ++si) {
+      const int f0 = b->cache_frame[si];
+      bool any_palette = false;
+      if (f0 >= 0)
+        for (int t = 0; t < b->fs[f0].pc.ptypes; ++t) any_palette |= !b->fs[f0].pc.colvec[t];
+      if (f0 < 0 || nfr[si] < 2 || !any_palette) {
+        b->cache_frame[si] = -1;
+        continue;
+      }
+      b->cache_off[si] = cache_n;
+      cache_n += b->sets[si].n;
+    }
+  }
   for (int f = 0; f < nf; ++f)
     if (ordered[f]) b->proj.push_back(f);
   // activity words in projection order, based per class
@@ -431,6 +476,7 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
       (st = dev_alloc(b, b->d_wbase, (nf + 1) * 4)) ||
       (st = dev_alloc(b, b->d_tbase, (nf + 1) * 4)) ||
       (st = dev_alloc(b, b->ftab, nf * sizeof(spl::FrameProj))) ||
+      (st = dev_alloc(b, b->pal_cache, cache_n * 16)) ||
       (st = dev_alloc(b, b->actv_add, (nf + 1) * 4)) ||
       (st = dev_alloc(b, b->actv_ord, (nf + 1) * 4)) ||
       (st = dev_alloc(b, b->fmap_add, (nf + 1) * 4)) ||
@@ -482,6 +528,8 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
     c.pal_xff = as<float2>(b->pal_xff) + o;
     c.pal_invff = as<float2>(b->pal_invff) + o;
     c.n_fallback = nullptr;
+    const int si = b->frames[f].set;
+    c.pal_cache = b->cache_frame[si] >= 0 ? as<float4>(b->pal_cache) + b->cache_off[si] : nullptr;
     b->pc[f] = c;
     for (int64_t t = 0; t < s.ntiles; ++t) fot[b->tbase[f] + t] = (uint32_t)f;
     fts[f].g = s.g;
@@ -598,6 +646,16 @@ spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
   const int n_add = b->n_add_frames, n_ord = nf - n_add;
   const int64_t nw_ord = b->nwords - b->nw_add;
   const spl::FrameProj *tab = as<spl::FrameProj>(b->ftab);
+  // palette colours of the sets that several frames share, once per render
+  for (int si = 0; si < (int)b->sets.size(); ++si) {
+    const int f0 = b->cache_frame[si];
+    if (f0 < 0) continue;
+    const spl_particles &p = b->sets[si];
+    const spl::SoAIn soa = set_soa(p);
+    spl::launch_palette_cache(set_aos(p), &soa, p.n, b->pc[f0],
+                              as<float4>(b->pal_cache) + b->cache_off[si], s);
+    ++launches;
+  }
   spl::launch_project_flags_multi(tab, nf, b->fblocks, s);
   ++launches;
   uint32_t *flags = as<uint32_t>(b->flags), *woff = as<uint32_t>(b->word_off);

@@ -199,6 +199,9 @@ struct ProjConst {
   int T, ncx, ncy;
   float rcell, cmid0;
   int sort_type;           // 0 = no key
+  // per particle of the set, the palette colour of palette types (computed
+  // once for frames sharing the set and its palettes), or null
+  const float4 *pal_cache;
 };
 
 struct Tiling {
@@ -268,6 +271,10 @@ struct SoAIn {
 // active-only form (the render path) over the full form.
 void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
                     ProjectOut o, bool compact, cudaStream_t s, int *launches);
+// Palette colour of each particle of a set (types with a palette) into out
+// (n entries), for ProjConst::pal_cache of the frames that share the set.
+void launch_palette_cache(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                          float4 *out, cudaStream_t s);
 // The two passes of the compact form on their own (the batch runs the
 // popcount scan once over every frame's activity words): o.flags and
 // o.word_off point at this frame's words, o.pos_c etc. at the arrays shared

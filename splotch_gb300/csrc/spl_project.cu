@@ -228,8 +228,19 @@ __device__ __forceinline__ bool project_geom(const ProjConst &c, const PIn &in, 
          !(miny >= c.yres) && !(maxy <= 0) && max(miny, 0) < min(maxy, c.yres);
 }
 
-__device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, uint32_t *err) {
+// linearMap colour of a palette particle (colour value v, type t): the
+// float-float form, or the double form when it cannot decide a rounding.
+__device__ __forceinline__ void palette_colour(const ProjConst &c, int t, float v, float &r,
+                                               float &g, float &b, bool &fell_back) {
   const bool fast = !c.exact_fp64;
+  if (fast && palette_fast(c, t, v, r, g, b)) return;
+  fell_back = fell_back || fast;
+  palette(c, t, v, r, g, b);
+}
+
+// i: the particle's index in its set (for the palette cache).
+__device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, int64_t i,
+                                             uint32_t *err) {
   bool fell_back = false;
   float x, y, z, r, I;
   float er = in.er, eg = in.eg, eb = in.eb;
@@ -238,14 +249,17 @@ __device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, 
   {
     if (active) {  // particle_colorize (splotch_host.cc:276-282)
       if (!c.colvec[t]) {
-        float pr, pg, pb;
-        if (fast && palette_fast(c, t, er, pr, pg, pb)) {
+        if (c.pal_cache) {  // computed once for the particle set (batched frames)
+          const float4 pc = __ldg(c.pal_cache + i);
+          er = pc.x;
+          eg = pc.y;
+          eb = pc.z;
+        } else {
+          float pr, pg, pb;
+          palette_colour(c, t, er, pr, pg, pb, fell_back);
           er = pr;
           eg = pg;
           eb = pb;
-        } else {
-          fell_back = fell_back || fast;
-          palette(c, t, er, er, eg, eb);
         }
       }
       const float fac = fmul(I, c.bright[t]);
@@ -313,7 +327,7 @@ __global__ void __launch_bounds__(256) k_project_full(L load, int64_t n, ProjCon
                                                       ProjectOut o) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const POut p = project_core(c, load(i), o.err);
+    const POut p = project_core(c, load(i), i, o.err);
     o.pos[i] = p.pos;
     o.col[i] = p.col;
     o.active[i] = p.active ? 1 : 0;
@@ -405,7 +419,7 @@ __device__ __forceinline__ void dense_block(const L &load, int64_t n, const Proj
   const uint32_t base = nw > 0 ? __ldg(word_off + w0) : 0u;
   for (uint32_t k = threadIdx.x; k < nloc; k += blockDim.x) {
     const uint32_t i = s_list[k];
-    const POut p = project_core(c, load(i), o.err);
+    const POut p = project_core(c, load(i), i, o.err);
     const uint32_t dst = base + k;
     if (dst >= o.cap_c) {
       atomicOr(o.err, 8u);
@@ -460,6 +474,24 @@ __global__ void __launch_bounds__(256) k_project_dense_multi(const FrameProj *__
     dense_block(LoadSoA{fp.soa.x, fp.soa.y, fp.soa.z, fp.soa.r, fp.soa.I, fp.soa.cr, fp.soa.cg,
                         fp.soa.cb, fp.soa.type},
                 fp.n, fp.c, fp.o.flags, fp.o.word_off, fp.o, w0, s_list, s_cnt);
+}
+
+// Palette colour of every particle of a set whose type has a palette (the
+// colourisation that does not depend on the camera), for frames that share
+// the set and its palettes; other particles' slots are left as they are.
+template <class L>
+__global__ void __launch_bounds__(256) k_palette_cache(L load, int64_t n, ProjConst c,
+                                                       float4 *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const PIn in = load(i);
+    const int t = in.type;
+    if (t < 0 || t >= c.ptypes || c.colvec[t]) continue;
+    float r, g, b;
+    bool fb = false;
+    palette_colour(c, t, in.er, r, g, b, fb);
+    out[i] = make_float4(r, g, b, 0.f);
+  }
 }
 
 // particle_sim writeback: e, x, y, z, r, I, type, active (36 bytes).
@@ -564,6 +596,20 @@ void launch_project_flags_multi(const FrameProj *tab, int nf, uint32_t nblocks,
 void launch_project_dense_multi(const FrameProj *tab, int nf, uint32_t nblocks,
                                 cudaStream_t s) {
   if (nf > 0 && nblocks > 0) k_project_dense_multi<<<nblocks, 256, 0, s>>>(tab, nf);
+}
+
+void launch_palette_cache(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &c,
+                          float4 *out, cudaStream_t s) {
+  if (n <= 0) return;
+  ProjConst cc = c;
+  cc.pal_cache = nullptr;
+  if (aos)
+    k_palette_cache<<<grid_for(n), 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n,
+                                                cc, out);
+  else
+    k_palette_cache<<<grid_for(n), 256, 0, s>>>(
+        LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type}, n,
+        cc, out);
 }
 
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,
