@@ -102,39 +102,63 @@ __global__ void k_compose_order(const uint32_t *__restrict__ perm_ord, uint32_t 
     order[s] = s < cap_add ? (uint32_t)s : cap_add + perm_ord[s - cap_add];
 }
 
+// Each thread takes kEmitUnroll records per step (a grid stride apart) and
+// issues their scattered loads together, as k_emit_narrow does.
+constexpr int kEmitUnroll = 4;
+
 __global__ void __launch_bounds__(256) k_emit_batch_narrow(
     const float4 *__restrict__ pos, const uint32_t *__restrict__ count,
     const uint32_t *__restrict__ order, const uint64_t *__restrict__ off, int64_t n,
     const uint32_t *__restrict__ frame, const FrameTile *__restrict__ ft, uint64_t cap,
     uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval, uint32_t *__restrict__ wide_list,
     uint32_t *__restrict__ wide_n, uint32_t *status) {
-  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
-       s += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = __ldg(count + s);
-    if (c == 0) continue;
-    const uint64_t o = __ldg(off + s);
-    if (o + c > cap) {
-      // over capacity: this render is redone after a re-plan; the slots it
-      // would have used below the capacity become sentinels (sorted last,
-      // never read as entries)
-      atomicOr(status, 2u);
-      for (uint64_t p = o; p < cap && p < o + c; ++p) {
-        tkey[p] = 0xffffffffu;
-        tval[p] = 0u;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s0 < n;
+       s0 += stride * kEmitUnroll) {
+    uint32_t c[kEmitUnroll], i[kEmitUnroll], fr[kEmitUnroll];
+    uint64_t o[kEmitUnroll];
+    float4 p[kEmitUnroll];
+#pragma unroll
+    for (int k = 0; k < kEmitUnroll; ++k) {
+      const int64_t s = s0 + k * stride;
+      c[k] = s < n ? __ldg(count + s) : 0u;
+      o[k] = s < n ? __ldg(off + s) : 0u;
+      i[k] = s < n ? (order ? __ldg(order + s) : (uint32_t)s) : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kEmitUnroll; ++k) {
+      if (c[k] > 0 && c[k] <= (uint32_t)kWide && o[k] + c[k] <= cap) {
+        p[k] = __ldg(pos + i[k]);
+        fr[k] = __ldg(frame + i[k]);
       }
-      continue;
     }
-    if (c > (uint32_t)kWide) {
-      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
-      continue;
+#pragma unroll
+    for (int k = 0; k < kEmitUnroll; ++k) {
+      const int64_t s = s0 + k * stride;
+      if (c[k] == 0) continue;
+      if (o[k] + c[k] > cap) {
+        // over capacity: this render is redone after a re-plan; the slots it
+        // would have used below the capacity become sentinels (sorted last,
+        // never read as entries)
+        atomicOr(status, 2u);
+        for (uint64_t q = o[k]; q < cap && q < o[k] + c[k]; ++q) {
+          tkey[q] = 0xffffffffu;
+          tval[q] = 0u;
+        }
+        continue;
+      }
+      if (c[k] > (uint32_t)kWide) {
+        wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+        continue;
+      }
+      const FrameTile t = ft[fr[k]];
+      const uint32_t ii = i[k];
+      const uint64_t ok = o[k];
+      for_each_tile(p[k].x, p[k].y, p[k].z, t.g, [&](int tile, int j) {
+        tkey[ok + j] = t.tile_base + (uint32_t)tile;
+        tval[ok + j] = ii;
+      });
     }
-    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
-    const FrameTile t = ft[__ldg(frame + i)];
-    const float4 p = __ldg(pos + i);
-    for_each_tile(p.x, p.y, p.z, t.g, [&](int tile, int j) {
-      tkey[o + j] = t.tile_base + (uint32_t)tile;
-      tval[o + j] = i;
-    });
   }
 }
 

@@ -21,6 +21,11 @@ namespace {
 
 constexpr int kWideTiles = 64;
 
+// Each thread takes kEmitUnroll records per step (a grid stride apart) and
+// issues their loads together: in visiting order the particles' positions
+// are gathered at scattered indices, and the independent loads overlap.
+constexpr int kEmitUnroll = 4;
+
 __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ pos,
                                                      const uint32_t *__restrict__ count,
                                                      const uint32_t *__restrict__ order,
@@ -30,21 +35,35 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
                                                      uint32_t *__restrict__ tval,
                                                      uint32_t *__restrict__ wide_list,
                                                      uint32_t *__restrict__ wide_n) {
-  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
-       s += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = __ldg(count + s);  // counts are in visiting order
-    if (c == 0) continue;
-    const uint32_t i = order ? __ldg(order + s) : (uint32_t)s;
-    if (c > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
-      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
-      continue;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s0 < n;
+       s0 += stride * kEmitUnroll) {
+    uint32_t c[kEmitUnroll], i[kEmitUnroll];
+    float4 p[kEmitUnroll];
+#pragma unroll
+    for (int k = 0; k < kEmitUnroll; ++k) {
+      const int64_t s = s0 + k * stride;
+      c[k] = s < n ? __ldg(count + s) : 0u;  // counts are in visiting order
+      i[k] = s < n ? (order ? __ldg(order + s) : (uint32_t)s) : 0u;
     }
-    const uint64_t o = __ldg(off + s);
-    const float4 p = __ldg(pos + i);
-    for_each_tile(p.x, p.y, p.z, g, [&](int tile, int j) {
-      tkey[o + j] = (uint32_t)tile;
-      tval[o + j] = i;
-    });
+#pragma unroll
+    for (int k = 0; k < kEmitUnroll; ++k)
+      if (c[k] > 0 && c[k] <= (uint32_t)kWideTiles) p[k] = __ldg(pos + i[k]);
+#pragma unroll
+    for (int k = 0; k < kEmitUnroll; ++k) {
+      const int64_t s = s0 + k * stride;
+      if (c[k] == 0) continue;
+      if (c[k] > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
+        wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+        continue;
+      }
+      const uint64_t o = __ldg(off + s);
+      const uint32_t ii = i[k];
+      for_each_tile(p[k].x, p[k].y, p[k].z, g, [&](int tile, int j) {
+        tkey[o + j] = (uint32_t)tile;
+        tval[o + j] = ii;
+      });
+    }
   }
 }
 
