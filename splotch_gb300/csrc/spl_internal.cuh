@@ -141,6 +141,15 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
   const ff v = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
   return fast_two_sum(v.h, __fadd_rn(t.l, v.l));
 }
+// a + b with an absolute error of at most 3u^2 (|a.h| + |b.h|) (u = 2^-24):
+// TwoSum of the high parts, the low parts added in float, and a final TwoSum
+// (exact, whatever the magnitudes).  No bound relative to the result under
+// cancellation: callers bound the error by the operands' magnitudes.
+__device__ __forceinline__ ff ff_add_abs(ff a, ff b) {
+  const ff s = two_sum(a.h, b.h);
+  const float w = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+  return two_sum(s.h, w);
+}
 // (a.h + a.l) * (b.h + b.l), relative error about 2^-45
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
   ff p = two_prod(a.h, b.h);

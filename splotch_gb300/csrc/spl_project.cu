@@ -46,12 +46,14 @@ __device__ __forceinline__ bool transpoint_fast(const float *m, float x, float y
       return true;
     }
   }
-  const ff s1 = ff_add(a, b);
-  const ff s2 = ff_add(s1, c);
-  const ff s3 = ff_add(s2, ff{m[3], 0.f});
-  // reference rounding (2^-53 per double add) + float-float error (3*2^-48
-  // per add), with a factor-4 margin
-  const float delta = 0x1p-44f * (fabsf(s1.h) + fabsf(s2.h) + fabsf(s3.h));
+  const ff s1 = ff_add_abs(a, b);
+  const ff s2 = ff_add_abs(s1, c);
+  const ff s3 = ff_add_abs(s2, ff{m[3], 0.f});
+  // reference rounding (2^-53 per double add, relative to each partial sum) +
+  // float-float error (3*2^-48 per add, relative to its operands), with a
+  // margin of at least 5
+  const float delta = 0x1p-44f * (fabsf(a.h) + fabsf(b.h) + fabsf(c.h) + fabsf(m[3]) +
+                                  fabsf(s1.h) + fabsf(s2.h) + fabsf(s3.h));
   out = s3.h;
   return rn24_decided(s3, delta);
 }
@@ -64,8 +66,8 @@ __device__ __forceinline__ bool shift_fast(ff A, float p, float &out) {
     out = fadd(A.h, p);
     return true;
   }
-  const ff s = ff_add(A, ff{p, 0.f});
-  const float delta = 0x1p-44f * (fabsf(A.h) + fabsf(s.h));
+  const ff s = ff_add_abs(A, ff{p, 0.f});
+  const float delta = 0x1p-44f * (fabsf(A.h) + fabsf(p) + fabsf(s.h));
   out = s.h;
   return s.h != 0.f && rn24_decided(s, delta);
 }
