@@ -10,8 +10,10 @@ reference's demo snapshot is not available.
 value : Mparticles/s with the SoA inputs already resident in HBM (CUDA events
         on the render stream around K frames; 1.8 GB of inputs per frame, far
         larger than L2, so no flush is needed).
-e2e   : the same metric through the C ABI with HOST buffers: particle_sim
-        records in pinned host memory, H2D + image D2H inside every timed call.
+e2e   : the same metric through the C ABI with HOST buffers: a sequence of
+        frames from particle_sim records in pinned host memory, each frame's
+        records copied ahead (spl_prefetch) while the frame before it renders;
+        every frame's H2D and image D2H lie inside the timed region.
 roofline: the dominant kernel of the frame, algorithmic work / its CUDA-event
         time, against MEASURED_PEAKS.json.
 cpu_baseline: the CPU restatement of the reference (bit-exact with it) timed
@@ -541,14 +543,22 @@ def run_gpu(args):
     host_aos.numpy()[:] = w.particles.view(np.uint8)
     host_pic = torch.empty((desc.xres, desc.yres, 3), dtype=torch.float32, pin_memory=True)
     r.set_stream(stream.cuda_stream)
-    r.render_aos(desc, host_aos, host_pic)  # warm the AoS path
-    e2e_t = []
-    for _ in range(args.e2e_steps):
+
+    # A sequence of frames from host memory, each frame's records copied ahead
+    # (spl_prefetch) while the frame before it renders: every step's 1.8 GB
+    # host->device copy and image read-back lie inside the timed region.
+    def frames_from_host(steps: int) -> float:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r.render_aos(desc, host_aos, host_pic)
-        e2e_t.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_t) / len(e2e_t)
+        r.prefetch_aos(host_aos)
+        for k in range(steps):
+            if k + 1 < steps:
+                r.prefetch_aos(host_aos)
+            r.render_aos(desc, host_aos, host_pic)
+        return (time.perf_counter() - t0) / steps
+
+    frames_from_host(3)  # warm-up: the AoS path and the three copy-ahead slots
+    e2e_s = frames_from_host(args.e2e_steps)
     if dist:
         t = torch.tensor([e2e_s], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)

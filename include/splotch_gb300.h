@@ -140,6 +140,16 @@ int spl_splat_config_valid(int cfg, int tile_size);
 /* ---- plain render: replaces host_rendering (splotch_host.cc:711-834) --- */
 spl_status spl_render(spl_context *ctx, const spl_frame_desc *d,
                       const spl_particles *p, spl_image *out, int writeback);
+
+/* Copy ahead the host particle arrays of a later spl_render on this context
+   (no counterpart in the reference, whose frames are rendered one call at a
+   time): the copy runs on a stream of its own while the current frame
+   renders, and the spl_render whose view names the same host arrays and count
+   waits for it instead of copying.  Up to two prefetches may be pending; they
+   are consumed in order, and a render of other arrays drops them.  The host
+   arrays must not change between the prefetch and that render; pinned memory
+   lets the copy overlap.  Device-memory views need no copy (no-op). */
+spl_status spl_prefetch(spl_context *ctx, const spl_particles *p);
 spl_status spl_get_stats(const spl_context *ctx, spl_stats *s);
 
 /* ---- test hooks: state of the last spl_render (host destinations) ----- */

@@ -302,6 +302,15 @@ class Renderer:
                                        else _abi.SPL_WRITEBACK_NONE))
         self._last_n = n
 
+    def prefetch_aos(self, particles) -> None:
+        """spl_prefetch of a host particle_sim array: its copy to the device
+        starts now, on a stream of its own, for a later render_aos of the same
+        array (which waits for it instead of copying)."""
+        n = len(particles) if isinstance(particles, np.ndarray) else particles.numel() // 36
+        p = _abi.Particles(n=n, layout=_abi.SPL_LAYOUT_AOS, memspace=_abi.SPL_MEM_HOST,
+                           aos=_abi.ptr(particles))
+        _abi.check(self.lib.spl_prefetch(self.ctx, C.byref(p)))
+
     def render_soa(self, desc: _abi.FrameDesc, soa: dict, pic, *, device: bool = True) -> None:
         """Render SoA fields x,y,z,r,I,cr[,cg,cb][,type] (float32 / uint16)."""
         n = int(soa["x"].shape[0])

@@ -44,6 +44,24 @@ struct spl_context {
   spl::SoAIn last_soa{};
   spl_stats stats{};
   cudaEvent_t ev[8]{};
+  // spl_prefetch: host inputs copied ahead on copy_stream into a ring of
+  // slots.  A slot is queued from its prefetch until the spl_render that
+  // reads it, then in use until the next spl_render (spl_render_backward
+  // reads the inputs again); `freed` is recorded on the render stream after
+  // the last kernel that read it, and a new prefetch into the slot waits on it.
+  struct InSlot {
+    Buf aos, soa[9];
+    const void *host[10] = {};  // aos, x, y, z, r, I, cr, cg, cb, type
+    int64_t n = 0;
+    int layout = -1;
+    cudaEvent_t ready = nullptr, freed = nullptr;
+    bool queued = false;
+  };
+  InSlot pf[3];
+  int pf_fifo[3] = {-1, -1, -1};  // queued slots, oldest first
+  int pf_len = 0;
+  int pf_in_use = -1;             // slot read by the last render
+  cudaStream_t copy_stream = nullptr;
 };
 
 namespace {
@@ -176,6 +194,35 @@ void spl::set_last_error(const char *msg) { g_err = msg; }
 
 spl_status spl::host_fail(spl_status code, const std::string &msg) { return fail(code, msg); }
 
+// The host arrays of a particle view, in a fixed order (aos, x, y, z, r, I,
+// cr, cg, cb, type), for matching a render to a prefetch.
+static void host_keys(const spl_particles *p, const void *k[10]) {
+  const void *v[10] = {p->aos, p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb, p->type};
+  for (int i = 0; i < 10; ++i) k[i] = p->layout == SPL_LAYOUT_AOS ? (i == 0 ? v[0] : nullptr)
+                                                                  : (i == 0 ? nullptr : v[i]);
+}
+
+// The oldest queued prefetch if it holds this view's host arrays (it leaves
+// the queue), else -1 and the queue is dropped (stale or out of order).
+static int take_prefetch(spl_context *c, const spl_particles *p) {
+  if (c->pf_len == 0) return -1;
+  const int slot = c->pf_fifo[0];
+  const spl_context::InSlot &q = c->pf[slot];
+  const void *k[10];
+  host_keys(p, k);
+  bool match = q.layout == p->layout && q.n == p->n;
+  for (int i = 0; match && i < 10; ++i) match = k[i] == q.host[i];
+  if (!match) {
+    for (int i = 0; i < c->pf_len; ++i) c->pf[c->pf_fifo[i]].queued = false;
+    c->pf_len = 0;
+    return -1;
+  }
+  c->pf[slot].queued = false;
+  for (int i = 1; i < c->pf_len; ++i) c->pf_fifo[i - 1] = c->pf_fifo[i];
+  --c->pf_len;
+  return slot;
+}
+
 spl_status spl::validate_frame(const spl_frame_desc *d, const spl_particles *p,
                                const spl_image *o) {
   return validate(d, p, o);
@@ -303,7 +350,8 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->pal_invff, &c->tcost, &c->tcost_s, &c->tord, &c->pos_c,
                               &c->col_c, &c->idx_c, &c->pstate, &c->poff, &c->gpic,
                               &c->gpos_c, &c->gcol_c, &c->camsum, &c->aux, &c->post_tab,
-                              &c->post_bar, &c->post_img, &c->post_bytes};
+                              &c->post_bar, &c->post_img, &c->post_bytes, &c->seg_cnt,
+                              &c->seg_off};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
@@ -312,6 +360,15 @@ spl_status spl_context_destroy(spl_context *c) {
     if (b.p) cudaFree(b.p);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
+  if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+  for (auto &q : c->pf) {
+    if (q.aos.p) cudaFree(q.aos.p);
+    for (auto &b : q.soa)
+      if (b.p) cudaFree(b.p);
+    if (q.ready) cudaEventDestroy(q.ready);
+    if (q.freed) cudaEventDestroy(q.freed);
+  }
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return SPL_OK;
@@ -407,7 +464,20 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   // ---- inputs --------------------------------------------------------------
   const void *aos_dev = nullptr;
   spl::SoAIn soa{p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb, p->type};
-  if (p->layout == SPL_LAYOUT_AOS) {
+  const int slot = p->memspace == SPL_MEM_HOST ? take_prefetch(c, p) : -1;
+  c->pf_in_use = slot;
+  if (slot >= 0) {  // copied ahead by spl_prefetch: wait for that copy
+    spl_context::InSlot &q = c->pf[slot];
+    SPL_CK(cudaStreamWaitEvent(s, q.ready, 0));
+    if (p->layout == SPL_LAYOUT_AOS) {
+      aos_dev = q.aos.p;
+    } else {
+      const float **f[8] = {&soa.x, &soa.y, &soa.z, &soa.r, &soa.I, &soa.cr, &soa.cg, &soa.cb};
+      for (int k = 0; k < 8; ++k)
+        if (*f[k]) *f[k] = as<float>(q.soa[k]);
+      if (p->type) soa.type = as<uint16_t>(q.soa[8]);
+    }
+  } else if (p->layout == SPL_LAYOUT_AOS) {
     if (p->memspace == SPL_MEM_HOST) {
       if ((st = ensure(c->aos_in, n * 36))) return st;
       SPL_CK(cudaMemcpyAsync(c->aos_in.p, p->aos, n * 36, cudaMemcpyHostToDevice, s));
@@ -606,6 +676,59 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   S.n_tiles = ntiles;
   S.kernel_launches = launches;
   S.n_active = na;
+  if (c->pf_in_use >= 0) cudaEventRecord(c->pf[c->pf_in_use].freed, s);
+  return SPL_OK;
+}
+
+spl_status spl_prefetch(spl_context *c, const spl_particles *p) {
+  if (!c || !p) return fail(SPL_ERR_INVALID, "null argument");
+  if (p->memspace != SPL_MEM_HOST) return SPL_OK;  // device inputs are not copied
+  if (p->n < 0 || p->n > 0xffffffffLL) return fail(SPL_ERR_INVALID, "particle count out of range");
+  const int64_t n = p->n;
+  if (p->layout == SPL_LAYOUT_AOS) {
+    if (n > 0 && !p->aos) return fail(SPL_ERR_INVALID, "null AoS pointer");
+  } else if (p->layout == SPL_LAYOUT_SOA) {
+    if (n > 0 && (!p->x || !p->y || !p->z || !p->r || !p->I || !p->cr))
+      return fail(SPL_ERR_INVALID, "null SoA pointer");
+  } else {
+    return fail(SPL_ERR_INVALID, "bad layout");
+  }
+  SPL_CK(cudaSetDevice(c->device));
+  if (c->pf_len >= 2)
+    return fail(SPL_ERR_INVALID, "spl_prefetch: two prefetches are already pending");
+  int slot = -1;  // not queued, and not the inputs of the last render
+  for (int k = 0; k < 3 && slot < 0; ++k)
+    if (!c->pf[k].queued && k != c->pf_in_use) slot = k;
+  if (slot < 0)
+    return fail(SPL_ERR_INVALID, "spl_prefetch: two prefetches are already pending");
+  if (!c->copy_stream) SPL_CK(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  spl_context::InSlot &q = c->pf[slot];
+  if (!q.ready) SPL_CK(cudaEventCreateWithFlags(&q.ready, cudaEventDisableTiming));
+  if (!q.freed) SPL_CK(cudaEventCreateWithFlags(&q.freed, cudaEventDisableTiming));
+  spl_status st;
+  SPL_CK(cudaStreamWaitEvent(c->copy_stream, q.freed, 0));
+  cudaStream_t cs = c->copy_stream;
+  if (p->layout == SPL_LAYOUT_AOS) {
+    if ((st = ensure(q.aos, n * 36))) return st;
+    if (n > 0) SPL_CK(cudaMemcpyAsync(q.aos.p, p->aos, n * 36, cudaMemcpyHostToDevice, cs));
+  } else {
+    const float *f[8] = {p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb};
+    for (int k = 0; k < 8; ++k) {
+      if (!f[k]) continue;
+      if ((st = ensure(q.soa[k], n * 4))) return st;
+      if (n > 0) SPL_CK(cudaMemcpyAsync(q.soa[k].p, f[k], n * 4, cudaMemcpyHostToDevice, cs));
+    }
+    if (p->type) {
+      if ((st = ensure(q.soa[8], n * 2))) return st;
+      if (n > 0) SPL_CK(cudaMemcpyAsync(q.soa[8].p, p->type, n * 2, cudaMemcpyHostToDevice, cs));
+    }
+  }
+  SPL_CK(cudaEventRecord(q.ready, cs));
+  host_keys(p, q.host);
+  q.n = n;
+  q.layout = p->layout;
+  q.queued = true;
+  c->pf_fifo[c->pf_len++] = slot;
   return SPL_OK;
 }
 
@@ -716,6 +839,7 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
   cudaEventElapsedTime(&S.bwd_splat_ms, c->ev[1], c->ev[2]);
   cudaEventElapsedTime(&S.bwd_project_ms, c->ev[2], c->ev[3]);
   cudaEventElapsedTime(&S.bwd_total_ms, c->ev[0], c->ev[4]);
+  if (c->pf_in_use >= 0) cudaEventRecord(c->pf[c->pf_in_use].freed, c->stream);
   return SPL_OK;
 }
 
