@@ -77,6 +77,27 @@ def test_batch_equals_plain_frames_fixed_tile(renderer):
         b.close()
 
 
+def test_batch_mixed_orders_and_palettes(renderer):
+    """Ordered frames compositing front-to-back and back-to-front in one batch
+    (the splat queue chooses the form per item), and a set whose frames do not
+    all share a palette (no per-set palette cache for it)."""
+    bw = synth.batched(n_sets=4, poses=3, scale=0.004, resolutions=SMALL_RES)
+    for i, (s, params, rc) in enumerate(bw.frames):
+        if not params.params["a_eq_e"] and i % 2:
+            params.params["gpu_order"] = "btf"
+        if s == 0 and i % 3 == 1:  # another palette for one frame of set 0
+            rc.amap = [synth.five_stop_palette(), None]
+    sets = _device_sets(bw)
+    b, frames, _ = _batch(renderer, bw, sets, tile_size=16, splat_config_additive=2,
+                          splat_config_absorption=2)
+    try:
+        b.render()
+        torch.cuda.synchronize()
+        _check_equal_plain(renderer, sets, frames, b.info())
+    finally:
+        b.close()
+
+
 def test_batch_autotuned_matches_plain_and_oracle(renderer, port):
     bw = synth.batched(n_sets=2, poses=2, scale=0.003, resolutions=SMALL_RES)
     sets = _device_sets(bw)
