@@ -277,6 +277,8 @@ struct spl_batch {
   spl_context *ctx = nullptr;
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;              // the ordered class's splat queue
+  cudaEvent_t fork = nullptr, join = nullptr;  // stream <-> stream2 (no timing)
   std::vector<spl_particles> sets;
   std::vector<spl_batch_frame> frames;  // descs point at the palette copies below
   std::vector<std::vector<double>> pal_x_copy;
@@ -764,11 +766,23 @@ spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
                         as<uint32_t>(b->work_tmp), as<uint32_t>(b->tcost_s),
                         as<uint32_t>(b->work), b->ntiles, 0, 9, false, b->radix_scr.p, s,
                         &launches, err, true);
-  // ---- splat: one persistent launch per class ---------------------------------------------
-  if (splat_class == -1 || splat_class == 0)
+  // ---- splat: one persistent launch per class; with both classes the ordered
+  //      queue runs on a second stream, so that its CTAs start on the SMs the
+  //      additive queue's CTAs leave as that queue drains -------------------------
+  const bool both = splat_class == -1 && b->n_add_tiles > 0 && b->ntiles > b->n_add_tiles;
+  if (both) {
+    BCK(cudaEventRecord(b->fork, s));
+    BCK(cudaStreamWaitEvent(b->stream2, b->fork, 0));
     launches += spl::launch_splat_queue(queue_args(b, 0), b->cfg_add, s);
-  if (splat_class == -1 || splat_class == 1)
-    launches += spl::launch_splat_queue(queue_args(b, 1), b->cfg_abs, s);
+    launches += spl::launch_splat_queue(queue_args(b, 1), b->cfg_abs, b->stream2);
+    BCK(cudaEventRecord(b->join, b->stream2));
+    BCK(cudaStreamWaitEvent(s, b->join, 0));
+  } else {
+    if (splat_class == -1 || splat_class == 0)
+      launches += spl::launch_splat_queue(queue_args(b, 0), b->cfg_add, s);
+    if (splat_class == -1 || splat_class == 1)
+      launches += spl::launch_splat_queue(queue_args(b, 1), b->cfg_abs, s);
+  }
   BCK(cudaMemcpyAsync(b->h_status, status, 32, cudaMemcpyDeviceToHost, s));
   BCK(cudaMemcpyAsync(b->h_entries, off + capA, 8, cudaMemcpyDeviceToHost, s));
   b->launches = launches;
@@ -924,6 +938,9 @@ void free_batch(spl_batch *b) {
   if (b->h_entries) cudaFreeHost(b->h_entries);
   if (b->ev0) cudaEventDestroy(b->ev0);
   if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->stream2) cudaStreamDestroy(b->stream2);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -976,6 +993,9 @@ spl_status spl_batch_create(spl_context *ctx, const spl_particles *sets, int nse
   cudaSetDevice(b->device);
   spl_status st = SPL_OK;
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
       cudaMallocHost((void **)&b->h_status, 64) != cudaSuccess ||
       cudaMallocHost((void **)&b->h_entries, 8) != cudaSuccess) {
