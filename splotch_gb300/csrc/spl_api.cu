@@ -31,7 +31,7 @@ struct spl_context {
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
       poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes,
-      seg_cnt, seg_off;
+      seg_cnt, seg_off, seg_state;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
   // state of the last frame (for the debug getters)
@@ -351,7 +351,7 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->col_c, &c->idx_c, &c->pstate, &c->poff, &c->gpic,
                               &c->gpos_c, &c->gcol_c, &c->camsum, &c->aux, &c->post_tab,
                               &c->post_bar, &c->post_img, &c->post_bytes, &c->seg_cnt,
-                              &c->seg_off};
+                              &c->seg_off, &c->seg_state};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   for (auto &b : c->soa_in)
@@ -771,9 +771,15 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
       dev[k] = as<float>(c->gout[k]);
     }
   }
+  // split ordered tiles: (U, V) per segment and tile pixel, 32 B
+  size_t seg_state_bytes = 16;
+  if (!f.a_eq_e)
+    seg_state_bytes = (size_t)(c->ntiles + c->ne / spl::adjoint_seg_len(f, c->ne) + 1) *
+                      (size_t)(f.T * f.T) * 32;
   if ((st = ensure(c->gpos_c, na * 16)) || (st = ensure(c->gcol_c, na * 16)) ||
       (st = ensure(c->camsum, 5 * 8)) || (st = ensure(c->seg_cnt, c->ntiles * 4 + 4)) ||
       (st = ensure(c->seg_off, (c->ntiles + 1) * 8)) ||
+      (st = ensure(c->seg_state, seg_state_bytes)) ||
       (st = ensure(c->scratch, spl::scan_scratch_bytes(c->ntiles + 1))))
     return st;
   const float *gpic_d = gp->pic;
@@ -799,6 +805,8 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
     aa.seg_cnt = as<uint32_t>(c->seg_cnt);
     aa.seg_off = as<uint64_t>(c->seg_off);
     aa.scan_scratch = c->scratch.p;
+    aa.seg_state = as<float4>(c->seg_state);
+    aa.seg_state_cap = c->seg_state.cap / 16;
     spl::launch_splat_adjoint(aa, s);
   }
   cudaEventRecord(c->ev[2], s);

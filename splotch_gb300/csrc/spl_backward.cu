@@ -117,7 +117,9 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
   }
   const int tile = f.tile_order ? (int)__ldg(f.tile_order + o) : o;
   const uint32_t tile_end = f.tile_start[tile + 1];
-  const uint32_t start = f.tile_start[tile] + (uint32_t)(item - a.seg_off[o]) * a.seg_len;
+  const uint32_t kseg = (uint32_t)(item - a.seg_off[o]);  // segment within the tile
+  const uint32_t rel0 = kseg * a.seg_len;                  // its first list position
+  const uint32_t start = f.tile_start[tile] + rel0;
   const uint32_t end = (uint32_t)min((uint64_t)tile_end, (uint64_t)start + a.seg_len);
 
   const int ix = tile % f.ncx, iy = tile / f.ncx;
@@ -181,11 +183,47 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
     }
   }
 
+  // A later segment of a split ordered tile starts from the state the walk
+  // would have reached: per earlier segment i (back to front) its optical depth
+  // U_i and its own back-to-front composite V_i (k_adj_ordered_state), so
+  // sb = sum U_i and bg = sum Tr_i*V_i with Tr_i = exp(-(od - sb after i)).
+  if (!ADD && kseg > 0) {
+    const float4 *st = a.seg_state + (size_t)a.seg_off[o] * (size_t)(T * T) * 2;
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+      float sbv[2][3] = {}, nbv[2][3] = {};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = 2 * p + h;
+        if (k >= K || row[k < K ? k : 0] == 255) continue;
+        const int px = (col[k] * T + row[k]) * 2;
+        const float odv[3] = {h ? f2hi(od[ADD ? 0 : p][0]) : f2lo(od[ADD ? 0 : p][0]),
+                              h ? f2hi(od[ADD ? 0 : p][1]) : f2lo(od[ADD ? 0 : p][1]),
+                              h ? f2hi(od[ADD ? 0 : p][2]) : f2lo(od[ADD ? 0 : p][2])};
+        for (uint32_t i = 0; i < kseg; ++i) {
+          const float4 U = __ldg(st + (size_t)i * (T * T) * 2 + px);
+          const float4 V = __ldg(st + (size_t)i * (T * T) * 2 + px + 1);
+          const float u3[3] = {U.x, U.y, U.z}, v3[3] = {V.x, V.y, V.z};
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            sbv[h][c] += u3[c];
+            nbv[h][c] = fmaf(-ex2((sbv[h][c] - odv[c]) * kLog2e), v3[c], nbv[h][c]);
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sb[ADD ? 0 : p][c] = f2(sbv[0][c], sbv[1][c]);
+        nbg[ADD ? 0 : p][c] = f2(nbv[0][c], nbv[1][c]);
+      }
+    }
+  }
+
   const int nbatch = (int)((end - start + B - 1) / B);
   // Ordered frames: the forward composited, per warp, list positions
-  // [stop, end) (a multiple of B); walk exactly those, in list order (back to
-  // front).  An ordered tile is one segment.  Additive frames: the whole
-  // segment.
+  // [stop, end) of the tile (stop a multiple of B); walk exactly those, in list
+  // order (back to front).  Positions are compared relative to the tile's
+  // list start (the segment starts at rel0).
   __shared__ uint32_t s_first;
   uint32_t wstop = 0;
   if (!ADD) {
@@ -195,7 +233,8 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
     if (lane == 0 && warp_has_pixels) atomicMin(&s_first, wstop);
     __syncthreads();
   }
-  const int b_first = ADD ? 0 : (int)min((uint32_t)nbatch, s_first / (uint32_t)B);
+  const int b_first =
+      ADD ? 0 : (int)min((uint32_t)nbatch, s_first > rel0 ? (s_first - rel0) / (uint32_t)B : 0u);
   const bool warp_idle = !warp_has_pixels;
 
   for (int bi = b_first; bi < nbatch; ++bi) {
@@ -219,7 +258,7 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
     }
     __syncthreads();
     // ---- per-fragment adjoint ----------------------------------------------
-    if (!warp_idle && (ADD || (uint32_t)bi * B >= wstop)) {
+    if (!warp_idle && (ADD || rel0 + (uint32_t)bi * B >= wstop)) {
 #pragma unroll 1
       for (int ch = 0; ch < B / 32; ++ch) {
         const bool hit = box_meets_warp(St.bb[ch * 32 + lane], wbx0, wbx1, wby0, wby1);
@@ -326,6 +365,133 @@ __global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
   }
 }
 
+// Pass 1 for split ordered tiles: for every segment but a tile's last, per
+// pixel, the optical depth U of the fragments the forward composited in it
+// and their own back-to-front composite V (V <- V*T + q*(1-T), from 0), into
+// seg_state[segment][pixel] = (U, V).  Same item mapping and pixel layout as
+// k_splat_adj.
+template <int NT, int WX, int WY, int B>
+__global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
+  constexpr int K = WX * WY;
+  constexpr int NP = (K + 1) / 2;
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  Stage<B> &St = *reinterpret_cast<Stage<B> *>(smem_raw);
+  uint16_t *srun = reinterpret_cast<uint16_t *>(smem_raw + sizeof(Stage<B>));
+  const SplatArgs &f = a.f;
+  const int T = f.T, RS = run_stride(T);
+  const uint64_t item = blockIdx.x;
+  if (item >= a.seg_off[a.ntiles]) return;
+  int o = 0, ohi = (int)a.ntiles;
+  while (ohi - o > 1) {
+    const int mid = (o + ohi) >> 1;
+    if (a.seg_off[mid] <= item) o = mid; else ohi = mid;
+  }
+  const uint32_t kseg = (uint32_t)(item - a.seg_off[o]);
+  if (kseg + 1 >= (uint32_t)(a.seg_off[o + 1] - a.seg_off[o])) return;  // last: not needed
+  const int tile = f.tile_order ? (int)__ldg(f.tile_order + o) : o;
+  const uint32_t rel0 = kseg * a.seg_len;
+  const uint32_t start = f.tile_start[tile] + rel0;
+  const uint32_t end = (uint32_t)min((uint64_t)f.tile_start[tile + 1], (uint64_t)start + a.seg_len);
+  const int ix = tile % f.ncx, iy = tile / f.ncx;
+  const int x0s = ix * T, y0s = iy * T;
+  const int tw = min(x0s + T, f.xres) - x0s;
+  const int th = min(y0s + T, f.yres) - y0s;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int nbx = (tw + IW - 1) / IW, nby = (th + IH - 1) / IH;
+  const int nwx = (nbx + WX - 1) / WX, nwy = (nby + WY - 1) / WY;
+  const int wx = w % nwx, wy = w / nwx;
+  const bool warp_has_pixels = wy < nwy;
+  const int wbx0 = wx * WX * IW, wby0 = wy * WY * IH;
+  const int wbx1 = min(wbx0 + WX * IW, tw), wby1 = min(wby0 + WY * IH, th);
+
+  int col[K], row[K];
+  F2 px2[NP], py2[NP], U[NP][3], V[NP][3];
+  uint32_t mystop = 0xffffffffu;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int x = wbx0 + (k % WX) * IW + (lane & 7);
+    const int y = wby0 + (k / WX) * IH + (lane >> 3);
+    const bool valid = warp_has_pixels && x < tw && y < th;
+    col[k] = valid ? x : 0;
+    row[k] = valid ? y : 255;
+    if (valid)
+      mystop = min(mystop, __float_as_uint(
+                               __ldg(f.aux + (size_t)(x0s + x) * f.yres + (y0s + y)).w));
+  }
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int x = wbx0 + ((2 * p) % WX) * IW + (lane & 7);
+    const int y = wby0 + ((2 * p) / WX) * IH + (lane >> 3);
+    px2[p] = f2((float)x, (float)(x + IW));
+    py2[p] = f2((float)y);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) U[p][c] = V[p][c] = f2(0.f);
+  }
+  const uint32_t wstop = __reduce_min_sync(0xffffffffu, mystop);
+  const int nbatch = (int)((end - start + B - 1) / B);
+  for (int bi = 0; bi < nbatch; ++bi) {
+#pragma unroll 1
+    for (int slot = threadIdx.x; slot < B; slot += NT)
+      stage_entry<B, false, false>(St, srun, RS, slot, f, start + (uint32_t)bi * B + slot, end,
+                                   x0s, y0s, tw, th);
+    __syncthreads();
+    if (warp_has_pixels && rel0 + (uint32_t)bi * B >= wstop) {
+#pragma unroll 1
+      for (int ch = 0; ch < B / 32; ++ch) {
+        const bool hit = box_meets_warp(St.bb[ch * 32 + lane], wbx0, wbx1, wby0, wby1);
+        uint32_t mask = __ballot_sync(0xffffffffu, hit);
+        while (mask) {
+          const int bit = __ffs(mask) - 1;
+          mask &= ~(1u << bit);
+          const int j = ch * 32 + bit;
+          const float4 pxy = St.pxy[j], es = St.es[j], e12 = St.e12[j];
+          const float4 q01 = St.q01[j];
+          const float2 q2 = St.q2[j];
+          uint32_t bbj = 0;
+          if (NP > 1) bbj = St.bb[j];
+          const uint16_t *run = srun + j * RS;
+#pragma unroll
+          for (int p = 0; p < NP; ++p) {
+            if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
+                                          wby0 + ((2 * p) / WX) * IH))
+              continue;
+            const bool in0 = covered(run, col[2 * p], row[2 * p]);
+            const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
+            if (!(in0 || in1)) continue;
+            const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
+            const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
+            const F2 arg = mul2(f2(es.z, es.w), fma2(dy, dy, mul2(dx, dx)));
+            const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
+            const F2 e[3] = {f2(es.x, es.y), f2(e12.x, e12.y), f2(e12.z, e12.w)};
+            const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const F2 u = mul2(e[c], att);
+              U[p][c] = add2(U[p][c], u);
+              V[p][c] = fma2(expm1_neg2(u), sub2(V[p][c], q[c]), V[p][c]);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+  float4 *st = a.seg_state + (size_t)item * (size_t)(T * T) * 2;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    if (row[k] == 255) continue;
+    float u3[3], v3[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      u3[c] = (k & 1) ? f2hi(U[k / 2][c]) : f2lo(U[k / 2][c]);
+      v3[c] = (k & 1) ? f2hi(V[k / 2][c]) : f2lo(V[k / 2][c]);
+    }
+    const int px = (col[k] * T + row[k]) * 2;
+    st[px] = make_float4(u3[0], u3[1], u3[2], 0.f);
+    st[px + 1] = make_float4(v3[0], v3[1], v3[2], 0.f);
+  }
+}
+
 template <int NT, int WX, int WY, int B>
 void launch_adj_cfg(const AdjArgs &a, uint32_t grid, cudaStream_t s) {
   const size_t sm = adj_smem_bytes<B>(a.f.T);
@@ -334,6 +500,12 @@ void launch_adj_cfg(const AdjArgs &a, uint32_t grid, cudaStream_t s) {
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, NT, sm, s>>>(a);
   } else {
+    if (a.seg_len != 0xffffffffu) {  // split ordered tiles: the state pass first
+      auto k1 = k_adj_ordered_state<NT, WX, WY, B>;
+      const size_t sm1 = sizeof(Stage<B>) + (size_t)B * run_stride(a.f.T) * 2;
+      cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
+      k1<<<grid, NT, sm1, s>>>(a);
+    }
     auto k = k_splat_adj<NT, WX, WY, B, false>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, NT, sm, s>>>(a);
@@ -491,33 +663,50 @@ __global__ void __launch_bounds__(256) k_project_adj(ProjAdjArgs a) {
 
 }  // namespace
 
+namespace {
+
+// The ordered adjoint walks the forward's warps (it reads where each warp
+// stopped); the additive one takes its own layout, four warps of 16x4
+// pixels, which shares each hit's reduction among 64 pixels.
+int adjoint_cfg(const SplatArgs &f) {
+  const bool add = f.a_eq_e != 0;
+  const int fwd_cfg = f.config >= 0 && splat_config_valid(f.config, f.T)
+                          ? f.config
+                          : splat_default_config(f.T, add);
+  return add && splat_config_valid(2, f.T) ? 2 : fwd_cfg;
+}
+
+}  // namespace
+
+// Segments of about 1/16 of an SM's share of the frame's entries (at least
+// four batches), so that the heaviest tiles spread over many SMs.
+uint32_t adjoint_seg_len(const SplatArgs &f, int64_t n_entries) {
+  const int cfg = adjoint_cfg(f);
+  const int64_t B = (cfg == 1 || cfg == 2) ? 128 : 256;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t per = (n_entries + (int64_t)nsm * 16 - 1) / ((int64_t)nsm * 16);
+  int64_t L = (per + B - 1) / B * B;
+  if (L < 4 * B) L = 4 * B;
+  if (L > 0x40000000) L = 0x40000000;
+  return (uint32_t)L;
+}
+
 int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
   const int64_t ntiles = (int64_t)a0.f.ncx * a0.f.ncy;
   if (ntiles <= 0) return 0;
   AdjArgs a = a0;
   const bool add = a.f.a_eq_e != 0;
   const int T = a.f.T;
-  const int fwd_cfg = a.f.config >= 0 && splat_config_valid(a.f.config, T)
-                          ? a.f.config
-                          : splat_default_config(T, add);
-  // The ordered adjoint walks the forward's warps (it reads where each warp
-  // stopped); the additive one takes its own layout, four warps of 16x4
-  // pixels, which shares each hit's reduction among 64 pixels.
-  const int cfg = add && splat_config_valid(2, T) ? 2 : fwd_cfg;
-  const uint32_t B = (cfg == 1 || cfg == 2) ? 128u : 256u;
-  // Additive tiles: segments of about 1/16 of an SM's share of the frame's
-  // entries (at least four batches), so that the heaviest tiles spread over
-  // many SMs; ordered tiles stay whole.
-  uint32_t seg_len = 0xffffffffu;
-  if (add) {
-    int dev = 0, nsm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    const int64_t per = (a.n_entries + (int64_t)nsm * 16 - 1) / ((int64_t)nsm * 16);
-    int64_t L = (per + B - 1) / B * B;
-    if (L < 4 * (int64_t)B) L = 4 * (int64_t)B;
-    if (L > 0x40000000) L = 0x40000000;
-    seg_len = (uint32_t)L;
+  const int cfg = adjoint_cfg(a.f);
+  uint32_t seg_len = adjoint_seg_len(a.f, a.n_entries);
+  // segments <= sum over tiles of (len / seg_len + 1)
+  int64_t grid64 = ntiles + a.n_entries / seg_len + 1;
+  // ordered tiles split only with room for the state of every segment
+  if (!add && (!a.seg_state || (size_t)grid64 * (size_t)(T * T) * 2 > a.seg_state_cap)) {
+    seg_len = 0xffffffffu;
+    grid64 = ntiles + 1;
   }
   a.ntiles = ntiles;
   a.seg_len = seg_len;
@@ -525,8 +714,6 @@ int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
   int cb = (int)std::min<int64_t>((ntiles + 255) / 256, 152 * 8);
   k_adj_seg_count<<<cb, 256, 0, s>>>(a.f.tile_start, ntiles, seg_len, a.seg_cnt);
   scan_counts(a.seg_cnt, a.f.tile_order, ntiles, a.seg_off, a.scan_scratch, s, &launches);
-  // segments <= sum over tiles of (len / seg_len + 1)
-  const int64_t grid64 = ntiles + (add ? a.n_entries / seg_len + 1 : 0);
   const uint32_t grid = (uint32_t)std::min<int64_t>(grid64, 0x7fffffff);
   switch (cfg) {
     case 0: launch_adj_cfg<256, 1, 1, 256>(a, grid, s); break;
@@ -535,7 +722,7 @@ int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
     case 3: launch_adj_cfg<256, 2, 2, 256>(a, grid, s); break;
     default: launch_adj_cfg<256, 4, 4, 256>(a, grid, s); break;
   }
-  return launches + 1;
+  return launches + (!add && seg_len != 0xffffffffu ? 2 : 1);
 }
 
 int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s) {

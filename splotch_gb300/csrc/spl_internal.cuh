@@ -450,9 +450,10 @@ int launch_splat_queue(const BatchSplatArgs &q, int cfg, cudaStream_t s);
 // Adjoint of the splat: per active particle, sums of dL/dE (gcol.xyz) and of
 // gatt*att*(dx, dy, dx^2+dy^2) (gpos.xyz), accumulated with atomics (zero them
 // first).  f is the forward's argument set, f.pic its final image.
-// The adjoint runs one CTA per segment of a tile's list: additive tiles are
-// cut into segments of seg_len entries (their per-particle sums do not depend
-// on list order), ordered tiles are one segment each.  seg_cnt (ntiles) and
+// The adjoint runs one CTA per segment of a tile's list, seg_len entries each:
+// additive segments are independent (their per-particle sums do not depend on
+// list order); an ordered segment after the first starts from state that a
+// first pass computes for the segments behind it.  seg_cnt (ntiles) and
 // seg_off (ntiles + 1) are scratch for the launch; scan_scratch holds
 // scan_scratch_bytes(ntiles + 1) bytes.
 struct AdjArgs {
@@ -466,7 +467,14 @@ struct AdjArgs {
   void *scan_scratch;
   int64_t ntiles;     // set by the launch
   uint32_t seg_len;   // set by the launch
+  // split ordered tiles: per segment and tile pixel (x*T + y) the pair
+  // (U, V) of k_adj_ordered_state; seg_state_cap float4 entries available
+  float4 *seg_state;
+  size_t seg_state_cap;
 };
+// The list-segment length the adjoint uses for frame f with n_entries bin
+// entries (a multiple of the launch's batch size).
+uint32_t adjoint_seg_len(const SplatArgs &f, int64_t n_entries);
 int launch_splat_adjoint(const AdjArgs &a, cudaStream_t s);
 
 // Chain rule from the splat sums to the inputs (written by particle index;
