@@ -150,6 +150,17 @@ spl_status spl_render(spl_context *ctx, const spl_frame_desc *d,
    arrays must not change between the prefetch and that render; pinned memory
    lets the copy overlap.  Device-memory views need no copy (no-op). */
 spl_status spl_prefetch(spl_context *ctx, const spl_particles *p);
+
+/* Cut heavy tiles into list segments in later spl_render calls (no
+   counterpart in the reference, whose tiles are dynamically scheduled CPU
+   work items): one GPU block per segment instead of per tile, so that a few
+   dense tiles do not keep most of the GPU idle; the segments' results are
+   then folded per pixel in list order.  Applies to additive and front-to-back
+   frames (not to ordered frames kept for spl_render_backward).  Off by
+   default: each pixel's sums are then grouped by segment, which changes
+   float rounding (within the usual tolerance) and so breaks the bit-for-bit
+   equality between spl_render and spl_batch_render frames. */
+spl_status spl_context_set_split_tiles(spl_context *ctx, int enable);
 spl_status spl_get_stats(const spl_context *ctx, spl_stats *s);
 
 /* ---- test hooks: state of the last spl_render (host destinations) ----- */

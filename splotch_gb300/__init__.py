@@ -329,6 +329,12 @@ class Renderer:
         _abi.check(self.lib.spl_get_stats(self.ctx, C.byref(s)))
         return s.as_dict()
 
+    def set_split_tiles(self, enable: bool = True) -> None:
+        """Cut heavy tiles into list segments in later renders (additive and
+        front-to-back frames): one GPU block per segment, results folded per
+        pixel.  Off by default (it regroups each pixel's float sums)."""
+        _abi.check(self.lib.spl_context_set_split_tiles(self.ctx, 1 if enable else 0))
+
     # -- gradients ------------------------------------------------------------
     def set_differentiable(self, enable: bool = True) -> None:
         """Ordered frames keep what spl_render_backward needs (per-pixel optical

@@ -27,7 +27,7 @@ EXPORTED = [
     "spl_render", "spl_get_stats", "spl_debug_get_projected", "spl_debug_get_order",
     "spl_debug_get_bins", "spl_debug_count_fragments", "spl_debug_set_options",
     "spl_splat_config_count", "spl_splat_config_valid", "spl_sort_pairs_noalloc",
-    "spl_prefetch",
+    "spl_prefetch", "spl_context_set_split_tiles",
     "spl_render_backward", "spl_context_set_differentiable", "spl_batch_options_defaults",
     "spl_batch_create", "spl_batch_render", "spl_batch_get_info", "spl_batch_destroy",
     "spl_post_desc_defaults", "spl_postprocess", "spl_image_encode", "spl_write_image",
@@ -174,6 +174,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_splat_config_valid": (C.c_int, [C.c_int, C.c_int]),
         "spl_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, i64, C.c_int, vp]),
         "spl_prefetch": (C.c_int, [vp, C.POINTER(Particles)]),
+        "spl_context_set_split_tiles": (C.c_int, [vp, C.c_int]),
         "spl_render_backward": (C.c_int, [vp, C.POINTER(Image), C.POINTER(Grads)]),
         "spl_context_set_differentiable": (C.c_int, [vp, C.c_int]),
         "spl_batch_options_defaults": (None, [C.POINTER(BatchOptions)]),

@@ -34,6 +34,7 @@ struct spl_context {
       seg_cnt, seg_off, seg_state;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
+  bool split_tiles = false;     // heavy tiles cut into list segments
   // state of the last frame (for the debug getters)
   int64_t n = 0, na = 0, ne = 0, ntiles = 0;
   bool has_order = false, writeback_done = false;
@@ -610,7 +611,35 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     if ((st = ensure(c->aux, (size_t)xres * yres * 16))) return st;
     sa.aux = as<float4>(c->aux);
   }
-  launches += spl::launch_splat(sa, s);
+  // Heavy tiles cut into list segments when asked (additive and front-to-back
+  // frames whose per-pixel data the adjoint does not need)
+  const bool split = c->split_tiles && !sa.aux && (sa.a_eq_e || sa.order_mode == 1) && ntiles > 0;
+  if (split) {
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t B = spl::splat_batch_size(sa);
+    // segments of about 1/16 of an SM's share of the entries, at least 4 batches
+    int64_t L = ((int64_t)ne + (int64_t)nsm * 16 - 1) / ((int64_t)nsm * 16);
+    L = std::max<int64_t>((L + B - 1) / B * B, 4 * B);
+    L = std::min<int64_t>(L, 0x40000000);
+    const int64_t nseg_max = ntiles + (int64_t)ne / L + 1;
+    if ((st = ensure(c->seg_cnt, ntiles * 4 + 4)) || (st = ensure(c->seg_off, (ntiles + 1) * 8)) ||
+        (st = ensure(c->scratch, spl::scan_scratch_bytes(ntiles + 1))) ||
+        (st = ensure(c->seg_state, (size_t)nseg_max * T * T * 32)))
+      return st;
+    spl::SplatSegs sg;
+    sg.seg_off = as<uint64_t>(c->seg_off);
+    sg.ntiles = ntiles;
+    sg.seg_len = (uint32_t)L;
+    sg.partial = as<float4>(c->seg_state);
+    spl::launch_seg_count(sa.tile_start, ntiles, (uint32_t)L, as<uint32_t>(c->seg_cnt), s);
+    spl::scan_counts(as<uint32_t>(c->seg_cnt), sa.tile_order, ntiles, as<uint64_t>(c->seg_off),
+                     c->scratch.p, s, &launches);
+    launches += 1 + spl::launch_splat_split(sa, sg, (uint32_t)std::min<int64_t>(nseg_max, 0x7fffffff), s);
+  } else {
+    launches += spl::launch_splat(sa, s);
+  }
   SPL_CK(cudaGetLastError());
   c->last_splat = sa;
   cudaEventRecord(c->ev[5], s);
@@ -729,6 +758,12 @@ spl_status spl_prefetch(spl_context *c, const spl_particles *p) {
   q.layout = p->layout;
   q.queued = true;
   c->pf_fifo[c->pf_len++] = slot;
+  return SPL_OK;
+}
+
+spl_status spl_context_set_split_tiles(spl_context *c, int enable) {
+  if (!c) return fail(SPL_ERR_INVALID, "null ctx");
+  c->split_tiles = enable != 0;
   return SPL_OK;
 }
 

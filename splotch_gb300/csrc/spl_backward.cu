@@ -725,6 +725,13 @@ int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
   return launches + (!add && seg_len != 0xffffffffu ? 2 : 1);
 }
 
+void launch_seg_count(const uint32_t *tile_start, int64_t ntiles, uint32_t seg_len,
+                      uint32_t *cnt, cudaStream_t s) {
+  if (ntiles <= 0) return;
+  const int cb = (int)std::min<int64_t>((ntiles + 255) / 256, 152 * 8);
+  k_adj_seg_count<<<cb, 256, 0, s>>>(tile_start, ntiles, seg_len, cnt);
+}
+
 int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s) {
   if (a.na <= 0) return 0;
   int blocks = (int)((a.na + 255) / 256);

@@ -422,6 +422,21 @@ struct SplatArgs {
   float4 *aux;
 };
 int launch_splat(const SplatArgs &a, cudaStream_t s);
+// Heavy tiles cut into list segments of seg_len entries (additive and
+// front-to-back frames without the adjoint's aux): seg_off (ntiles + 1, tile
+// order) numbers the segments; partial holds two float4 per tile pixel for
+// every segment of a split tile.  grid >= seg_off[ntiles].
+struct SplatSegs {
+  const uint64_t *seg_off;
+  int64_t ntiles;
+  uint32_t seg_len;
+  float4 *partial;
+};
+int launch_splat_split(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s);
+int splat_batch_size(const SplatArgs &a);  // list entries staged per batch
+// Segments per tile: ceil(len / seg_len), 0 for an empty tile.
+void launch_seg_count(const uint32_t *tile_start, int64_t ntiles, uint32_t seg_len,
+                      uint32_t *cnt, cudaStream_t s);
 int splat_config_count();
 bool splat_config_valid(int cfg, int T);
 int splat_default_config(int T, bool additive);

@@ -52,8 +52,13 @@ size_t smem_bytes(int T) {
 // AUX (ordered frames only): also accumulate each pixel's optical depth and
 // record where the warp stopped, for the adjoint (SplatArgs::aux).
 template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false>
+// [start, end): the part of the tile's list to composite (the whole list, or
+// one segment of a heavy tile).  partial: null to write the tile into the
+// image, else the segment's own result per tile pixel (x*T + y): its
+// composite and its transmittance, two float4.
 __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
-                                           uint8_t *smem_raw) {
+                                           uint8_t *smem_raw, const uint32_t start,
+                                           const uint32_t end, float4 *partial) {
   constexpr int K = WX * WY;
   constexpr int NP = (K + 1) / 2;  // pixel pairs per lane: items (2p, 2p+1)
   static_assert(!(AUX && ADD), "optical depth is kept for ordered frames only");
@@ -106,7 +111,6 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
     }
   }
 
-  const uint32_t start = a.tile_start[tile], end = a.tile_start[tile + 1];
   const int nbatch = (int)((end - start + B - 1) / B);
   bool warp_done = !warp_has_pixels;
 
@@ -206,7 +210,17 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
   // ---- write the tile (pic is x-major: pixel (x,y) at (x*yres + y)*3) ----
 #pragma unroll
   for (int k = 0; k < K; ++k) {
-    if (row[k] != 255) {
+    if (row[k] != 255 && partial) {
+      float v[3], t[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        v[c] = (k & 1) ? f2hi(acc[k / 2][c]) : f2lo(acc[k / 2][c]);
+        t[c] = (k & 1) ? f2hi(tr[k / 2][c]) : f2lo(tr[k / 2][c]);
+      }
+      const int px = (col[k] * T + row[k]) * 2;
+      partial[px] = make_float4(v[0], v[1], v[2], 0.f);
+      partial[px + 1] = make_float4(t[0], t[1], t[2], 0.f);
+    } else if (row[k] != 255) {
       const size_t pix = (size_t)(x0s + col[k]) * a.yres + (y0s + row[k]);
       float v[3], d[3];
 #pragma unroll
@@ -227,7 +241,8 @@ template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX>
 __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const int tile = a.tile_order ? (int)__ldg(a.tile_order + blockIdx.x) : (int)blockIdx.x;
-  splat_tile<NT, WX, WY, B, ADD, FTB, AUX>(a, tile, smem_raw);
+  splat_tile<NT, WX, WY, B, ADD, FTB, AUX>(a, tile, smem_raw, a.tile_start[tile],
+                                           a.tile_start[tile + 1], nullptr);
 }
 
 // Persistent splat over a queue of (frame, tile) items: each CTA takes the
@@ -254,17 +269,82 @@ __global__ void __launch_bounds__(NT) k_splat_queue(BatchSplatArgs q) {
     const uint32_t f = __ldg(q.frame_of_tile + gt);
     const SplatArgs &a = s_args;
     const int tile = (int)(gt - q.tile_base[f]);
+    const uint32_t t0 = a.tile_start[tile], t1 = a.tile_start[tile + 1];
     if (MODE == 0)
-      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw);
+      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw, t0, t1, nullptr);
     else if (MODE == 1)
-      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw);
+      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw, t0, t1, nullptr);
     else if (a.a_eq_e)
-      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw);
+      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw, t0, t1, nullptr);
     else if (a.order_mode == 1)
-      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw);
+      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw, t0, t1, nullptr);
     else
-      splat_tile<NT, WX, WY, B, false, false>(a, tile, smem_raw);
+      splat_tile<NT, WX, WY, B, false, false>(a, tile, smem_raw, t0, t1, nullptr);
     __syncthreads();  // s_item and the staging buffers are reused
+  }
+}
+
+// Heavy tiles cut into list segments (spl_context_set_split_tiles): CTA i of
+// the launch takes segment i, numbered in tile order (SplatSegs::seg_off).  A
+// tile of one segment is rendered into the image directly; each segment of a
+// longer tile writes its own composite and transmittance, and
+// k_splat_combine folds them.
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB>
+__global__ void __launch_bounds__(NT) k_splat_seg(SplatArgs a, SplatSegs g) {
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  const uint64_t item = blockIdx.x;
+  if (item >= g.seg_off[g.ntiles]) return;
+  int o = 0, ohi = (int)g.ntiles;  // seg_off[o] <= item < seg_off[ohi]
+  while (ohi - o > 1) {
+    const int mid = (o + ohi) >> 1;
+    if (g.seg_off[mid] <= item) o = mid; else ohi = mid;
+  }
+  const int tile = a.tile_order ? (int)__ldg(a.tile_order + o) : o;
+  const uint32_t nseg = (uint32_t)(g.seg_off[o + 1] - g.seg_off[o]);
+  const uint32_t k = (uint32_t)(item - g.seg_off[o]);
+  const uint32_t t1 = a.tile_start[tile + 1];
+  const uint32_t s0 = a.tile_start[tile] + k * g.seg_len;
+  const uint32_t s1 = (uint32_t)min((uint64_t)t1, (uint64_t)s0 + g.seg_len);
+  float4 *part = nseg > 1 ? g.partial + item * (size_t)(a.T * a.T) * 2 : nullptr;
+  splat_tile<NT, WX, WY, B, ADD, FTB>(a, tile, smem_raw, s0, s1, part);
+}
+
+// One CTA per tile (tile order): a tile of several segments gets, per pixel,
+// the segments' results folded in list order (back to front): additive
+// C = the parts' sum in order; front-to-back C <- acc_k + tr_k * C.
+template <bool ADD>
+__global__ void __launch_bounds__(256) k_splat_combine(SplatArgs a, SplatSegs g) {
+  const int o = blockIdx.x;
+  const uint32_t nseg = (uint32_t)(g.seg_off[o + 1] - g.seg_off[o]);
+  if (nseg <= 1) return;
+  const int tile = a.tile_order ? (int)__ldg(a.tile_order + o) : o;
+  const int T = a.T;
+  const int ix = tile % a.ncx, iy = tile / a.ncx;
+  const int x0s = ix * T, y0s = iy * T;
+  const int tw = min(x0s + T, a.xres) - x0s;
+  const int th = min(y0s + T, a.yres) - y0s;
+  const float4 *part = g.partial + g.seg_off[o] * (size_t)(T * T) * 2;
+  for (int px = threadIdx.x; px < tw * th; px += blockDim.x) {
+    const int x = px / th, y = px - (px / th) * th;
+    const int lp = (x * T + y) * 2;
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    for (uint32_t k = 0; k < nseg; ++k) {
+      const float4 v = __ldg(part + (size_t)k * (T * T) * 2 + lp);
+      if (ADD) {
+        c0 += v.x;
+        c1 += v.y;
+        c2 += v.z;
+      } else {
+        const float4 t = __ldg(part + (size_t)k * (T * T) * 2 + lp + 1);
+        c0 = fmaf(t.x, c0, v.x);
+        c1 = fmaf(t.y, c1, v.y);
+        c2 = fmaf(t.z, c2, v.z);
+      }
+    }
+    float *out = a.pic + ((size_t)(x0s + x) * a.yres + (y0s + y)) * 3;
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
   }
 }
 
@@ -374,6 +454,52 @@ int launch_splat(const SplatArgs &a, cudaStream_t s) {
     case 3: return launch_cfg<256, 2, 2, 256>(a, s);
     default: return launch_cfg<256, 4, 4, 256>(a, s);
   }
+}
+
+namespace {
+
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB>
+void launch_seg_one(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s) {
+  const size_t sm = smem_bytes<B>(a.T);
+  auto k = k_splat_seg<NT, WX, WY, B, ADD, FTB>;
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  k<<<grid, NT, sm, s>>>(a, g);
+}
+
+template <int NT, int WX, int WY, int B>
+void launch_seg_cfg(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s) {
+  if (a.a_eq_e)
+    launch_seg_one<NT, WX, WY, B, true, false>(a, g, grid, s);
+  else
+    launch_seg_one<NT, WX, WY, B, false, true>(a, g, grid, s);
+}
+
+}  // namespace
+
+int splat_batch_size(const SplatArgs &a) {
+  const int cfg = a.config >= 0 && splat_config_valid(a.config, a.T)
+                      ? a.config
+                      : splat_default_config(a.T, a.a_eq_e != 0);
+  return (cfg == 1 || cfg == 2) ? 128 : 256;
+}
+
+int launch_splat_split(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s) {
+  if (a.ncx * a.ncy <= 0) return 0;
+  const int cfg = a.config >= 0 && splat_config_valid(a.config, a.T)
+                      ? a.config
+                      : splat_default_config(a.T, a.a_eq_e != 0);
+  switch (cfg) {
+    case 0: launch_seg_cfg<256, 1, 1, 256>(a, g, grid, s); break;
+    case 1: launch_seg_cfg<64, 2, 2, 128>(a, g, grid, s); break;
+    case 2: launch_seg_cfg<128, 2, 1, 128>(a, g, grid, s); break;
+    case 3: launch_seg_cfg<256, 2, 2, 256>(a, g, grid, s); break;
+    default: launch_seg_cfg<256, 4, 4, 256>(a, g, grid, s); break;
+  }
+  if (a.a_eq_e)
+    k_splat_combine<true><<<a.ncx * a.ncy, 256, 0, s>>>(a, g);
+  else
+    k_splat_combine<false><<<a.ncx * a.ncy, 256, 0, s>>>(a, g);
+  return 2;
 }
 
 namespace {
