@@ -67,6 +67,8 @@ def parse():
     ap.add_argument("--large-scale", type=float, default=1.0)
     ap.add_argument("--large-steps", type=int, default=2)
     ap.add_argument("--fwd-bwd-particles", type=int, default=4_000_000)
+    ap.add_argument("--split-tiles", action="store_true",
+                    help="cut heavy tiles into list segments in the main workload's frames")
     ap.add_argument("--scale", type=float, default=1.0,
                     help="particle-count multiplier (profiling runs use a smaller frame)")
     return ap.parse_args()
@@ -444,6 +446,19 @@ def batched(args, local: int) -> dict:
         for k in stage_keys:
             plain_stages[k] += float(st[k])
     out["plain_stage_ms_sum"] = {k: round(v, 3) for k, v in plain_stages.items()}
+    # the plain path with heavy tiles cut into list segments (an option, off by
+    # default), timed the same way
+    r.set_split_tiles(True)
+    plain_pass()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        plain_pass()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    r.set_split_tiles(False)
+    out["plain_split_tiles_ms"] = e0.elapsed_time(e1) / reps
+    out["plain_split_tiles_frames_per_s"] = nf / (out["plain_split_tiles_ms"] * 1e-3)
 
     t0 = time.perf_counter()
     b = sg.Batch(r, sets, frames)
@@ -499,6 +514,9 @@ def run_gpu(args):
     cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
     n = len(w.particles)
     r = sg.Renderer(local)
+    if args.split_tiles:
+        r.set_split_tiles(True)
+        cfg["split_tiles"] = True
     stream = torch.cuda.Stream()
     r.set_stream(stream.cuda_stream)
     keep: list = []
