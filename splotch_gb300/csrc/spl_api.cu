@@ -633,7 +633,12 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     sg.ntiles = ntiles;
     sg.seg_len = (uint32_t)L;
     sg.partial = as<float4>(c->seg_state);
-    spl::launch_seg_count(sa.tile_start, ntiles, (uint32_t)L, as<uint32_t>(c->seg_cnt), s);
+    // a front-to-back tile is split only when it dominates the frame (8x the
+    // mean list): its segments lose early termination across segment bounds
+    const int64_t split_min = sa.a_eq_e ? L : std::max<int64_t>(L, 8 * ((int64_t)ne / ntiles));
+    spl::launch_seg_count(sa.tile_start, ntiles, (uint32_t)L,
+                          (uint32_t)std::min<int64_t>(split_min, 0xffffffffLL),
+                          as<uint32_t>(c->seg_cnt), s);
     spl::scan_counts(as<uint32_t>(c->seg_cnt), sa.tile_order, ntiles, as<uint64_t>(c->seg_off),
                      c->scratch.p, s, &launches);
     launches += 1 + spl::launch_splat_split(sa, sg, (uint32_t)std::min<int64_t>(nseg_max, 0x7fffffff), s);
