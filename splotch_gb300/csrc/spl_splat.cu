@@ -304,7 +304,8 @@ __global__ void __launch_bounds__(NT) k_splat_seg(SplatArgs a, SplatSegs g) {
   const uint32_t k = (uint32_t)(item - g.seg_off[o]);
   const uint32_t t1 = a.tile_start[tile + 1];
   const uint32_t s0 = a.tile_start[tile] + k * g.seg_len;
-  const uint32_t s1 = (uint32_t)min((uint64_t)t1, (uint64_t)s0 + g.seg_len);
+  // a tile of one segment is its whole list (it may be longer than seg_len)
+  const uint32_t s1 = nseg == 1 ? t1 : (uint32_t)min((uint64_t)t1, (uint64_t)s0 + g.seg_len);
   float4 *part = nseg > 1 ? g.partial + item * (size_t)(a.T * a.T) * 2 : nullptr;
   splat_tile<NT, WX, WY, B, ADD, FTB>(a, tile, smem_raw, s0, s1, part);
 }
