@@ -641,6 +641,9 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
                           as<uint32_t>(c->seg_cnt), s);
     spl::scan_counts(as<uint32_t>(c->seg_cnt), sa.tile_order, ntiles, as<uint64_t>(c->seg_off),
                      c->scratch.p, s, &launches);
+    // the counts are consumed: the same words become the per-tile opaque flags
+    sg.opaque = as<uint32_t>(c->seg_cnt);
+    SPL_CK(cudaMemsetAsync(c->seg_cnt.p, 0, ntiles * 4, s));
     launches += 1 + spl::launch_splat_split(sa, sg, (uint32_t)std::min<int64_t>(nseg_max, 0x7fffffff), s);
   } else {
     launches += spl::launch_splat(sa, s);

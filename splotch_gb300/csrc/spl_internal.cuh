@@ -431,6 +431,7 @@ struct SplatSegs {
   int64_t ntiles;
   uint32_t seg_len;
   float4 *partial;
+  uint32_t *opaque;  // per tile (tile order), zero before the launch
 };
 int launch_splat_split(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s);
 int splat_batch_size(const SplatArgs &a);  // list entries staged per batch

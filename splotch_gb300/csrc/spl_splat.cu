@@ -55,10 +55,14 @@ template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false>
 // [start, end): the part of the tile's list to composite (the whole list, or
 // one segment of a heavy tile).  partial: null to write the tile into the
 // image, else the segment's own result per tile pixel (x*T + y): its
-// composite and its transmittance, two float4.
+// composite and its transmittance, two float4.  opaque (front-to-back
+// segments, may be null): a per-tile flag that the tile's front segment sets
+// once all its pixels are opaque, after which the segments behind it stop.
 __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
                                            uint8_t *smem_raw, const uint32_t start,
-                                           const uint32_t end, float4 *partial) {
+                                           const uint32_t end, float4 *partial,
+                                           uint32_t *opaque = nullptr, bool front = false) {
+  __shared__ uint32_t s_opaque;
   constexpr int K = WX * WY;
   constexpr int NP = (K + 1) / 2;  // pixel pairs per lane: items (2p, 2p+1)
   static_assert(!(AUX && ADD), "optical depth is kept for ordered frames only");
@@ -121,7 +125,12 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
     for (int slot = threadIdx.x; slot < B; slot += NT)
       stage_entry<B, ADD, FTB>(S, srun, RS, slot, a, start + (uint32_t)bi * B + slot, end, x0s,
                                y0s, tw, th);
+    if (FTB && opaque && threadIdx.x == 0)
+      s_opaque = *reinterpret_cast<volatile uint32_t *>(opaque);
     __syncthreads();
+    // the segment in front made every pixel opaque: what lies behind is
+    // weighted below ftb_eps (this segment's partial is folded behind it)
+    if (FTB && opaque && !front && s_opaque) break;
     // ---- accumulate ---------------------------------------------------------
     if (!warp_done) {
 #pragma unroll 1
@@ -201,7 +210,10 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
       }
     }
     if (FTB) {
-      if (__syncthreads_and(warp_done ? 1 : 0)) break;
+      if (__syncthreads_and(warp_done ? 1 : 0)) {
+        if (front && opaque && threadIdx.x == 0) *reinterpret_cast<volatile uint32_t *>(opaque) = 1u;
+        break;
+      }
     } else {
       __syncthreads();
     }
@@ -302,12 +314,17 @@ __global__ void __launch_bounds__(NT) k_splat_seg(SplatArgs a, SplatSegs g) {
   const int tile = a.tile_order ? (int)__ldg(a.tile_order + o) : o;
   const uint32_t nseg = (uint32_t)(g.seg_off[o + 1] - g.seg_off[o]);
   const uint32_t k = (uint32_t)(item - g.seg_off[o]);
+  // front-to-back: the front segment (last in list order) takes the first
+  // item of its tile, so that it starts first and can stop the others early
+  const uint32_t ls = (FTB && nseg > 1) ? nseg - 1 - k : k;  // segment in list order
   const uint32_t t1 = a.tile_start[tile + 1];
-  const uint32_t s0 = a.tile_start[tile] + k * g.seg_len;
+  const uint32_t s0 = a.tile_start[tile] + ls * g.seg_len;
   // a tile of one segment is its whole list (it may be longer than seg_len)
   const uint32_t s1 = nseg == 1 ? t1 : (uint32_t)min((uint64_t)t1, (uint64_t)s0 + g.seg_len);
-  float4 *part = nseg > 1 ? g.partial + item * (size_t)(a.T * a.T) * 2 : nullptr;
-  splat_tile<NT, WX, WY, B, ADD, FTB>(a, tile, smem_raw, s0, s1, part);
+  float4 *part =
+      nseg > 1 ? g.partial + (g.seg_off[o] + ls) * (size_t)(a.T * a.T) * 2 : nullptr;
+  uint32_t *opq = (FTB && nseg > 1) ? g.opaque + o : nullptr;
+  splat_tile<NT, WX, WY, B, ADD, FTB>(a, tile, smem_raw, s0, s1, part, opq, ls == nseg - 1);
 }
 
 // One CTA per tile (tile order): a tile of several segments gets, per pixel,
