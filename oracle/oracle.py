@@ -36,13 +36,13 @@ PARTICLE_DTYPE = np.dtype({
 def build_port(force: bool = False) -> Path:
     """Compile spl_oracle.c (plain C, OpenMP, no fused multiply-add)."""
     BUILD.mkdir(exist_ok=True)
-    src = HERE / "spl_oracle.c"
+    srcs = [HERE / "spl_oracle.c", HERE / "spl_oracle_rays.c"]
     hdr = HERE / "spl_oracle.h"
-    if (not force and PORT_LIB.exists()
-            and PORT_LIB.stat().st_mtime >= max(src.stat().st_mtime, hdr.stat().st_mtime)):
+    newest = max(f.stat().st_mtime for f in srcs + [hdr])
+    if not force and PORT_LIB.exists() and PORT_LIB.stat().st_mtime >= newest:
         return PORT_LIB
     cmd = ["gcc", "-O2", "-std=c11", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           str(src), "-o", str(PORT_LIB), "-lm"]
+           *[str(s) for s in srcs], "-o", str(PORT_LIB), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
         raise RuntimeError(f"oracle build failed:\n{r.stderr}")
@@ -73,6 +73,10 @@ class SpoCamera(C.Structure):
     _fields_ = [("mat", C.c_float * 12), ("res2", C.c_float), ("ycorr", C.c_float),
                 ("fovfct", C.c_float), ("xfac", C.c_float), ("xshift", C.c_double),
                 ("yshift", C.c_double)]
+
+
+class SpoRaysParams(C.Structure):
+    _fields_ = [("dome", C.c_int), ("fov", C.c_double), ("minrad_pix", C.c_double)]
 
 
 class SpoNormParams(C.Structure):
@@ -201,6 +205,7 @@ class Port:
             ("spo_postprocess", i32, [vp, vp, vp, i32, i32]),
             ("spo_image_bytes", i64, [vp, i32, i32, i32, vp, i64]),
             ("spo_particle_normalize", i32, [vp, vp, i64, vp]),
+            ("spo_render_rays", i32, [vp, vp, vp, i64, i32, vp, vp, vp]),
         ]:
             f = getattr(lib, name)
             f.restype = res
@@ -287,6 +292,29 @@ class Port:
         self.lib.spo_postprocess(C.byref(prm), C.byref(post), _vp(out), out.shape[0],
                                  out.shape[1])
         return out
+
+    def render_rays(self, params: dict, rc, p: np.ndarray, exact: bool = True):
+        """host_rendering with new_renderer=true (new_renderer.cc:522-641) on a
+        copy of p.  Returns (image, stats): float64 with exact exp and double
+        sums when exact, else float32 in the reference's arithmetic."""
+        keep: list = []
+        prm = make_params(params, rc, keep)
+        rp = SpoRaysParams(dome=1 if _get(params, "dome", False) else 0,
+                           fov=_get(params, "fov", 45.0),
+                           minrad_pix=_get(params, "minrad_pix", 1.0))
+        q = np.ascontiguousarray(p).copy()
+        shape = (prm.xres, prm.yres, 3)
+        pic = None if exact else np.zeros(shape, np.float32)
+        pic64 = np.zeros(shape, np.float64) if exact else None
+        stats = np.zeros(5, np.int64)
+        rc_ = self.lib.spo_render_rays(C.byref(prm), C.byref(rp), _vp(q), len(q), int(exact),
+                                       _vp(pic), _vp(pic64), _vp(stats))
+        if rc_ == -1:
+            raise ValueError("inconsistent: the ray-sphere renderer needs a_eq_e")
+        if rc_ == -2:
+            raise ValueError("inconsistency: a dome needs xres == yres")
+        names = ("n_used", "n_grid", "n_overlap", "levels", "fragments")
+        return (pic64 if exact else pic), dict(zip(names, (int(v) for v in stats)))
 
     def particle_normalize(self, params: dict, p: np.ndarray) -> dict:
         """In place on particle_sim records; returns the per-type ranges it

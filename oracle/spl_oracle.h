@@ -210,6 +210,25 @@ typedef struct {
 int spo_particle_normalize(const spo_norm_params *np, spo_particle *p, int64_t n,
                            spo_norm_out *out);
 
+/* ---- host_rendering_new: the ray-sphere renderer -------------------------
+   splotch/new_renderer.cc:522-641, selected by new_renderer=true
+   (splotch/splotch_host.cc:714-723).  Reads xres, yres, zmax, ptypes,
+   brightness, color_is_vector, palettes, b_brightness and the camera vectors
+   from prm; fov and minrad_pix come from rp because this renderer reads them
+   as double.  p is changed as the reference changes it before emptying its
+   vector (I, r, active, e).  exact = 0: the reference's arithmetic into pic
+   (float); exact = 1: exact exp and double sums into pic64.  stats (may be
+   NULL): particles used, particles on the level grids, spheres around the
+   camera, levels, covered (pixel, particle) pairs.  Returns -1 when !a_eq_e,
+   -2 for a dome with xres != yres. */
+typedef struct {
+  int dome;          /* "dome" (false) */
+  double fov;        /* "fov" (45) */
+  double minrad_pix; /* "minrad_pix" (1) */
+} spo_rays_params;
+int spo_render_rays(const spo_params *prm, const spo_rays_params *rp, spo_particle *p,
+                    int64_t n, int exact, float *pic, double *pic64, int64_t *stats);
+
 #ifdef __cplusplus
 }
 #endif

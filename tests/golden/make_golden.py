@@ -6,7 +6,8 @@ render_new and host_rendering on small seeded inputs, and stores inputs and
 outputs under tests/golden/*.npz.  The CPU tests pin the oracle restatement to
 these files; the GPU tests compare the CUDA path with them.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py          # every fixture
+    python tests/golden/make_golden.py rays     # the ray-sphere renderer's only
 """
 from __future__ import annotations
 
@@ -48,6 +49,9 @@ def main() -> int:
     if not oracle.build_ref():
         print("reference sources not available; fixtures unchanged")
         return 1
+    if sys.argv[1:] == ["rays"]:
+        rays_cases(oracle.Ref(scalar=False), oracle.Ref(scalar=True), oracle.Port())
+        return 0
     refs = {"simd": oracle.Ref(scalar=False), "scalar": oracle.Ref(scalar=True)}
     port = oracle.Port()
     for name, w in cases():
@@ -81,7 +85,72 @@ def main() -> int:
               f"{frags} fragments")
     post_cases(refs["simd"])
     norm_cases(refs["simd"])
+    rays_cases(refs["simd"], refs["scalar"], port)
     return 0
+
+
+def with_camera_spheres(w, k: int, seed: int):
+    """k particles moved next to the camera with radii that enclose it: the
+    spheres host_rendering_new renders through add_overlap2."""
+    p = w.particles
+    rng = np.random.default_rng(seed)
+    cam = np.asarray(w.rc.campos, np.float64)
+    for i in rng.choice(len(p), k, replace=False):
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        dist = rng.uniform(0.5, 5.0)
+        p["x"][i], p["y"][i], p["z"][i] = cam + d * dist
+        p["r"][i] = dist * rng.uniform(0.3, 2.0)
+    return w
+
+
+def rays_inputs():
+    """Seeded frames for host_rendering with new_renderer=true
+    (new_renderer.cc:522-641): plane and dome projectors, spheres around the
+    camera, a tilted camera with centerpos != campos, a distance cut and two
+    particle types, and a grid smaller than one leaf region."""
+    w = with_camera_spheres(synth.plain_additive(n=4000, xres=96, yres=80, tile=16, seed=21), 6,
+                            31)
+    w.params.params.update({"fov": "33.3", "minrad_pix": "1.5"})
+    yield "rays_plane", w
+    w = with_camera_spheres(synth.plain_additive(n=4000, xres=72, tile=16, seed=22), 6, 32)
+    w.rc.sky = np.array([0.1, 2.0, 0.3])
+    w.params.params.update({"dome": "T"})
+    yield "rays_dome", w
+    w = synth.plain_absorption(n_gas=3000, n_star=1000, xres=80, yres=64, tile=16, seed=23)
+    w.rc.campos = np.array([620.0, 430.0, -180.0])
+    w.rc.centerpos = np.array([600.0, 420.0, -170.0])
+    w.rc.lookat = np.array([250.0, 240.0, 260.0])
+    w.rc.sky = np.array([0.1, 1.0, 0.2])
+    w.rc.b_brightness = 0.7
+    w.params.params.update({"a_eq_e": "T", "zmax": "900.0", "brightness1": "2.0",
+                            "fov": "41.5"})
+    yield "rays_two_types", w
+    w = synth.plain_additive(n=1500, xres=7, yres=5, tile=16, seed=24)
+    yield "rays_tiny", w
+
+
+def rays_cases(ref, ref_scalar, port) -> None:
+    """The reference's own host_rendering_new (both compiled branches) and the
+    FP64 restatement on the same inputs."""
+    for name, w in rays_inputs():
+        prm = dict(w.params.params)
+        prm["new_renderer"] = "T"
+        rc: RenderContext = w.rc
+        out = {"particles_in": w.particles.view(np.uint8).copy()}
+        out["host_rendering_simd"] = ref.host_rendering(prm, rc, w.particles.copy())
+        out["host_rendering_scalar"] = ref_scalar.host_rendering(prm, rc, w.particles.copy())
+        pic64, st = port.render_rays(prm, rc, w.particles, exact=True)
+        out["render_fp64"] = pic64
+        out["stats"] = np.array([st[k] for k in ("n_used", "n_grid", "n_overlap", "levels",
+                                                 "fragments")])
+        meta = {"params": prm, "campos": list(rc.campos), "centerpos": list(rc.centerpos),
+                "lookat": list(rc.lookat), "sky": list(rc.sky), "b_brightness": rc.b_brightness,
+                "palettes": [None if p is None else {"x": p.x.tolist(), "rgb": p.rgb.tolist()}
+                             for p in rc.amap]}
+        out["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+        np.savez_compressed(OUT / f"{name}.npz", **out)
+        print(f"{name}: {len(w.particles)} particles, {st}")
 
 
 NORM_VARIANTS = {

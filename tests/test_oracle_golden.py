@@ -16,7 +16,7 @@ from splotch_gb300 import Palette, RenderContext
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 CASES = sorted(p.stem for p in GOLDEN.glob("*.npz")
-               if not p.stem.startswith(("post_", "norm_")))
+               if not p.stem.startswith(("post_", "norm_", "rays_")))
 X86 = platform.machine() in ("x86_64", "AMD64")
 
 
