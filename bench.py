@@ -62,7 +62,10 @@ def parse():
     ap.add_argument("--batch-scale", type=float, default=1.0,
                     help="particle-count multiplier of the batched workload")
     ap.add_argument("--batch-steps", type=int, default=3)
-    ap.add_argument("--only", default="all", choices=["all", "fwd_bwd", "batched", "large"],
+    ap.add_argument("--no-rays", action="store_true")
+    ap.add_argument("--rays-particles", type=int, default=1_000_000)
+    ap.add_argument("--only", default="all",
+                    choices=["all", "fwd_bwd", "batched", "large", "rays"],
                     help="run one section alone (profiling; 'large' runs only this way)")
     ap.add_argument("--large-scale", type=float, default=1.0)
     ap.add_argument("--large-steps", type=int, default=2)
@@ -323,6 +326,86 @@ def fwd_bwd(args, local: int) -> dict:
     return out
 
 
+def rays(args, local: int) -> dict:
+    """The ray-sphere renderer (host_rendering with new_renderer=true,
+    splotch/new_renderer.cc:522-641) on the plain additive frame's particles
+    (halo mixture in [0,100]^3, fov 30): the 800x800 plane view, the 800x800
+    dome (fisheye) view, and the 1920x1080 plane view.  value: SoA inputs
+    resident in HBM, CUDA events on the render stream; e2e: particle_sim
+    records from pinned host memory and the image back, per frame; cpu: the
+    oracle's restatement in the reference's arithmetic (bit-exact with it) on
+    all host cores, on the whole frame."""
+    import torch
+
+    import splotch_gb300 as sg
+    from oracle.oracle import Port
+    from splotch_gb300 import synth
+
+    dev = f"cuda:{local}"
+    n = int(args.rays_particles * min(args.scale, 1.0))
+    port = Port()
+    out = {}
+    for name, extra in (("plane_800", {}), ("dome_800", {"dome": "T"}),
+                        ("plane_1920x1080", {"xres": "1920", "yres": "1080"})):
+        w = synth.plain_additive(n=n, seed=0)
+        prm = dict(w.params.params, new_renderer="T", **extra)
+        pf = sg.ParamFile(dict(prm))
+        keep: list = []
+        desc = sg.frame_desc(pf, w.rc, keep)
+        rd = sg.rays_desc(pf)
+        r = sg.Renderer(local)
+        stream = torch.cuda.Stream(device=dev)
+        r.set_stream(stream.cuda_stream)
+        soa = {k: torch.from_numpy(v).to(dev) for k, v in synth.soa_from_aos(w.particles).items()}
+        pic = torch.zeros((desc.xres, desc.yres, 3), dtype=torch.float32, device=dev)
+        for _ in range(args.warmup):
+            r.render_rays(desc, rd, soa, pic, device=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        stages = {k: 0.0 for k in ("project_ms", "sort_ms", "bin_ms", "splat_ms")}
+        e0.record(stream)
+        for _ in range(args.steps):
+            r.render_rays(desc, rd, soa, pic, device=True)
+            st = r.stats()
+            for k in stages:
+                stages[k] += st[k] / args.steps
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        host_aos = torch.empty(n * 36, dtype=torch.uint8, pin_memory=True)
+        host_aos.numpy()[:] = w.particles.view(np.uint8)
+        host_pic = torch.empty((desc.xres, desc.yres, 3), dtype=torch.float32, pin_memory=True)
+        r.render_rays(desc, rd, host_aos, host_pic)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r.render_rays(desc, rd, host_aos, host_pic)
+        e2e_ms = (time.perf_counter() - t0) / args.steps * 1e3
+        ts = []
+        for i in range(3):
+            t0 = time.perf_counter()
+            _, ost = port.render_rays(prm, w.rc, w.particles, exact=False)
+            if i:
+                ts.append(time.perf_counter() - t0)
+        cpu_s = statistics.median(ts)
+        out[name] = {"particles": n, "image": [int(desc.xres), int(desc.yres)], "ms": ms,
+                     "mparticles_per_s": n / (ms * 1e-3) / 1e6, "frames_per_s": 1e3 / ms,
+                     "stages_ms": {"particles": stages["project_ms"],
+                                   "level_sort": stages["sort_ms"],
+                                   "walk_and_leaf_sort": stages["bin_ms"],
+                                   "leaves": stages["splat_ms"]},
+                     "e2e_ms": e2e_ms, "e2e_mparticles_per_s": n / (e2e_ms * 1e-3) / 1e6,
+                     "spheres": int(st["n_active"]), "leaf_entries": int(st["n_entries"]),
+                     "leaf_regions": int(st["n_tiles"]), "levels": ost["levels"],
+                     "fragments": ost["fragments"],
+                     "fragments_per_s": ost["fragments"] / (ms * 1e-3),
+                     "cpu": {"ms": cpu_s * 1e3, "mparticles_per_s": n / cpu_s / 1e6,
+                             "cores": port.threads, "kind": "port",
+                             "sample": "the whole frame, reference arithmetic"},
+                     "speedup_vs_cpu": cpu_s * 1e3 / ms}
+        r.close()
+    return out
+
+
 def large(args, local: int) -> dict:
     """Large render, forward+backward (opt-in, --only large): 400M particles x
     large_scale, ordered absorption, per-particle RGB, Pareto hsml, 4096^2.
@@ -506,7 +589,8 @@ def run_gpu(args):
 
     if args.only != "all":  # one section alone (profiling runs); prints its own line
         torch.cuda.set_device(local)
-        res = {"fwd_bwd": fwd_bwd, "batched": batched, "large": large}[args.only](args, local)
+        res = {"fwd_bwd": fwd_bwd, "batched": batched, "large": large,
+               "rays": rays}[args.only](args, local)
         print(json.dumps({"section": args.only, "result": res}), flush=True)
         return 0
 
@@ -601,6 +685,7 @@ def run_gpu(args):
         cb = cpu_baseline(w)
     fb = None if args.no_fwd_bwd else fwd_bwd(args, local)
     bt = None if args.no_batched else batched(args, local)
+    ry = None if args.no_rays else rays(args, local)
     line = {"metric": METRIC, "value": world * n / (ms * 1e-3) / 1e6, "unit": "Mparticles/s",
             "frames_per_s": world * 1e3 / ms, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -608,7 +693,7 @@ def run_gpu(args):
             "data": "synthetic (seeded halo mixture; no snapshot available)", "config": cfg,
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "roofline": top,
             "stages": st, "fragments": frags, "bin_entries": int(last["n_entries"]),
-            "cpu_baseline": cb, "fwd_bwd": fb, "batched": bt}
+            "cpu_baseline": cb, "fwd_bwd": fb, "batched": bt, "rays": ry}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -190,6 +190,27 @@ spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
 #define SPL_DEBUG_RADIX_REDUCE_SCAN 2
 spl_status spl_debug_set_options(spl_context *ctx, int flags);
 
+/* ---- ray-sphere render: host_rendering with new_renderer=true ---------- */
+/* The second renderer behind host_rendering (splotch/splotch_host.cc:714-723
+   -> host_rendering_new, splotch/new_renderer.cc:522-641): every particle is
+   a sphere seen from campos, every pixel a ray that collects
+   -e*exp(-sin^2(angle)/(r*h2sigma)^2) from the spheres it meets; additive
+   only.  Keys of this renderer that spl_frame_desc does not hold, or holds
+   at another precision (it reads fov and minrad_pix as double): */
+typedef struct {
+  int dome;          /* "dome" (false): fisheye projector; needs xres == yres */
+  double fov;        /* "fov" (45), degrees */
+  double minrad_pix; /* "minrad_pix" (1) */
+} spl_rays_desc;
+void spl_rays_desc_defaults(spl_rays_desc *r);
+/* Reads from d: xres, yres, zmax, ptypes, brightness, color_is_vector,
+   palettes, b_brightness, a_eq_e (must be true: SPL_ERR_INVALID otherwise, the
+   reference's planck_assert) and campos, centerpos, lookat, sky.  out gets
+   the x-major xres*yres*3 image.  The reference empties the particle vector
+   afterwards (new_renderer.cc:584); the particle view is not written. */
+spl_status spl_render_rays(spl_context *ctx, const spl_frame_desc *d, const spl_rays_desc *r,
+                           const spl_particles *p, spl_image *out);
+
 /* ---- gradients ---------------------------------------------------------- */
 /* Per-particle gradient arrays (n floats each, by particle index, in
    memspace; NULL = not wanted) and the camera-position gradient.  Colour:

@@ -262,6 +262,17 @@ def frame_desc(params: ParamFile, rc: RenderContext, keep: list | None = None) -
     return d
 
 
+def rays_desc(params: ParamFile) -> _abi.RaysDesc:
+    """The keys host_rendering_new reads beyond frame_desc's, at its precision
+    (splotch/new_renderer.cc:588-613: dome, fov and minrad_pix as double)."""
+    r = _abi.RaysDesc()
+    _abi.load().spl_rays_desc_defaults(C.byref(r))
+    r.dome = 1 if params.find("dome", False) else 0
+    r.fov = float(params.find("fov", 45.0))
+    r.minrad_pix = float(params.find("minrad_pix", 1.0))
+    return r
+
+
 class Renderer:
     """Owns one spl_context (device buffers pooled across frames)."""
 
@@ -323,6 +334,27 @@ class Renderer:
         _abi.check(self.lib.spl_render(self.ctx, C.byref(desc), C.byref(p), C.byref(img),
                                        _abi.SPL_WRITEBACK_NONE))
         self._last_n = n
+
+    # -- ray-sphere frame (new_renderer=true) ---------------------------------
+    def render_rays(self, desc: _abi.FrameDesc, rays: _abi.RaysDesc, particles, pic, *,
+                    device: bool = False) -> None:
+        """spl_render_rays: host_rendering_new (splotch/new_renderer.cc:522-641)
+        of a particle_sim array (numpy, or a torch uint8 tensor of n*36 bytes
+        when device=True) or of a dict of SoA fields, into pic (x-major)."""
+        mem = _abi.SPL_MEM_DEVICE if device else _abi.SPL_MEM_HOST
+        if isinstance(particles, dict):
+            p = _abi.Particles(n=int(particles["x"].shape[0]), layout=_abi.SPL_LAYOUT_SOA,
+                               memspace=mem)
+            for f in ("x", "y", "z", "r", "I", "cr", "cg", "cb", "type"):
+                setattr(p, f, _abi.ptr(particles.get(f)))
+        else:
+            n = len(particles) if isinstance(particles, np.ndarray) else particles.numel() // 36
+            p = _abi.Particles(n=n, layout=_abi.SPL_LAYOUT_AOS, memspace=mem,
+                               aos=_abi.ptr(particles))
+        img = _abi.Image(pic=_abi.ptr(pic), memspace=mem)
+        _abi.check(self.lib.spl_render_rays(self.ctx, C.byref(desc), C.byref(rays), C.byref(p),
+                                            C.byref(img)))
+        self._last_n = 0
 
     def stats(self) -> dict:
         s = _abi.Stats()
@@ -553,17 +585,18 @@ _default_renderer: Renderer | None = None
 
 
 def host_rendering(params: ParamFile, particles: np.ndarray, rc: RenderContext,
-                   renderer: Renderer | None = None) -> None:
+                   renderer: Renderer | None = None) -> np.ndarray:
     """Drop-in for ``host_rendering`` (splotch/splotch_host.cc:711-834).
 
     Overwrites ``rc.pic`` and mutates ``particles`` in place exactly as the
     reference does: projected x,y,z,r,I, colourised e, active flags, and the
-    stable z order when ``a_eq_e`` is false.
+    stable z order when ``a_eq_e`` is false.  Returns the particles the
+    caller's vector still holds: all of them, or none after the ray-sphere
+    renderer (``new_renderer=true``, splotch_host.cc:714-723), which empties
+    the reference's vector (new_renderer.cc:584) and leaves this array as it
+    was.
     """
     global _default_renderer
-    if params.find("new_renderer", False):
-        raise SplotchError(_abi.SPL_ERR_UNSUPPORTED,
-                           "new_renderer=true selects the ray-sphere renderer, not this path")
     if particles.dtype != PARTICLE_DTYPE or not particles.flags.c_contiguous:
         raise TypeError("particles must be a C-contiguous PARTICLE_DTYPE array")
     if renderer is None:
@@ -575,4 +608,8 @@ def host_rendering(params: ParamFile, particles: np.ndarray, rc: RenderContext,
     if rc.pic is None or rc.pic.shape != (desc.xres, desc.yres, 3):
         rc.pic = np.zeros((desc.xres, desc.yres, 3), dtype=np.float32)
     n = int(rc.npart) if rc.npart else len(particles)
+    if params.find("new_renderer", False):
+        renderer.render_rays(desc, rays_desc(params), particles[:n], rc.pic)
+        return particles[:0]
     renderer.render_aos(desc, particles[:n], rc.pic, writeback=True)
+    return particles

@@ -31,7 +31,7 @@ EXPORTED = [
     "spl_render_backward", "spl_context_set_differentiable", "spl_batch_options_defaults",
     "spl_batch_create", "spl_batch_render", "spl_batch_get_info", "spl_batch_destroy",
     "spl_post_desc_defaults", "spl_postprocess", "spl_image_encode", "spl_write_image",
-    "spl_particle_normalize",
+    "spl_particle_normalize", "spl_rays_desc_defaults", "spl_render_rays",
 ]
 SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
@@ -133,6 +133,11 @@ class BatchInfo(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class RaysDesc(C.Structure):
+    """spl_rays_desc: the ray-sphere renderer's own keys."""
+    _fields_ = [("dome", C.c_int), ("fov", C.c_double), ("minrad_pix", C.c_double)]
+
+
 class SplotchError(RuntimeError):
     """A non-zero spl_status; the message is spl_last_error_string()."""
 
@@ -185,6 +190,9 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_batch_destroy": (C.c_int, [vp]),
         "spl_particle_normalize": (C.c_int, [vp, C.POINTER(NormalizeDesc), C.POINTER(Particles),
                                              C.POINTER(NormalizeResult)]),
+        "spl_rays_desc_defaults": (None, [C.POINTER(RaysDesc)]),
+        "spl_render_rays": (C.c_int, [vp, C.POINTER(FrameDesc), C.POINTER(RaysDesc),
+                                      C.POINTER(Particles), C.POINTER(Image)]),
         "spl_post_desc_defaults": (None, [C.POINTER(PostDesc)]),
         "spl_postprocess": (C.c_int, [vp, C.POINTER(FrameDesc), C.POINTER(PostDesc),
                                       C.POINTER(Image)]),

@@ -20,7 +20,7 @@ LIB = PKG / "libsplgpu.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["spl_api.cu", "spl_project.cu", "spl_sort.cu", "spl_bin.cu", "spl_splat.cu",
-              "spl_noalloc.cu", "spl_backward.cu", "spl_batch.cu", "spl_post.cu",
+              "spl_rays.cu", "spl_noalloc.cu", "spl_backward.cu", "spl_batch.cu", "spl_post.cu",
               "spl_normalize.cu"]
 CPP_SOURCES = ["spl_camera.cpp"]
 

@@ -31,7 +31,15 @@ struct spl_context {
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
       poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes,
-      seg_cnt, seg_off, seg_state;
+      seg_cnt, seg_off, seg_state, ray_rc, ray_cf, ray_pod, ray_cov, ray_code, ray_lev,
+      ray_nodes, ray_regs, ray_box, ray_leaf_start, ray_img[2], ray_jstop;
+  // spl_render_rays: the host-built region trees of the last geometry
+  struct RayKey {
+    int xres, yres, dome;
+    double fov, minrad_pix, v[12];  // campos, centerpos, lookat, sky
+  };
+  RayKey ray_key{};
+  spl::RayFrame *rays = nullptr;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
   bool split_tiles = false;     // heavy tiles cut into list segments
@@ -237,9 +245,11 @@ int spl::bits_for(int64_t v) {
   return b;
 }
 
-spl_status spl::frame_setup(const spl_frame_desc *d, int T, bool exact_fp64, FrameSetup &fs) {
+spl_status spl::frame_setup(const spl_frame_desc *d, int T, bool exact_fp64, FrameSetup &fs,
+                            bool camera) {
   spl_camera cam;
-  if (spl_camera_setup(d, &cam))
+  std::memset(&cam, 0, sizeof(cam));
+  if (camera && spl_camera_setup(d, &cam))
     return fail(SPL_ERR_INVALID, "degenerate matrix in TRANSMAT::Inverse()");
   const int xres = d->xres, yres = d->yres;
   ProjConst &pc = fs.pc;
@@ -352,9 +362,13 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->col_c, &c->idx_c, &c->pstate, &c->poff, &c->gpic,
                               &c->gpos_c, &c->gcol_c, &c->camsum, &c->aux, &c->post_tab,
                               &c->post_bar, &c->post_img, &c->post_bytes, &c->seg_cnt,
-                              &c->seg_off, &c->seg_state};
+                              &c->seg_off, &c->seg_state, &c->ray_rc, &c->ray_cf,
+                              &c->ray_pod, &c->ray_cov, &c->ray_code, &c->ray_lev,
+                              &c->ray_nodes, &c->ray_regs, &c->ray_box, &c->ray_leaf_start,
+                              &c->ray_img[0], &c->ray_img[1], &c->ray_jstop};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
+  delete c->rays;
   for (auto &b : c->soa_in)
     if (b.p) cudaFree(b.p);
   for (auto &b : c->gout)
@@ -895,6 +909,243 @@ spl_status spl_render_backward(spl_context *c, const spl_image *gp, spl_grads *g
 }
 
 // ---- particle normalisation ---------------------------------------------------
+void spl_rays_desc_defaults(spl_rays_desc *r) {
+  if (!r) return;
+  r->dome = 0;
+  r->fov = 45.0;
+  r->minrad_pix = 1.0;
+}
+
+// host_rendering_new (splotch/new_renderer.cc:522-641): particle pass, level
+// sort, region-tree walk, leaf sort, per-level leaf rendering, dome mask.
+spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_rays_desc *r,
+                           const spl_particles *p, spl_image *out) {
+  if (!c || !r) return fail(SPL_ERR_INVALID, "null argument");
+  SPL_CK(cudaSetDevice(c->device));
+  spl_status st = validate(d, p, out);
+  if (st) return st;
+  if (!d->a_eq_e)
+    return fail(SPL_ERR_INVALID, "inconsistent: the ray-sphere renderer needs a_eq_e=true");
+  cudaStream_t s = c->stream;
+  const int64_t n = p->n;
+  const int xres = d->xres, yres = d->yres;
+  int launches = 0;
+  // spl_render_backward and the debug getters describe a spl_render frame
+  c->last_T = 0;
+  c->has_order = false;
+  c->pf_in_use = -1;
+
+  spl::FrameSetup fs;
+  if ((st = spl::frame_setup(d, 16, (c->debug_flags & 1) != 0, fs, false))) return st;
+  spl::ProjConst pc = fs.pc;
+  const int npal = fs.npal;
+
+  // ---- projector, levels and region trees (kept while the geometry holds) --
+  spl_context::RayKey key{};
+  key.xres = xres;
+  key.yres = yres;
+  key.dome = r->dome ? 1 : 0;
+  key.fov = r->fov;
+  key.minrad_pix = r->minrad_pix;
+  for (int a = 0; a < 3; ++a) {
+    key.v[a] = d->campos[a];
+    key.v[3 + a] = d->centerpos[a];
+    key.v[6 + a] = d->lookat[a];
+    key.v[9 + a] = d->sky[a];
+  }
+  const bool rebuild = !c->rays || std::memcmp(&key, &c->ray_key, sizeof(key)) != 0;
+  if (rebuild) {
+    delete c->rays;
+    c->rays = new spl::RayFrame;
+    if ((st = spl::rays_setup(d, r, *c->rays))) {
+      delete c->rays;
+      c->rays = nullptr;
+      return st;
+    }
+    c->ray_key = key;
+  }
+  spl::RayFrame &F = *c->rays;
+  spl::RayConst k = F.k;
+  k.zmax = d->zmax;
+  const int nlev = k.nlev;
+  const int64_t nnodes = (int64_t)F.nodes.size(), nleaves = (int64_t)F.leaf_box.size();
+
+  // ---- buffers ---------------------------------------------------------------
+  size_t img_floats = 1;
+  for (int L = 0; L + 1 < nlev; ++L)
+    img_floats = std::max(img_floats, (size_t)k.lev[L].xdim * k.lev[L].ydim * 3);
+  const size_t pic_bytes = (size_t)xres * yres * 3 * 4;
+  if ((st = ensure(c->ray_rc, n * 32)) || (st = ensure(c->ray_cf, n * 16)) ||
+      (st = ensure(c->ray_pod, n * 16)) || (st = ensure(c->ray_cov, n * 8)) ||
+      (st = ensure(c->ray_code, n * 4)) || (st = ensure(c->ray_lev, (nlev + 3) * 4)) ||
+      (st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
+      (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)) ||
+      (st = ensure(c->count, n * 4)) || (st = ensure(c->off, (n + 1) * 8)) ||
+      (st = ensure(c->small, 256)) || (st = ensure(c->ray_leaf_start, (nleaves + 1) * 4)) ||
+      (st = ensure(c->ray_img[0], img_floats * 4)) || (st = ensure(c->ray_img[1], img_floats * 4)) ||
+      (st = ensure(c->ray_jstop, (xres / 2 + 1) * 4)) ||
+      (out->memspace == SPL_MEM_HOST && (st = ensure(c->pic, pic_bytes))) ||
+      (st = ensure(c->pal_x, (npal + 1) * 8)) || (st = ensure(c->pal_rgb, (npal + 1) * 12)) ||
+      (st = ensure(c->pal_thr, (npal + 1) * 4)) || (st = ensure(c->pal_xff, (npal + 1) * 8)) ||
+      (st = ensure(c->pal_invff, (npal + 1) * 8)))
+    return st;
+  size_t scr = std::max(spl::scan_scratch_bytes(n + 1), spl::radix_scratch_bytes(n));
+  if ((st = ensure(c->scratch, scr))) return st;
+  if (rebuild) {
+    if ((st = ensure(c->ray_nodes, nnodes * sizeof(spl::RayNode))) ||
+        (st = ensure(c->ray_regs, nnodes * sizeof(spl::RayRegion))) ||
+        (st = ensure(c->ray_box, nleaves * sizeof(ushort4))))
+      return st;
+    SPL_CK(cudaMemcpyAsync(c->ray_nodes.p, F.nodes.data(), nnodes * sizeof(spl::RayNode),
+                           cudaMemcpyHostToDevice, s));
+    SPL_CK(cudaMemcpyAsync(c->ray_regs.p, F.regs.data(), nnodes * sizeof(spl::RayRegion),
+                           cudaMemcpyHostToDevice, s));
+    SPL_CK(cudaMemcpyAsync(c->ray_box.p, F.leaf_box.data(), nleaves * sizeof(ushort4),
+                           cudaMemcpyHostToDevice, s));
+  }
+  SPL_CK(cudaMemcpyAsync(c->pal_x.p, fs.pal_x.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_rgb.p, fs.pal_rgb.data(), (npal + 1) * 12, cudaMemcpyHostToDevice,
+                         s));
+  SPL_CK(cudaMemcpyAsync(c->pal_thr.p, fs.thr.data(), (npal + 1) * 4, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_xff.p, fs.xff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_invff.p, fs.invff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice,
+                         s));
+  SPL_CK(cudaStreamSynchronize(s));  // the host tables live in fs and F
+  pc.pal_x = as<double>(c->pal_x);
+  pc.pal_rgb = as<float>(c->pal_rgb);
+  pc.pal_thr = as<float>(c->pal_thr);
+  pc.pal_xff = as<float2>(c->pal_xff);
+  pc.pal_invff = as<float2>(c->pal_invff);
+  uint32_t *d_err = as<uint32_t>(c->small);
+  SPL_CK(cudaMemsetAsync(d_err, 0, 32, s));
+
+  cudaEventRecord(c->ev[0], s);
+  // ---- inputs ------------------------------------------------------------------
+  const void *aos_dev = nullptr;
+  spl::SoAIn soa{p->x, p->y, p->z, p->r, p->I, p->cr, p->cg, p->cb, p->type};
+  if (p->layout == SPL_LAYOUT_AOS) {
+    if (p->memspace == SPL_MEM_HOST) {
+      if ((st = ensure(c->aos_in, n * 36))) return st;
+      if (n > 0) SPL_CK(cudaMemcpyAsync(c->aos_in.p, p->aos, n * 36, cudaMemcpyHostToDevice, s));
+      aos_dev = c->aos_in.p;
+    } else {
+      aos_dev = p->aos;
+    }
+  } else if (p->memspace == SPL_MEM_HOST) {
+    const float **f[8] = {&soa.x, &soa.y, &soa.z, &soa.r, &soa.I, &soa.cr, &soa.cg, &soa.cb};
+    for (int a = 0; a < 8; ++a) {
+      if (!*f[a]) continue;
+      if ((st = ensure(c->soa_in[a], n * 4))) return st;
+      if (n > 0) SPL_CK(cudaMemcpyAsync(c->soa_in[a].p, *f[a], n * 4, cudaMemcpyHostToDevice, s));
+      *f[a] = as<float>(c->soa_in[a]);
+    }
+    if (p->type) {
+      if ((st = ensure(c->soa_in[8], n * 2))) return st;
+      if (n > 0) SPL_CK(cudaMemcpyAsync(c->soa_in[8].p, p->type, n * 2, cudaMemcpyHostToDevice, s));
+      soa.type = as<uint16_t>(c->soa_in[8]);
+    }
+  }
+  cudaEventRecord(c->ev[1], s);
+
+  // ---- particle pass, then the particles grouped by level (stable) ------------
+  spl::RayParts rp{as<double4>(c->ray_rc), as<float4>(c->ray_cf), as<float4>(c->ray_pod),
+                   as<float2>(c->ray_cov), as<uint32_t>(c->ray_code), d_err};
+  spl::launch_rays_prep(aos_dev, &soa, n, pc, k, rp, s);
+  ++launches;
+  cudaEventRecord(c->ev[2], s);
+  uint32_t *code_s = as<uint32_t>(c->key), *order = as<uint32_t>(c->perm);
+  uint32_t *lev_start = as<uint32_t>(c->ray_lev);
+  if (n > 0) {
+    spl::radix_sort_pairs(rp.code, nullptr, as<uint32_t>(c->ktmp), as<uint32_t>(c->vtmp), code_s,
+                          order, n, 0, spl::bits_for(nlev + 2), true, c->scratch.p, s, &launches,
+                          d_err, (c->debug_flags & 2) == 0);
+  }
+  spl::launch_tile_ranges(code_s, n, nlev + 2, lev_start, s);
+  ++launches;
+  cudaEventRecord(c->ev[3], s);
+
+  // ---- region-tree walk: (leaf, particle) pairs, grouped by leaf (stable) -----
+  const spl::RayNode *d_nodes = as<spl::RayNode>(c->ray_nodes);
+  const spl::RayRegion *d_regs = as<spl::RayRegion>(c->ray_regs);
+  spl::launch_rays_walk(false, k, d_nodes, d_regs, order, code_s, n, rp, as<uint32_t>(c->count),
+                        nullptr, nullptr, nullptr, s);
+  ++launches;
+  spl::scan_counts(as<uint32_t>(c->count), nullptr, n, as<uint64_t>(c->off), c->scratch.p, s,
+                   &launches);
+  uint64_t ne64 = 0;
+  std::vector<uint32_t> hlev(nlev + 3, 0);
+  SPL_CK(cudaMemcpyAsync(&ne64, as<uint64_t>(c->off) + n, 8, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaMemcpyAsync(hlev.data(), lev_start, (nlev + 3) * 4, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));
+  if (ne64 > 0xffffffffULL) return fail(SPL_ERR_CAPACITY, "more than 2^32 leaf-list entries");
+  const int64_t ne = (int64_t)ne64;
+  if ((st = ensure(c->tkey, ne * 4)) || (st = ensure(c->tval, ne * 4)) ||
+      (st = ensure(c->tkey2, ne * 4)) || (st = ensure(c->tval2, ne * 4)) ||
+      (st = ensure(c->tkey_s, ne * 4)) || (st = ensure(c->tval_s, ne * 4)) ||
+      (st = ensure(c->scratch, std::max(scr, spl::radix_scratch_bytes(ne)))))
+    return st;
+  spl::launch_rays_walk(true, k, d_nodes, d_regs, order, code_s, n, rp, nullptr,
+                        as<uint64_t>(c->off), as<uint32_t>(c->tkey), as<uint32_t>(c->tval), s);
+  ++launches;
+  if (ne > 0)
+    spl::radix_sort_pairs(as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->tkey2),
+                          as<uint32_t>(c->tval2), as<uint32_t>(c->tkey_s), as<uint32_t>(c->tval_s),
+                          ne, 0, std::max(1, spl::bits_for(nleaves)), true, c->scratch.p, s,
+                          &launches, d_err,
+                          (c->debug_flags & 2) == 0);
+  spl::launch_tile_ranges(as<uint32_t>(c->tkey_s), ne, nleaves, as<uint32_t>(c->ray_leaf_start),
+                          s);
+  ++launches;
+  cudaEventRecord(c->ev[4], s);
+
+  // ---- the pyramid, coarsest level first -----------------------------------------
+  float *final_pic = out->memspace == SPL_MEM_HOST ? as<float>(c->pic) : out->pic;
+  spl::RayLeafArgs la{};
+  la.leaf_box = as<ushort4>(c->ray_box);
+  la.leaf_start = as<uint32_t>(c->ray_leaf_start);
+  la.vals = as<uint32_t>(c->tval_s);
+  la.order = order;
+  la.lev_start = lev_start;
+  for (int L = 0; L < nlev; ++L) {
+    la.out = L == nlev - 1 ? final_pic : as<float>(c->ray_img[L & 1]);
+    la.coarse = L > 0 ? as<float>(c->ray_img[(L - 1) & 1]) : nullptr;
+    la.cdim_y = L > 0 ? k.lev[L - 1].ydim : 0;
+    spl::launch_rays_leaves(k, L, rp, la, s);
+    ++launches;
+  }
+  if (k.dome) {
+    spl::launch_rays_dome_mask(final_pic, xres, as<int>(c->ray_jstop), s);
+    launches += 2;
+  }
+  cudaEventRecord(c->ev[5], s);
+  if (out->memspace == SPL_MEM_HOST)
+    SPL_CK(cudaMemcpyAsync(out->pic, final_pic, pic_bytes, cudaMemcpyDeviceToHost, s));
+  cudaEventRecord(c->ev[6], s);
+  uint32_t err = 0;
+  SPL_CK(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaStreamSynchronize(s));
+  SPL_CK(cudaGetLastError());
+  if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
+  if (err & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
+  if (err & 16u) return fail(SPL_ERR_CAPACITY, "region-tree walk stack overflow");
+  if (err & 32u) return fail(SPL_ERR_INVALID, "a particle fell in two pyramid levels");
+
+  spl_stats &S = c->stats;
+  S = spl_stats{};
+  cudaEventElapsedTime(&S.h2d_ms, c->ev[0], c->ev[1]);
+  cudaEventElapsedTime(&S.project_ms, c->ev[1], c->ev[2]);
+  cudaEventElapsedTime(&S.sort_ms, c->ev[2], c->ev[3]);
+  cudaEventElapsedTime(&S.bin_ms, c->ev[3], c->ev[4]);
+  cudaEventElapsedTime(&S.splat_ms, c->ev[4], c->ev[5]);
+  cudaEventElapsedTime(&S.d2h_ms, c->ev[5], c->ev[6]);
+  cudaEventElapsedTime(&S.total_ms, c->ev[0], c->ev[6]);
+  S.n_active = hlev[nlev + 1];  // spheres rendered: level grids and around the camera
+  S.n_entries = ne;
+  S.n_tiles = nleaves;
+  S.kernel_launches = launches;
+  return SPL_OK;
+}
+
 
 spl_status spl_particle_normalize(spl_context *c, const spl_normalize_desc *d,
                                   spl_particles *p, spl_normalize_result *res) {

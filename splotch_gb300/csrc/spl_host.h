@@ -36,6 +36,20 @@ struct FrameSetup {
   std::vector<float> pal_rgb, thr;
   std::vector<float2> xff, invff;
 };
-spl_status frame_setup(const spl_frame_desc *d, int T, bool exact_fp64, FrameSetup &fs);
+// camera false: the main path's camera (spl_camera_setup) is not needed and
+// not checked (the ray-sphere renderer has its own projector).
+spl_status frame_setup(const spl_frame_desc *d, int T, bool exact_fp64, FrameSetup &fs,
+                       bool camera = true);
+
+// The ray-sphere renderer's frame on the host: projector, pyramid levels and
+// every level's region tree (nodes and their reduceList constants, leaf
+// regions), in the reference's double arithmetic.
+struct RayFrame {
+  RayConst k;
+  std::vector<RayNode> nodes;
+  std::vector<RayRegion> regs;
+  std::vector<ushort4> leaf_box;
+};
+spl_status rays_setup(const spl_frame_desc *d, const spl_rays_desc *r, RayFrame &f);
 
 }  // namespace spl

@@ -511,4 +511,90 @@ struct ProjAdjArgs {
 };
 int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Ray-sphere renderer: host_rendering_new (splotch/new_renderer.cc:522-641),
+// which host_rendering selects with new_renderer=true.  Every particle is a
+// sphere of angular radius r around the unit direction c from campos; a pixel
+// ray d collects -e*exp(-sin^2(d,c)/(r*h2sigma)^2) from every sphere it meets.
+// Particles go to a pyramid of pixel grids by angular radius; each grid is a
+// tree of image regions (the reference's recursive subdivision) whose
+// culling test (reduceList) decides which particles a leaf region lists.
+constexpr int kRayMaxLevels = 16;
+constexpr int kRayLeafThreads = 96;  // a leaf region holds at most 9 x 9 pixels
+
+// reduceList parameters of one region (new_renderer.cc:77-101, 164-213),
+// computed on the host in double exactly as the reference computes them.
+struct RayRegion {
+  float nf[4][3];      // plane: the side normals rounded to float (screening)
+  double n[4][3];      // plane: side normals; dome: n[0] = nx0, n[1] = nx1
+  double cthetamin, cthetamax, thetamin, thetamax;  // dome
+  int centered;        // dome
+  int pad;
+};
+struct RayNode {
+  int first_child;  // children are contiguous; -1 for a leaf
+  int nchild;
+  int leaf;         // global leaf id, or -1
+  int pad;
+};
+struct RayLevel {
+  int fact, xdim, ydim;
+  int root;          // node of the whole grid (never tested: the reference
+                     // skips reduceList for the whole image)
+  int leaf0, nleaves;
+  double minrad, maxrad;  // radius range (minrad, maxrad] of the level's particles
+};
+struct RayConst {
+  int dome, nlev;      // level 0 is the coarsest grid
+  double p0[3], dpx[3], dpy[3];    // PlaneProjector
+  double zen[3], ex[3], ey[3], dp; // DomeProjector (zenith, x, y, 1/res)
+  double campos[3], centerpos[3];
+  float zmax;
+  double half_bfak;    // 0.5*bfak
+  double mr2pr2;       // minrad_pix^2 * pixrad^2
+  double h2sigma;
+  RayLevel lev[kRayMaxLevels];
+  RayRegion screen;    // reduceList(0, xres, 0, yres): the screen cut
+};
+// Per particle (indexed by particle): code = level (0..nlev-1), nlev for a
+// sphere around the camera (r > 1), nlev+1 for a particle not rendered.
+struct RayParts {
+  double4 *rc;     // unit direction c and angular radius r, as the reference has them
+  float4 *cf;      // the same rounded to float
+  float4 *pod;     // colour after the radius correction
+  float2 *cov;     // per sphere: chord^2 limit 2r^2/(1+sqrt(1-r^2)) (-1: always decide in
+                   // double), 1/(r*h2sigma)^2
+  uint32_t *code;
+  uint32_t *err;   // bit 0: type outside [0, ptypes); bit 5: two levels claim a particle
+};
+void launch_rays_prep(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &pc,
+                      const RayConst &k, const RayParts &o, cudaStream_t s);
+// Walk of every particle of the level grids (order/code: the particles sorted
+// by code, n entries) through its level's region tree: count (EMIT false:
+// leaves reached per sorted position) or emit (leaf id, particle) pairs at
+// off[s].  Bit 4 of *err: the walk's stack overflowed.
+void launch_rays_walk(bool emit, const RayConst &k, const RayNode *nodes, const RayRegion *regs,
+                      const uint32_t *order, const uint32_t *code, int64_t n, const RayParts &p,
+                      uint32_t *count, const uint64_t *off, uint32_t *keys, uint32_t *vals,
+                      cudaStream_t s);
+// One pyramid level: every leaf region of level L (leaf ranges in leaf_start,
+// entries' particles in vals).  The coarsest level adds the spheres around
+// the camera (order[ov0, ov1)); the others add the coarser level's grid
+// (coarse, cdim_y rows per column) upsampled.  out: x-major xdim*ydim*3.
+struct RayLeafArgs {
+  const ushort4 *leaf_box;   // x0, x1, y0, y1 in level pixels
+  const uint32_t *leaf_start;
+  const uint32_t *vals;
+  const uint32_t *order;
+  const uint32_t *lev_start; // code ranges in the sorted order (nlev + 3)
+  const float *coarse;
+  int cdim_y;
+  float *out;
+};
+void launch_rays_leaves(const RayConst &k, int L, const RayParts &p, const RayLeafArgs &a,
+                        cudaStream_t s);
+// The dome's post step (new_renderer.cc:619-639): pixels outside the fisheye
+// circle are zeroed, in the reference's row order.  jstop: res/2 + 1 ints.
+void launch_rays_dome_mask(float *pic, int res, int *jstop, cudaStream_t s);
+
 }  // namespace spl

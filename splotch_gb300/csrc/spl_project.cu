@@ -10,6 +10,7 @@
 // multiply-adds.  The outputs x, y, z, r, I and active are therefore
 // bit-identical to the reference's.
 #include "spl_internal.cuh"
+#include "spl_rays.cuh"
 
 namespace spl {
 
@@ -496,6 +497,91 @@ __global__ void __launch_bounds__(256) k_palette_cache(L load, int64_t n, ProjCo
   }
 }
 
+// ---- ray-sphere renderer: the per-particle pass ----------------------------
+// host_rendering_new's particle loop and colourisation
+// (splotch/new_renderer.cc:530-582), real_host_rendering's normalisation
+// (:402-415) and screen cut (:418-446), and each particle's pyramid level
+// (:488-501).  Double operations in the reference's order, none fused.
+template <class L>
+__global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst c, RayConst k,
+                                                   RayParts o) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const PIn in = load(i);
+    const int t = in.type;
+    uint32_t code = (uint32_t)k.nlev + 1;
+    if (t < 0 || t >= c.ptypes) {
+      atomicOr(o.err, 1u);
+      o.code[i] = code;
+      continue;
+    }
+    // SPLOTCH_CLASSIC: I *= 0.5f*bfak/r (double bfak), r *= 2
+    const float I = __double2float_rn(dmul((double)in.I, ddiv(k.half_bfak, (double)in.r)));
+    const float r2 = fmul(in.r, 2.f);
+    const double dx = dsub(k.centerpos[0], (double)in.x);
+    const double dy = dsub(k.centerpos[1], (double)in.y);
+    const double dz = dsub(k.centerpos[2], (double)in.z);
+    const float dist =
+        __double2float_rn(__dsqrt_rn(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz))));
+    if (!(dist < k.zmax)) {
+      o.code[i] = code;
+      continue;
+    }
+    float er = in.er, eg = in.eg, eb = in.eb;
+    if (!c.colvec[t]) {  // particle_colorize (splotch_host.cc:276-282)
+      bool fb = false;
+      float pr, pg, pb;
+      palette_colour(c, t, er, pr, pg, pb, fb);
+      er = pr;
+      eg = pg;
+      eb = pb;
+    }
+    const float fac = fmul(I, c.bright[t]);
+    er = fmul(er, fac);
+    eg = fmul(eg, fac);
+    eb = fmul(eb, fac);
+    double cc[3] = {dsub((double)in.x, k.campos[0]), dsub((double)in.y, k.campos[1]),
+                    dsub((double)in.z, k.campos[2])};
+    const double xl = ddiv(
+        1.0, __dsqrt_rn(dadd(dadd(dmul(cc[0], cc[0]), dmul(cc[1], cc[1])), dmul(cc[2], cc[2]))));
+    for (int a = 0; a < 3; ++a) cc[a] = dmul(cc[a], xl);
+    double r = dmul((double)r2, xl);
+    const double rcorr = ddiv(__dsqrt_rn(dadd(dmul(r, r), k.mr2pr2)), r);
+    r = dmul(r, rcorr);
+    const float f2 = __double2float_rn(ddiv(1.0, dmul(rcorr, rcorr)));
+    er = fmul(er, f2);
+    eg = fmul(eg, f2);
+    eb = fmul(eb, f2);
+    const double4 rc = make_double4(cc[0], cc[1], cc[2], r);
+    const float4 cf = make_float4(__double2float_rn(cc[0]), __double2float_rn(cc[1]),
+                                  __double2float_rn(cc[2]), __double2float_rn(r));
+    if (ray_region_keeps(k, k.screen, ray_part(k, rc, cf))) {
+      if (r > 1) {
+        code = (uint32_t)k.nlev;  // a sphere around the camera
+      } else {
+        int hits = 0;
+        for (int lv = 0; lv < k.nlev; ++lv)
+          if ((r > k.lev[lv].minrad) && (r <= k.lev[lv].maxrad)) {
+            code = (uint32_t)lv;
+            ++hits;
+          }
+        if (hits > 1) atomicOr(o.err, 32u);
+      }
+    }
+    o.code[i] = code;
+    o.rc[i] = rc;
+    o.cf[i] = cf;
+    o.pod[i] = make_float4(er, eg, eb, 0.f);
+    // a ray meets the sphere iff |d - c|^2 <= 2 - 2 sqrt(1 - r^2) = 2r^2/(1 + sqrt(1 - r^2));
+    // near r = 1 that limit is ill-conditioned and the test is always made in double
+    const float cm = r <= 0.99 ? __double2float_rn(ddiv(dmul(2.0, dmul(r, r)),
+                                                        dadd(1.0, __dsqrt_rn(dsub(1.0, dmul(r, r))))))
+                               : -1.f;
+    const float inv = __double2float_rn(ddiv(1.0, dmul(dmul(dmul(r, r), k.h2sigma), k.h2sigma)));
+    o.cov[i] = make_float2(cm, inv);
+  }
+}
+
 // particle_sim writeback: e, x, y, z, r, I, type, active (36 bytes).
 __global__ void __launch_bounds__(256) k_writeback_aos(
     const float4 *__restrict__ pos, const float4 *__restrict__ col,
@@ -612,6 +698,20 @@ void launch_palette_cache(const void *aos, const SoAIn *soa, int64_t n, const Pr
     k_palette_cache<<<grid_for(n), 256, 0, s>>>(
         LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type}, n,
         cc, out);
+}
+
+void launch_rays_prep(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &pc,
+                      const RayConst &k, const RayParts &o, cudaStream_t s) {
+  if (n <= 0) return;
+  ProjConst cc = pc;
+  cc.pal_cache = nullptr;
+  if (aos)
+    k_rays_prep<<<grid_for(n), 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n, cc,
+                                            k, o);
+  else
+    k_rays_prep<<<grid_for(n), 256, 0, s>>>(
+        LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type}, n,
+        cc, k, o);
 }
 
 void launch_writeback_aos(const float4 *pos, const float4 *col, const uint8_t *active,

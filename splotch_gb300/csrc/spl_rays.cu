@@ -1,0 +1,542 @@
+// spl_rays.cu -- the ray-sphere renderer (host_rendering_new,
+// splotch/new_renderer.cc:522-641), selected in the reference by
+// new_renderer=true (splotch/splotch_host.cc:714-723).
+//
+//   particle pass (spl_project.cu: k_rays_prep) -> stable sort by pyramid
+//   level -> per particle, a walk of its level's region tree (count, scan,
+//   emit (leaf, particle) pairs) -> stable sort by leaf -> leaf ranges ->
+//   per level, coarsest first: one CTA per leaf region (k_rays_leaf), which
+//   also adds the spheres around the camera (coarsest level) or the coarser
+//   level upsampled -> dome mask.
+//
+// The reference renders each level by recursive subdivision of the image:
+// a region's list is its parent's list culled by the region's reduceList
+// test, and a region smaller than 10x10 pixels is rendered by testing every
+// pixel against every listed sphere.  Here the region tree is built on the
+// host once per camera and level (it depends on nothing else), and each
+// particle walks it on the GPU, emitting the leaf regions it survives to.  A
+// leaf's list is therefore exactly the reference's list for that region, in
+// the same (ascending particle) order.
+//
+// The pixel-vs-sphere test is screened in float: with d and c expressed
+// relative to a direction u of the leaf (in double, then rounded), the chord
+// |d - c|^2 is known to float precision relative to its own size, so it is
+// compared with the sphere's chord limit with a margin that bounds every
+// rounding; only a chord inside the margin is decided by the reference's
+// double test.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "spl_host.h"
+#include "spl_rays.cuh"
+
+namespace spl {
+
+namespace {
+
+int grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return (int)std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 64);
+}
+
+// ---------------------------------------------------------------------------
+// Host side: projector, pyramid levels and region trees, in double with the
+// reference's operation order (this file's host code is built without fused
+// multiply-adds).
+struct V3 {
+  double x, y, z;
+};
+V3 v3(double x, double y, double z) { return V3{x, y, z}; }
+V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+V3 operator*(V3 a, double f) { return v3(a.x * f, a.y * f, a.z * f); }
+double dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+double length(V3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+V3 cross(V3 a, V3 b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+V3 norm(V3 a) {  // vec3_t::Normalize: scale by 1/length
+  const double l = 1. / std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z);
+  return v3(a.x * l, a.y * l, a.z * l);
+}
+V3 from(const double *p) { return v3(p[0], p[1], p[2]); }
+void put(double *p, V3 a) {
+  p[0] = a.x;
+  p[1] = a.y;
+  p[2] = a.z;
+}
+
+constexpr double kPi = 3.141592653589793238462643383279502884197;
+
+// reduceList's region constants for full-resolution pixel columns [ix0,ix1)
+// and rows [iy0,iy1) (new_renderer.cc:77-94, 164-194).
+RayRegion region_setup(const RayConst &k, int ix0, int ix1, int iy0, int iy1) {
+  RayRegion g;
+  std::memset(&g, 0, sizeof(g));
+  if (!k.dome) {
+    double x0 = ix0, x1 = ix1, y0 = iy0, y1 = iy1;
+    if (ix1 == ix0 + 1) x1 += 0.001;
+    if (iy1 == iy0 + 1) y1 += 0.001;
+    const V3 p0 = from(k.p0), dpx = from(k.dpx), dpy = from(k.dpy);
+    V3 corner[4];
+    corner[0] = p0 + dpx * x0 + dpy * y0;
+    corner[1] = p0 + dpx * (x1 - 1) + dpy * y0;
+    corner[2] = p0 + dpx * (x1 - 1) + dpy * (y1 - 1);
+    corner[3] = p0 + dpx * x0 + dpy * (y1 - 1);
+    for (int i = 0; i < 4; ++i) {
+      const V3 n = norm(cross(corner[i], corner[(i + 1) & 3]));
+      put(g.n[i], n);
+      g.nf[i][0] = (float)n.x;
+      g.nf[i][1] = (float)n.y;
+      g.nf[i][2] = (float)n.z;
+    }
+    return g;
+  }
+  const double dp = k.dp, halfpi = kRayHalfPi;
+  double x0 = 2. * dp * (ix0 + .5) - 1., x1 = 2. * dp * (ix1 - .5) - 1.;
+  double y0 = 2. * dp * (iy0 + .5) - 1., y1 = 2. * dp * (iy1 - .5) - 1.;
+  if (ix1 == ix0 + 1) x1 += 0.001 * dp;
+  if (iy1 == iy0 + 1) y1 += 0.001 * dp;
+  const bool centered = ((x0 * x1) <= 0) && ((y0 * y1) <= 0);
+  const double amaxx = std::max(std::abs(x0), std::abs(x1));
+  const double amaxy = std::max(std::abs(y0), std::abs(y1));
+  const double aminx = std::min(std::abs(x0), std::abs(x1));
+  const double aminy = std::min(std::abs(y0), std::abs(y1));
+  const double thetamax = halfpi * std::sqrt(amaxx * amaxx + amaxy * amaxy);
+  double thetamin = 0;
+  if (!centered) {
+    if (x0 * x1 <= 0) thetamin = halfpi * aminy;
+    else if (y0 * y1 <= 0) thetamin = halfpi * aminx;
+    else thetamin = halfpi * std::sqrt(aminx * aminx + aminy * aminy);
+  }
+  const V3 ex = from(k.ex), ey = from(k.ey);
+  const V3 c = ex * ((x0 + x1) * .5) + ey * ((y0 + y1) * .5);
+  V3 n[4];
+  n[0] = norm(ex * y0 - ey * x0);
+  n[1] = norm(ex * y1 - ey * x0);
+  n[2] = norm(ex * y0 - ey * x1);
+  n[3] = norm(ex * y1 - ey * x1);
+  V3 nx0 = n[0], nx1 = n[1];
+  double curmin = 1.5;
+  for (int i = 0; i < 4; ++i)
+    for (int j = i + 1; j < 4; ++j)
+      if (dot(n[i], n[j]) < curmin) {
+        curmin = dot(n[i], n[j]);
+        nx0 = n[i];
+        nx1 = n[j];
+      }
+  if (dot(c, nx0) > 0) nx0 = v3(-nx0.x, -nx0.y, -nx0.z);
+  if (dot(c, nx1) > 0) nx1 = v3(-nx1.x, -nx1.y, -nx1.z);
+  put(g.n[0], nx0);
+  put(g.n[1], nx1);
+  g.centered = centered ? 1 : 0;
+  g.thetamin = thetamin;
+  g.thetamax = thetamax;
+  g.cthetamin = std::cos(thetamin);
+  g.cthetamax = std::cos(thetamax);
+  return g;
+}
+
+// subrender4's subdivision of one level's grid (new_renderer.cc:280-360):
+// a region of 10 or more pixels in either direction splits in two along a
+// direction more than sqrt(2) times longer than the other, else in four.
+void build_tree(RayConst &k, int L, RayFrame &f) {
+  RayLevel &lv = k.lev[L];
+  std::vector<int4> box;  // x0, x1, y0, y1 of each node of this level
+  const int base = (int)f.nodes.size();
+  lv.root = base;
+  lv.leaf0 = (int)f.leaf_box.size();
+  f.nodes.push_back(RayNode{-1, 0, -1, 0});
+  f.regs.push_back(RayRegion{});
+  box.push_back(make_int4(0, lv.xdim, 0, lv.ydim));
+  const int fact = lv.fact;
+  for (size_t q = 0; q < box.size(); ++q) {
+    const int4 b = box[q];
+    const int nx = b.y - b.x, ny = b.w - b.z;
+    if (nx < 10 && ny < 10) {
+      f.nodes[base + q].leaf = (int)f.leaf_box.size();
+      f.leaf_box.push_back(make_ushort4((unsigned short)b.x, (unsigned short)b.y,
+                                        (unsigned short)b.z, (unsigned short)b.w));
+      continue;
+    }
+    const int xm = (b.x + b.y) >> 1, ym = (b.z + b.w) >> 1;
+    int4 ch[4];
+    int nch;
+    if (nx > std::sqrt(2.) * ny) {
+      ch[0] = make_int4(b.x, xm, b.z, b.w);
+      ch[1] = make_int4(xm, b.y, b.z, b.w);
+      nch = 2;
+    } else if (ny > std::sqrt(2.) * nx) {
+      ch[0] = make_int4(b.x, b.y, b.z, ym);
+      ch[1] = make_int4(b.x, b.y, ym, b.w);
+      nch = 2;
+    } else {
+      ch[0] = make_int4(b.x, xm, b.z, ym);
+      ch[1] = make_int4(b.x, xm, ym, b.w);
+      ch[2] = make_int4(xm, b.y, b.z, ym);
+      ch[3] = make_int4(xm, b.y, ym, b.w);
+      nch = 4;
+    }
+    f.nodes[base + q].first_child = (int)f.nodes.size();
+    f.nodes[base + q].nchild = nch;
+    for (int i = 0; i < nch; ++i) {
+      const int4 c = ch[i];
+      f.nodes.push_back(RayNode{-1, 0, -1, 0});
+      f.regs.push_back(region_setup(k, c.x * fact, (c.y - 1) * fact + 1, c.z * fact,
+                                    (c.w - 1) * fact + 1));
+      box.push_back(c);
+    }
+  }
+  lv.nleaves = (int)f.leaf_box.size() - lv.leaf0;
+}
+
+}  // namespace
+
+spl_status rays_setup(const spl_frame_desc *d, const spl_rays_desc *r, RayFrame &f) {
+  RayConst &k = f.k;
+  std::memset(&k, 0, sizeof(k));
+  f.nodes.clear();
+  f.regs.clear();
+  f.leaf_box.clear();
+  const int xres = d->xres, yres = d->yres;
+  if (xres > 65535 || yres > 65535)  // leaf regions hold 16-bit pixel bounds
+    return host_fail(SPL_ERR_UNSUPPORTED, "the ray-sphere renderer takes up to 65535 pixels a side");
+  if (r->dome && xres != yres)
+    return host_fail(SPL_ERR_INVALID, "inconsistency: a dome needs xres == yres");
+  const V3 campos = from(d->campos), centerpos = from(d->centerpos), lookat = from(d->lookat);
+  V3 sky = from(d->sky);
+  k.dome = r->dome ? 1 : 0;
+  // projector (new_renderer.cc:588-612)
+  if (k.dome) {
+    k.dp = 1. / xres;
+    const V3 zen = norm(lookat - campos);
+    const V3 y = norm(cross(zen, sky));
+    const V3 x = norm(cross(y, zen));
+    put(k.zen, zen);
+    put(k.ex, x);
+    put(k.ey, y);
+  } else {
+    const double fovfct = std::tan(r->fov * 0.5f * (kPi / 180.0));
+    sky = norm(sky);
+    const V3 zaxis = norm(centerpos - lookat);
+    const V3 xaxis = norm(cross(sky, zaxis));
+    const V3 yaxis = norm(cross(zaxis, xaxis));
+    const V3 dpx = xaxis * (fovfct / (0.5 * xres));
+    const V3 dpy = yaxis * (fovfct / (0.5 * xres));
+    const V3 newcenter = (centerpos - campos) * (1. / length(centerpos - lookat));
+    const V3 corner = newcenter - zaxis - dpx * (0.5 * xres) - dpy * (0.5 * yres);
+    put(k.p0, corner + dpx * .5 + dpy * .5);
+    put(k.dpx, dpx);
+    put(k.dpy, dpy);
+  }
+  put(k.campos, campos);
+  put(k.centerpos, centerpos);
+  k.zmax = d->zmax;
+  k.half_bfak = 0.5f * (0.5 * std::pow(kPi, -5. / 6.));
+  k.h2sigma = 0.5 * std::pow(kPi, -1. / 6.);
+  // real_host_rendering (new_renderer.cc:398-501)
+  double pixrad;
+  if (k.dome) {
+    pixrad = k.dp * kPi;
+  } else {
+    const V3 p0 = from(k.p0), dpx = from(k.dpx), dpy = from(k.dpy);
+    const double screendist = std::abs(dot(p0, norm(cross(dpx, dpy))));
+    pixrad = std::min(length(dpx), length(dpy)) / screendist;
+  }
+  const double mr = r->minrad_pix;
+  k.mr2pr2 = mr * mr * pixrad * pixrad;
+  k.screen = region_setup(k, 0, xres, 0, yres);
+  const double minpixperrad = 15;
+  double maxfac = 1. / (minpixperrad * pixrad);
+  maxfac = std::min(maxfac, std::min(xres, yres) / 10.);
+  int nsteps = 0;
+  while ((1 << nsteps) < maxfac) ++nsteps;
+  nsteps = std::max(nsteps - 1, 0);
+  if (nsteps + 1 > kRayMaxLevels)
+    return host_fail(SPL_ERR_UNSUPPORTED, "too many pyramid levels");
+  k.nlev = nsteps + 1;
+  for (int L = 0; L < k.nlev; ++L) {
+    const int fact = 1 << (nsteps - L);
+    RayLevel &lv = k.lev[L];
+    lv.fact = fact;
+    lv.xdim = xres;
+    lv.ydim = yres;
+    for (int f2 = fact; f2 > 1; f2 >>= 1) {
+      lv.xdim = (lv.xdim >> 1) + 1;
+      lv.ydim = (lv.ydim >> 1) + 1;
+    }
+    double minrad = minpixperrad * pixrad * fact;
+    double maxrad = std::min(1., 2 * minrad);
+    if (fact == 1) minrad = 0.;
+    if (fact == 1 << nsteps) maxrad = 1;
+    lv.minrad = minrad;
+    lv.maxrad = maxrad;
+    build_tree(k, L, f);
+  }
+  return SPL_OK;
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Device side.
+
+// Each particle of a level grid walks its level's region tree depth first;
+// a region it fails is not entered (its list would not hold the particle).
+constexpr int kWalkStack = 96;
+
+template <bool EMIT>
+__global__ void __launch_bounds__(128) k_rays_walk(RayConst k, const RayNode *__restrict__ nodes,
+                                                   const RayRegion *__restrict__ regs,
+                                                   const uint32_t *__restrict__ order,
+                                                   const uint32_t *__restrict__ code, int64_t n,
+                                                   RayParts p, uint32_t *__restrict__ count,
+                                                   const uint64_t *__restrict__ off,
+                                                   uint32_t *__restrict__ keys,
+                                                   uint32_t *__restrict__ vals) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t L = code[s];
+    if (L >= (uint32_t)k.nlev) {
+      if (!EMIT) count[s] = 0;
+      continue;
+    }
+    const uint32_t i = order[s];
+    const RayPart part = ray_part(k, p.rc[i], p.cf[i]);
+    uint64_t o = EMIT ? off[s] : 0;
+    uint32_t cnt = 0;
+    const RayNode root = nodes[k.lev[L].root];
+    if (root.leaf >= 0) {  // the whole grid is one leaf region: no test
+      if (EMIT) {
+        keys[o] = (uint32_t)root.leaf;
+        vals[o] = i;
+      }
+      cnt = 1;
+    } else {
+      int stack[kWalkStack];
+      int sp = 0;
+      for (int c = root.nchild - 1; c >= 0; --c) stack[sp++] = root.first_child + c;
+      while (sp > 0) {
+        const int nd = stack[--sp];
+        if (!ray_region_keeps(k, regs[nd], part)) continue;
+        const RayNode node = nodes[nd];
+        if (node.leaf >= 0) {
+          if (EMIT) {
+            keys[o + cnt] = (uint32_t)node.leaf;
+            vals[o + cnt] = i;
+          }
+          ++cnt;
+        } else if (sp + node.nchild <= kWalkStack) {
+          for (int c = node.nchild - 1; c >= 0; --c) stack[sp++] = node.first_child + c;
+        } else {
+          atomicOr(p.err, 16u);
+          break;
+        }
+      }
+    }
+    if (!EMIT) count[s] = cnt;
+  }
+}
+
+// One leaf region of level L per CTA, one pixel per thread (a leaf holds at
+// most 9 x 9 pixels).  The leaf's list is staged through shared memory in
+// list order; each pixel accumulates -e*w over the spheres its ray meets.
+template <bool TOP>
+__global__ void __launch_bounds__(kRayLeafThreads) k_rays_leaf(RayConst k, int L, RayParts p,
+                                                               RayLeafArgs a) {
+  const RayLevel &lv = k.lev[L];
+  const int leaf = lv.leaf0 + blockIdx.x;
+  const ushort4 box = a.leaf_box[leaf];
+  const int nx = box.y - box.x, ny = box.w - box.z;
+  const int t = threadIdx.x;
+  const bool has = t < nx * ny;
+  const int ix = box.x + (has ? t / ny : 0), iy = box.z + (has ? t % ny : 0);
+  __shared__ double s_u[3];
+  __shared__ unsigned s_rd;
+  __shared__ float4 s_a[kRayLeafThreads], s_b[kRayLeafThreads];
+  __shared__ float s_inv[kRayLeafThreads];
+  __shared__ uint32_t s_idx[kRayLeafThreads];
+  if (t == 0) {  // the leaf's reference direction: its middle pixel's
+    double u[3];
+    ray_pix_dir(k, (box.x + nx / 2) * lv.fact, (box.z + ny / 2) * lv.fact, u);
+    s_u[0] = u[0];
+    s_u[1] = u[1];
+    s_u[2] = u[2];
+    s_rd = 0u;
+  }
+  __syncthreads();
+  double d[3];
+  ray_pix_dir(k, ix * lv.fact, iy * lv.fact, d);
+  float dd[3];
+  for (int c = 0; c < 3; ++c) dd[c] = __double2float_rn(dsub(d[c], s_u[c]));
+  // largest |d - u|_1 of the leaf (non-negative floats order as their bits)
+  if (has)
+    atomicMax(&s_rd, __float_as_uint((fabsf(dd[0]) + fabsf(dd[1]) + fabsf(dd[2])) * 1.0001f));
+  __syncthreads();
+  const float rd1 = __uint_as_float(s_rd);
+
+  float od0 = 0.f, od1 = 0.f, od2 = 0.f;
+  const uint32_t e0 = a.leaf_start[leaf], e1 = a.leaf_start[leaf + 1];
+  for (uint32_t b0 = e0; b0 < e1; b0 += kRayLeafThreads) {
+    const uint32_t cnt = min((uint32_t)kRayLeafThreads, e1 - b0);
+    if ((uint32_t)t < cnt) {
+      const uint32_t i = a.vals[b0 + t];
+      const double4 rc = p.rc[i];
+      const float2 cv = p.cov[i];
+      const float4 e = p.pod[i];
+      const float c0 = __double2float_rn(dsub(rc.x, s_u[0]));
+      const float c1 = __double2float_rn(dsub(rc.y, s_u[1]));
+      const float c2 = __double2float_rn(dsub(rc.z, s_u[2]));
+      // |q - |d - c|^2| <= 2|d - c| E + E^2 + 3 ulp(q), E = 2^-23 (|d-u|_1 + |c-u|_1)
+      // + 7e-16 (the roundings of d-u, c-u and their difference); the margin
+      // doubles that at the limit cm and adds the rounding of cm itself.  No
+      // limit (cm < 0): every pixel is decided in double.
+      float lo = -1.f, hi = INFINITY;
+      if (cv.x >= 0.f) {
+        const float E = 1.2e-7f * (rd1 + fabsf(c0) + fabsf(c1) + fabsf(c2)) + 1e-15f;
+        const float m = 4.f * sqrtf(cv.x) * E + 2.f * E * E + 1e-6f * cv.x + 1e-13f;
+        lo = cv.x - m;
+        hi = cv.x + m;
+      }
+      s_a[t] = make_float4(c0, c1, c2, lo);
+      s_b[t] = make_float4(-e.x, -e.y, -e.z, hi);
+      s_inv[t] = cv.y * kLog2e;
+      s_idx[t] = i;
+    }
+    __syncthreads();
+    if (has) {
+#pragma unroll 4
+      for (uint32_t j = 0; j < cnt; ++j) {
+        const float4 A = s_a[j];
+        const float x0 = dd[0] - A.x, x1 = dd[1] - A.y, x2 = dd[2] - A.z;
+        const float q = fmaf(x2, x2, fmaf(x1, x1, x0 * x0));
+        const float4 B = s_b[j];
+        if (q > B.w) continue;  // the ray misses the sphere
+        float w;
+        if (q < A.w) {  // it meets it: sin^2 = q (1 - q/4)
+          const float sasq = q * fmaf(-0.25f, q, 1.f);
+          w = ex2(-sasq * s_inv[j]);
+        } else if (!ray_exact_hit(d, p.rc[s_idx[j]], k.h2sigma, w)) {
+          continue;
+        }
+        od0 = fmaf(B.x, w, od0);
+        od1 = fmaf(B.y, w, od1);
+        od2 = fmaf(B.z, w, od2);
+      }
+    }
+    __syncthreads();
+  }
+  if (!has) return;
+  if (TOP) {  // add_overlap2 (new_renderer.cc:367-393): spheres around the camera
+    const uint32_t s0 = a.lev_start[k.nlev], s1 = a.lev_start[k.nlev + 1];
+    float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+    for (uint32_t s = s0; s < s1; ++s) {
+      const uint32_t i = a.order[s];
+      const double4 rc = p.rc[i];
+      const double c[3] = {rc.x, rc.y, rc.z};
+      const double cosang = ddot3(d, c);
+      const double sasq = dmul(dsub(1.0, cosang), dadd(1.0, cosang));
+      const double fract = ddiv(sasq, dmul(dmul(dmul(rc.w, rc.w), k.h2sigma), k.h2sigma));
+      const double er = dmul(0.5, erfc(ddiv(-cosang, dmul(rc.w, k.h2sigma))));
+      const float w = fract != fract ? 1.f : (float)exp(-fract);
+      const float ew = __double2float_rn(er) * w;
+      const float4 e = p.pod[i];
+      o0 = fmaf(-e.x, ew, o0);
+      o1 = fmaf(-e.y, ew, o1);
+      o2 = fmaf(-e.z, ew, o2);
+    }
+    od0 = fadd(od0, o0);
+    od1 = fadd(od1, o1);
+    od2 = fadd(od2, o2);
+  } else {  // the coarser grid, upsampled (new_renderer.cc:509-515)
+    const float *C = a.coarse;
+    const size_t cy = (size_t)a.cdim_y;
+    const size_t pa = ((size_t)(ix >> 1) * cy + (iy >> 1)) * 3;
+    const size_t pb = ((size_t)((ix + 1) >> 1) * cy + (iy >> 1)) * 3;
+    const size_t pc = ((size_t)(ix >> 1) * cy + ((iy + 1) >> 1)) * 3;
+    const size_t pd = ((size_t)((ix + 1) >> 1) * cy + ((iy + 1) >> 1)) * 3;
+    float up[3];
+    for (int c = 0; c < 3; ++c)
+      up[c] = fmul(fadd(fadd(fadd(C[pa + c], C[pb + c]), C[pc + c]), C[pd + c]), 0.25f);
+    od0 = fadd(od0, up[0]);
+    od1 = fadd(od1, up[1]);
+    od2 = fadd(od2, up[2]);
+  }
+  float *o = a.out + ((size_t)ix * lv.ydim + iy) * 3;
+  o[0] = od0;
+  o[1] = od1;
+  o[2] = od2;
+}
+
+// First column j of each row i <= res/2 inside the fisheye circle, with the
+// reference's double arithmetic (new_renderer.cc:622-637).
+__global__ void k_dome_rows(int res, int *jstop) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > res / 2) return;
+  const double xf = ddiv(1.0, (double)(res - 1));
+  double x = dmul(dadd((double)i, 0.5), xf);
+  x = dsub(dmul(2.0, x), 1.0);
+  const double xx = dmul(x, x);
+  int j = 0;
+  for (; j < res; ++j) {
+    double y = dmul(dadd((double)j, 0.5), xf);
+    y = dsub(dmul(2.0, y), 1.0);
+    if (!(dadd(xx, dmul(y, y)) > 1.)) break;
+  }
+  jstop[i] = j;
+}
+
+// The reference zeroes (i, j), (i, res-1-j), (res-1-i, res-1-j), (res-1-i, j)
+// for every i <= res/2 and j < jstop[i].
+__global__ void k_dome_mask(float *pic, int res, const int *__restrict__ jstop) {
+  const int64_t np = (int64_t)res * res;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int a = (int)(q / res), b = (int)(q % res);
+    const int is[2] = {a, res - 1 - a}, js[2] = {b, res - 1 - b};
+    bool zero = false;
+    for (int u = 0; u < 2; ++u)
+      if (is[u] <= res / 2)
+        for (int v = 0; v < 2; ++v) zero = zero || js[v] < jstop[is[u]];
+    if (zero) {
+      pic[q * 3] = 0.f;
+      pic[q * 3 + 1] = 0.f;
+      pic[q * 3 + 2] = 0.f;
+    }
+  }
+}
+
+}  // namespace
+
+void launch_rays_walk(bool emit, const RayConst &k, const RayNode *nodes, const RayRegion *regs,
+                      const uint32_t *order, const uint32_t *code, int64_t n, const RayParts &p,
+                      uint32_t *count, const uint64_t *off, uint32_t *keys, uint32_t *vals,
+                      cudaStream_t s) {
+  if (n <= 0) return;
+  if (emit)
+    k_rays_walk<true><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, order, code, n, p, count,
+                                                        off, keys, vals);
+  else
+    k_rays_walk<false><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, order, code, n, p, count,
+                                                         off, keys, vals);
+}
+
+void launch_rays_leaves(const RayConst &k, int L, const RayParts &p, const RayLeafArgs &a,
+                        cudaStream_t s) {
+  const int nl = k.lev[L].nleaves;
+  if (nl <= 0) return;
+  if (L == 0)
+    k_rays_leaf<true><<<nl, kRayLeafThreads, 0, s>>>(k, L, p, a);
+  else
+    k_rays_leaf<false><<<nl, kRayLeafThreads, 0, s>>>(k, L, p, a);
+}
+
+void launch_rays_dome_mask(float *pic, int res, int *jstop, cudaStream_t s) {
+  if (res <= 0) return;
+  k_dome_rows<<<(res / 2 + 1 + 127) / 128, 128, 0, s>>>(res, jstop);
+  k_dome_mask<<<grid_for((int64_t)res * res, 256), 256, 0, s>>>(pic, res, jstop);
+}
+
+}  // namespace spl

@@ -2,7 +2,9 @@
 // with host_rendering_gb300.cc in place of splotch/splotch_host.cc.  It shows
 // that the shim is a drop-in at the link level: built against the Splotch
 // headers, resolved against libsplgpu.so.  Prints "rendered" after a frame, or
-// the PlanckError text when no GPU is present (exit code 3).
+// the PlanckError text when no GPU is present (exit code 3).  With the
+// argument "rays" the frame goes through the ray-sphere renderer
+// (new_renderer=true), after which the particle vector is empty.
 #include <cstdio>
 #include <map>
 #include <string>
@@ -10,9 +12,11 @@
 
 #include "splotch/splotch_host.h"
 
-int main() {
+int main(int argc, char **argv) {
+  const bool rays = argc > 1 && std::string(argv[1]) == "rays";
   std::map<std::string, std::string> kv = {
       {"xres", "48"}, {"yres", "40"}, {"fov", "45"}, {"tile_size_cpu", "16"}};
+  if (rays) kv["new_renderer"] = "T";
   paramfile params(kv, false);
   render_context rc;
   rc.campos = vec3(0, 0, 100);
@@ -37,6 +41,11 @@ int main() {
   } catch (PlanckError &e) {
     std::printf("planck: %s\n", e.what());
     return 3;
+  }
+  if (rays) {
+    std::printf("rendered rays, %d particles left, pic[24][20].b = %g\n", (int)p.size(),
+                rc.pic[24][20].b);
+    return p.empty() ? 0 : 4;
   }
   int active = 0;
   for (const auto &q : p) active += q.active;

@@ -36,9 +36,10 @@ def test_shim_links_in_place_of_splotch_host(built, tmp_path):
             f"-Wl,-rpath,{ROOT / 'splotch_gb300'}", "-o", str(exe)])
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
-    run = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
-    assert run.returncode in (0, 3), run.stdout + run.stderr
-    if run.returncode == 3:
-        assert "GB300 renderer" in run.stdout
-    else:
-        assert "rendered" in run.stdout
+    for args in ([], ["rays"]):  # the splat path, then new_renderer=true
+        run = subprocess.run([str(exe), *args], capture_output=True, text=True, timeout=120)
+        assert run.returncode in (0, 3), run.stdout + run.stderr
+        if run.returncode == 3:
+            assert "GB300 renderer" in run.stdout
+        else:
+            assert "rendered" in run.stdout
