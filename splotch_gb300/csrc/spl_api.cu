@@ -31,7 +31,8 @@ struct spl_context {
       tval, tkey2, tval2, tkey_s, tval_s, tile_start, wide_list, small, pic, pal_x, pal_rgb,
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
       poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes,
-      seg_cnt, seg_off, seg_state, ray_rc, ray_cf, ray_pod, ray_cov, ray_code, ray_lev,
+      seg_cnt, seg_off, seg_state, ray_rc, ray_cf, ray_pod, ray_cov, ray_code, ray_lev, ray_slots,
+      ray_kd, ray_segcnt, ray_segoff, ray_items, ray_partial,
       ray_nodes, ray_regs, ray_box, ray_leaf_start, ray_img[2], ray_jstop;
   // spl_render_rays: the host-built region trees of the last geometry
   struct RayKey {
@@ -365,7 +366,9 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->seg_off, &c->seg_state, &c->ray_rc, &c->ray_cf,
                               &c->ray_pod, &c->ray_cov, &c->ray_code, &c->ray_lev,
                               &c->ray_nodes, &c->ray_regs, &c->ray_box, &c->ray_leaf_start,
-                              &c->ray_img[0], &c->ray_img[1], &c->ray_jstop};
+                              &c->ray_img[0], &c->ray_img[1], &c->ray_jstop, &c->ray_slots,
+                              &c->ray_kd, &c->ray_segcnt, &c->ray_segoff, &c->ray_items,
+                              &c->ray_partial};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   delete c->rays;
@@ -978,6 +981,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   if ((st = ensure(c->ray_rc, n * 32)) || (st = ensure(c->ray_cf, n * 16)) ||
       (st = ensure(c->ray_pod, n * 16)) || (st = ensure(c->ray_cov, n * 8)) ||
       (st = ensure(c->ray_code, n * 4)) || (st = ensure(c->ray_lev, (nlev + 3) * 4)) ||
+      (st = ensure(c->ray_slots, n * 4 * spl::kRayWalkSlots)) ||
       (st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
       (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)) ||
       (st = ensure(c->count, n * 4)) || (st = ensure(c->off, (n + 1) * 8)) ||
@@ -1068,7 +1072,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   const spl::RayNode *d_nodes = as<spl::RayNode>(c->ray_nodes);
   const spl::RayRegion *d_regs = as<spl::RayRegion>(c->ray_regs);
   spl::launch_rays_walk(false, k, d_nodes, d_regs, order, code_s, n, rp, as<uint32_t>(c->count),
-                        nullptr, nullptr, nullptr, s);
+                        as<uint32_t>(c->ray_slots), nullptr, nullptr, nullptr, s);
   ++launches;
   spl::scan_counts(as<uint32_t>(c->count), nullptr, n, as<uint64_t>(c->off), c->scratch.p, s,
                    &launches);
@@ -1084,8 +1088,9 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
       (st = ensure(c->tkey_s, ne * 4)) || (st = ensure(c->tval_s, ne * 4)) ||
       (st = ensure(c->scratch, std::max(scr, spl::radix_scratch_bytes(ne)))))
     return st;
-  spl::launch_rays_walk(true, k, d_nodes, d_regs, order, code_s, n, rp, nullptr,
-                        as<uint64_t>(c->off), as<uint32_t>(c->tkey), as<uint32_t>(c->tval), s);
+  spl::launch_rays_walk(true, k, d_nodes, d_regs, order, code_s, n, rp, as<uint32_t>(c->count),
+                        as<uint32_t>(c->ray_slots), as<uint64_t>(c->off), as<uint32_t>(c->tkey),
+                        as<uint32_t>(c->tval), s);
   ++launches;
   if (ne > 0)
     spl::radix_sort_pairs(as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->tkey2),
@@ -1096,13 +1101,32 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   spl::launch_tile_ranges(as<uint32_t>(c->tkey_s), ne, nleaves, as<uint32_t>(c->ray_leaf_start),
                           s);
   ++launches;
+  // leaf lists cut into segments of kRaySegLen entries, one warp each
+  const int64_t max_items = nleaves + ne / spl::kRaySegLen + 1;
+  if ((st = ensure(c->ray_kd, sizeof(spl::RayConst))) ||
+      (st = ensure(c->ray_segcnt, nleaves * 4)) || (st = ensure(c->ray_segoff, (nleaves + 1) * 8)) ||
+      (st = ensure(c->ray_items, max_items * 4)) ||
+      (st = ensure(c->ray_partial, (size_t)max_items * spl::kRayLeafPixels * 3 * 4)) ||
+      (st = ensure(c->scratch, std::max(c->scratch.cap, spl::scan_scratch_bytes(nleaves + 1)))))
+    return st;
+  SPL_CK(cudaMemcpyAsync(c->ray_kd.p, &k, sizeof(k), cudaMemcpyHostToDevice, s));
+  spl::launch_rays_segments(as<uint32_t>(c->ray_leaf_start), nleaves, as<uint32_t>(c->ray_segcnt),
+                            s);
+  spl::scan_counts(as<uint32_t>(c->ray_segcnt), nullptr, nleaves, as<uint64_t>(c->ray_segoff),
+                   c->scratch.p, s, &launches);
+  spl::launch_rays_items(as<uint64_t>(c->ray_segoff), nleaves, as<uint32_t>(c->ray_items), s);
+  launches += 2;
   cudaEventRecord(c->ev[4], s);
 
   // ---- the pyramid, coarsest level first -----------------------------------------
   float *final_pic = out->memspace == SPL_MEM_HOST ? as<float>(c->pic) : out->pic;
   spl::RayLeafArgs la{};
+  la.kd = as<spl::RayConst>(c->ray_kd);
   la.leaf_box = as<ushort4>(c->ray_box);
   la.leaf_start = as<uint32_t>(c->ray_leaf_start);
+  la.seg_off = as<uint64_t>(c->ray_segoff);
+  la.item_leaf = as<uint32_t>(c->ray_items);
+  la.partial = as<float>(c->ray_partial);
   la.vals = as<uint32_t>(c->tval_s);
   la.order = order;
   la.lev_start = lev_start;
@@ -1111,7 +1135,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
     la.coarse = L > 0 ? as<float>(c->ray_img[(L - 1) & 1]) : nullptr;
     la.cdim_y = L > 0 ? k.lev[L - 1].ydim : 0;
     spl::launch_rays_leaves(k, L, rp, la, s);
-    ++launches;
+    launches += 2;
   }
   if (k.dome) {
     spl::launch_rays_dome_mask(final_pic, xres, as<int>(c->ray_jstop), s);
@@ -1127,7 +1151,6 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   SPL_CK(cudaGetLastError());
   if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
   if (err & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
-  if (err & 16u) return fail(SPL_ERR_CAPACITY, "region-tree walk stack overflow");
   if (err & 32u) return fail(SPL_ERR_INVALID, "a particle fell in two pyramid levels");
 
   spl_stats &S = c->stats;

@@ -520,22 +520,26 @@ int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s);
 // tree of image regions (the reference's recursive subdivision) whose
 // culling test (reduceList) decides which particles a leaf region lists.
 constexpr int kRayMaxLevels = 16;
-constexpr int kRayLeafThreads = 96;  // a leaf region holds at most 9 x 9 pixels
+constexpr int kRayLeafWarps = 4;  // leaf regions per CTA, one warp each
+constexpr int kRayWalkSlots = 8;  // leaves a particle's first walk keeps
 
 // reduceList parameters of one region (new_renderer.cc:77-101, 164-213),
 // computed on the host in double exactly as the reference computes them.
 struct RayRegion {
-  float nf[4][3];      // plane: the side normals rounded to float (screening)
+  float nf[4][3];      // n rounded to float (screening)
   double n[4][3];      // plane: side normals; dome: n[0] = nx0, n[1] = nx1
   double cthetamin, cthetamax, thetamin, thetamax;  // dome
   int centered;        // dome
   int pad;
 };
+// One region of a level's tree as the walk reads it (64 bytes): the float
+// test vectors and the links of a depth-first walk without a stack.
 struct RayNode {
-  int first_child;  // children are contiguous; -1 for a leaf
-  int nchild;
+  float4 f[3];      // RayRegion::nf
+  int first_child;  // -1 for a leaf
+  int skip;         // the next node after this subtree in depth-first order (-1: none)
   int leaf;         // global leaf id, or -1
-  int pad;
+  int centered;     // dome: RayRegion::centered
 };
 struct RayLevel {
   int fact, xdim, ydim;
@@ -570,27 +574,45 @@ struct RayParts {
 void launch_rays_prep(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &pc,
                       const RayConst &k, const RayParts &o, cudaStream_t s);
 // Walk of every particle of the level grids (order/code: the particles sorted
-// by code, n entries) through its level's region tree: count (EMIT false:
-// leaves reached per sorted position) or emit (leaf id, particle) pairs at
-// off[s].  Bit 4 of *err: the walk's stack overflowed.
+// by code, n entries) through its level's region tree.  Count pass (emit
+// false): leaves reached per sorted position into count, the first
+// kRayWalkSlots of them into slots (n * kRayWalkSlots).  Emit pass: (leaf id,
+// particle) pairs at off[s], copied from the slots, or walked again for a
+// particle that reached more leaves.
 void launch_rays_walk(bool emit, const RayConst &k, const RayNode *nodes, const RayRegion *regs,
                       const uint32_t *order, const uint32_t *code, int64_t n, const RayParts &p,
-                      uint32_t *count, const uint64_t *off, uint32_t *keys, uint32_t *vals,
-                      cudaStream_t s);
+                      uint32_t *count, uint32_t *slots, const uint64_t *off, uint32_t *keys,
+                      uint32_t *vals, cudaStream_t s);
 // One pyramid level: every leaf region of level L (leaf ranges in leaf_start,
-// entries' particles in vals).  The coarsest level adds the spheres around
-// the camera (order[ov0, ov1)); the others add the coarser level's grid
-// (coarse, cdim_y rows per column) upsampled.  out: x-major xdim*ydim*3.
+// entries' particles in vals).  A leaf's list is cut into segments of
+// kRaySegLen entries, one warp each (seg_off: exclusive scan of the segments
+// per leaf, item_leaf: the leaf of each segment); a leaf of one segment is
+// finished by its warp, the segments of a longer one leave partial sums that
+// a second kernel folds in segment order.  Finishing adds the spheres around
+// the camera (order[lev_start[nlev] .. lev_start[nlev+1]]) on the coarsest
+// level, the coarser level's grid (coarse, cdim_y rows per column) upsampled
+// on the others.  out: x-major xdim*ydim*3.
+constexpr uint32_t kRaySegLen = 256;
+constexpr int kRayLeafPixels = 81;  // a leaf region holds at most 9 x 9 pixels
 struct RayLeafArgs {
+  const RayConst *kd;        // the frame's constants in device memory
   const ushort4 *leaf_box;   // x0, x1, y0, y1 in level pixels
   const uint32_t *leaf_start;
+  const uint64_t *seg_off;   // nleaves + 1
+  const uint32_t *item_leaf;
   const uint32_t *vals;
   const uint32_t *order;
   const uint32_t *lev_start; // code ranges in the sorted order (nlev + 3)
+  float *partial;            // per segment item, kRayLeafPixels * 3 floats
   const float *coarse;
   int cdim_y;
   float *out;
 };
+// Segments per leaf (every leaf, at least one) and the item -> leaf table.
+void launch_rays_segments(const uint32_t *leaf_start, int64_t nleaves, uint32_t *cnt,
+                          cudaStream_t s);
+void launch_rays_items(const uint64_t *seg_off, int64_t nleaves, uint32_t *item_leaf,
+                       cudaStream_t s);
 void launch_rays_leaves(const RayConst &k, int L, const RayParts &p, const RayLeafArgs &a,
                         cudaStream_t s);
 // The dome's post step (new_renderer.cc:619-639): pixels outside the fisheye

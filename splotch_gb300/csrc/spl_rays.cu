@@ -131,6 +131,8 @@ RayRegion region_setup(const RayConst &k, int ix0, int ix1, int iy0, int iy1) {
   if (dot(c, nx1) > 0) nx1 = v3(-nx1.x, -nx1.y, -nx1.z);
   put(g.n[0], nx0);
   put(g.n[1], nx1);
+  for (int i = 0; i < 2; ++i)
+    for (int a = 0; a < 3; ++a) g.nf[i][a] = (float)g.n[i][a];
   g.centered = centered ? 1 : 0;
   g.thetamin = thetamin;
   g.thetamax = thetamax;
@@ -142,14 +144,27 @@ RayRegion region_setup(const RayConst &k, int ix0, int ix1, int iy0, int iy1) {
 // subrender4's subdivision of one level's grid (new_renderer.cc:280-360):
 // a region of 10 or more pixels in either direction splits in two along a
 // direction more than sqrt(2) times longer than the other, else in four.
+// Children are stored together; skip links give the depth-first order.
+RayNode node_of(const RayRegion &g) {
+  RayNode nd;
+  std::memset(&nd, 0, sizeof(nd));
+  const float *f = &g.nf[0][0];
+  for (int i = 0; i < 3; ++i) nd.f[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
+  nd.first_child = -1;
+  nd.skip = -1;
+  nd.leaf = -1;
+  nd.centered = g.centered;
+  return nd;
+}
+
 void build_tree(RayConst &k, int L, RayFrame &f) {
   RayLevel &lv = k.lev[L];
   std::vector<int4> box;  // x0, x1, y0, y1 of each node of this level
   const int base = (int)f.nodes.size();
   lv.root = base;
   lv.leaf0 = (int)f.leaf_box.size();
-  f.nodes.push_back(RayNode{-1, 0, -1, 0});
   f.regs.push_back(RayRegion{});
+  f.nodes.push_back(node_of(f.regs.back()));
   box.push_back(make_int4(0, lv.xdim, 0, lv.ydim));
   const int fact = lv.fact;
   for (size_t q = 0; q < box.size(); ++q) {
@@ -179,13 +194,16 @@ void build_tree(RayConst &k, int L, RayFrame &f) {
       ch[3] = make_int4(xm, b.y, ym, b.w);
       nch = 4;
     }
-    f.nodes[base + q].first_child = (int)f.nodes.size();
-    f.nodes[base + q].nchild = nch;
+    const int first = (int)f.nodes.size();
+    const int parent_skip = f.nodes[base + q].skip;
+    f.nodes[base + q].first_child = first;
     for (int i = 0; i < nch; ++i) {
       const int4 c = ch[i];
-      f.nodes.push_back(RayNode{-1, 0, -1, 0});
       f.regs.push_back(region_setup(k, c.x * fact, (c.y - 1) * fact + 1, c.z * fact,
                                     (c.w - 1) * fact + 1));
+      RayNode nd = node_of(f.regs.back());
+      nd.skip = i + 1 < nch ? first + i + 1 : parent_skip;
+      f.nodes.push_back(nd);
       box.push_back(c);
     }
   }
@@ -283,19 +301,15 @@ namespace {
 // ---------------------------------------------------------------------------
 // Device side.
 
-// Each particle of a level grid walks its level's region tree depth first;
-// a region it fails is not entered (its list would not hold the particle).
-constexpr int kWalkStack = 96;
-
+// Each particle of a level grid walks its level's region tree depth first,
+// without a stack: a region it passes is entered (its first child next), a
+// region it fails is stepped over (its skip link next).
 template <bool EMIT>
-__global__ void __launch_bounds__(128) k_rays_walk(RayConst k, const RayNode *__restrict__ nodes,
-                                                   const RayRegion *__restrict__ regs,
-                                                   const uint32_t *__restrict__ order,
-                                                   const uint32_t *__restrict__ code, int64_t n,
-                                                   RayParts p, uint32_t *__restrict__ count,
-                                                   const uint64_t *__restrict__ off,
-                                                   uint32_t *__restrict__ keys,
-                                                   uint32_t *__restrict__ vals) {
+__global__ void __launch_bounds__(128) k_rays_walk(
+    RayConst k, const RayNode *__restrict__ nodes, const RayRegion *__restrict__ regs,
+    const uint32_t *__restrict__ order, const uint32_t *__restrict__ code, int64_t n, RayParts p,
+    uint32_t *__restrict__ count, uint32_t *__restrict__ slots, const uint64_t *__restrict__ off,
+    uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
        s += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t L = code[s];
@@ -304,35 +318,45 @@ __global__ void __launch_bounds__(128) k_rays_walk(RayConst k, const RayNode *__
       continue;
     }
     const uint32_t i = order[s];
+    uint64_t o = 0;
+    if (EMIT) {
+      const uint32_t c = count[s];
+      o = off[s];
+      if (c <= (uint32_t)kRayWalkSlots) {  // the first walk kept them all
+        for (uint32_t j = 0; j < c; ++j) {
+          keys[o + j] = slots[(size_t)s * kRayWalkSlots + j];
+          vals[o + j] = i;
+        }
+        continue;
+      }
+    }
     const RayPart part = ray_part(k, p.rc[i], p.cf[i]);
-    uint64_t o = EMIT ? off[s] : 0;
     uint32_t cnt = 0;
+    auto emit = [&](int leaf) {
+      if (EMIT) {
+        keys[o + cnt] = (uint32_t)leaf;
+        vals[o + cnt] = i;
+      } else if (cnt < (uint32_t)kRayWalkSlots) {
+        slots[(size_t)s * kRayWalkSlots + cnt] = (uint32_t)leaf;
+      }
+      ++cnt;
+    };
     const RayNode root = nodes[k.lev[L].root];
     if (root.leaf >= 0) {  // the whole grid is one leaf region: no test
-      if (EMIT) {
-        keys[o] = (uint32_t)root.leaf;
-        vals[o] = i;
-      }
-      cnt = 1;
+      emit(root.leaf);
     } else {
-      int stack[kWalkStack];
-      int sp = 0;
-      for (int c = root.nchild - 1; c >= 0; --c) stack[sp++] = root.first_child + c;
-      while (sp > 0) {
-        const int nd = stack[--sp];
-        if (!ray_region_keeps(k, regs[nd], part)) continue;
+      int nd = root.first_child;
+      while (nd >= 0) {
         const RayNode node = nodes[nd];
-        if (node.leaf >= 0) {
-          if (EMIT) {
-            keys[o + cnt] = (uint32_t)node.leaf;
-            vals[o + cnt] = i;
+        if (ray_keeps(k, &node.f[0].x, node.centered, regs[nd], part, false)) {
+          if (node.leaf >= 0) {
+            emit(node.leaf);
+            nd = node.skip;
+          } else {
+            nd = node.first_child;
           }
-          ++cnt;
-        } else if (sp + node.nchild <= kWalkStack) {
-          for (int c = node.nchild - 1; c >= 0; --c) stack[sp++] = node.first_child + c;
         } else {
-          atomicOr(p.err, 16u);
-          break;
+          nd = node.skip;
         }
       }
     }
@@ -340,134 +364,248 @@ __global__ void __launch_bounds__(128) k_rays_walk(RayConst k, const RayNode *__
   }
 }
 
-// One leaf region of level L per CTA, one pixel per thread (a leaf holds at
-// most 9 x 9 pixels).  The leaf's list is staged through shared memory in
-// list order; each pixel accumulates -e*w over the spheres its ray meets.
-template <bool TOP>
-__global__ void __launch_bounds__(kRayLeafThreads) k_rays_leaf(RayConst k, int L, RayParts p,
-                                                               RayLeafArgs a) {
-  const RayLevel &lv = k.lev[L];
-  const int leaf = lv.leaf0 + blockIdx.x;
-  const ushort4 box = a.leaf_box[leaf];
-  const int nx = box.y - box.x, ny = box.w - box.z;
-  const int t = threadIdx.x;
-  const bool has = t < nx * ny;
-  const int ix = box.x + (has ? t / ny : 0), iy = box.z + (has ? t % ny : 0);
-  __shared__ double s_u[3];
-  __shared__ unsigned s_rd;
-  __shared__ float4 s_a[kRayLeafThreads], s_b[kRayLeafThreads];
-  __shared__ float s_inv[kRayLeafThreads];
-  __shared__ uint32_t s_idx[kRayLeafThreads];
-  if (t == 0) {  // the leaf's reference direction: its middle pixel's
-    double u[3];
-    ray_pix_dir(k, (box.x + nx / 2) * lv.fact, (box.z + ny / 2) * lv.fact, u);
-    s_u[0] = u[0];
-    s_u[1] = u[1];
-    s_u[2] = u[2];
-    s_rd = 0u;
-  }
-  __syncthreads();
+// Direction of full-resolution pixel (X, Y) in double, out of line (once
+// per pixel and leaf segment).
+__device__ __noinline__ double3 ray_dir3(const RayConst *__restrict__ kd, int X, int Y) {
   double d[3];
-  ray_pix_dir(k, ix * lv.fact, iy * lv.fact, d);
-  float dd[3];
-  for (int c = 0; c < 3; ++c) dd[c] = __double2float_rn(dsub(d[c], s_u[c]));
-  // largest |d - u|_1 of the leaf (non-negative floats order as their bits)
-  if (has)
-    atomicMax(&s_rd, __float_as_uint((fabsf(dd[0]) + fabsf(dd[1]) + fabsf(dd[2])) * 1.0001f));
-  __syncthreads();
-  const float rd1 = __uint_as_float(s_rd);
+  ray_pix_dir(*kd, X, Y, d);
+  return make_double3(d[0], d[1], d[2]);
+}
 
-  float od0 = 0.f, od1 = 0.f, od2 = 0.f;
-  const uint32_t e0 = a.leaf_start[leaf], e1 = a.leaf_start[leaf + 1];
-  for (uint32_t b0 = e0; b0 < e1; b0 += kRayLeafThreads) {
-    const uint32_t cnt = min((uint32_t)kRayLeafThreads, e1 - b0);
-    if ((uint32_t)t < cnt) {
-      const uint32_t i = a.vals[b0 + t];
-      const double4 rc = p.rc[i];
-      const float2 cv = p.cov[i];
-      const float4 e = p.pod[i];
-      const float c0 = __double2float_rn(dsub(rc.x, s_u[0]));
-      const float c1 = __double2float_rn(dsub(rc.y, s_u[1]));
-      const float c2 = __double2float_rn(dsub(rc.z, s_u[2]));
-      // |q - |d - c|^2| <= 2|d - c| E + E^2 + 3 ulp(q), E = 2^-23 (|d-u|_1 + |c-u|_1)
-      // + 7e-16 (the roundings of d-u, c-u and their difference); the margin
-      // doubles that at the limit cm and adds the rounding of cm itself.  No
-      // limit (cm < 0): every pixel is decided in double.
-      float lo = -1.f, hi = INFINITY;
-      if (cv.x >= 0.f) {
-        const float E = 1.2e-7f * (rd1 + fabsf(c0) + fabsf(c1) + fabsf(c2)) + 1e-15f;
-        const float m = 4.f * sqrtf(cv.x) * E + 2.f * E * E + 1e-6f * cv.x + 1e-13f;
-        lo = cv.x - m;
-        hi = cv.x + m;
-      }
-      s_a[t] = make_float4(c0, c1, c2, lo);
-      s_b[t] = make_float4(-e.x, -e.y, -e.z, hi);
-      s_inv[t] = cv.y * kLog2e;
-      s_idx[t] = i;
-    }
-    __syncthreads();
-    if (has) {
-#pragma unroll 4
-      for (uint32_t j = 0; j < cnt; ++j) {
-        const float4 A = s_a[j];
-        const float x0 = dd[0] - A.x, x1 = dd[1] - A.y, x2 = dd[2] - A.z;
-        const float q = fmaf(x2, x2, fmaf(x1, x1, x0 * x0));
-        const float4 B = s_b[j];
-        if (q > B.w) continue;  // the ray misses the sphere
-        float w;
-        if (q < A.w) {  // it meets it: sin^2 = q (1 - q/4)
-          const float sasq = q * fmaf(-0.25f, q, 1.f);
-          w = ex2(-sasq * s_inv[j]);
-        } else if (!ray_exact_hit(d, p.rc[s_idx[j]], k.h2sigma, w)) {
-          continue;
-        }
-        od0 = fmaf(B.x, w, od0);
-        od1 = fmaf(B.y, w, od1);
-        od2 = fmaf(B.z, w, od2);
-      }
-    }
-    __syncthreads();
+// add_overlap2 (new_renderer.cc:367-393) at full-resolution pixel (X, Y):
+// the spheres around the camera, order[s0, s1), each weighted by the erfc
+// of its near half (no coverage test).
+__device__ __noinline__ float4 ray_overlap(const RayConst *__restrict__ kd, int X, int Y,
+                                           const uint32_t *__restrict__ order, uint32_t s0,
+                                           uint32_t s1, const double4 *__restrict__ rcs,
+                                           const float4 *__restrict__ pods) {
+  double d[3];
+  ray_pix_dir(*kd, X, Y, d);
+  const double h2 = kd->h2sigma;
+  float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+  for (uint32_t s = s0; s < s1; ++s) {
+    const uint32_t i = order[s];
+    const double4 rc = rcs[i];
+    const double c[3] = {rc.x, rc.y, rc.z};
+    const double cosang = ddot3(d, c);
+    const double sasq = dmul(dsub(1.0, cosang), dadd(1.0, cosang));
+    const double fract = ddiv(sasq, dmul(dmul(dmul(rc.w, rc.w), h2), h2));
+    const double er = dmul(0.5, erfc(ddiv(-cosang, dmul(rc.w, h2))));
+    const float w = fract != fract ? 1.f : (float)exp(-fract);
+    const float ew = __double2float_rn(er) * w;
+    const float4 e = pods[i];
+    o0 = fmaf(-e.x, ew, o0);
+    o1 = fmaf(-e.y, ew, o1);
+    o2 = fmaf(-e.z, ew, o2);
   }
-  if (!has) return;
-  if (TOP) {  // add_overlap2 (new_renderer.cc:367-393): spheres around the camera
-    const uint32_t s0 = a.lev_start[k.nlev], s1 = a.lev_start[k.nlev + 1];
-    float o0 = 0.f, o1 = 0.f, o2 = 0.f;
-    for (uint32_t s = s0; s < s1; ++s) {
-      const uint32_t i = a.order[s];
-      const double4 rc = p.rc[i];
-      const double c[3] = {rc.x, rc.y, rc.z};
-      const double cosang = ddot3(d, c);
-      const double sasq = dmul(dsub(1.0, cosang), dadd(1.0, cosang));
-      const double fract = ddiv(sasq, dmul(dmul(dmul(rc.w, rc.w), k.h2sigma), k.h2sigma));
-      const double er = dmul(0.5, erfc(ddiv(-cosang, dmul(rc.w, k.h2sigma))));
-      const float w = fract != fract ? 1.f : (float)exp(-fract);
-      const float ew = __double2float_rn(er) * w;
-      const float4 e = p.pod[i];
-      o0 = fmaf(-e.x, ew, o0);
-      o1 = fmaf(-e.y, ew, o1);
-      o2 = fmaf(-e.z, ew, o2);
-    }
-    od0 = fadd(od0, o0);
-    od1 = fadd(od1, o1);
-    od2 = fadd(od2, o2);
-  } else {  // the coarser grid, upsampled (new_renderer.cc:509-515)
+  return make_float4(o0, o1, o2, 0.f);
+}
+
+// A leaf pixel's final value: its sum over the leaf's list plus the spheres
+// around the camera (coarsest level) or the coarser grid upsampled
+// (new_renderer.cc:509-515).
+template <bool TOP>
+__device__ __forceinline__ void ray_finish(const RayConst &k, const RayLevel &lv,
+                                           const RayLeafArgs &a, const RayParts &p, int x, int y,
+                                           float od0, float od1, float od2) {
+  if (TOP) {
+    const float4 o = ray_overlap(a.kd, x * lv.fact, y * lv.fact, a.order, a.lev_start[k.nlev],
+                                 a.lev_start[k.nlev + 1], p.rc, p.pod);
+    od0 = fadd(od0, o.x);
+    od1 = fadd(od1, o.y);
+    od2 = fadd(od2, o.z);
+  } else {
     const float *C = a.coarse;
     const size_t cy = (size_t)a.cdim_y;
-    const size_t pa = ((size_t)(ix >> 1) * cy + (iy >> 1)) * 3;
-    const size_t pb = ((size_t)((ix + 1) >> 1) * cy + (iy >> 1)) * 3;
-    const size_t pc = ((size_t)(ix >> 1) * cy + ((iy + 1) >> 1)) * 3;
-    const size_t pd = ((size_t)((ix + 1) >> 1) * cy + ((iy + 1) >> 1)) * 3;
-    float up[3];
-    for (int c = 0; c < 3; ++c)
-      up[c] = fmul(fadd(fadd(fadd(C[pa + c], C[pb + c]), C[pc + c]), C[pd + c]), 0.25f);
-    od0 = fadd(od0, up[0]);
-    od1 = fadd(od1, up[1]);
-    od2 = fadd(od2, up[2]);
+    const size_t pa = ((size_t)(x >> 1) * cy + (y >> 1)) * 3;
+    const size_t pb = ((size_t)((x + 1) >> 1) * cy + (y >> 1)) * 3;
+    const size_t pc = ((size_t)(x >> 1) * cy + ((y + 1) >> 1)) * 3;
+    const size_t pd = ((size_t)((x + 1) >> 1) * cy + ((y + 1) >> 1)) * 3;
+    od0 = fadd(od0, fmul(fadd(fadd(fadd(C[pa], C[pb]), C[pc]), C[pd]), 0.25f));
+    od1 = fadd(od1, fmul(fadd(fadd(fadd(C[pa + 1], C[pb + 1]), C[pc + 1]), C[pd + 1]), 0.25f));
+    od2 = fadd(od2, fmul(fadd(fadd(fadd(C[pa + 2], C[pb + 2]), C[pc + 2]), C[pd + 2]), 0.25f));
   }
-  float *o = a.out + ((size_t)ix * lv.ydim + iy) * 3;
+  float *o = a.out + ((size_t)x * lv.ydim + y) * 3;
   o[0] = od0;
   o[1] = od1;
   o[2] = od2;
+}
+
+// One segment (kRaySegLen list entries) of one leaf region per warp, over
+// every segment of level L (persistent warps).  Lane l owns pixels l, l+32,
+// l+64 of the leaf (column-major within it).  The segment is staged through
+// the warp's shared slice 32 entries at a time, in list order; each pixel
+// accumulates -e*w over the spheres its ray meets.
+template <bool TOP>
+__global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, int L, RayParts p,
+                                                                  RayLeafArgs a) {
+  const RayLevel &lv = k.lev[L];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ float4 s_a[kRayLeafWarps][32], s_b[kRayLeafWarps][32];
+  __shared__ float s_inv[kRayLeafWarps][32];
+  __shared__ uint32_t s_idx[kRayLeafWarps][32];
+  __shared__ double s_d[kRayLeafWarps][3][96];  // the pixels' directions in double
+  const uint64_t it0 = a.seg_off[lv.leaf0], it1 = a.seg_off[lv.leaf0 + lv.nleaves];
+  const int fact = lv.fact;
+  for (uint64_t item = it0 + (uint64_t)blockIdx.x * kRayLeafWarps + warp; item < it1;
+       item += (uint64_t)gridDim.x * kRayLeafWarps) {
+    const uint32_t leaf = a.item_leaf[item];
+    const uint64_t first = a.seg_off[leaf];
+    const uint32_t nseg = (uint32_t)(a.seg_off[leaf + 1] - first);
+    const uint32_t sidx = (uint32_t)(item - first);
+    const ushort4 box = a.leaf_box[leaf];
+    const int nx = box.y - box.x, ny = box.w - box.z;
+    const int npx = nx * ny;
+    const int npl = (npx + 31) >> 5;  // pixels per lane, warp-uniform
+
+    // the leaf's reference direction u: its first pixel's
+    double3 u = make_double3(0.0, 0.0, 0.0);
+    if (lane == 0) u = ray_dir3(a.kd, box.x * fact, box.z * fact);
+    u.x = __shfl_sync(0xffffffffu, u.x, 0);
+    u.y = __shfl_sync(0xffffffffu, u.y, 0);
+    u.z = __shfl_sync(0xffffffffu, u.z, 0);
+    float dd[3][3], od[3][3];
+    int ix[3], iy[3];
+    bool has[3];
+    float l1max = 0.f;
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const int q = lane + 32 * m;
+      has[m] = q < npx;
+      ix[m] = box.x + (has[m] ? q / ny : 0);
+      iy[m] = box.z + (has[m] ? q % ny : 0);
+      od[m][0] = od[m][1] = od[m][2] = 0.f;
+      dd[m][0] = dd[m][1] = dd[m][2] = 0.f;
+      if (m < npl) {
+        const double3 d = ray_dir3(a.kd, ix[m] * fact, iy[m] * fact);
+        s_d[warp][0][lane + 32 * m] = d.x;
+        s_d[warp][1][lane + 32 * m] = d.y;
+        s_d[warp][2][lane + 32 * m] = d.z;
+        dd[m][0] = __double2float_rn(dsub(d.x, u.x));
+        dd[m][1] = __double2float_rn(dsub(d.y, u.y));
+        dd[m][2] = __double2float_rn(dsub(d.z, u.z));
+        const float l1 = fabsf(dd[m][0]) + fabsf(dd[m][1]) + fabsf(dd[m][2]);
+        if (has[m]) l1max = l1 == l1 ? fmaxf(l1max, l1) : INFINITY;  // NaN: a NaN direction
+      }
+    }
+    // largest |d - u|_1 of the leaf (non-negative floats order as their bits)
+    const float rd1 = __uint_as_float(
+        __reduce_max_sync(0xffffffffu, __float_as_uint(l1max * 1.0001f)));
+
+    const uint32_t l0 = a.leaf_start[leaf];
+    const uint32_t e0 = l0 + sidx * kRaySegLen;
+    const uint32_t e1 = min(a.leaf_start[leaf + 1], e0 + kRaySegLen);
+    for (uint32_t b0 = e0; b0 < e1; b0 += 32) {
+      const uint32_t cnt = min(32u, e1 - b0);
+      if ((uint32_t)lane < cnt) {
+        const uint32_t i = a.vals[b0 + lane];
+        const double4 rc = p.rc[i];
+        const float2 cv = p.cov[i];
+        const float4 e = p.pod[i];
+        const float c0 = __double2float_rn(dsub(rc.x, u.x));
+        const float c1 = __double2float_rn(dsub(rc.y, u.y));
+        const float c2 = __double2float_rn(dsub(rc.z, u.z));
+        // |q - |d - c|^2| <= 2|d - c| E + E^2 + 3 ulp(q), E = 2^-23 (|d-u|_1 + |c-u|_1)
+        // + 7e-16 (the roundings of d-u, c-u and their difference); the
+        // margin doubles that at the limit cm and adds the rounding of cm
+        // itself.  No limit (cm < 0), or a NaN direction in the leaf (rd1
+        // infinite): every pixel is decided in double.
+        float lo = -1.f, hi = INFINITY;
+        if (cv.x >= 0.f && rd1 < INFINITY) {
+          const float E = 1.2e-7f * (rd1 + fabsf(c0) + fabsf(c1) + fabsf(c2)) + 1e-15f;
+          const float mg = 4.f * sqrtf(cv.x) * E + 2.f * E * E + 1e-6f * cv.x + 1e-13f;
+          lo = cv.x - mg;
+          hi = cv.x + mg;
+        }
+        s_a[warp][lane] = make_float4(c0, c1, c2, lo);
+        s_b[warp][lane] = make_float4(-e.x, -e.y, -e.z, hi);
+        s_inv[warp][lane] = cv.y * kLog2e;
+        s_idx[warp][lane] = i;
+      }
+      __syncwarp();
+      for (uint32_t j = 0; j < cnt; ++j) {
+        const float4 A = s_a[warp][j];
+        const float4 B = s_b[warp][j];
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          if (m >= npl) break;
+          const float x0 = dd[m][0] - A.x, x1 = dd[m][1] - A.y, x2 = dd[m][2] - A.z;
+          const float q = fmaf(x2, x2, fmaf(x1, x1, x0 * x0));
+          if (!has[m] || q > B.w) continue;  // the ray misses the sphere
+          float w;
+          if (q < A.w) {  // it meets it: sin^2 = q (1 - q/4)
+            const float sasq = q * fmaf(-0.25f, q, 1.f);
+            w = ex2(-sasq * s_inv[warp][j]);
+          } else {  // within the margin: the reference's double test
+            const int q = lane + 32 * m;
+            const double d[3] = {s_d[warp][0][q], s_d[warp][1][q], s_d[warp][2][q]};
+            if (!ray_exact_hit(d, p.rc[s_idx[warp][j]], k.h2sigma, w)) continue;
+          }
+          od[m][0] = fmaf(B.x, w, od[m][0]);
+          od[m][1] = fmaf(B.y, w, od[m][1]);
+          od[m][2] = fmaf(B.z, w, od[m][2]);
+        }
+      }
+      __syncwarp();
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (!has[m]) continue;
+      if (nseg == 1) {
+        ray_finish<TOP>(k, lv, a, p, ix[m], iy[m], od[m][0], od[m][1], od[m][2]);
+      } else {  // this segment's sums, folded by k_rays_fold
+        float *pp = a.partial + (size_t)item * (kRayLeafPixels * 3) + (lane + 32 * m) * 3;
+        pp[0] = od[m][0];
+        pp[1] = od[m][1];
+        pp[2] = od[m][2];
+      }
+    }
+  }
+}
+
+// Leaves of level L cut into several segments: each pixel's segment sums
+// added in segment order (list order), then finished.  One warp per leaf.
+template <bool TOP>
+__global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_fold(RayConst k, int L, RayParts p,
+                                                                  RayLeafArgs a) {
+  const RayLevel &lv = k.lev[L];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int li = blockIdx.x * kRayLeafWarps + warp; li < lv.nleaves;
+       li += gridDim.x * kRayLeafWarps) {
+    const uint32_t leaf = lv.leaf0 + li;
+    const uint64_t first = a.seg_off[leaf];
+    const uint32_t nseg = (uint32_t)(a.seg_off[leaf + 1] - first);
+    if (nseg < 2) continue;
+    const ushort4 box = a.leaf_box[leaf];
+    const int ny = box.w - box.z;
+    const int npx = (box.y - box.x) * ny;
+    for (int q = lane; q < npx; q += 32) {
+      float v0 = 0.f, v1 = 0.f, v2 = 0.f;
+      for (uint32_t sg = 0; sg < nseg; ++sg) {
+        const float *pp = a.partial + (size_t)(first + sg) * (kRayLeafPixels * 3) + q * 3;
+        v0 = fadd(v0, pp[0]);
+        v1 = fadd(v1, pp[1]);
+        v2 = fadd(v2, pp[2]);
+      }
+      ray_finish<TOP>(k, lv, a, p, box.x + q / ny, box.z + q % ny, v0, v1, v2);
+    }
+  }
+}
+
+__global__ void k_rays_segments(const uint32_t *__restrict__ leaf_start, int64_t nleaves,
+                                uint32_t *__restrict__ cnt) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nleaves;
+       l += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t len = leaf_start[l + 1] - leaf_start[l];
+    cnt[l] = max(1u, (len + kRaySegLen - 1) / kRaySegLen);
+  }
+}
+
+__global__ void k_rays_items(const uint64_t *__restrict__ seg_off, int64_t nleaves,
+                             uint32_t *__restrict__ item_leaf) {
+  for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < nleaves;
+       l += (int64_t)gridDim.x * blockDim.x)
+    for (uint64_t it = seg_off[l]; it < seg_off[l + 1]; ++it) item_leaf[it] = (uint32_t)l;
 }
 
 // First column j of each row i <= res/2 inside the fisheye circle, with the
@@ -512,25 +650,42 @@ __global__ void k_dome_mask(float *pic, int res, const int *__restrict__ jstop) 
 
 void launch_rays_walk(bool emit, const RayConst &k, const RayNode *nodes, const RayRegion *regs,
                       const uint32_t *order, const uint32_t *code, int64_t n, const RayParts &p,
-                      uint32_t *count, const uint64_t *off, uint32_t *keys, uint32_t *vals,
-                      cudaStream_t s) {
+                      uint32_t *count, uint32_t *slots, const uint64_t *off, uint32_t *keys,
+                      uint32_t *vals, cudaStream_t s) {
   if (n <= 0) return;
   if (emit)
     k_rays_walk<true><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, order, code, n, p, count,
-                                                        off, keys, vals);
+                                                        slots, off, keys, vals);
   else
     k_rays_walk<false><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, order, code, n, p, count,
-                                                         off, keys, vals);
+                                                         slots, off, keys, vals);
+}
+
+void launch_rays_segments(const uint32_t *leaf_start, int64_t nleaves, uint32_t *cnt,
+                          cudaStream_t s) {
+  if (nleaves > 0) k_rays_segments<<<grid_for(nleaves, 256), 256, 0, s>>>(leaf_start, nleaves, cnt);
+}
+
+void launch_rays_items(const uint64_t *seg_off, int64_t nleaves, uint32_t *item_leaf,
+                       cudaStream_t s) {
+  if (nleaves > 0)
+    k_rays_items<<<grid_for(nleaves, 256), 256, 0, s>>>(seg_off, nleaves, item_leaf);
 }
 
 void launch_rays_leaves(const RayConst &k, int L, const RayParts &p, const RayLeafArgs &a,
                         cudaStream_t s) {
   const int nl = k.lev[L].nleaves;
   if (nl <= 0) return;
-  if (L == 0)
-    k_rays_leaf<true><<<nl, kRayLeafThreads, 0, s>>>(k, L, p, a);
-  else
-    k_rays_leaf<false><<<nl, kRayLeafThreads, 0, s>>>(k, L, p, a);
+  // persistent warps over the level's segments (their count stays on the device)
+  const int grid = 152 * 16;
+  const int fgrid = std::min((nl + kRayLeafWarps - 1) / kRayLeafWarps, 152 * 8);
+  if (L == 0) {
+    k_rays_leaf<true><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+    k_rays_fold<true><<<fgrid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+  } else {
+    k_rays_leaf<false><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+    k_rays_fold<false><<<fgrid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+  }
 }
 
 void launch_rays_dome_mask(float *pic, int res, int *jstop, cudaStream_t s) {

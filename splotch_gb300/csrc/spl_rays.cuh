@@ -21,12 +21,12 @@ __device__ __forceinline__ double ddot3(const double a[3], const double b[3]) {
 
 // One particle as the region tests see it: c, r in double (the reference's
 // values), the float copies, and for the dome the zenith terms of
-// new_renderer.cc:203-211 (dot(zenith, c), the angle of c from the zenith and
-// the sphere's angular half-width).
+// new_renderer.cc:203-211 (dot(zenith, c), and the angle of c from the
+// zenith plus and minus the sphere's angular half-width).
 struct RayPart {
   double c[3], r;
   float cf[3], rf;
-  double zdot, pth, dpth;
+  double zdot, th_hi, th_lo;
 };
 
 __device__ __forceinline__ RayPart ray_part(const RayConst &k, double4 rc, float4 cf) {
@@ -39,42 +39,48 @@ __device__ __forceinline__ RayPart ray_part(const RayConst &k, double4 rc, float
   p.cf[1] = cf.y;
   p.cf[2] = cf.z;
   p.rf = cf.w;
-  p.zdot = p.pth = p.dpth = 0.0;
+  p.zdot = p.th_hi = p.th_lo = 0.0;
   if (k.dome) {
     p.zdot = ddot3(k.zen, p.c);
     const double cx = dsub(dmul(k.zen[1], p.c[2]), dmul(k.zen[2], p.c[1]));
     const double cy = dsub(dmul(k.zen[2], p.c[0]), dmul(k.zen[0], p.c[2]));
     const double cz = dsub(dmul(k.zen[0], p.c[1]), dmul(k.zen[1], p.c[0]));
     const double cl = __dsqrt_rn(dadd(dadd(dmul(cx, cx), dmul(cy, cy)), dmul(cz, cz)));
-    p.pth = atan2(cl, p.zdot);  // v_angle (cxxsupport/geom_utils.h:59-63)
-    p.dpth = atan2(p.r, __dsqrt_rn(dmul(dadd(1.0, p.r), dsub(1.0, p.r))));
+    const double pth = atan2(cl, p.zdot);  // v_angle (cxxsupport/geom_utils.h:59-63)
+    const double dpth = atan2(p.r, __dsqrt_rn(dmul(dadd(1.0, p.r), dsub(1.0, p.r))));
+    p.th_hi = dadd(pth, dpth);
+    p.th_lo = dsub(pth, dpth);
   }
   return p;
 }
 
-// r > dot(c, n_k) of PlaneProjector::reduceList.  The float dot product is
-// within 4e-7 of the double one (unit vectors, float copies within 2^-24 per
-// component) and the float radius within 6e-8 of the double radius, so a
-// float difference beyond 1e-6 decides the double comparison.
-__device__ __forceinline__ bool ray_plane_side(const RayRegion &g, int k, const RayPart &p) {
-  const float df = fmaf(p.cf[2], g.nf[k][2], fmaf(p.cf[1], g.nf[k][1], p.cf[0] * g.nf[k][0]));
-  const float s = p.rf - df;
-  if (s > 1e-6f) return true;
-  if (s < -1e-6f) return false;
-  return p.r > ddot3(p.c, g.n[k]);
+// Sign of r - dot(c, n): +1, -1, or 0 (equal, or a NaN).  The float dot
+// product is within 4e-7 of the double one (unit vectors, float copies within
+// 2^-24 per component) and the float radius within 6e-8 of the double
+// radius, so a float difference beyond 1e-6 has the double difference's
+// sign; otherwise n (double) is read and the reference's comparison made.
+__device__ __forceinline__ int ray_side(const float *nf, const double *n, const RayPart &p) {
+  const float s = p.rf - fmaf(p.cf[2], nf[2], fmaf(p.cf[1], nf[1], p.cf[0] * nf[0]));
+  if (s > 1e-6f) return 1;
+  if (s < -1e-6f) return -1;
+  const double dt = ddot3(p.c, n);
+  return p.r > dt ? 1 : (p.r < dt ? -1 : 0);
 }
 
-// reduceList's per-particle test (new_renderer.cc:95-100, 195-212).
-__device__ __forceinline__ bool ray_region_keeps(const RayConst &k, const RayRegion &g,
-                                                 const RayPart &p) {
+// reduceList's per-particle test (new_renderer.cc:95-100, 195-212) for the
+// region g with float test vectors nf (12 floats) and the dome's centered
+// flag.  The dome's halfspace check depends on the particle alone: made at
+// the screen cut (halfspace true), it holds for every region after it.
+__device__ __forceinline__ bool ray_keeps(const RayConst &k, const float *nf, int centered,
+                                          const RayRegion &g, const RayPart &p, bool halfspace) {
   if (!k.dome)
-    return ray_plane_side(g, 0, p) && ray_plane_side(g, 1, p) && ray_plane_side(g, 2, p) &&
-           ray_plane_side(g, 3, p);
-  if (p.r < -p.zdot) return false;  // halfspace check
-  if (!g.centered && ((p.r < ddot3(p.c, g.n[0])) || (p.r < ddot3(p.c, g.n[1]))))
+    return ray_side(nf, g.n[0], p) > 0 && ray_side(nf + 3, g.n[1], p) > 0 &&
+           ray_side(nf + 6, g.n[2], p) > 0 && ray_side(nf + 9, g.n[3], p) > 0;
+  if (halfspace && p.r < -p.zdot) return false;
+  if (!centered && (ray_side(nf, g.n[0], p) < 0 || ray_side(nf + 3, g.n[1], p) < 0))
     return false;  // phi check
   if ((p.zdot > g.cthetamin) || (p.zdot < g.cthetamax)) {  // theta check
-    if ((dadd(p.pth, p.dpth) < g.thetamin) || (dsub(p.pth, p.dpth) > g.thetamax)) return false;
+    if ((p.th_hi < g.thetamin) || (p.th_lo > g.thetamax)) return false;
   }
   return true;
 }
