@@ -32,6 +32,7 @@ struct spl_context {
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
       poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes,
       seg_cnt, seg_off, seg_state, ray_rc, ray_cf, ray_pod, ray_cov, ray_code, ray_lev, ray_slots,
+      ray_rc2, ray_cf2, ray_pod2, ray_cov2,
       ray_kd, ray_segcnt, ray_segoff, ray_items, ray_partial,
       ray_nodes, ray_regs, ray_box, ray_leaf_start, ray_img[2], ray_jstop;
   // spl_render_rays: the host-built region trees of the last geometry
@@ -368,7 +369,8 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->ray_nodes, &c->ray_regs, &c->ray_box, &c->ray_leaf_start,
                               &c->ray_img[0], &c->ray_img[1], &c->ray_jstop, &c->ray_slots,
                               &c->ray_kd, &c->ray_segcnt, &c->ray_segoff, &c->ray_items,
-                              &c->ray_partial};
+                              &c->ray_partial, &c->ray_rc2, &c->ray_cf2, &c->ray_pod2,
+                              &c->ray_cov2};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   delete c->rays;
@@ -982,6 +984,8 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
       (st = ensure(c->ray_pod, n * 16)) || (st = ensure(c->ray_cov, n * 8)) ||
       (st = ensure(c->ray_code, n * 4)) || (st = ensure(c->ray_lev, (nlev + 3) * 4)) ||
       (st = ensure(c->ray_slots, n * 4 * spl::kRayWalkSlots)) ||
+      (st = ensure(c->ray_rc2, n * 32)) || (st = ensure(c->ray_cf2, n * 16)) ||
+      (st = ensure(c->ray_pod2, n * 16)) || (st = ensure(c->ray_cov2, n * 8)) ||
       (st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
       (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)) ||
       (st = ensure(c->count, n * 4)) || (st = ensure(c->off, (n + 1) * 8)) ||
@@ -1051,27 +1055,29 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   }
   cudaEventRecord(c->ev[1], s);
 
-  // ---- particle pass, then the particles grouped by level (stable) ------------
+  // ---- particle pass, then the particles sorted by level and direction -------
   spl::RayParts rp{as<double4>(c->ray_rc), as<float4>(c->ray_cf), as<float4>(c->ray_pod),
                    as<float2>(c->ray_cov), as<uint32_t>(c->ray_code), d_err};
   spl::launch_rays_prep(aos_dev, &soa, n, pc, k, rp, s);
   ++launches;
   cudaEventRecord(c->ev[2], s);
-  uint32_t *code_s = as<uint32_t>(c->key), *order = as<uint32_t>(c->perm);
+  uint32_t *key_s = as<uint32_t>(c->key), *order = as<uint32_t>(c->perm);
   uint32_t *lev_start = as<uint32_t>(c->ray_lev);
   if (n > 0) {
-    spl::radix_sort_pairs(rp.code, nullptr, as<uint32_t>(c->ktmp), as<uint32_t>(c->vtmp), code_s,
-                          order, n, 0, spl::bits_for(nlev + 2), true, c->scratch.p, s, &launches,
-                          d_err, (c->debug_flags & 2) == 0);
+    spl::radix_sort_pairs(rp.key, nullptr, as<uint32_t>(c->ktmp), as<uint32_t>(c->vtmp), key_s,
+                          order, n, 0, 32, true, c->scratch.p, s, &launches, d_err,
+                          (c->debug_flags & 2) == 0);
   }
-  spl::launch_tile_ranges(code_s, n, nlev + 2, lev_start, s);
-  ++launches;
+  spl::RayParts rs{as<double4>(c->ray_rc2), as<float4>(c->ray_cf2), as<float4>(c->ray_pod2),
+                   as<float2>(c->ray_cov2), key_s, d_err};
+  spl::launch_rays_sorted(key_s, order, n, nlev, lev_start, rp, rs, s);
+  launches += 2;
   cudaEventRecord(c->ev[3], s);
 
   // ---- region-tree walk: (leaf, particle) pairs, grouped by leaf (stable) -----
   const spl::RayNode *d_nodes = as<spl::RayNode>(c->ray_nodes);
   const spl::RayRegion *d_regs = as<spl::RayRegion>(c->ray_regs);
-  spl::launch_rays_walk(false, k, d_nodes, d_regs, order, code_s, n, rp, as<uint32_t>(c->count),
+  spl::launch_rays_walk(false, k, d_nodes, d_regs, key_s, n, rs, as<uint32_t>(c->count),
                         as<uint32_t>(c->ray_slots), nullptr, nullptr, nullptr, s);
   ++launches;
   spl::scan_counts(as<uint32_t>(c->count), nullptr, n, as<uint64_t>(c->off), c->scratch.p, s,
@@ -1088,7 +1094,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
       (st = ensure(c->tkey_s, ne * 4)) || (st = ensure(c->tval_s, ne * 4)) ||
       (st = ensure(c->scratch, std::max(scr, spl::radix_scratch_bytes(ne)))))
     return st;
-  spl::launch_rays_walk(true, k, d_nodes, d_regs, order, code_s, n, rp, as<uint32_t>(c->count),
+  spl::launch_rays_walk(true, k, d_nodes, d_regs, key_s, n, rs, as<uint32_t>(c->count),
                         as<uint32_t>(c->ray_slots), as<uint64_t>(c->off), as<uint32_t>(c->tkey),
                         as<uint32_t>(c->tval), s);
   ++launches;
@@ -1128,13 +1134,12 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   la.item_leaf = as<uint32_t>(c->ray_items);
   la.partial = as<float>(c->ray_partial);
   la.vals = as<uint32_t>(c->tval_s);
-  la.order = order;
   la.lev_start = lev_start;
   for (int L = 0; L < nlev; ++L) {
     la.out = L == nlev - 1 ? final_pic : as<float>(c->ray_img[L & 1]);
     la.coarse = L > 0 ? as<float>(c->ray_img[(L - 1) & 1]) : nullptr;
     la.cdim_y = L > 0 ? k.lev[L - 1].ydim : 0;
-    spl::launch_rays_leaves(k, L, rp, la, s);
+    spl::launch_rays_leaves(k, L, rs, la, s);
     launches += 2;
   }
   if (k.dome) {

@@ -560,29 +560,39 @@ struct RayConst {
   RayLevel lev[kRayMaxLevels];
   RayRegion screen;    // reduceList(0, xres, 0, yres): the screen cut
 };
-// Per particle (indexed by particle): code = level (0..nlev-1), nlev for a
-// sphere around the camera (r > 1), nlev+1 for a particle not rendered.
+// Per particle: key = code << kRayCodeShift | a Morton code of c (27 bits),
+// code = level (0..nlev-1), nlev for a sphere around the camera (r > 1),
+// nlev+1 for a particle not rendered.  Sorting by key groups the particles
+// by level and, within a level, by direction: neighbouring threads of the
+// walk then follow neighbouring paths, and a leaf's list is close in memory.
+constexpr int kRayCodeShift = 27;
 struct RayParts {
   double4 *rc;     // unit direction c and angular radius r, as the reference has them
   float4 *cf;      // the same rounded to float
   float4 *pod;     // colour after the radius correction
   float2 *cov;     // per sphere: chord^2 limit 2r^2/(1+sqrt(1-r^2)) (-1: always decide in
                    // double), 1/(r*h2sigma)^2
-  uint32_t *code;
+  uint32_t *key;
   uint32_t *err;   // bit 0: type outside [0, ptypes); bit 5: two levels claim a particle
 };
 void launch_rays_prep(const void *aos, const SoAIn *soa, int64_t n, const ProjConst &pc,
                       const RayConst &k, const RayParts &o, cudaStream_t s);
-// Walk of every particle of the level grids (order/code: the particles sorted
-// by code, n entries) through its level's region tree.  Count pass (emit
+// Level ranges of the sorted keys (lev_start: nlev + 3 entries) and the
+// records of every rendered particle gathered into key order (dst indexed
+// by sorted position).
+void launch_rays_sorted(const uint32_t *key_s, const uint32_t *order, int64_t n, int nlev,
+                        uint32_t *lev_start, const RayParts &src, const RayParts &dst,
+                        cudaStream_t s);
+// Walk of every particle of the level grids (key_s: the sorted keys, p: the
+// records in that order, n entries) through its level's region tree.  Count pass (emit
 // false): leaves reached per sorted position into count, the first
 // kRayWalkSlots of them into slots (n * kRayWalkSlots).  Emit pass: (leaf id,
 // particle) pairs at off[s], copied from the slots, or walked again for a
 // particle that reached more leaves.
 void launch_rays_walk(bool emit, const RayConst &k, const RayNode *nodes, const RayRegion *regs,
-                      const uint32_t *order, const uint32_t *code, int64_t n, const RayParts &p,
-                      uint32_t *count, uint32_t *slots, const uint64_t *off, uint32_t *keys,
-                      uint32_t *vals, cudaStream_t s);
+                      const uint32_t *key_s, int64_t n, const RayParts &p, uint32_t *count,
+                      uint32_t *slots, const uint64_t *off, uint32_t *keys, uint32_t *vals,
+                      cudaStream_t s);
 // One pyramid level: every leaf region of level L (leaf ranges in leaf_start,
 // entries' particles in vals).  A leaf's list is cut into segments of
 // kRaySegLen entries, one warp each (seg_off: exclusive scan of the segments
@@ -600,8 +610,7 @@ struct RayLeafArgs {
   const uint32_t *leaf_start;
   const uint64_t *seg_off;   // nleaves + 1
   const uint32_t *item_leaf;
-  const uint32_t *vals;
-  const uint32_t *order;
+  const uint32_t *vals;      // sorted positions of the entries' particles
   const uint32_t *lev_start; // code ranges in the sorted order (nlev + 3)
   float *partial;            // per segment item, kRayLeafPixels * 3 floats
   const float *coarse;

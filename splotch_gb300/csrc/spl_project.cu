@@ -501,30 +501,69 @@ __global__ void __launch_bounds__(256) k_palette_cache(L load, int64_t n, ProjCo
 // host_rendering_new's particle loop and colourisation
 // (splotch/new_renderer.cc:530-582), real_host_rendering's normalisation
 // (:402-415) and screen cut (:418-446), and each particle's pyramid level
-// (:488-501).  Double operations in the reference's order, none fused.
+// (:488-501).  What decides which particles reach which pixels -- the
+// distance cut, the unit direction c and the radius r -- follows the
+// reference's double operations in order, none fused (the distance cut is
+// first screened in float with a bound on its rounding); the intensity and
+// colour, which only scale a particle's contribution, are computed in float.
+
+// 9-bit-per-axis Morton code of a unit direction (a sort key for locality).
+__device__ __forceinline__ uint32_t morton27(float x, float y, float z) {
+  auto q = [](float v) {
+    const int t = (int)((v + 1.f) * 256.f);
+    uint32_t u = (uint32_t)min(max(t, 0), 511);
+    u = (u | (u << 16)) & 0x030000FFu;
+    u = (u | (u << 8)) & 0x0300F00Fu;
+    u = (u | (u << 4)) & 0x030C30C3u;
+    u = (u | (u << 2)) & 0x09249249u;
+    return u;
+  };
+  return q(x) | (q(y) << 1) | (q(z) << 2);
+}
+
 template <class L>
 __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst c, RayConst k,
                                                    RayParts o) {
+  const uint32_t none = (uint32_t)(k.nlev + 1) << kRayCodeShift;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const PIn in = load(i);
     const int t = in.type;
-    uint32_t code = (uint32_t)k.nlev + 1;
     if (t < 0 || t >= c.ptypes) {
       atomicOr(o.err, 1u);
-      o.code[i] = code;
+      o.key[i] = none;
       continue;
     }
-    // SPLOTCH_CLASSIC: I *= 0.5f*bfak/r (double bfak), r *= 2
-    const float I = __double2float_rn(dmul((double)in.I, ddiv(k.half_bfak, (double)in.r)));
+    // SPLOTCH_CLASSIC: I *= 0.5f*bfak/r, r *= 2
+    const float I = in.I * ((float)k.half_bfak / in.r);
     const float r2 = fmul(in.r, 2.f);
-    const double dx = dsub(k.centerpos[0], (double)in.x);
-    const double dy = dsub(k.centerpos[1], (double)in.y);
-    const double dz = dsub(k.centerpos[2], (double)in.z);
-    const float dist =
-        __double2float_rn(__dsqrt_rn(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz))));
-    if (!(dist < k.zmax)) {
-      o.code[i] = code;
+    // the distance cut: float(|centerpos - x|) < zmax
+    bool active;
+    {
+      const float fx = (float)k.centerpos[0] - in.x, fy = (float)k.centerpos[1] - in.y;
+      const float fz = (float)k.centerpos[2] - in.z;
+      const float d2 = fmaf(fz, fz, fmaf(fy, fy, fx * fx));
+      // roundings of centerpos, the differences and the sum of squares
+      const float E = 2.5e-7f * (fabsf((float)k.centerpos[0]) + fabsf(in.x) +
+                                 fabsf((float)k.centerpos[1]) + fabsf(in.y) +
+                                 fabsf((float)k.centerpos[2]) + fabsf(in.z));
+      const float bound = 2.f * sqrtf(d2) * E + E * E + 5e-7f * d2;
+      const float z2 = k.zmax * k.zmax;
+      if (d2 + bound < z2 * 0.9999f) {
+        active = true;
+      } else if (d2 - bound > z2 * 1.0001f && z2 < INFINITY) {
+        active = false;
+      } else {
+        const double dx = dsub(k.centerpos[0], (double)in.x);
+        const double dy = dsub(k.centerpos[1], (double)in.y);
+        const double dz = dsub(k.centerpos[2], (double)in.z);
+        const float dist =
+            __double2float_rn(__dsqrt_rn(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz))));
+        active = dist < k.zmax;
+      }
+    }
+    if (!active) {
+      o.key[i] = none;
       continue;
     }
     float er = in.er, eg = in.eg, eb = in.eb;
@@ -536,10 +575,7 @@ __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst 
       eg = pg;
       eb = pb;
     }
-    const float fac = fmul(I, c.bright[t]);
-    er = fmul(er, fac);
-    eg = fmul(eg, fac);
-    eb = fmul(eb, fac);
+    const float fac = I * c.bright[t];
     double cc[3] = {dsub((double)in.x, k.campos[0]), dsub((double)in.y, k.campos[1]),
                     dsub((double)in.z, k.campos[2])};
     const double xl = ddiv(
@@ -548,13 +584,12 @@ __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst 
     double r = dmul((double)r2, xl);
     const double rcorr = ddiv(__dsqrt_rn(dadd(dmul(r, r), k.mr2pr2)), r);
     r = dmul(r, rcorr);
-    const float f2 = __double2float_rn(ddiv(1.0, dmul(rcorr, rcorr)));
-    er = fmul(er, f2);
-    eg = fmul(eg, f2);
-    eb = fmul(eb, f2);
+    const float rc1 = (float)rcorr;
+    const float f2 = fac / (rc1 * rc1);  // brightness / rcorr^2
     const double4 rc = make_double4(cc[0], cc[1], cc[2], r);
     const float4 cf = make_float4(__double2float_rn(cc[0]), __double2float_rn(cc[1]),
                                   __double2float_rn(cc[2]), __double2float_rn(r));
+    uint32_t code = (uint32_t)k.nlev + 1;
     if (ray_keeps(k, &k.screen.nf[0][0], k.screen.centered, k.screen, ray_part(k, rc, cf),
                   true)) {
       if (r > 1) {
@@ -569,17 +604,17 @@ __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst 
         if (hits > 1) atomicOr(o.err, 32u);
       }
     }
-    o.code[i] = code;
+    o.key[i] = (code << kRayCodeShift) | morton27(cf.x, cf.y, cf.z);
     o.rc[i] = rc;
     o.cf[i] = cf;
-    o.pod[i] = make_float4(er, eg, eb, 0.f);
+    o.pod[i] = make_float4(er * f2, eg * f2, eb * f2, 0.f);
     // a ray meets the sphere iff |d - c|^2 <= 2 - 2 sqrt(1 - r^2) = 2r^2/(1 + sqrt(1 - r^2));
-    // near r = 1 that limit is ill-conditioned and the test is always made in double
-    const float cm = r <= 0.99 ? __double2float_rn(ddiv(dmul(2.0, dmul(r, r)),
-                                                        dadd(1.0, __dsqrt_rn(dsub(1.0, dmul(r, r))))))
-                               : -1.f;
-    const float inv = __double2float_rn(ddiv(1.0, dmul(dmul(dmul(r, r), k.h2sigma), k.h2sigma)));
-    o.cov[i] = make_float2(cm, inv);
+    // in float within 1e-7 of that for r <= 0.9; beyond, the limit is
+    // ill-conditioned and every pixel is decided in double
+    const float rf = cf.w;
+    const float cm = rf <= 0.9f ? 2.f * rf * rf / (1.f + sqrtf(1.f - rf * rf)) : -1.f;
+    const float h2 = (float)k.h2sigma;
+    o.cov[i] = make_float2(cm, 1.f / (rf * rf * h2 * h2));
   }
 }
 

@@ -307,17 +307,17 @@ namespace {
 template <bool EMIT>
 __global__ void __launch_bounds__(128) k_rays_walk(
     RayConst k, const RayNode *__restrict__ nodes, const RayRegion *__restrict__ regs,
-    const uint32_t *__restrict__ order, const uint32_t *__restrict__ code, int64_t n, RayParts p,
-    uint32_t *__restrict__ count, uint32_t *__restrict__ slots, const uint64_t *__restrict__ off,
-    uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const uint32_t *__restrict__ key_s, int64_t n, RayParts p, uint32_t *__restrict__ count,
+    uint32_t *__restrict__ slots, const uint64_t *__restrict__ off, uint32_t *__restrict__ keys,
+    uint32_t *__restrict__ vals) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
        s += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t L = code[s];
+    const uint32_t L = key_s[s] >> kRayCodeShift;
     if (L >= (uint32_t)k.nlev) {
       if (!EMIT) count[s] = 0;
       continue;
     }
-    const uint32_t i = order[s];
+    const uint32_t i = (uint32_t)s;  // records are in sorted order
     uint64_t o = 0;
     if (EMIT) {
       const uint32_t c = count[s];
@@ -364,6 +364,35 @@ __global__ void __launch_bounds__(128) k_rays_walk(
   }
 }
 
+// Level ranges of the sorted keys: lev_start[c] = first sorted position of
+// code c (c = 0 .. nlev + 2).
+__global__ void __launch_bounds__(256) k_rays_level_ranges(const uint32_t *__restrict__ key_s,
+                                                           int64_t n, int ncodes,
+                                                           uint32_t *__restrict__ lev_start) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q <= n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cprev = q > 0 ? (int64_t)(key_s[q - 1] >> kRayCodeShift) : -1;
+    const int64_t ccur = q < n ? (int64_t)(key_s[q] >> kRayCodeShift) : ncodes;
+    for (int64_t c = cprev + 1; c <= ccur; ++c) lev_start[c] = (uint32_t)q;
+  }
+}
+
+// Records of the rendered particles (levels and spheres around the camera)
+// gathered into sorted order.
+__global__ void __launch_bounds__(256) k_rays_gather(const uint32_t *__restrict__ key_s,
+                                                     const uint32_t *__restrict__ order, int64_t n,
+                                                     int nlev, RayParts src, RayParts dst) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    if ((key_s[q] >> kRayCodeShift) > (uint32_t)nlev) continue;
+    const uint32_t i = order[q];
+    dst.rc[q] = src.rc[i];
+    dst.cf[q] = src.cf[i];
+    dst.pod[q] = src.pod[i];
+    dst.cov[q] = src.cov[i];
+  }
+}
+
 // Direction of full-resolution pixel (X, Y) in double, out of line (once
 // per pixel and leaf segment).
 __device__ __noinline__ double3 ray_dir3(const RayConst *__restrict__ kd, int X, int Y) {
@@ -373,18 +402,17 @@ __device__ __noinline__ double3 ray_dir3(const RayConst *__restrict__ kd, int X,
 }
 
 // add_overlap2 (new_renderer.cc:367-393) at full-resolution pixel (X, Y):
-// the spheres around the camera, order[s0, s1), each weighted by the erfc
+// the spheres around the camera (sorted positions s0 .. s1), each weighted by the erfc
 // of its near half (no coverage test).
 __device__ __noinline__ float4 ray_overlap(const RayConst *__restrict__ kd, int X, int Y,
-                                           const uint32_t *__restrict__ order, uint32_t s0,
-                                           uint32_t s1, const double4 *__restrict__ rcs,
+                                           uint32_t s0, uint32_t s1,
+                                           const double4 *__restrict__ rcs,
                                            const float4 *__restrict__ pods) {
   double d[3];
   ray_pix_dir(*kd, X, Y, d);
   const double h2 = kd->h2sigma;
   float o0 = 0.f, o1 = 0.f, o2 = 0.f;
-  for (uint32_t s = s0; s < s1; ++s) {
-    const uint32_t i = order[s];
+  for (uint32_t i = s0; i < s1; ++i) {
     const double4 rc = rcs[i];
     const double c[3] = {rc.x, rc.y, rc.z};
     const double cosang = ddot3(d, c);
@@ -409,7 +437,7 @@ __device__ __forceinline__ void ray_finish(const RayConst &k, const RayLevel &lv
                                            const RayLeafArgs &a, const RayParts &p, int x, int y,
                                            float od0, float od1, float od2) {
   if (TOP) {
-    const float4 o = ray_overlap(a.kd, x * lv.fact, y * lv.fact, a.order, a.lev_start[k.nlev],
+    const float4 o = ray_overlap(a.kd, x * lv.fact, y * lv.fact, a.lev_start[k.nlev],
                                  a.lev_start[k.nlev + 1], p.rc, p.pod);
     od0 = fadd(od0, o.x);
     od1 = fadd(od1, o.y);
@@ -609,21 +637,20 @@ __global__ void k_rays_items(const uint64_t *__restrict__ seg_off, int64_t nleav
 }
 
 // First column j of each row i <= res/2 inside the fisheye circle, with the
-// reference's double arithmetic (new_renderer.cc:622-637).
+// reference's double arithmetic (new_renderer.cc:622-637): the least j whose
+// point is inside (jstop starts above any column: a row with none keeps it).
 __global__ void k_dome_rows(int res, int *jstop) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i > res / 2) return;
-  const double xf = ddiv(1.0, (double)(res - 1));
-  double x = dmul(dadd((double)i, 0.5), xf);
-  x = dsub(dmul(2.0, x), 1.0);
-  const double xx = dmul(x, x);
-  int j = 0;
-  for (; j < res; ++j) {
+  const int64_t np = (int64_t)(res / 2 + 1) * res;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < np;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q / res), j = (int)(q % res);
+    const double xf = ddiv(1.0, (double)(res - 1));
+    double x = dmul(dadd((double)i, 0.5), xf);
+    x = dsub(dmul(2.0, x), 1.0);
     double y = dmul(dadd((double)j, 0.5), xf);
     y = dsub(dmul(2.0, y), 1.0);
-    if (!(dadd(xx, dmul(y, y)) > 1.)) break;
+    if (!(dadd(dmul(x, x), dmul(y, y)) > 1.)) atomicMin(jstop + i, j);
   }
-  jstop[i] = j;
 }
 
 // The reference zeroes (i, j), (i, res-1-j), (res-1-i, res-1-j), (res-1-i, j)
@@ -649,16 +676,23 @@ __global__ void k_dome_mask(float *pic, int res, const int *__restrict__ jstop) 
 }  // namespace
 
 void launch_rays_walk(bool emit, const RayConst &k, const RayNode *nodes, const RayRegion *regs,
-                      const uint32_t *order, const uint32_t *code, int64_t n, const RayParts &p,
-                      uint32_t *count, uint32_t *slots, const uint64_t *off, uint32_t *keys,
-                      uint32_t *vals, cudaStream_t s) {
+                      const uint32_t *key_s, int64_t n, const RayParts &p, uint32_t *count,
+                      uint32_t *slots, const uint64_t *off, uint32_t *keys, uint32_t *vals,
+                      cudaStream_t s) {
   if (n <= 0) return;
   if (emit)
-    k_rays_walk<true><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, order, code, n, p, count,
-                                                        slots, off, keys, vals);
+    k_rays_walk<true><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, key_s, n, p, count, slots,
+                                                        off, keys, vals);
   else
-    k_rays_walk<false><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, order, code, n, p, count,
-                                                         slots, off, keys, vals);
+    k_rays_walk<false><<<grid_for(n, 128), 128, 0, s>>>(k, nodes, regs, key_s, n, p, count, slots,
+                                                         off, keys, vals);
+}
+
+void launch_rays_sorted(const uint32_t *key_s, const uint32_t *order, int64_t n, int nlev,
+                        uint32_t *lev_start, const RayParts &src, const RayParts &dst,
+                        cudaStream_t s) {
+  k_rays_level_ranges<<<grid_for(n + 1, 256), 256, 0, s>>>(key_s, n, nlev + 2, lev_start);
+  if (n > 0) k_rays_gather<<<grid_for(n, 256), 256, 0, s>>>(key_s, order, n, nlev, src, dst);
 }
 
 void launch_rays_segments(const uint32_t *leaf_start, int64_t nleaves, uint32_t *cnt,
@@ -690,7 +724,8 @@ void launch_rays_leaves(const RayConst &k, int L, const RayParts &p, const RayLe
 
 void launch_rays_dome_mask(float *pic, int res, int *jstop, cudaStream_t s) {
   if (res <= 0) return;
-  k_dome_rows<<<(res / 2 + 1 + 127) / 128, 128, 0, s>>>(res, jstop);
+  cudaMemsetAsync(jstop, 0x7f, (size_t)(res / 2 + 1) * sizeof(int), s);
+  k_dome_rows<<<grid_for((int64_t)(res / 2 + 1) * res, 256), 256, 0, s>>>(res, jstop);
   k_dome_mask<<<grid_for((int64_t)res * res, 256), 256, 0, s>>>(pic, res, jstop);
 }
 
