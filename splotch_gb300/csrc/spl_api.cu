@@ -32,7 +32,7 @@ struct spl_context {
       aos_out, pal_thr, pal_xff, pal_invff, tcost, tcost_s, tord, pos_c, col_c, idx_c, pstate,
       poff, gpic, gpos_c, gcol_c, camsum, gout[8], aux, post_tab, post_bar, post_img, post_bytes,
       seg_cnt, seg_off, seg_state, ray_rc, ray_cf, ray_pod, ray_cov, ray_code, ray_lev, ray_slots,
-      ray_rc2, ray_cf2, ray_pod2, ray_cov2,
+      ray_rc2, ray_cf2, ray_pod2, ray_cov2, ray_clo, ray_clo2,
       ray_kd, ray_segcnt, ray_segoff, ray_items, ray_partial,
       ray_nodes, ray_regs, ray_box, ray_leaf_start, ray_img[2], ray_jstop;
   // spl_render_rays: the host-built region trees of the last geometry
@@ -370,7 +370,7 @@ spl_status spl_context_destroy(spl_context *c) {
                               &c->ray_img[0], &c->ray_img[1], &c->ray_jstop, &c->ray_slots,
                               &c->ray_kd, &c->ray_segcnt, &c->ray_segoff, &c->ray_items,
                               &c->ray_partial, &c->ray_rc2, &c->ray_cf2, &c->ray_pod2,
-                              &c->ray_cov2};
+                              &c->ray_cov2, &c->ray_clo, &c->ray_clo2};
   for (auto *b : bufs)
     if (b->p) cudaFree(b->p);
   delete c->rays;
@@ -986,6 +986,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
       (st = ensure(c->ray_slots, n * 4 * spl::kRayWalkSlots)) ||
       (st = ensure(c->ray_rc2, n * 32)) || (st = ensure(c->ray_cf2, n * 16)) ||
       (st = ensure(c->ray_pod2, n * 16)) || (st = ensure(c->ray_cov2, n * 8)) ||
+      (st = ensure(c->ray_clo, n * 16)) || (st = ensure(c->ray_clo2, n * 16)) ||
       (st = ensure(c->key, n * 4)) || (st = ensure(c->perm, n * 4)) ||
       (st = ensure(c->ktmp, n * 4)) || (st = ensure(c->vtmp, n * 4)) ||
       (st = ensure(c->count, n * 4)) || (st = ensure(c->off, (n + 1) * 8)) ||
@@ -1056,8 +1057,9 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   cudaEventRecord(c->ev[1], s);
 
   // ---- particle pass, then the particles sorted by level and direction -------
-  spl::RayParts rp{as<double4>(c->ray_rc), as<float4>(c->ray_cf), as<float4>(c->ray_pod),
-                   as<float2>(c->ray_cov), as<uint32_t>(c->ray_code), d_err};
+  spl::RayParts rp{as<double4>(c->ray_rc), as<float4>(c->ray_cf), as<float4>(c->ray_clo),
+                   as<float4>(c->ray_pod), as<float2>(c->ray_cov), as<uint32_t>(c->ray_code),
+                   d_err};
   spl::launch_rays_prep(aos_dev, &soa, n, pc, k, rp, s);
   ++launches;
   cudaEventRecord(c->ev[2], s);
@@ -1068,8 +1070,8 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
                           order, n, 0, 32, true, c->scratch.p, s, &launches, d_err,
                           (c->debug_flags & 2) == 0);
   }
-  spl::RayParts rs{as<double4>(c->ray_rc2), as<float4>(c->ray_cf2), as<float4>(c->ray_pod2),
-                   as<float2>(c->ray_cov2), key_s, d_err};
+  spl::RayParts rs{as<double4>(c->ray_rc2), as<float4>(c->ray_cf2), as<float4>(c->ray_clo2),
+                   as<float4>(c->ray_pod2), as<float2>(c->ray_cov2), key_s, d_err};
   spl::launch_rays_sorted(key_s, order, n, nlev, lev_start, rp, rs, s);
   launches += 2;
   cudaEventRecord(c->ev[3], s);

@@ -551,6 +551,7 @@ struct RayLevel {
 struct RayConst {
   int dome, nlev;      // level 0 is the coarsest grid
   double p0[3], dpx[3], dpy[3];    // PlaneProjector
+  float p0f[3], dpxf[3], dpyf[3];  // the same rounded to float
   double zen[3], ex[3], ey[3], dp; // DomeProjector (zenith, x, y, 1/res)
   double campos[3], centerpos[3];
   float zmax;
@@ -569,6 +570,7 @@ constexpr int kRayCodeShift = 27;
 struct RayParts {
   double4 *rc;     // unit direction c and angular radius r, as the reference has them
   float4 *cf;      // the same rounded to float
+  float4 *clo;     // c - cf (float), the low parts of c as a float-float pair
   float4 *pod;     // colour after the radius correction
   float2 *cov;     // per sphere: chord^2 limit 2r^2/(1+sqrt(1-r^2)) (-1: always decide in
                    // double), 1/(r*h2sigma)^2

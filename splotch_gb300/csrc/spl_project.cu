@@ -607,6 +607,9 @@ __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst 
     o.key[i] = (code << kRayCodeShift) | morton27(cf.x, cf.y, cf.z);
     o.rc[i] = rc;
     o.cf[i] = cf;
+    o.clo[i] = make_float4(__double2float_rn(dsub(cc[0], (double)cf.x)),
+                           __double2float_rn(dsub(cc[1], (double)cf.y)),
+                           __double2float_rn(dsub(cc[2], (double)cf.z)), 0.f);
     o.pod[i] = make_float4(er * f2, eg * f2, eb * f2, 0.f);
     // a ray meets the sphere iff |d - c|^2 <= 2 - 2 sqrt(1 - r^2) = 2r^2/(1 + sqrt(1 - r^2));
     // in float within 1e-7 of that for r <= 0.9; beyond, the limit is

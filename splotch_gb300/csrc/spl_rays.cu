@@ -248,6 +248,11 @@ spl_status rays_setup(const spl_frame_desc *d, const spl_rays_desc *r, RayFrame 
     put(k.p0, corner + dpx * .5 + dpy * .5);
     put(k.dpx, dpx);
     put(k.dpy, dpy);
+    for (int a = 0; a < 3; ++a) {
+      k.p0f[a] = (float)k.p0[a];
+      k.dpxf[a] = (float)k.dpx[a];
+      k.dpyf[a] = (float)k.dpy[a];
+    }
   }
   put(k.campos, campos);
   put(k.centerpos, centerpos);
@@ -388,6 +393,7 @@ __global__ void __launch_bounds__(256) k_rays_gather(const uint32_t *__restrict_
     const uint32_t i = order[q];
     dst.rc[q] = src.rc[i];
     dst.cf[q] = src.cf[i];
+    dst.clo[q] = src.clo[i];
     dst.pod[q] = src.pod[i];
     dst.cov[q] = src.cov[i];
   }
@@ -399,6 +405,17 @@ __device__ __noinline__ double3 ray_dir3(const RayConst *__restrict__ kd, int X,
   double d[3];
   ray_pix_dir(*kd, X, Y, d);
   return make_double3(d[0], d[1], d[2]);
+}
+
+// The plane projector's sphere-vs-ray test in double at full-resolution
+// pixel (X, Y), out of line (a chord within the float screen's margin): the
+// weight on a hit, -1 on a miss.
+__device__ __noinline__ float ray_plane_exact(const RayConst *__restrict__ kd, int X, int Y,
+                                              double4 rc) {
+  double d[3];
+  ray_pix_dir_plane(*kd, X, Y, d);
+  float w;
+  return ray_exact_hit(d, rc, kd->h2sigma, w) ? w : -1.f;
 }
 
 // add_overlap2 (new_renderer.cc:367-393) at full-resolution pixel (X, Y):
@@ -464,15 +481,21 @@ __device__ __forceinline__ void ray_finish(const RayConst &k, const RayLevel &lv
 // l+64 of the leaf (column-major within it).  The segment is staged through
 // the warp's shared slice 32 entries at a time, in list order; each pixel
 // accumulates -e*w over the spheres its ray meets.
-template <bool TOP>
-__global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, int L, RayParts p,
+//
+// The float screen works with directions relative to u, the leaf's first
+// pixel's direction: c - u from the float-float pair of c, and d - u for a
+// plane projector from the float pixel grid (d - u = dt/|t| - t_u g with
+// t = t_u + dt and g = (2 t_u.dt + dt.dt) / (|t| |t_u| (|t| + |t_u|)), which
+// loses nothing to cancellation), for the dome from the double directions.
+template <bool TOP, bool DOME>
+__global__ void __launch_bounds__(32 * kRayLeafWarps, 6) k_rays_leaf(RayConst k, int L, RayParts p,
                                                                   RayLeafArgs a) {
   const RayLevel &lv = k.lev[L];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   __shared__ float4 s_a[kRayLeafWarps][32], s_b[kRayLeafWarps][32];
   __shared__ float s_inv[kRayLeafWarps][32];
   __shared__ uint32_t s_idx[kRayLeafWarps][32];
-  __shared__ double s_d[kRayLeafWarps][3][96];  // the pixels' directions in double
+  __shared__ double s_d[kRayLeafWarps][3][DOME ? 96 : 1];  // dome: the pixels' directions
   const uint64_t it0 = a.seg_off[lv.leaf0], it1 = a.seg_off[lv.leaf0 + lv.nleaves];
   const int fact = lv.fact;
   for (uint64_t item = it0 + (uint64_t)blockIdx.x * kRayLeafWarps + warp; item < it1;
@@ -486,32 +509,55 @@ __global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, in
     const int npx = nx * ny;
     const int npl = (npx + 31) >> 5;  // pixels per lane, warp-uniform
 
-    // the leaf's reference direction u: its first pixel's
-    double3 u = make_double3(0.0, 0.0, 0.0);
-    if (lane == 0) u = ray_dir3(a.kd, box.x * fact, box.z * fact);
-    u.x = __shfl_sync(0xffffffffu, u.x, 0);
-    u.y = __shfl_sync(0xffffffffu, u.y, 0);
-    u.z = __shfl_sync(0xffffffffu, u.z, 0);
+    // u: the leaf's first pixel's direction, in double and as a float-float pair
+    const int X0 = box.x * fact, Y0 = box.z * fact;
+    const double3 ud = ray_dir3(a.kd, X0, Y0);
+    const float uh0 = __double2float_rn(ud.x), uh1 = __double2float_rn(ud.y);
+    const float uh2 = __double2float_rn(ud.z);
+    const float ul0 = __double2float_rn(dsub(ud.x, (double)uh0));
+    const float ul1 = __double2float_rn(dsub(ud.y, (double)uh1));
+    const float ul2 = __double2float_rn(dsub(ud.z, (double)uh2));
+    float tu0 = 0.f, tu1 = 0.f, tu2 = 0.f, ntu = 1.f;
+    if (!DOME) {
+      tu0 = fmaf((float)Y0, k.dpyf[0], fmaf((float)X0, k.dpxf[0], k.p0f[0]));
+      tu1 = fmaf((float)Y0, k.dpyf[1], fmaf((float)X0, k.dpxf[1], k.p0f[1]));
+      tu2 = fmaf((float)Y0, k.dpyf[2], fmaf((float)X0, k.dpxf[2], k.p0f[2]));
+      ntu = sqrtf(fmaf(tu2, tu2, fmaf(tu1, tu1, tu0 * tu0)));
+    }
     float dd[3][3], od[3][3];
-    int ix[3], iy[3];
     bool has[3];
     float l1max = 0.f;
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
       const int q = lane + 32 * m;
       has[m] = q < npx;
-      ix[m] = box.x + (has[m] ? q / ny : 0);
-      iy[m] = box.z + (has[m] ? q % ny : 0);
+      const int ixm = box.x + (has[m] ? q / ny : 0), iym = box.z + (has[m] ? q % ny : 0);
       od[m][0] = od[m][1] = od[m][2] = 0.f;
       dd[m][0] = dd[m][1] = dd[m][2] = 0.f;
       if (m < npl) {
-        const double3 d = ray_dir3(a.kd, ix[m] * fact, iy[m] * fact);
-        s_d[warp][0][lane + 32 * m] = d.x;
-        s_d[warp][1][lane + 32 * m] = d.y;
-        s_d[warp][2][lane + 32 * m] = d.z;
-        dd[m][0] = __double2float_rn(dsub(d.x, u.x));
-        dd[m][1] = __double2float_rn(dsub(d.y, u.y));
-        dd[m][2] = __double2float_rn(dsub(d.z, u.z));
+        if (DOME) {
+          const double3 d = ray_dir3(a.kd, ixm * fact, iym * fact);
+          s_d[warp][0][q] = d.x;
+          s_d[warp][1][q] = d.y;
+          s_d[warp][2][q] = d.z;
+          dd[m][0] = __double2float_rn(dsub(d.x, ud.x));
+          dd[m][1] = __double2float_rn(dsub(d.y, ud.y));
+          dd[m][2] = __double2float_rn(dsub(d.z, ud.z));
+        } else {
+          const float gx = (float)(ixm * fact - X0), gy = (float)(iym * fact - Y0);
+          const float t0 = gx * k.dpxf[0] + gy * k.dpyf[0];
+          const float t1 = gx * k.dpxf[1] + gy * k.dpyf[1];
+          const float t2 = gx * k.dpxf[2] + gy * k.dpyf[2];
+          const float a0 = tu0 + t0, a1 = tu1 + t1, a2 = tu2 + t2;
+          const float nt = sqrtf(fmaf(a2, a2, fmaf(a1, a1, a0 * a0)));
+          const float num = fmaf(t2, fmaf(2.f, tu2, t2), fmaf(t1, fmaf(2.f, tu1, t1),
+                                                              t0 * fmaf(2.f, tu0, t0)));
+          const float g = num / (nt * ntu * (nt + ntu));
+          const float it = 1.f / nt;
+          dd[m][0] = fmaf(t0, it, -tu0 * g);
+          dd[m][1] = fmaf(t1, it, -tu1 * g);
+          dd[m][2] = fmaf(t2, it, -tu2 * g);
+        }
         const float l1 = fabsf(dd[m][0]) + fabsf(dd[m][1]) + fabsf(dd[m][2]);
         if (has[m]) l1max = l1 == l1 ? fmaxf(l1max, l1) : INFINITY;  // NaN: a NaN direction
       }
@@ -527,20 +573,22 @@ __global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, in
       const uint32_t cnt = min(32u, e1 - b0);
       if ((uint32_t)lane < cnt) {
         const uint32_t i = a.vals[b0 + lane];
-        const double4 rc = p.rc[i];
+        const float4 cf = p.cf[i];
+        const float4 cl = p.clo[i];
         const float2 cv = p.cov[i];
         const float4 e = p.pod[i];
-        const float c0 = __double2float_rn(dsub(rc.x, u.x));
-        const float c1 = __double2float_rn(dsub(rc.y, u.y));
-        const float c2 = __double2float_rn(dsub(rc.z, u.z));
-        // |q - |d - c|^2| <= 2|d - c| E + E^2 + 3 ulp(q), E = 2^-23 (|d-u|_1 + |c-u|_1)
-        // + 7e-16 (the roundings of d-u, c-u and their difference); the
-        // margin doubles that at the limit cm and adds the rounding of cm
-        // itself.  No limit (cm < 0), or a NaN direction in the leaf (rd1
-        // infinite): every pixel is decided in double.
+        const float c0 = (cf.x - uh0) + (cl.x - ul0);
+        const float c1 = (cf.y - uh1) + (cl.y - ul1);
+        const float c2 = (cf.z - uh2) + (cl.z - ul2);
+        // |q - |d - c|^2| <= 2|d - c| E + E^2 + 3 ulp(q) with E bounding the
+        // error of d - c: 4 ulp of d - u (the float grid form) and 2 ulp of
+        // c - u plus the float-float pairs' 2^-48, 1e-13 in all; the margin
+        // doubles that at the limit cm and adds the rounding of cm itself.
+        // No limit (cm < 0), or a NaN direction in the leaf (rd1 infinite):
+        // every pixel is decided in double.
         float lo = -1.f, hi = INFINITY;
         if (cv.x >= 0.f && rd1 < INFINITY) {
-          const float E = 1.2e-7f * (rd1 + fabsf(c0) + fabsf(c1) + fabsf(c2)) + 1e-15f;
+          const float E = 6e-7f * (rd1 + fabsf(c0) + fabsf(c1) + fabsf(c2)) + 1e-13f;
           const float mg = 4.f * sqrtf(cv.x) * E + 2.f * E * E + 1e-6f * cv.x + 1e-13f;
           lo = cv.x - mg;
           hi = cv.x + mg;
@@ -551,6 +599,10 @@ __global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, in
         s_idx[warp][lane] = i;
       }
       __syncwarp();
+      // entries whose chord falls within the screen's margin, per pixel:
+      // decided after the batch (out of the inner loop, which keeps its
+      // register footprint small); only the order of those few additions moves
+      uint32_t und[3] = {0u, 0u, 0u};
       for (uint32_t j = 0; j < cnt; ++j) {
         const float4 A = s_a[warp][j];
         const float4 B = s_b[warp][j];
@@ -560,15 +612,34 @@ __global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, in
           const float x0 = dd[m][0] - A.x, x1 = dd[m][1] - A.y, x2 = dd[m][2] - A.z;
           const float q = fmaf(x2, x2, fmaf(x1, x1, x0 * x0));
           if (!has[m] || q > B.w) continue;  // the ray misses the sphere
-          float w;
           if (q < A.w) {  // it meets it: sin^2 = q (1 - q/4)
             const float sasq = q * fmaf(-0.25f, q, 1.f);
-            w = ex2(-sasq * s_inv[warp][j]);
-          } else {  // within the margin: the reference's double test
-            const int q = lane + 32 * m;
-            const double d[3] = {s_d[warp][0][q], s_d[warp][1][q], s_d[warp][2][q]};
-            if (!ray_exact_hit(d, p.rc[s_idx[warp][j]], k.h2sigma, w)) continue;
+            const float w = ex2(-sasq * s_inv[warp][j]);
+            od[m][0] = fmaf(B.x, w, od[m][0]);
+            od[m][1] = fmaf(B.y, w, od[m][1]);
+            od[m][2] = fmaf(B.z, w, od[m][2]);
+          } else {
+            und[m] |= 1u << j;
           }
+        }
+      }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        while (und[m]) {  // the reference's double test
+          const int j = __ffs(und[m]) - 1;
+          und[m] &= und[m] - 1;
+          float w;
+          if (DOME) {
+            const int qq = lane + 32 * m;
+            const double d[3] = {s_d[warp][0][DOME ? qq : 0], s_d[warp][1][DOME ? qq : 0],
+                                 s_d[warp][2][DOME ? qq : 0]};
+            if (!ray_exact_hit(d, p.rc[s_idx[warp][j]], k.h2sigma, w)) continue;
+          } else {
+            w = ray_plane_exact(a.kd, (box.x + (lane + 32 * m) / ny) * fact,
+                                (box.z + (lane + 32 * m) % ny) * fact, p.rc[s_idx[warp][j]]);
+            if (w < 0.f) continue;
+          }
+          const float4 B = s_b[warp][j];
           od[m][0] = fmaf(B.x, w, od[m][0]);
           od[m][1] = fmaf(B.y, w, od[m][1]);
           od[m][2] = fmaf(B.z, w, od[m][2]);
@@ -580,7 +651,9 @@ __global__ void __launch_bounds__(32 * kRayLeafWarps) k_rays_leaf(RayConst k, in
     for (int m = 0; m < 3; ++m) {
       if (!has[m]) continue;
       if (nseg == 1) {
-        ray_finish<TOP>(k, lv, a, p, ix[m], iy[m], od[m][0], od[m][1], od[m][2]);
+        const int q = lane + 32 * m;
+        ray_finish<TOP>(k, lv, a, p, box.x + q / ny, box.z + q % ny, od[m][0], od[m][1],
+                        od[m][2]);
       } else {  // this segment's sums, folded by k_rays_fold
         float *pp = a.partial + (size_t)item * (kRayLeafPixels * 3) + (lane + 32 * m) * 3;
         pp[0] = od[m][0];
@@ -714,10 +787,16 @@ void launch_rays_leaves(const RayConst &k, int L, const RayParts &p, const RayLe
   const int grid = 152 * 16;
   const int fgrid = std::min((nl + kRayLeafWarps - 1) / kRayLeafWarps, 152 * 8);
   if (L == 0) {
-    k_rays_leaf<true><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+    if (k.dome)
+      k_rays_leaf<true, true><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+    else
+      k_rays_leaf<true, false><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
     k_rays_fold<true><<<fgrid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
   } else {
-    k_rays_leaf<false><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+    if (k.dome)
+      k_rays_leaf<false, true><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
+    else
+      k_rays_leaf<false, false><<<grid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
     k_rays_fold<false><<<fgrid, 32 * kRayLeafWarps, 0, s>>>(k, L, p, a);
   }
 }

@@ -85,15 +85,20 @@ __device__ __forceinline__ bool ray_keeps(const RayConst &k, const float *nf, in
   return true;
 }
 
+// PlaneProjector::getPixDir: (p0 + dpx*ix + dpy*iy).Norm() (new_renderer.cc:71-72).
+__device__ __forceinline__ void ray_pix_dir_plane(const RayConst &k, int ix, int iy, double d[3]) {
+  const double X = (double)ix, Y = (double)iy;
+  double t[3];
+  for (int c = 0; c < 3; ++c) t[c] = dadd(dadd(k.p0[c], dmul(k.dpx[c], X)), dmul(k.dpy[c], Y));
+  const double l =
+      ddiv(1.0, __dsqrt_rn(dadd(dadd(dmul(t[0], t[0]), dmul(t[1], t[1])), dmul(t[2], t[2]))));
+  for (int c = 0; c < 3; ++c) d[c] = dmul(t[c], l);
+}
+
 // Projector::getPixDir at full-resolution pixel (ix, iy).
 __device__ __forceinline__ void ray_pix_dir(const RayConst &k, int ix, int iy, double d[3]) {
-  if (!k.dome) {  // (p0 + dpx*ix + dpy*iy).Norm()  (new_renderer.cc:71-72)
-    const double X = (double)ix, Y = (double)iy;
-    double t[3];
-    for (int c = 0; c < 3; ++c) t[c] = dadd(dadd(k.p0[c], dmul(k.dpx[c], X)), dmul(k.dpy[c], Y));
-    const double l =
-        ddiv(1.0, __dsqrt_rn(dadd(dadd(dmul(t[0], t[0]), dmul(t[1], t[1])), dmul(t[2], t[2]))));
-    for (int c = 0; c < 3; ++c) d[c] = dmul(t[c], l);
+  if (!k.dome) {
+    ray_pix_dir_plane(k, ix, iy, d);
     return;
   }
   // DomeProjector::getPixDir / igetPixDir (new_renderer.cc:126-138)
