@@ -521,7 +521,7 @@ int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s);
 // culling test (reduceList) decides which particles a leaf region lists.
 constexpr int kRayMaxLevels = 16;
 constexpr int kRayLeafWarps = 4;  // leaf regions per CTA, one warp each
-constexpr int kRayWalkSlots = 8;  // leaves a particle's first walk keeps
+constexpr int kRayWalkSlots = 8;   // leaves a particle's first walk keeps
 
 // reduceList parameters of one region (new_renderer.cc:77-101, 164-213),
 // computed on the host in double exactly as the reference computes them.

@@ -590,8 +590,8 @@ __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst 
     const float4 cf = make_float4(__double2float_rn(cc[0]), __double2float_rn(cc[1]),
                                   __double2float_rn(cc[2]), __double2float_rn(r));
     uint32_t code = (uint32_t)k.nlev + 1;
-    if (ray_keeps(k, &k.screen.nf[0][0], k.screen.centered, k.screen, ray_part(k, rc, cf),
-                  true)) {
+    RayPart part = ray_part(k, rc, cf);
+    if (ray_keeps(k, &k.screen.nf[0][0], k.screen.centered, k.screen, part, true)) {
       if (r > 1) {
         code = (uint32_t)k.nlev;  // a sphere around the camera
       } else {

@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(128) k_rays_walk(
         continue;
       }
     }
-    const RayPart part = ray_part(k, p.rc[i], p.cf[i]);
+    RayPart part = ray_part(k, p.rc[i], p.cf[i]);
     uint32_t cnt = 0;
     auto emit = [&](int leaf) {
       if (EMIT) {

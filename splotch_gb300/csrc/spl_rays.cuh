@@ -21,12 +21,12 @@ __device__ __forceinline__ double ddot3(const double a[3], const double b[3]) {
 
 // One particle as the region tests see it: c, r in double (the reference's
 // values), the float copies, and for the dome the zenith terms of
-// new_renderer.cc:203-211 (dot(zenith, c), and the angle of c from the
-// zenith plus and minus the sphere's angular half-width).
+// new_renderer.cc:203-211.
 struct RayPart {
   double c[3], r;
   float cf[3], rf;
   double zdot, th_hi, th_lo;
+  bool th_ready;  // th_hi, th_lo computed (on first use)
 };
 
 __device__ __forceinline__ RayPart ray_part(const RayConst &k, double4 rc, float4 cf) {
@@ -40,18 +40,24 @@ __device__ __forceinline__ RayPart ray_part(const RayConst &k, double4 rc, float
   p.cf[2] = cf.z;
   p.rf = cf.w;
   p.zdot = p.th_hi = p.th_lo = 0.0;
-  if (k.dome) {
-    p.zdot = ddot3(k.zen, p.c);
-    const double cx = dsub(dmul(k.zen[1], p.c[2]), dmul(k.zen[2], p.c[1]));
-    const double cy = dsub(dmul(k.zen[2], p.c[0]), dmul(k.zen[0], p.c[2]));
-    const double cz = dsub(dmul(k.zen[0], p.c[1]), dmul(k.zen[1], p.c[0]));
-    const double cl = __dsqrt_rn(dadd(dadd(dmul(cx, cx), dmul(cy, cy)), dmul(cz, cz)));
-    const double pth = atan2(cl, p.zdot);  // v_angle (cxxsupport/geom_utils.h:59-63)
-    const double dpth = atan2(p.r, __dsqrt_rn(dmul(dadd(1.0, p.r), dsub(1.0, p.r))));
-    p.th_hi = dadd(pth, dpth);
-    p.th_lo = dsub(pth, dpth);
-  }
+  p.th_ready = false;
+  if (k.dome) p.zdot = ddot3(k.zen, p.c);
   return p;
+}
+
+// The angle of c from the zenith plus and minus the sphere's angular
+// half-width (new_renderer.cc:207-209), computed when a theta check first
+// needs them.
+__device__ __forceinline__ void ray_part_theta(const RayConst &k, RayPart &p) {
+  const double cx = dsub(dmul(k.zen[1], p.c[2]), dmul(k.zen[2], p.c[1]));
+  const double cy = dsub(dmul(k.zen[2], p.c[0]), dmul(k.zen[0], p.c[2]));
+  const double cz = dsub(dmul(k.zen[0], p.c[1]), dmul(k.zen[1], p.c[0]));
+  const double cl = __dsqrt_rn(dadd(dadd(dmul(cx, cx), dmul(cy, cy)), dmul(cz, cz)));
+  const double pth = atan2(cl, p.zdot);  // v_angle (cxxsupport/geom_utils.h:59-63)
+  const double dpth = atan2(p.r, __dsqrt_rn(dmul(dadd(1.0, p.r), dsub(1.0, p.r))));
+  p.th_hi = dadd(pth, dpth);
+  p.th_lo = dsub(pth, dpth);
+  p.th_ready = true;
 }
 
 // Sign of r - dot(c, n): +1, -1, or 0 (equal, or a NaN).  The float dot
@@ -72,7 +78,7 @@ __device__ __forceinline__ int ray_side(const float *nf, const double *n, const 
 // flag.  The dome's halfspace check depends on the particle alone: made at
 // the screen cut (halfspace true), it holds for every region after it.
 __device__ __forceinline__ bool ray_keeps(const RayConst &k, const float *nf, int centered,
-                                          const RayRegion &g, const RayPart &p, bool halfspace) {
+                                          const RayRegion &g, RayPart &p, bool halfspace) {
   if (!k.dome)
     return ray_side(nf, g.n[0], p) > 0 && ray_side(nf + 3, g.n[1], p) > 0 &&
            ray_side(nf + 6, g.n[2], p) > 0 && ray_side(nf + 9, g.n[3], p) > 0;
@@ -80,6 +86,7 @@ __device__ __forceinline__ bool ray_keeps(const RayConst &k, const float *nf, in
   if (!centered && (ray_side(nf, g.n[0], p) < 0 || ray_side(nf + 3, g.n[1], p) < 0))
     return false;  // phi check
   if ((p.zdot > g.cthetamin) || (p.zdot < g.cthetamax)) {  // theta check
+    if (!p.th_ready) ray_part_theta(k, p);
     if ((p.th_hi < g.thetamin) || (p.th_lo > g.thetamax)) return false;
   }
   return true;
