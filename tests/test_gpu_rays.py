@@ -158,3 +158,15 @@ def test_errors(renderer):
     # the context stays usable
     pic = gpu_rays(renderer, prm, w.rc, w.particles)
     assert pic.any()
+
+
+def test_full_size_1080p(renderer, port):
+    """4M particles at 1920x1080 (seven levels, ~40M leaf entries, a billion
+    covered pairs) against the FP64 restatement."""
+    w = with_camera_spheres(synth.plain_additive(n=4_000_000, seed=47), 20, 48)
+    prm = dict(w.params.params, new_renderer="T", xres="1920", yres="1080")
+    pic = gpu_rays(renderer, prm, w.rc, w.particles)
+    want, st = port.render_rays(prm, w.rc, w.particles, exact=True)
+    assert st["levels"] == 7 and st["n_overlap"] > 0
+    assert renderer.stats()["n_entries"] > 10_000_000
+    assert rel_linf(pic, want) <= TOL
