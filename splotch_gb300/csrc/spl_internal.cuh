@@ -96,20 +96,14 @@ __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
   return r;
 }
 
-// The Taylor branch of expm1_neg2 alone: its value wherever both lanes of u
-// are below 0.05.
-__device__ __forceinline__ F2 expm1_neg2_small(F2 u) {
-  F2 p = fma2(u, f2(1.f / 24.f), f2(-1.f / 6.f));
-  p = fma2(p, u, f2(0.5f));
-  p = fma2(p, u, f2(-1.f));
-  return mul2(p, u);
-}
-
 // expm1(-u) for u >= 0 on a pair, lane for lane the value of expm1_neg(-u):
 // the same Taylor polynomial (its coefficients negated with u) below 0.05 and
 // ex2(-u*log2e)-1 above.
 __device__ __forceinline__ F2 expm1_neg2(F2 u) {
-  const F2 p = expm1_neg2_small(u);
+  F2 p = fma2(u, f2(1.f / 24.f), f2(-1.f / 6.f));
+  p = fma2(p, u, f2(0.5f));
+  p = fma2(p, u, f2(-1.f));
+  p = mul2(p, u);
   const F2 a = mul2(u, f2(-kLog2e));
   const F2 t = add2(f2(ex2(f2lo(a)), ex2(f2hi(a))), f2(-1.f));
   return f2(f2lo(u) < 0.05f ? f2lo(p) : f2lo(t), f2hi(u) < 0.05f ? f2hi(p) : f2hi(t));

@@ -153,10 +153,6 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
           }
           uint32_t bbj = 0;
           if (NP > 1) bbj = S.bb[j];
-          // every exponent of this particle is e*att <= e (att <= 1): with all
-          // three e below 0.05 each expm1 takes the Taylor branch (uniform
-          // over the warp: one particle)
-          const bool small = !ADD && fmaxf(fmaxf(es.x, e12.x), e12.z) < 0.0499f;
           const uint16_t *run = srun + j * RS;
 #pragma unroll
           for (int p = 0; p < NP; ++p) {
@@ -182,7 +178,7 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
                 } else {
                   const F2 u = mul2(e[c], att);
                   if (AUX) od[AUX ? p : 0][c] = add2(od[AUX ? p : 0][c], u);
-                  const F2 m = small ? expm1_neg2_small(u) : expm1_neg2(u);
+                  const F2 m = expm1_neg2(u);
                   if (!FTB) {
                     acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
                   } else {
