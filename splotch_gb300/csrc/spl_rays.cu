@@ -2,12 +2,14 @@
 // splotch/new_renderer.cc:522-641), selected in the reference by
 // new_renderer=true (splotch/splotch_host.cc:714-723).
 //
-//   particle pass (spl_project.cu: k_rays_prep) -> stable sort by pyramid
-//   level -> per particle, a walk of its level's region tree (count, scan,
-//   emit (leaf, particle) pairs) -> stable sort by leaf -> leaf ranges ->
-//   per level, coarsest first: one CTA per leaf region (k_rays_leaf), which
-//   also adds the spheres around the camera (coarsest level) or the coarser
-//   level upsampled -> dome mask.
+//   particle pass (spl_project.cu: k_rays_prep) -> radix sort by pyramid
+//   level and direction, records gathered into that order -> per particle, a
+//   walk of its level's region tree (count, scan, emit (leaf, particle)
+//   pairs) -> stable sort by leaf -> leaf ranges -> leaf lists cut into
+//   segments -> per level, coarsest first: one warp per segment
+//   (k_rays_leaf), segment sums folded per pixel (k_rays_fold), plus the
+//   spheres around the camera (coarsest level) or the coarser level
+//   upsampled -> dome mask.
 //
 // The reference renders each level by recursive subdivision of the image:
 // a region's list is its parent's list culled by the region's reduceList
@@ -15,15 +17,15 @@
 // pixel against every listed sphere.  Here the region tree is built on the
 // host once per camera and level (it depends on nothing else), and each
 // particle walks it on the GPU, emitting the leaf regions it survives to.  A
-// leaf's list is therefore exactly the reference's list for that region, in
-// the same (ascending particle) order.
+// leaf's list therefore holds exactly the reference's particles for that
+// region (ordered by direction rather than by index: the sums differ from
+// the reference's by rounding only).
 //
 // The pixel-vs-sphere test is screened in float: with d and c expressed
-// relative to a direction u of the leaf (in double, then rounded), the chord
-// |d - c|^2 is known to float precision relative to its own size, so it is
-// compared with the sphere's chord limit with a margin that bounds every
-// rounding; only a chord inside the margin is decided by the reference's
-// double test.
+// relative to a direction u of the leaf, the chord |d - c|^2 is known to
+// float precision relative to its own size, so it is compared with the
+// sphere's chord limit with a margin that bounds every rounding; only a
+// chord inside the margin is decided by the reference's double test.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
