@@ -946,7 +946,8 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   const int npal = fs.npal;
 
   // ---- projector, levels and region trees (kept while the geometry holds) --
-  spl_context::RayKey key{};
+  spl_context::RayKey key;
+  std::memset(&key, 0, sizeof(key));  // compared byte for byte, padding included
   key.xres = xres;
   key.yres = yres;
   key.dome = r->dome ? 1 : 0;
