@@ -358,7 +358,8 @@ spl_status spl_batch_destroy(spl_batch *b);
 
    keys_in   device, 16-byte aligned, n keys
    vals_in   device, n values; NULL sorts the indices 0..n-1
-   keys_out, vals_out  device, n entries each, overlapping neither input
+   keys_out  device, 16-byte aligned, n entries
+   vals_out  device, n entries; neither output overlaps the other or an input
    key_bits  1..32
    stream    cudaStream_t as void*, NULL = legacy default stream
    The call only enqueues work on the stream.  n > SPL_NOALLOC_MAX_PAIRS
@@ -366,8 +367,12 @@ spl_status spl_batch_destroy(spl_batch *b);
    (about 19 MB per device) is shared by all calls on a device: calls that may
    run at the same time, on different streams or host threads, race and
    corrupt each other's results; serialise them.  The first call on a device
-   (n == 0 is enough) looks up the array's address with that device current;
-   make it before any stream capture begins. */
+   (n == 0 is enough) loads the library's device code there and checks the
+   array's capacity; make it before any stream capture begins.  Every call
+   looks up the array's address on the current device, so a
+   cudaDeviceReset between calls is harmless.  A CUDA error already pending on
+   the calling thread is reported (SPL_ERR_CUDA), not cleared, and nothing is
+   launched. */
 #define SPL_NOALLOC_MAX_PAIRS (1 << 21)
 spl_status spl_sort_pairs_noalloc(const uint32_t *keys_in, const uint32_t *vals_in,
                                   uint32_t *keys_out, uint32_t *vals_out, int64_t n,

@@ -2,8 +2,10 @@
 # build_ref.sh -- compile the reference's host render path, in place, into
 # oracle/_ref/ (test infrastructure only: the checker, never the product).
 #
-# Reads the reference sources where they lie (default /root/reference, or
-# $SPLOTCH_REF_DIR) and writes only under oracle/_ref/.  Two libraries:
+# Reads the reference sources where they lie ($SPLOTCH_REF_DIR, else the
+# reference checkout named below -- the one place that names it) and writes
+# only under oracle/_ref/.  `build_ref.sh --where` prints that location.
+# Two libraries:
 #   libsplotch_ref.so         default flags (on x86-64 __SSE2__ is defined, so
 #                             render_new takes its V4sf absorption branch)
 #   libsplotch_ref_scalar.so  the same with -U__SSE2__: the scalar branch that
@@ -13,6 +15,7 @@
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 REF="${SPLOTCH_REF_DIR:-/root/reference}"
+if [ "${1:-}" = "--where" ]; then echo "$REF"; exit 0; fi
 OUT="$HERE/_ref"
 if [ ! -f "$REF/splotch/splotch_host.cc" ]; then
   echo "reference sources not found at $REF; skipping oracle/_ref" >&2

@@ -49,6 +49,13 @@ def build_port(force: bool = False) -> Path:
     return PORT_LIB
 
 
+def ref_dir() -> Path:
+    """Where the reference sources are read from (build_ref.sh decides)."""
+    r = subprocess.run(["bash", str(HERE / "build_ref.sh"), "--where"], capture_output=True,
+                       text=True)
+    return Path(r.stdout.strip())
+
+
 def build_ref() -> bool:
     """Compile the reference sources into oracle/_ref (no-op without them)."""
     r = subprocess.run(["bash", str(HERE / "build_ref.sh")], capture_output=True, text=True)

@@ -35,7 +35,7 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_sort_scratch[2 * kPairBytes + kRadixBytes];
 
 std::mutex g_mu;
-void *g_base[kMaxDevices];  // address of g_sort_scratch per device, once known
+bool g_checked[kMaxDevices];  // capacity checked on this device
 
 spl_status fail(spl_status code, const char *fmt, ...) {
   char buf[512];
@@ -52,7 +52,12 @@ spl_status cuda_fail(const char *what, cudaError_t e) {
   return fail(SPL_ERR_CUDA, "spl_sort_pairs_noalloc: %s: %s", what, cudaGetErrorString(e));
 }
 
-// Set-up, once per device: the scratch array's address on the current device.
+// Set-up: the capacity check, once per device, and the scratch array's
+// address on the current device.  The first call on a device also loads the
+// library's device code there (lazy module loading).  The address is looked
+// up again on every call -- a host-side table lookup that allocates nothing --
+// so that a cudaDeviceReset or another context on the device between calls
+// never leaves a stale address behind.
 spl_status scratch_base(int *dev_out, unsigned char **base_out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -60,20 +65,22 @@ spl_status scratch_base(int *dev_out, unsigned char **base_out) {
   if (dev < 0 || dev >= kMaxDevices)
     return fail(SPL_ERR_UNSUPPORTED, "spl_sort_pairs_noalloc: device %d is beyond the %d supported",
                 dev, kMaxDevices);
-  std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_base[dev]) {
-    const size_t need = spl::radix_scratch_bytes(kMaxPairs);
-    if (need > kRadixBytes)
-      return fail(SPL_ERR_CAPACITY,
-                  "spl_sort_pairs_noalloc: digit-count scratch of %zu bytes exceeds the %zu "
-                  "reserved", need, kRadixBytes);
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_sort_scratch);
-    if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
-    g_base[dev] = p;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_checked[dev]) {
+      const size_t need = spl::radix_scratch_bytes(kMaxPairs);
+      if (need > kRadixBytes)
+        return fail(SPL_ERR_CAPACITY,
+                    "spl_sort_pairs_noalloc: digit-count scratch of %zu bytes exceeds the %zu "
+                    "reserved", need, kRadixBytes);
+      g_checked[dev] = true;
+    }
   }
+  void *p = nullptr;
+  e = cudaGetSymbolAddress(&p, g_sort_scratch);
+  if (e != cudaSuccess) return cuda_fail("cudaGetSymbolAddress", e);
   *dev_out = dev;
-  *base_out = static_cast<unsigned char *>(g_base[dev]);
+  *base_out = static_cast<unsigned char *>(p);
   return SPL_OK;
 }
 
@@ -119,8 +126,12 @@ extern "C" spl_status spl_sort_pairs_noalloc(const uint32_t *keys_in, const uint
   if (!keys_in || !keys_out || !vals_out)
     return fail(SPL_ERR_INVALID, "spl_sort_pairs_noalloc: keys_in, keys_out and vals_out are "
                                  "required");
+  // the digit-count pass reads its keys 16 bytes at a time, and with three or
+  // four digit passes one of them reads keys_out
   if (reinterpret_cast<uintptr_t>(keys_in) & 15u)
     return fail(SPL_ERR_INVALID, "spl_sort_pairs_noalloc: keys_in must be 16-byte aligned");
+  if (reinterpret_cast<uintptr_t>(keys_out) & 15u)
+    return fail(SPL_ERR_INVALID, "spl_sort_pairs_noalloc: keys_out must be 16-byte aligned");
   if ((st = check_device_ptr(keys_in, dev, "keys_in")) != SPL_OK) return st;
   if (vals_in && (st = check_device_ptr(vals_in, dev, "vals_in")) != SPL_OK) return st;
   if ((st = check_device_ptr(keys_out, dev, "keys_out")) != SPL_OK) return st;
@@ -134,7 +145,12 @@ extern "C" spl_status spl_sort_pairs_noalloc(const uint32_t *keys_in, const uint
   uint32_t *keys_tmp = reinterpret_cast<uint32_t *>(base);
   uint32_t *vals_tmp = reinterpret_cast<uint32_t *>(base + kPairBytes);
   void *digit_scratch = base + 2 * kPairBytes;
-  cudaGetLastError();
+  // an error that the caller's earlier work left pending is reported, not
+  // cleared, and nothing is launched
+  const cudaError_t pending = cudaPeekAtLastError();
+  if (pending != cudaSuccess)
+    return fail(SPL_ERR_CUDA, "spl_sort_pairs_noalloc: a CUDA error is already pending on this "
+                              "thread (%s); nothing was launched", cudaGetErrorString(pending));
   spl::radix_sort_pairs(keys_in, vals_in, keys_tmp, vals_tmp, keys_out, vals_out, n, 0, key_bits,
                         true, digit_scratch, static_cast<cudaStream_t>(stream), nullptr, nullptr,
                         false);

@@ -5,7 +5,7 @@
 // (declared at splotch/splotch_host.h:43) and runs the whole frame -- project,
 // colourise, depth sort, binning, splat -- through libsplgpu.so's C ABI
 // (include/splotch_gb300.h).  It is compiled inside the Splotch tree against the
-// Splotch headers and linked instead of splotch_host.o.
+// Splotch headers and linked instead of splotch_host.o (and new_renderer.o).
 //
 // Behaviour kept from the reference:
 //   * the same paramfile keys with the same defaults (find() inserts them);

@@ -6,14 +6,15 @@ builds oracle/_ref, compiles the shim and a small caller, links them with the
 reference's support objects minus splotch_host.cc.o and with libsplgpu.so,
 and runs the program.  Without a GPU the frame fails cleanly with a
 PlanckError (exit 3); with one it renders (exit 0)."""
-import os
 import subprocess
 from pathlib import Path
 
 import pytest
 
 ROOT = Path(__file__).resolve().parent.parent
-REF = Path(os.environ.get("SPLOTCH_REF_DIR", "/root/reference"))
+from oracle.oracle import ref_dir
+
+REF = ref_dir()
 
 
 @pytest.mark.skipif(not (REF / "splotch" / "splotch_host.h").exists(),
@@ -31,7 +32,7 @@ def test_shim_links_in_place_of_splotch_host(built, tmp_path):
     inc = ["-I", str(REF), "-I", str(REF / "cxxsupport"), "-I", str(ROOT / "include")]
     cmd = (["g++", "-O2", "-std=c++11", "-fopenmp", "-w", *inc,
             str(ROOT / "splotch_gb300" / "shim" / "host_rendering_gb300.cc"),
-            str(ROOT / "splotch_gb300" / "shim" / "link_check.cc"), *map(str, objs),
+            str(ROOT / "tests" / "shim" / "link_check.cc"), *map(str, objs),
             "-L", str(ROOT / "splotch_gb300"), "-lsplgpu",
             f"-Wl,-rpath,{ROOT / 'splotch_gb300'}", "-o", str(exe)])
     r = subprocess.run(cmd, capture_output=True, text=True)
