@@ -18,10 +18,18 @@ e2e   : the same metric through the C ABI with HOST buffers: a sequence of
 roofline: the dominant kernel of the frame, algorithmic work / its CUDA-event
         time, against MEASURED_PEAKS.json.
 cpu_baseline: the CPU restatement of the reference (bit-exact with it) timed
-        on this host's cores on a 1-in-5 subsample of the same frame.
+        on this host's cores on the whole frame; the same leg, as the checker,
+        measures the timed frame's image against the FP64 oracle
+        (image_rel_linf) and the reference's own FP32 arithmetic beside it.
+drop_in_default: the frame through host_rendering() with the drop-in's
+        defaults (back-to-front compositing, every particle projected,
+        colourised and sorted back into the caller's array), from pageable
+        host memory, as a Splotch caller would make the call.
+large : the large render (400M particles, 4096^2, forward and
+        forward+backward), batched / fwd_bwd / rays: the other workloads.
 
 --impl reference runs that CPU implementation alone (rank 0) on the same
-config and prints its own line.  Multi-GPU (torchrun): replicas -- every rank
+frame and prints its own line.  Multi-GPU (torchrun): replicas -- every rank
 renders its own seeded frame, value = all ranks' particles / max time.
 """
 from __future__ import annotations
@@ -42,7 +50,17 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Mparticles/s & frames/s (plain, batched, fwd+bwd) on 1 GB300 at ≤1e-4 rel err"
-CPU_SAMPLE_STRIDE = 5
+
+# The splat's DRAM traffic and issue / shared-memory figures come from the
+# committed one-kernel ncu capture (the bench itself runs no profiler); the
+# traffic is scaled to the timed frame by its reference fragment count.
+SPLAT_CAPTURE = {
+    "source": "profiles/k_splat_ftb_pairs_10M.md",
+    "fragments": 7.53e8,          # reference fragments of the captured launch
+    "dram_bytes": 90.4e6,         # dram__bytes_read.sum + dram__bytes_write.sum
+    "issue_frac": 0.744,          # issue slots busy per SMSP while active
+    "smem_wavefront_frac": 0.19,  # shared wavefronts / (SM cycles x SMs)
+}
 
 
 def parse():
@@ -64,10 +82,13 @@ def parse():
                     help="particle-count multiplier of the batched workload")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-rays", action="store_true")
+    ap.add_argument("--no-large", action="store_true")
+    ap.add_argument("--no-drop-in", action="store_true")
+    ap.add_argument("--drop-in-steps", type=int, default=3)
     ap.add_argument("--rays-particles", type=int, default=1_000_000)
     ap.add_argument("--only", default="all",
                     choices=["all", "fwd_bwd", "batched", "large", "rays"],
-                    help="run one section alone (profiling; 'large' runs only this way)")
+                    help="run one section alone (profiling)")
     ap.add_argument("--large-scale", type=float, default=1.0)
     ap.add_argument("--large-steps", type=int, default=2)
     ap.add_argument("--fwd-bwd-particles", type=int, default=4_000_000)
@@ -155,28 +176,80 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(w, steps: int = 2, warmup: int = 1) -> dict:
-    """The oracle's restatement of host_rendering (bit-exact with the
-    reference) on this host's cores, on a 1-in-5 particle subsample."""
+def host_cpu() -> dict:
+    """The host CPU as the reference arm sees it: model, cores, OpenMP binding."""
+    model = None
+    try:
+        r = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10)
+        for line in r.stdout.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.TimeoutExpired):
+        pass
+    return {"cpu_model": model, "logical_cpus": os.cpu_count(),
+            "omp_proc_bind": os.environ.get("OMP_PROC_BIND"),
+            "omp_num_threads": os.environ.get("OMP_NUM_THREADS")}
+
+
+def _oracle_port():
+    """The oracle's restatement of host_rendering, loaded with every host core
+    and threads bound close (set before its OpenMP runtime starts)."""
+    os.environ.setdefault("OMP_PROC_BIND", "close")
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
     from oracle.oracle import Port
 
-    port = Port()
+    return Port()
+
+
+def _time_host_rendering(port, w, steps: int, warmup: int) -> list:
+    """Wall time of the restatement's host_rendering on the whole frame, at
+    the reference's own default tile size (tile_size_cpu=50)."""
     prm = dict(w.params.params)
-    prm["tile_size_cpu"] = "50"  # the reference's own default tile size
-    sample = np.ascontiguousarray(w.particles[::CPU_SAMPLE_STRIDE])
+    prm["tile_size_cpu"] = "50"
     ts = []
     for i in range(warmup + steps):
-        p = sample.copy()
+        p = w.particles.copy()
         t0 = time.perf_counter()
         port.host_rendering(prm, w.rc, p)
         if i >= warmup:
             ts.append(time.perf_counter() - t0)
+    return ts
+
+
+def cpu_baseline(w, pic_gpu: np.ndarray, steps: int = 2, warmup: int = 1) -> dict:
+    """The oracle's restatement of host_rendering (bit-exact with the
+    reference) timed on this host's cores on the whole frame; then, as the
+    checker, the FP64 oracle image of the same frame at the GPU's tile size,
+    against which the GPU image and the reference's FP32 arithmetic (the
+    scalar render_new branch an AArch64 host compiles) are measured."""
+    from oracle.oracle import rel_linf
+
+    port = _oracle_port()
+    ts = _time_host_rendering(port, w, steps, warmup)
     t = statistics.median(ts)
-    return {"value": len(sample) / t / 1e6, "unit": "Mparticles/s", "cores": port.threads,
-            "kind": "port", "seconds_per_frame": t,
-            "sample": f"every {CPU_SAMPLE_STRIDE}th particle ({len(sample)}) of the same frame, "
-                      f"same image and camera, reference default tile_size_cpu=50; median of "
-                      f"{steps} after {warmup} warm-up"}
+    out = {"value": len(w.particles) / t / 1e6, "unit": "Mparticles/s", "cores": port.threads,
+           "kind": "port", "seconds_per_frame": t, **host_cpu(),
+           "sample": f"the whole frame ({len(w.particles)} particles), same image and camera, "
+                     f"reference default tile_size_cpu=50; median of {steps} after {warmup} "
+                     "warm-up"}
+    # the checker: FP64 image of the timed frame (coverage and order as the GPU's)
+    prm = dict(w.params.params)
+    T = int(prm["tile_size_cpu"])
+    xres, yres = int(prm["xres"]), int(prm["yres"])
+    a_eq_e = prm.get("a_eq_e", "T") == "T"
+    gray = float(prm.get("gray_absorption", 0.2))
+    p = w.particles.copy()
+    port.project_colorize(prm, w.rc, p)
+    order = None if a_eq_e else port.sort_perm(p, int(prm.get("sort_type", 1)))
+    pic64, _ = port.render_fp64(p, order, xres, yres, T, a_eq_e, gray)
+    pic32 = port.render_fp32(p, order, xres, yres, T, a_eq_e, gray, simd=False)[0]
+    out["image_check"] = {
+        "image_rel_linf": rel_linf(pic_gpu, pic64),
+        "reference_fp32_rel_linf": rel_linf(pic32, pic64),
+        "tolerance": 1e-4, "floor": "1e-6 x max|pixel|",
+        "against": f"FP64 oracle at the GPU tile size {T}, same coverage and order"}
+    return out
 
 
 def run_reference(args):
@@ -184,25 +257,17 @@ def run_reference(args):
     if rank != 0:
         return 0
     w, cfg = make_workload(args)
-    from oracle.oracle import Port
-
-    port = Port()
-    prm = dict(w.params.params)
-    prm["tile_size_cpu"] = "50"  # the reference's own default tile size
-    sample = np.ascontiguousarray(w.particles[::CPU_SAMPLE_STRIDE])
-    ts = []
-    for i in range(args.warmup + args.steps):
-        p = sample.copy()
-        t0 = time.perf_counter()
-        port.host_rendering(prm, w.rc, p)
-        if i >= args.warmup:
-            ts.append(time.perf_counter() - t0)
+    port = _oracle_port()
+    ts = _time_host_rendering(port, w, args.steps, args.warmup)
     t = sum(ts) / len(ts)
-    v = len(sample) / t / 1e6
+    n = len(w.particles)
+    v = n / t / 1e6
     cb = {"value": v, "unit": "Mparticles/s", "cores": port.threads, "kind": "port",
-          "sample": f"every {CPU_SAMPLE_STRIDE}th particle ({len(sample)}) of the frame per "
-                    f"step; the reference itself cannot be compiled on this host, its "
-                    f"bit-exact C restatement (oracle/spl_oracle.c) runs instead"}
+          **host_cpu(),
+          "sample": f"the whole frame ({n} particles) every step, at the reference's default "
+                    "tile_size_cpu=50; the reference's own build cannot run on this host (its "
+                    "sources do not travel and x86 binaries are removed), so its bit-exact C "
+                    "restatement (oracle/spl_oracle.c) runs instead"}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Mparticles/s",
             "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
             "frames_per_s": 1.0 / t, "higher_is_better": True, "scaling": "weak",
@@ -215,7 +280,7 @@ def run_reference(args):
 
 
 def roofline(stage_ms: dict, n: int, n_act: int, n_entries: int, n_tiles: int, frags: int,
-             args, pk: dict, a_eq_e: bool) -> tuple[dict, dict]:
+             args, pk: dict, a_eq_e: bool, n_sm: int) -> tuple[dict, dict]:
     """Per-stage rooflines; the top-level one is the dominant stage's.
     Algorithmic bytes: project reads every particle's SoA fields (x,y,z,r,I,
     e.r,e.g,e.b: 32 B + type 2 B) and writes the projected record of each
@@ -224,7 +289,8 @@ def roofline(stage_ms: dict, n: int, n_act: int, n_entries: int, n_tiles: int, f
     active particle (12 B), writes one 4-byte entry per (particle, tile) and
     4 B per tile."""
     hbm = pk["hbm_gbs"]
-    fp32_peak = 2 * 128 * 152 * pk["sm_max_mhz"] * 1e6 / 1e12  # TFLOP/s, nominal issue
+    # nominal FP32 rate: 128 FMA lanes per SM per clock at the maximum SM clock
+    fp32_peak = 2 * 128 * n_sm * pk["sm_max_mhz"] * 1e6 / 1e12  # TFLOP/s
     st = {}
     proj_bytes = n * 34 + n_act * 32
     st["project"] = {"bound": "hbm", "unit": "GB/s", "algorithmic_bytes": proj_bytes,
@@ -246,14 +312,29 @@ def roofline(stage_ms: dict, n: int, n_act: int, n_entries: int, n_tiles: int, f
         v["ms"] = stage_ms[k + "_ms"]
         v["peak"] = hbm if v["bound"] == "hbm" else fp32_peak
         v["frac"] = v["achieved"] / v["peak"]
+    kernels = {"project": "k_project_flags+scan_popc+k_project_dense",
+               "sort": "k_os_hist+k_os_prefix+k_rs_downsweep",
+               "bin": "k_gather_u32+scan+k_emit_narrow+k_emit_wide+tile sort+k_tile_ranges",
+               "splat": "k_splat"}
+    for k, v in st.items():
+        v["kernels"] = kernels[k]
     dom = max(st, key=lambda k: st[k]["ms"])
     d = st[dom]
-    top = {"kernel": {"project": "k_project_soa", "sort": "k_rs_downsweep+k_rs_upsweep+scan",
-                      "bin": "k_emit_*+tile sort+k_tile_ranges", "splat": "k_splat"}[dom],
-           "stage": dom, "bound": d["bound"], "achieved": d["achieved"], "peak": d["peak"],
-           "unit": d["unit"], "frac": d["frac"], "traffic": None,
-           "peak_source": (pk["source"] if d["bound"] == "hbm"
-                           else "nominal FP32 issue rate at max SM clock")}
+    top = {"kernel": kernels[dom], "stage": dom, "bound": d["bound"], "achieved": d["achieved"],
+           "peak": d["peak"], "unit": d["unit"], "frac": d["frac"], "traffic": None,
+           "peak_source": (f"{pk['source']} HBM copy bandwidth" if d["bound"] == "hbm"
+                           else f"nominal FP32 rate, 128 lanes x {n_sm} SMs x "
+                                f"{pk['sm_max_mhz']:.0f} MHz (no FP32 peak in "
+                                "MEASURED_PEAKS.json)"),
+           "sm_count": n_sm}
+    if dom == "splat":
+        c = SPLAT_CAPTURE
+        top["traffic"] = c["dram_bytes"] * frags / c["fragments"]
+        top["traffic_note"] = (f"DRAM read+write bytes per launch from {c['source']}, scaled "
+                               "to this frame by its reference fragment count")
+        top["issue_frac"] = c["issue_frac"]
+        top["smem_wavefront_frac"] = c["smem_wavefront_frac"]
+        top["capture"] = c["source"]
     return top, st
 
 
@@ -556,20 +637,74 @@ def batched(args, local: int) -> dict:
         ts.append(time.perf_counter() - t1)
     info = b.info()
     batch_ms = statistics.median(ts) * 1e3
+    b.close()
+    # a second batch of the same shape: the autotuner's choice from its cache
+    t0 = time.perf_counter()
+    b2 = sg.Batch(r, sets, frames)
+    create2_s = time.perf_counter() - t0
+    info2 = b2.info()
+    b2.close()
     out.update({"plain_ms": plain_ms, "plain_frames_per_s": nf / (plain_ms * 1e-3),
                 "batched_ms": batch_ms, "batched_device_ms": info["render_ms"],
                 "batched_frames_per_s": nf / (batch_ms * 1e-3),
                 "batched_mparticle_frames_per_s": pf_total / (batch_ms * 1e-3) / 1e6,
                 "speedup_frames_per_s": plain_ms / batch_ms,
+                "speedup_vs_plain_split_tiles": out["plain_split_tiles_ms"] / batch_ms,
                 "tile_size": info["tile_size"],
                 "splat_config_additive": info["splat_config_additive"],
                 "splat_config_absorption": info["splat_config_absorption"],
                 "graph": info["graph"], "create_s": create_s, "tune_ms": info["tune_ms"],
+                "plan_ms": info["plan_ms"],
+                "second_create": {"create_s": create2_s, "tune_ms": info2["tune_ms"],
+                                  "tune_cached": info2["tune_cached"],
+                                  "plan_ms": info2["plan_ms"]},
                 "kernel_launches_per_render": info["kernel_launches"],
                 "active_records": info["n_active"], "bin_entries": info["n_entries"]})
-    b.close()
     r.close()
     return out
+
+
+def drop_in_default(args, w, local: int) -> dict:
+    """The frame through host_rendering() with the drop-in's defaults, the way
+    a Splotch caller makes the call (splotch/splotch.cc:261): particle_sim
+    records in pageable host memory, back-to-front compositing, and the
+    reference's side effects -- every particle projected, colourised and
+    stably depth-sorted back into the caller's array -- plus the image.  Wall
+    time per call, copies included; the median of the timed calls."""
+    import copy
+
+    import torch
+
+    import splotch_gb300 as sg
+
+    prm = dict(w.params.params)
+    prm.pop("gpu_order", None)  # the drop-in's default order: back-to-front
+    r = sg.Renderer(local)
+    n = len(w.particles)
+    ts, stages = [], None
+    for i in range(1 + max(1, args.drop_in_steps)):
+        pf = sg.ParamFile(dict(prm))
+        rc = copy.copy(w.rc)
+        rc.pic = None
+        parts = w.particles.copy()  # the caller's vector (mutated in place)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sg.host_rendering(pf, parts, rc, renderer=r)
+        dt = time.perf_counter() - t0
+        if i:
+            ts.append(dt)
+            stages = r.stats()
+    r.close()
+    t = statistics.median(ts)
+    return {"ms": t * 1e3, "mparticles_per_s": n / t / 1e6, "frames_per_s": 1.0 / t,
+            "order": "btf", "writeback": "full (projected, colourised, sorted particle_sim "
+                                          "array copied back)",
+            "input": "pageable host particle_sim records",
+            "h2d_bytes": n * 36, "d2h_bytes": n * 36 + int(prm["xres"]) * int(prm["yres"]) * 12,
+            "calls_ms": [round(x * 1e3, 2) for x in ts],
+            "stages_ms": {k: round(float(stages[k]), 3) for k in
+                          ("h2d_ms", "project_ms", "sort_ms", "bin_ms", "splat_ms", "d2h_ms",
+                           "total_ms")}}
 
 
 def run_gpu(args):
@@ -633,6 +768,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
+    pic_host = pic.cpu().numpy()  # the timed frame's image, for the checker
     if dist:
         t = torch.tensor([ms], device=f"cuda:{local}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -683,14 +819,20 @@ def run_gpu(args):
             dist.destroy_process_group()
         return 0
     pk = peaks()
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
     top, st = roofline(stages, n, int(last["n_active"]), int(last["n_entries"]),
-                       int(last["n_tiles"]), frags, args, pk, bool(desc.a_eq_e))
+                       int(last["n_tiles"]), frags, args, pk, bool(desc.a_eq_e), n_sm)
+    r.close()
+    del soa, host_aos, host_pic
+    di = None if args.no_drop_in else drop_in_default(args, w, local)
     cb = None
     if world == 1 and not args.no_cpu_baseline:
-        cb = cpu_baseline(w)
+        cb = cpu_baseline(w, pic_host)
+    del w
     fb = None if args.no_fwd_bwd else fwd_bwd(args, local)
     bt = None if args.no_batched else batched(args, local)
     ry = None if args.no_rays else rays(args, local)
+    lg = None if args.no_large else large(args, local)
     line = {"metric": METRIC, "value": world * n / (ms * 1e-3) / 1e6, "unit": "Mparticles/s",
             "frames_per_s": world * 1e3 / ms, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
@@ -698,7 +840,9 @@ def run_gpu(args):
             "data": "synthetic (seeded halo mixture; no snapshot available)", "config": cfg,
             "e2e": e2e, "gpu_launches": launches, "clocks": clk, "roofline": top,
             "stages": st, "fragments": frags, "bin_entries": int(last["n_entries"]),
-            "cpu_baseline": cb, "fwd_bwd": fb, "batched": bt, "rays": ry}
+            "image_check": cb.pop("image_check") if cb else None,
+            "cpu_baseline": cb, "drop_in_default": di, "fwd_bwd": fb, "batched": bt,
+            "rays": ry, "large": lg}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -185,10 +185,22 @@ spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
 /* Debug options for later spl_render calls.  Bit 0: project through the
    exact FP64 arithmetic only (no float-float fast path); the two must agree
    bit for bit.  Bit 1: radix sorts in the reduce-then-scan form instead of
-   onesweep (no inter-block waits); results are identical. */
+   onesweep (no inter-block waits); results are identical.  Bit 2 (failure
+   test): the depth sort's first scatter pass never takes its first tile, so
+   the next tile's look-back finds that status unpublished and gives up after
+   a short bounded spin; spl_render then returns SPL_ERR_TIMEOUT before the
+   invalid permutation is used, and the context stays usable. */
 #define SPL_DEBUG_EXACT_FP64 1
 #define SPL_DEBUG_RADIX_REDUCE_SCAN 2
+#define SPL_DEBUG_LOOKBACK_STALL 4
 spl_status spl_debug_set_options(spl_context *ctx, int flags);
+
+/* Failure test of device allocation (process-wide): the nth device buffer
+   allocation the library makes from now on -- a spl_context growing a
+   buffer, or a batch's buffers -- fails once with SPL_ERR_ALLOC without
+   calling cudaMalloc; nth = 0 cancels.  The reference's analogue is the
+   abort on a device allocation error (cuda/cuda_splotch.cc:105). */
+spl_status spl_debug_fail_alloc(int64_t nth);
 
 /* ---- ray-sphere render: host_rendering with new_renderer=true ---------- */
 /* The second renderer behind host_rendering (splotch/splotch_host.cc:714-723
@@ -316,6 +328,10 @@ typedef struct {
   float capacity_margin;        /* buffer headroom over the measured counts (1.1);
                                    below 1 forces a re-plan (test hook) */
   int use_graph;                /* 1: capture and replay a CUDA graph; 0: launch eagerly */
+  int tune_cache;               /* 1 (default): the autotuner's choice is kept per batch
+                                   shape for the life of the process, and a later batch
+                                   of the same shape takes it without timing anything;
+                                   0: always search */
 } spl_batch_options;
 
 typedef struct {
@@ -324,9 +340,14 @@ typedef struct {
   int64_t cap_active, cap_entries, total_tiles;
   int64_t n_active, n_entries;  /* last render */
   float render_ms;              /* last spl_batch_render, launch to completion */
-  float tune_ms;                /* autotuning time spent in spl_batch_create */
+  float tune_ms;                /* spl_batch_create's search: timed candidate tile sizes
+                                   and launch configurations (0 when the choice came
+                                   from the tuning cache) */
   int kernel_launches;          /* kernels per render */
   int replans;                  /* capacity re-plans so far */
+  int tune_cached;              /* 1 when the choice came from the tuning cache */
+  float plan_ms;                /* spl_batch_create's measured plan at the chosen tile
+                                   size (one plain render of every frame) */
 } spl_batch_info;
 
 typedef struct spl_batch spl_batch;

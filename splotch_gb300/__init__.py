@@ -534,7 +534,8 @@ class Batch:
 
     def __init__(self, renderer: Renderer, sets: list, frames: list, *, tile_size: int = 0,
                  splat_config_additive: int = -1, splat_config_absorption: int = -1,
-                 capacity_margin: float = 1.1, use_graph: bool = True):
+                 capacity_margin: float = 1.1, use_graph: bool = True,
+                 tune_cache: bool = True):
         self.lib = renderer.lib
         self._keep = [sets, frames]
         psets = (_abi.Particles * max(1, len(sets)))()
@@ -557,6 +558,7 @@ class Batch:
         opt.splat_config_absorption = splat_config_absorption
         opt.capacity_margin = capacity_margin
         opt.use_graph = 1 if use_graph else 0
+        opt.tune_cache = 1 if tune_cache else 0
         self.handle = C.c_void_p()
         _abi.check(self.lib.spl_batch_create(renderer.ctx, psets, len(sets), pframes,
                                              len(frames), C.byref(opt), C.byref(self.handle)))

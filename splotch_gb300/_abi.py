@@ -32,9 +32,12 @@ EXPORTED = [
     "spl_batch_create", "spl_batch_render", "spl_batch_get_info", "spl_batch_destroy",
     "spl_post_desc_defaults", "spl_postprocess", "spl_image_encode", "spl_write_image",
     "spl_particle_normalize", "spl_rays_desc_defaults", "spl_render_rays",
+    "spl_debug_fail_alloc",
 ]
 SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
+SPL_DEBUG_RADIX_REDUCE_SCAN = 2
+SPL_DEBUG_LOOKBACK_STALL = 4
 
 
 class Camera(C.Structure):
@@ -118,7 +121,7 @@ class BatchFrame(C.Structure):
 class BatchOptions(C.Structure):
     _fields_ = [("tile_size", C.c_int), ("splat_config_additive", C.c_int),
                 ("splat_config_absorption", C.c_int), ("capacity_margin", C.c_float),
-                ("use_graph", C.c_int)]
+                ("use_graph", C.c_int), ("tune_cache", C.c_int)]
 
 
 class BatchInfo(C.Structure):
@@ -127,7 +130,7 @@ class BatchInfo(C.Structure):
                 ("cap_active", C.c_int64), ("cap_entries", C.c_int64),
                 ("total_tiles", C.c_int64), ("n_active", C.c_int64), ("n_entries", C.c_int64),
                 ("render_ms", C.c_float), ("tune_ms", C.c_float), ("kernel_launches", C.c_int),
-                ("replans", C.c_int)]
+                ("replans", C.c_int), ("tune_cached", C.c_int), ("plan_ms", C.c_float)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -175,6 +178,7 @@ def load(path: Path | str | None = None) -> C.CDLL:
         "spl_debug_get_bins": (C.c_int, [vp, vp, i64, vp, i64]),
         "spl_debug_count_fragments": (C.c_int, [vp, vp]),
         "spl_debug_set_options": (C.c_int, [vp, C.c_int]),
+        "spl_debug_fail_alloc": (C.c_int, [i64]),
         "spl_splat_config_count": (C.c_int, []),
         "spl_splat_config_valid": (C.c_int, [C.c_int, C.c_int]),
         "spl_sort_pairs_noalloc": (C.c_int, [vp, vp, vp, vp, i64, C.c_int, vp]),

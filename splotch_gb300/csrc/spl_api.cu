@@ -9,6 +9,7 @@
 // All device memory is owned by the context and grows on demand; a frame that
 // fits the current capacity allocates nothing.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -91,6 +92,8 @@ spl_status fail(spl_status code, const std::string &msg) {
       return fail(SPL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
   } while (0)
 
+std::atomic<int64_t> g_alloc_countdown{0};  // spl_debug_fail_alloc
+
 spl_status ensure(spl_context::Buf &b, size_t bytes) {
   if (bytes == 0) bytes = 16;
   if (b.cap >= bytes) return SPL_OK;
@@ -98,6 +101,9 @@ spl_status ensure(spl_context::Buf &b, size_t bytes) {
   b.p = nullptr;
   b.cap = 0;
   size_t want = bytes + bytes / 8;  // headroom for slowly growing frames
+  if (spl::alloc_failure_due())
+    return fail(SPL_ERR_ALLOC, "cudaMalloc(" + std::to_string(want) +
+                                   "): failure injected by spl_debug_fail_alloc");
   cudaError_t e = cudaMalloc(&b.p, want);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -202,6 +208,14 @@ spl_status project_full(spl_context *c, int64_t n, bool with_key, int *launches)
 }  // namespace
 
 void spl::set_last_error(const char *msg) { g_err = msg; }
+
+bool spl::alloc_failure_due() {
+  int64_t v = g_alloc_countdown.load();
+  while (v > 0) {  // count this allocation; the one that reaches zero fails
+    if (g_alloc_countdown.compare_exchange_weak(v, v - 1)) return v == 1;
+  }
+  return false;
+}
 
 spl_status spl::host_fail(spl_status code, const std::string &msg) { return fail(code, msg); }
 
@@ -550,7 +564,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
     spl::radix_sort_pairs(as<uint32_t>(c->key), nullptr, as<uint32_t>(c->ktmp),
                           as<uint32_t>(c->vtmp), as<uint32_t>(c->key) /*unused out*/,
                           as<uint32_t>(c->perm), na, 0, 32, false, c->scratch.p, s, &launches,
-                          d_err, onesweep);
+                          d_err, onesweep, (c->debug_flags & SPL_DEBUG_LOOKBACK_STALL) != 0);
     order = as<uint32_t>(c->perm);
   }
   cudaEventRecord(c->ev[3], s);
@@ -559,15 +573,24 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   // tile counts in visiting order (one gather; the sort's key scratch is free)
   const uint32_t *count_seq = as<uint32_t>(c->count);
   if (order) {
-    spl::launch_gather_u32(as<uint32_t>(c->count), order, na, as<uint32_t>(c->ktmp), s);
+    // a permutation that a look-back left invalid reads nothing out of range
+    spl::launch_gather_u32(as<uint32_t>(c->count), order, na, as<uint32_t>(c->ktmp), s, na,
+                           d_err);
     ++launches;
     count_seq = as<uint32_t>(c->ktmp);
   }
   uint64_t *off = as<uint64_t>(c->off);
   spl::scan_counts(count_seq, nullptr, na, off, c->scratch.p, s, &launches);
   uint64_t ne = 0;
+  uint32_t err_mid = 0;
   SPL_CK(cudaMemcpyAsync(&ne, off + na, 8, cudaMemcpyDeviceToHost, s));
+  SPL_CK(cudaMemcpyAsync(&err_mid, d_err, 4, cudaMemcpyDeviceToHost, s));
   SPL_CK(cudaStreamSynchronize(s));
+  // the depth sort's permutation is consumed from here on: stop if it is invalid
+  if (err_mid & 2u) {
+    c->has_order = false;
+    return fail(SPL_ERR_TIMEOUT, "a look-back wait of the depth sort gave up");
+  }
   if (ne >= 0xffffffffULL) return fail(SPL_ERR_CAPACITY, "more than 2^32-1 bin entries");
   if ((st = ensure(c->tkey, ne * 4)) || (st = ensure(c->tval, ne * 4)) ||
       (st = ensure(c->tkey2, ne * 4)) || (st = ensure(c->tval2, ne * 4)) ||
@@ -1531,6 +1554,12 @@ int spl_splat_config_valid(int cfg, int tile_size) {
 spl_status spl_debug_set_options(spl_context *c, int flags) {
   if (!c) return fail(SPL_ERR_INVALID, "null ctx");
   c->debug_flags = flags;
+  return SPL_OK;
+}
+
+spl_status spl_debug_fail_alloc(int64_t nth) {
+  if (nth < 0) return fail(SPL_ERR_INVALID, "spl_debug_fail_alloc: nth must be >= 0");
+  g_alloc_countdown.store(nth);
   return SPL_OK;
 }
 

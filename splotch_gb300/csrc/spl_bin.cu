@@ -186,15 +186,24 @@ void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
 
 __global__ void __launch_bounds__(256) k_gather_u32(const uint32_t *__restrict__ src,
                                                     const uint32_t *__restrict__ perm,
-                                                    int64_t n, uint32_t *__restrict__ out) {
+                                                    int64_t n, uint32_t *__restrict__ out,
+                                                    uint64_t nsrc, uint32_t *err) {
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n;
-       s += (int64_t)gridDim.x * blockDim.x)
-    out[s] = __ldg(src + __ldg(perm + s));
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t v = __ldg(perm + s);
+    if (v < nsrc) {
+      out[s] = __ldg(src + v);
+    } else {
+      out[s] = 0u;
+      if (err) atomicOr(err, 2u);
+    }
+  }
 }
 
 void launch_gather_u32(const uint32_t *src, const uint32_t *perm, int64_t n, uint32_t *out,
-                       cudaStream_t s) {
-  if (n > 0) k_gather_u32<<<grid_for(n, 256), 256, 0, s>>>(src, perm, n, out);
+                       cudaStream_t s, int64_t nsrc, uint32_t *err) {
+  const uint64_t lim = nsrc > 0 ? (uint64_t)nsrc : ~0ull;
+  if (n > 0) k_gather_u32<<<grid_for(n, 256), 256, 0, s>>>(src, perm, n, out, lim, err);
 }
 
 void launch_tile_cost(const uint32_t *tile_start, int64_t ntiles, uint32_t *key,

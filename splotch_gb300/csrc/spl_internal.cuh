@@ -329,13 +329,21 @@ size_t radix_scratch_bytes(int64_t n);
 // onesweep: one histogram pass then one decoupled-look-back pass per digit
 // (bounded waits; a wait that gives up sets bit 1 of *err); otherwise the
 // reduce-then-scan form (no inter-block waits).
+// stall_test (onesweep, a debug option of spl_render): the first scatter pass
+// never takes tile 0, so tile 1's look-back finds its status unpublished and
+// gives up after a short spin limit; every write stays in bounds, the
+// permutation is invalid and bit 1 of *err is set.
 int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_tmp,
                      uint32_t *vals_tmp, uint32_t *keys_out, uint32_t *vals_out, int64_t n,
                      int bit0, int bit1, bool keys_needed, void *scratch, cudaStream_t s,
-                     int *launches, uint32_t *err, bool onesweep);
+                     int *launches, uint32_t *err, bool onesweep, bool stall_test = false);
 
 // Message returned by spl_last_error_string() on this host thread.
 void set_last_error(const char *msg);
+
+// The allocation failure test (spl_debug_fail_alloc): true when the device
+// allocation about to be made is the one chosen to fail.
+bool alloc_failure_due();
 
 // Post-processing and output (spl_post.cu).  exptable_tables builds the two
 // 1024-entry tables, expfac and taylorlimit of exptable<float32>(maxexp) on the
@@ -388,8 +396,11 @@ void scan_counts(const uint32_t *count, const uint32_t *order, int64_t n, uint64
 // its index; order null = identity).  wide_list must hold n entries, wide_n
 // one counter (particles with more than 64 tiles go to the warp-per-particle
 // emitter through this list).
+// out[i] = src[perm[i]]; with nsrc > 0, a perm value >= nsrc reads nothing,
+// gives 0 and sets bit 1 of *err (a permutation left invalid by a look-back
+// that gave up).
 void launch_gather_u32(const uint32_t *src, const uint32_t *perm, int64_t n, uint32_t *out,
-                       cudaStream_t s);
+                       cudaStream_t s, int64_t nsrc = 0, uint32_t *err = nullptr);
 void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order,
                  const uint64_t *off, int64_t n, Tiling g, uint32_t *tkey, uint32_t *tval,
                  uint32_t *wide_list, uint32_t *wide_n, cudaStream_t s);

@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_upsweep(const uint32_t *__res
 constexpr int OS_EPOCH_SHIFT = 56, OS_KIND_SHIFT = 54;
 constexpr unsigned long long OS_VALUE_MASK = (1ull << OS_KIND_SHIFT) - 1ull;
 constexpr uint32_t OS_SPIN_LIMIT = 1u << 22;  // bounded wait, then error flag
+constexpr uint32_t OS_SPIN_LIMIT_TEST = 4096u;  // the stall test's limit (~1 ms)
 
 __device__ __forceinline__ unsigned long long os_word(uint32_t epoch, uint32_t kind,
                                                       unsigned long long v) {
@@ -88,7 +89,7 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n, int shift,
     int nbits, const uint32_t *__restrict__ offsets, int nblocks,
     const unsigned long long *__restrict__ digit_base, unsigned long long *state,
-    uint32_t *tile_ctr, uint32_t *err, uint32_t epoch) {
+    uint32_t *tile_ctr, uint32_t *err, uint32_t epoch, uint32_t spin_limit) {
   __shared__ uint32_t whist[RS_WARPS][RS_BINS];
   __shared__ uint32_t boff[RS_BINS];
   __shared__ uint32_t lstart[RS_BINS];
@@ -163,7 +164,10 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
               reinterpret_cast<volatile unsigned long long *>(state)[(size_t)t * RS_BINS + d];
           const uint32_t kind = (uint32_t)(v >> OS_KIND_SHIFT) & 3u;
           if ((uint32_t)(v >> OS_EPOCH_SHIFT) != epoch || kind == 0u) {
-            if (++spins > OS_SPIN_LIMIT) {  // give up: results invalid, host reports it
+            // give up: this tile's offsets come from a partial prefix (never
+            // above the true one, so its writes stay inside [0, n)); the
+            // results are invalid and the host reports it
+            if (++spins > spin_limit) {
               atomicOr(err, 2u);
               break;
             }
@@ -202,6 +206,8 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     vals_out[dst] = sval[i];
   }
 }
+
+__global__ void k_set_u32(uint32_t *p, uint32_t v) { *p = v; }
 
 // All digit histograms of the onesweep passes in one read of the keys.
 constexpr int OS_MAX_PASS = 4;
@@ -382,7 +388,7 @@ size_t radix_scratch_bytes(int64_t n) {
 int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_tmp,
                      uint32_t *vals_tmp, uint32_t *keys_out, uint32_t *vals_out, int64_t n,
                      int bit0, int bit1, bool keys_needed, void *scratch, cudaStream_t s,
-                     int *launches, uint32_t *err, bool onesweep) {
+                     int *launches, uint32_t *err, bool onesweep, bool stall_test) {
   if (n <= 0) return 0;
   const int nblocks = (int)((n + RS_TILE - 1) / RS_TILE);
   const int64_t m = (int64_t)nblocks * RS_BINS;
@@ -418,16 +424,22 @@ int radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t 
     uint32_t *vo = to_out ? vals_out : vals_tmp;
     uint32_t *kout = (last && !keys_needed) ? nullptr : ko;
     if (onesweep) {
-      k_rs_downsweep<true><<<nblocks, RS_THREADS, 0, s>>>(
+      // the stall test: the pass's tile counter starts at 1, so tiles
+      // 1..nblocks-1 run (one block each) and tile 0 never publishes
+      const bool stall = stall_test && pass == 0 && nblocks >= 2;
+      if (stall) k_set_u32<<<1, 1, 0, s>>>(tile_ctr + pass, 1u);
+      k_rs_downsweep<true><<<stall ? nblocks - 1 : nblocks, RS_THREADS, 0, s>>>(
           kin, vin, kout, vo, n, b, nbits, nullptr, nblocks, hist + pass * RS_BINS, state,
-          tile_ctr + pass, err, (uint32_t)(pass + 1));
-      if (launches) *launches += 1;
+          tile_ctr + pass, err, (uint32_t)(pass + 1),
+          stall_test ? OS_SPIN_LIMIT_TEST : OS_SPIN_LIMIT);
+      if (launches) *launches += stall ? 2 : 1;
     } else {
       k_rs_upsweep<<<nblocks, RS_THREADS, 0, s>>>(kin, n, b, nbits, counts, nblocks);
       exclusive_scan<uint32_t>(LoadU32{counts}, m, offsets, (uint32_t *)nullptr, sc, s,
                                launches);
       k_rs_downsweep<false><<<nblocks, RS_THREADS, 0, s>>>(
-          kin, vin, kout, vo, n, b, nbits, offsets, nblocks, nullptr, nullptr, nullptr, nullptr, 0);
+          kin, vin, kout, vo, n, b, nbits, offsets, nblocks, nullptr, nullptr, nullptr, nullptr, 0,
+          0u);
       if (launches) *launches += 2;
     }
     kin = ko;

@@ -53,8 +53,16 @@ def test_roofline_arithmetic():
     pk = {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0, "source": "measured"}
     top, st = bench.roofline(stages, n=50_000_000, n_act=7_800_000, n_entries=37_000_000,
                              n_tiles=8160, frags=3_770_000_000, args=SimpleNamespace(),
-                             pk=pk, a_eq_e=False)
+                             pk=pk, a_eq_e=False, n_sm=152)
     assert top["stage"] == "splat" and top["kernel"] == "k_splat"
+    # the FP32 rate follows the SM count it is given; the splat's traffic is the
+    # committed capture's bytes scaled by the fragment count
+    assert top["peak"] == pytest.approx(2 * 128 * 152 * 2070e6 / 1e12)
+    assert top["traffic"] == pytest.approx(bench.SPLAT_CAPTURE["dram_bytes"] * 3_770_000_000 /
+                                           bench.SPLAT_CAPTURE["fragments"])
+    top148, _ = bench.roofline(stages, 50_000_000, 7_800_000, 37_000_000, 8160, 3_770_000_000,
+                               SimpleNamespace(), pk, False, n_sm=148)
+    assert top148["peak"] == pytest.approx(top["peak"] * 148 / 152)
     for v in st.values():
         assert v["frac"] == pytest.approx(v["achieved"] / v["peak"])
     assert st["project"]["achieved"] == pytest.approx(
@@ -63,5 +71,5 @@ def test_roofline_arithmetic():
     assert st["project"]["peak"] == 6800.0
     # additive frames have no depth sort stage in the roofline
     _, st_add = bench.roofline(dict(stages, sort_ms=0.0), 1_000_000, 900_000, 5_000_000,
-                               2500, 60_000_000, SimpleNamespace(), pk, True)
+                               2500, 60_000_000, SimpleNamespace(), pk, True, 152)
     assert "sort" not in st_add and st_add["splat"]["ops_per_fragment"] == 7

@@ -155,3 +155,37 @@ def test_batch_eager_equals_graph(renderer):
     finally:
         ga.close()
         ea.close()
+
+
+def test_autotuner_cache(renderer):
+    """A second batch of the same shape (per frame: resolution, mode class and
+    the size bucket of its set) takes the tuned choice from the cache and times
+    nothing; another shape is tuned afresh; tune_cache=0 always searches."""
+    bw = synth.batched(n_sets=2, poses=2, scale=0.003, resolutions=((88, 72), (120, 96)))
+    sets = _device_sets(bw)
+    made = []
+    try:
+        b0, f0, _ = _batch(renderer, bw, sets, tune_cache=False)
+        made.append(b0)
+        i0 = b0.info()
+        assert i0["tune_cached"] == 0 and i0["tune_ms"] > 0
+        b1, _, _ = _batch(renderer, bw, sets)  # searches (or hits) and fills the cache
+        made.append(b1)
+        b2, f2, _ = _batch(renderer, bw, sets)
+        made.append(b2)
+        i1, i2 = b1.info(), b2.info()
+        assert i2["tune_cached"] == 1 and i2["tune_ms"] == 0.0 and i2["plan_ms"] > 0
+        for k in ("tile_size", "splat_config_additive", "splat_config_absorption"):
+            assert i2[k] == i1[k], k
+        b2.render()
+        torch.cuda.synchronize()
+        _check_equal_plain(renderer, sets, f2, b2.info())
+        # another shape: one frame at another resolution
+        s, params, rc = bw.frames[0]
+        params.params["xres"] = "104"
+        b3, _, _ = _batch(renderer, bw, sets)
+        made.append(b3)
+        assert b3.info()["tune_cached"] == 0
+    finally:
+        for b in made:
+            b.close()

@@ -1,0 +1,160 @@
+"""Parity on the workloads the benchmark times, at the sizes it times them.
+
+* The plain ordered emission-absorption frame -- 40M gas + 10M star
+  particles, 1920x1080, tile 16 -- in both compositing orders (front-to-back,
+  which the benchmark times, and back-to-front, the recurrence of
+  splotch/splotch_host.cc:663-665 in list order).  Projected particles, the
+  visiting order (about 7.8M active particles through the onesweep look-back
+  over ~1,900 scatter blocks), tile ranges, the ~37M bin entries and the
+  fragment count must be bit-exact with the oracle; the image must lie within
+  1e-4 per-pixel relative L-inf of the FP64 oracle.  The reference's own FP32
+  arithmetic (the scalar render_new branch an AArch64 host compiles) is
+  measured against the same FP64 image and printed beside ours.
+* A frame shaped like the large render: ordered absorption, per-particle RGB,
+  hsml ~ Pareto(1.5, 0.1) clipped at a quarter of the image width, at 8M
+  particles and 2048^2.  Particles covering more than 64 tiles take the
+  many-tile emission path; the test asserts that some do.  Forward image
+  against FP64; gradients against FP64 central finite differences on 256
+  particles and against the FP64 adjoint of every active particle.
+* The batched workload at 5% of its particle counts with its real
+  resolutions (512^2, 1024^2, 1920x1080, 2048^2), additive and ordered sets,
+  autotuned: every frame bit-equal to its per-frame render and within 1e-4 of
+  the FP64 oracle.
+"""
+import numpy as np
+import pytest
+
+import splotch_gb300 as sg
+from oracle.oracle import rel_linf
+from splotch_gb300 import synth
+
+from .helpers import IMAGE_TOL, assert_parity, gpu_frame, oracle_frame
+from .test_gpu_grad import FIELDS, GRAD_TOL, _frame, _gpu_matrix, check_field, describe
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def absorption_50m(port):
+    """The benchmark frame and its oracle results (shared by both orders)."""
+    w = synth.plain_absorption(order="ftb")
+    prm = dict(w.params.params)
+    o = oracle_frame(port, prm, w.rc, w.particles, fp32=True)
+    return w, o
+
+
+@pytest.mark.parametrize("order", ["ftb", "btf"])
+def test_benchmark_frame_50m(order, absorption_50m, renderer):
+    w, o = absorption_50m
+    prm = dict(w.params.params)
+    prm["gpu_order"] = order
+    assert len(w.particles) == 50_000_000 and prm["tile_size_cpu"] == "16"
+    g = gpu_frame(renderer, prm, w.rc, w.particles)
+    info = assert_parity(g, o, IMAGE_TOL)
+    assert g.stats["n_active"] > 7_000_000 and g.stats["n_entries"] > 30_000_000
+    # the reference's FP32 error is measured, not bounded: its first-order
+    # expm1 below taylorlimit puts it near 3e-3 on absorption frames
+    print(f"50M {order}: GPU rel Linf {info['gpu_err']:.3e}, reference FP32 arithmetic "
+          f"{info['ref_fp32_err']:.3e}, {info['frags']} fragments, "
+          f"{g.stats['n_entries']} bin entries")
+
+
+def _large_target(p: np.ndarray, seed: int) -> np.ndarray:
+    """The loss target: intensities scaled by lognormal(0, 0.2) noise and
+    positions moved by N(0, 0.1 hsml)."""
+    rng = np.random.default_rng(seed)
+    t = p.copy()
+    t["I"] = (p["I"] * rng.lognormal(0.0, 0.2, len(p))).astype(np.float32)
+    for ax in ("x", "y", "z"):
+        t[ax] = (p[ax] + rng.standard_normal(len(p)) * 0.1 * p["r"]).astype(np.float32)
+    return t
+
+
+def test_large_render_shape_8m(renderer, port):
+    w = synth.large(n=8_000_000, xres=2048, tile=16, order="ftb")
+    prm = dict(w.params.params)
+    # forward: bins, order and image against the oracle
+    g = gpu_frame(renderer, prm, w.rc, w.particles)
+    o = oracle_frame(port, prm, w.rc, w.particles, fp32=False)
+    info = assert_parity(g, o, IMAGE_TOL)
+    assert g.stats["n_wide"] > 0, "no particle took the many-tile emission path"
+    big = (0.75 * o.projected["r"][o.projected["active"].astype(bool)] > 56.5).sum()
+    print(f"large-shape 8M 2048^2: rel Linf {info['gpu_err']:.3e}, {g.stats['n_wide']} "
+          f"many-tile particles, {big} covering over 10^4 pixels")
+    assert big > 0
+    # gradients of L = sum((pic - target)^2)
+    target_p = _large_target(w.particles, 4)
+    _, target, gpic, grads = _frame(renderer, w, target_p)
+    raw = w.particles.copy()
+    cov = raw.copy()
+    port.project_colorize(prm, w.rc, cov)
+    order = port.sort_perm(cov, 1)
+    g32 = _gpu_matrix(grads, len(raw))
+    act = np.nonzero(cov["active"])[0]
+    g64, _ = port.grad_fp64(prm, w.rc, raw, cov, order, gpic.astype(np.float64))
+    bad = []
+    for j, f in enumerate(FIELDS):
+        print("large-shape", f, "vs FP64 adjoint:", describe(g32[act, j], g64[act, j]))
+        bad += check_field(g32[act, j], g64[act, j], f)
+    sel = np.sort(np.random.default_rng(4).choice(act, size=256, replace=False))
+    fd, excluded = port.fd_particles(prm, w.rc, raw, cov, order, target, sel, h=1e-4)
+    for j, f in enumerate(FIELDS):
+        keep = ~excluded[:, j]
+        print("large-shape", f, "vs FD:", describe(g32[sel][keep, j], fd[keep, j]))
+        bad += check_field(g32[sel][keep, j], fd[keep, j], f + " (FD)")
+    assert not bad, bad
+    fdc = port.fd_campos(prm, w.rc, raw, cov, order, target, h=1e-4)
+    ec = np.abs(grads["campos"] - fdc).max() / np.abs(fdc).max()
+    print("large-shape campos", grads["campos"], fdc, ec)
+    assert ec <= GRAD_TOL
+
+
+def test_batch_real_resolutions(renderer, port):
+    torch = pytest.importorskip("torch")
+    bw = synth.batched(n_sets=2, poses=4, scale=0.05)
+    # every resolution of the batched workload, in each class
+    for i, (_, params, _) in enumerate(bw.frames):
+        xres, yres = synth.BATCH_RESOLUTIONS[i % 4]
+        params.params["xres"], params.params["yres"] = str(xres), str(yres)
+    sets = [{k: torch.from_numpy(v).cuda() for k, v in synth.soa_from_aos(p).items()}
+            for p in bw.sets]
+    keep: list = []
+    frames = []
+    for s, params, rc in bw.frames:
+        desc = sg.frame_desc(params, rc, keep)
+        frames.append((s, desc, torch.full((desc.xres, desc.yres, 3), float("nan"),
+                                           dtype=torch.float32, device="cuda")))
+    torch.cuda.synchronize()
+    b = sg.Batch(renderer, sets, frames)
+    try:
+        b.render()
+        torch.cuda.synchronize()
+        info = b.info()
+        T = info["tile_size"]
+        errs = []
+        for k, (s, desc, pic) in enumerate(frames):
+            got = pic.cpu().numpy()
+            cfg = (info["splat_config_additive"] if desc.a_eq_e
+                   else info["splat_config_absorption"])
+            d = type(desc).from_buffer_copy(desc)
+            d.tile_size, d.splat_config = T, cfg
+            want = torch.zeros_like(pic)
+            renderer.render_soa(d, sets[s], want, device=True)
+            torch.cuda.synchronize()
+            assert np.array_equal(got, want.cpu().numpy()), f"frame {k} differs from spl_render"
+            _, params, rc = bw.frames[k]
+            prm = dict(params.params)
+            prm["tile_size_cpu"] = str(T)
+            p = bw.sets[s].copy()
+            port.project_colorize(prm, rc, p)
+            add = bool(desc.a_eq_e)
+            order = None if add else port.sort_perm(p, 1)
+            pic64, _ = port.render_fp64(p, order, desc.xres, desc.yres, T, add, 0.2)
+            err = rel_linf(got, pic64)
+            errs.append((desc.xres, desc.yres, add, len(bw.sets[s]), err))
+            assert err <= IMAGE_TOL, errs[-1]
+        print("batch at 5% scale, tile", T, errs)
+        assert {(x, y) for x, y, *_ in errs} == set(synth.BATCH_RESOLUTIONS)
+        assert {a for _, _, a, *_ in errs} == {True, False}
+    finally:
+        b.close()

@@ -247,3 +247,21 @@ def test_full_size_additive_1M(renderer, port):
     o = oracle_frame(port, prm, w.rc, w.particles, fp32=False)
     info = assert_parity(g, o)
     print("full additive", info, g.stats)
+
+
+@pytest.mark.parametrize("order", ["btf", "ftb"])
+@pytest.mark.parametrize("sort_type", [0, 2, 3, 4])
+def test_sort_types(sort_type, order, renderer, port):
+    """Every sort_type of particle_sort (splotch/splotch_host.cc:289-321,
+    comparators splotch/splotchutils.h:74-96) on an ordered frame: 0 keeps
+    particle order, 2/3 sort by the colourised red channel descending /
+    ascending, 4 by pixel radius descending; the stable permutation must equal
+    the oracle's bit for bit (ties keep particle order)."""
+    w = _absorption(n_gas=40000, n_star=10000, xres=192, yres=108, tile=16, order=order)
+    prm = dict(w.params.params)
+    prm["sort_type"] = str(sort_type)
+    g = gpu_frame(renderer, prm, w.rc, w.particles)
+    o = oracle_frame(port, prm, w.rc, w.particles, fp32=False)
+    assert_parity(g, o)
+    if sort_type:
+        assert not np.array_equal(g.order, np.sort(g.order)), "the sort left particle order"
