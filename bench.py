@@ -22,9 +22,10 @@ cpu_baseline: the CPU restatement of the reference (bit-exact with it) timed
         measures the timed frame's image against the FP64 oracle
         (image_rel_linf) and the reference's own FP32 arithmetic beside it.
 drop_in_default: the frame through host_rendering() with the drop-in's
-        defaults (back-to-front compositing, every particle projected,
+        defaults (front-to-back compositing, every particle projected,
         colourised and sorted back into the caller's array), from pageable
-        host memory, as a Splotch caller would make the call.
+        host memory, as a Splotch caller would make the call; and the same
+        with back-to-front compositing.
 large : the large render (400M particles, 4096^2, forward and
         forward+backward), batched / fwd_bwd / rays: the other workloads.
 
@@ -667,44 +668,52 @@ def batched(args, local: int) -> dict:
 def drop_in_default(args, w, local: int) -> dict:
     """The frame through host_rendering() with the drop-in's defaults, the way
     a Splotch caller makes the call (splotch/splotch.cc:261): particle_sim
-    records in pageable host memory, back-to-front compositing, and the
+    records in pageable host memory, the default compositing order, and the
     reference's side effects -- every particle projected, colourised and
     stably depth-sorted back into the caller's array -- plus the image.  Wall
-    time per call, copies included; the median of the timed calls."""
+    time per call, copies included; the median of the timed calls.  The
+    back-to-front order (gpu_order=btf) is timed the same way beside it."""
     import copy
 
     import torch
 
     import splotch_gb300 as sg
 
-    prm = dict(w.params.params)
-    prm.pop("gpu_order", None)  # the drop-in's default order: back-to-front
-    r = sg.Renderer(local)
     n = len(w.particles)
-    ts, stages = [], None
-    for i in range(1 + max(1, args.drop_in_steps)):
-        pf = sg.ParamFile(dict(prm))
-        rc = copy.copy(w.rc)
-        rc.pic = None
-        parts = w.particles.copy()  # the caller's vector (mutated in place)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        sg.host_rendering(pf, parts, rc, renderer=r)
-        dt = time.perf_counter() - t0
-        if i:
-            ts.append(dt)
-            stages = r.stats()
+    r = sg.Renderer(local)
+
+    def calls(prm: dict) -> dict:
+        ts, stages = [], None
+        for i in range(1 + max(1, args.drop_in_steps)):
+            pf = sg.ParamFile(dict(prm))
+            rc = copy.copy(w.rc)
+            rc.pic = None
+            parts = w.particles.copy()  # the caller's vector (mutated in place)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            sg.host_rendering(pf, parts, rc, renderer=r)
+            dt = time.perf_counter() - t0
+            if i:
+                ts.append(dt)
+                stages = r.stats()
+        t = statistics.median(ts)
+        return {"ms": t * 1e3, "mparticles_per_s": n / t / 1e6, "frames_per_s": 1.0 / t,
+                "calls_ms": [round(x * 1e3, 2) for x in ts],
+                "stages_ms": {k: round(float(stages[k]), 3) for k in
+                              ("h2d_ms", "project_ms", "sort_ms", "bin_ms", "splat_ms",
+                               "d2h_ms", "total_ms")}}
+
+    prm = dict(w.params.params)
+    prm.pop("gpu_order", None)  # the drop-in's default order (front-to-back)
+    out = calls(prm)
+    out.update({"order": "ftb (default)",
+                "writeback": "full (projected, colourised, sorted particle_sim array copied "
+                             "back)",
+                "input": "pageable host particle_sim records", "h2d_bytes": n * 36,
+                "d2h_bytes": n * 36 + int(prm["xres"]) * int(prm["yres"]) * 12})
+    out["back_to_front"] = calls(dict(prm, gpu_order="btf"))
     r.close()
-    t = statistics.median(ts)
-    return {"ms": t * 1e3, "mparticles_per_s": n / t / 1e6, "frames_per_s": 1.0 / t,
-            "order": "btf", "writeback": "full (projected, colourised, sorted particle_sim "
-                                          "array copied back)",
-            "input": "pageable host particle_sim records",
-            "h2d_bytes": n * 36, "d2h_bytes": n * 36 + int(prm["xres"]) * int(prm["yres"]) * 12,
-            "calls_ms": [round(x * 1e3, 2) for x in ts],
-            "stages_ms": {k: round(float(stages[k]), 3) for k in
-                          ("h2d_ms", "project_ms", "sort_ms", "bin_ms", "splat_ms", "d2h_ms",
-                           "total_ms")}}
+    return out
 
 
 def run_gpu(args):

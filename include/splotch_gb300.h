@@ -47,8 +47,11 @@ enum { SPL_LAYOUT_AOS = 0, SPL_LAYOUT_SOA = 1 };
 enum { SPL_WRITEBACK_NONE = 0, SPL_WRITEBACK_FULL = 1 };
 /* Compositing order for the ordered (a_eq_e=false) splat.  BACK_TO_FRONT
    applies particles in list order exactly like render_new; FRONT_TO_BACK
-   evaluates the same sum in reverse with early exit once every channel's
-   transmittance is below spl_frame_desc.ftb_epsilon. */
+   (the default) evaluates the same sum, term for term, in reverse and stops
+   once every channel's transmittance is below spl_frame_desc.ftb_epsilon
+   (1e-9: what lies behind then adds less than 1e-9 of its colour).  Both are
+   within 1e-4 of the FP64 oracle; front-to-back skips the opaque depths of
+   dense tiles, which back-to-front must walk in full. */
 enum { SPL_ORDER_BACK_TO_FRONT = 0, SPL_ORDER_FRONT_TO_BACK = 1 };
 
 typedef struct spl_context spl_context;
@@ -83,7 +86,7 @@ typedef struct {
   int tile_size;            /* "tile_size_cpu" (50); 1..64 on the GPU */
   double campos[3], lookat[3], sky[3], centerpos[3]; /* render_context */
   /* GPU-only knobs (no reference counterpart) */
-  int order_mode;           /* SPL_ORDER_* (default BACK_TO_FRONT) */
+  int order_mode;           /* SPL_ORDER_* (default FRONT_TO_BACK) */
   float ftb_epsilon;        /* transmittance cut for FRONT_TO_BACK (1e-9) */
   int splat_config;         /* splat launch configuration, -1 = default for the
                                tile size (see spl_splat_config_valid) */

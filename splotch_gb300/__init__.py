@@ -236,7 +236,7 @@ def frame_desc(params: ParamFile, rc: RenderContext, keep: list | None = None) -
     d.tile_size = int(params.find("tile_size_cpu", 50.0))  # read as float32, then int
     if params.param_present("gpu_order"):
         d.order_mode = (_abi.SPL_ORDER_FRONT_TO_BACK
-                        if params.find("gpu_order", "btf", typ=str) == "ftb"
+                        if params.find("gpu_order", "ftb", typ=str) == "ftb"
                         else _abi.SPL_ORDER_BACK_TO_FRONT)
     if params.param_present("gpu_ftb_epsilon"):
         d.ftb_epsilon = params.find("gpu_ftb_epsilon", 1e-9)

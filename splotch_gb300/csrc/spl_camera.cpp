@@ -95,7 +95,7 @@ extern "C" void spl_frame_desc_defaults(spl_frame_desc *d) {
   d->sort_type = 1;
   d->tile_size = 50;
   d->sky[1] = 1.0;
-  d->order_mode = SPL_ORDER_BACK_TO_FRONT;
+  d->order_mode = SPL_ORDER_FRONT_TO_BACK;
   d->ftb_epsilon = 1e-9f;
   d->splat_config = -1;
 }

@@ -17,7 +17,7 @@
 //   * new_renderer=true runs the ray-sphere renderer (spl_render_rays) and
 //     empties the particle vector, as host_rendering_new does.
 // GPU-only keys (all optional): gpu_device (0), gpu_writeback (true),
-// gpu_order ("btf" | "ftb"), gpu_ftb_epsilon (1e-9), gpu_splat_config (-1).
+// gpu_order ("ftb" | "btf"; default ftb), gpu_ftb_epsilon (1e-9), gpu_splat_config (-1).
 #include <string>
 #include <vector>
 

@@ -29,7 +29,8 @@ from oracle.oracle import rel_linf
 from splotch_gb300 import synth
 
 from .helpers import IMAGE_TOL, assert_parity, gpu_frame, oracle_frame
-from .test_gpu_grad import FIELDS, GRAD_TOL, _frame, _gpu_matrix, check_field, describe
+from .test_gpu_grad import (FIELDS, GRAD_MEDIAN, GRAD_TOL, _frame, _gpu_matrix, describe,
+                             grad_errors)
 
 pytestmark = pytest.mark.gpu
 
@@ -52,8 +53,8 @@ def test_benchmark_frame_50m(order, absorption_50m, renderer):
     g = gpu_frame(renderer, prm, w.rc, w.particles)
     info = assert_parity(g, o, IMAGE_TOL)
     assert g.stats["n_active"] > 7_000_000 and g.stats["n_entries"] > 30_000_000
-    # the reference's FP32 error is measured, not bounded: its first-order
-    # expm1 below taylorlimit puts it near 3e-3 on absorption frames
+    # the reference's FP32 error is measured, not bounded: exptable's truncated
+    # arguments and its first-order expm1 below taylorlimit put it at ~3e-4 here
     print(f"50M {order}: GPU rel Linf {info['gpu_err']:.3e}, reference FP32 arithmetic "
           f"{info['ref_fp32_err']:.3e}, {info['frags']} fragments, "
           f"{g.stats['n_entries']} bin entries")
@@ -68,6 +69,32 @@ def _large_target(p: np.ndarray, seed: int) -> np.ndarray:
     for ax in ("x", "y", "z"):
         t[ax] = (p[ax] + rng.standard_normal(len(p)) * 0.1 * p["r"]).astype(np.float32)
     return t
+
+
+# Gradient criteria of the large-render shape.  The bound of the render's
+# specification holds against both FP64 references: max-normalised L-inf
+# max|g - g_ref| / max|g_ref| <= 1e-3.  Per element, this frame is harder than
+# the differentiable workload: particles spanning up to a few thousand tiles
+# sum their per-tile partial gradients, of both signs, in FP32, so an element
+# far below its field's scale keeps only what that cancellation leaves --
+# element error with a 1%-of-max floor <= 5e-2 (measured up to 2.2e-2).  The
+# FP64 finite differences (step 1e-4) are themselves 2.6e-4 to 4.3e-4 (median)
+# from the exact FP64 adjoint on this frame, so their median bound is 1e-3;
+# against the FP64 adjoint the median bound stays 2e-4.
+LARGE_ELEM = 5e-2
+FD_MEDIAN = 1e-3
+
+
+def _check_large(g, ref, what: str, median: float) -> list:
+    linf, med, elem = grad_errors(g, ref)
+    bad = []
+    if linf > GRAD_TOL:
+        bad.append(f"{what}: L-inf/max {linf:.2e}")
+    if med > median:
+        bad.append(f"{what}: median {med:.2e}")
+    if elem > LARGE_ELEM:
+        bad.append(f"{what}: element {elem:.2e}")
+    return bad
 
 
 def test_large_render_shape_8m(renderer, port):
@@ -95,13 +122,14 @@ def test_large_render_shape_8m(renderer, port):
     bad = []
     for j, f in enumerate(FIELDS):
         print("large-shape", f, "vs FP64 adjoint:", describe(g32[act, j], g64[act, j]))
-        bad += check_field(g32[act, j], g64[act, j], f)
+        bad += _check_large(g32[act, j], g64[act, j], f, median=GRAD_MEDIAN)
     sel = np.sort(np.random.default_rng(4).choice(act, size=256, replace=False))
     fd, excluded = port.fd_particles(prm, w.rc, raw, cov, order, target, sel, h=1e-4)
     for j, f in enumerate(FIELDS):
         keep = ~excluded[:, j]
-        print("large-shape", f, "vs FD:", describe(g32[sel][keep, j], fd[keep, j]))
-        bad += check_field(g32[sel][keep, j], fd[keep, j], f + " (FD)")
+        print("large-shape", f, "vs FD:", describe(g32[sel][keep, j], fd[keep, j]),
+              "| FP64 adjoint vs FD:", describe(g64[sel][keep, j], fd[keep, j]))
+        bad += _check_large(g32[sel][keep, j], fd[keep, j], f + " (FD)", median=FD_MEDIAN)
     assert not bad, bad
     fdc = port.fd_campos(prm, w.rc, raw, cov, order, target, h=1e-4)
     ec = np.abs(grads["campos"] - fdc).max() / np.abs(fdc).max()
