@@ -942,13 +942,37 @@ void spo_model_vjp(const spo_model *m, const spo_model_in *p, const double gin[6
   gout[7] = gh;
 }
 
+/* The model is anchored at the render's own values.  The render projects in
+   double and stores float (splotch_host.cc:134), so its X, Y, R, E sit up to
+   half a float ulp (1.2e-4 px at X ~ 2048) from the smooth model's; for a
+   particle whose Gaussian is under a pixel wide that moves weights and their
+   derivatives by ~1e-3.  Per particle, a constant off = float value - model
+   value at the base camera carries the model onto the render's values there;
+   derivatives are the smooth model's (the float rounding's own derivative is
+   zero almost everywhere), and the splat -- adjoint and finite differences
+   alike -- is evaluated where the render evaluated it. */
+static void model_offsets(const spo_model *m0, const spo_particle *raw, const spo_particle *cov,
+                          int64_t n, double *off) {
+#pragma omp parallel for schedule(static) num_threads(spo_get_threads())
+  for (int64_t i = 0; i < n; ++i) {
+    double *o = off + 6 * i;
+    if (!cov[i].active) { memset(o, 0, 6 * sizeof(double)); continue; }
+    const spo_model_in q = model_in_of(&raw[i]);
+    double wd[6];
+    spo_model_project(m0, &q, wd);
+    const double f[6] = {cov[i].x, cov[i].y, cov[i].r, cov[i].er, cov[i].eg, cov[i].eb};
+    for (int j = 0; j < 6; ++j) o[j] = f[j] - wd[j];
+  }
+}
+
 static void model_all(const spo_model *m, const spo_particle *raw, const spo_particle *cov,
-                      int64_t n, double *w) {
+                      int64_t n, const double *off, double *w) {
 #pragma omp parallel for schedule(static) num_threads(spo_get_threads())
   for (int64_t i = 0; i < n; ++i) {
     if (cov[i].active) {
       const spo_model_in q = model_in_of(&raw[i]);
       spo_model_project(m, &q, w + 6 * i);
+      for (int j = 0; j < 6; ++j) w[6 * i + j] += off[6 * i + j];
     } else {
       memset(w + 6 * i, 0, 6 * sizeof(double));
     }
@@ -1112,8 +1136,11 @@ int spo_grad_fp64(const spo_params *prm, const spo_particle *raw, const spo_part
   if (spo_model_setup(prm, &m)) return -1;
   double *w = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
   double *gw = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
-  if (!w || !gw) { free(w); free(gw); return -2; }
-  model_all(&m, raw, cov, n, w);
+  double *off = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  if (!w || !gw || !off) { free(w); free(gw); free(off); return -2; }
+  model_offsets(&m, raw, cov, n, off);
+  model_all(&m, raw, cov, n, off, w);
+  free(off);
   int rc = spo_render_frozen_vjp_fp64(cov, w, order, n, prm->xres, prm->yres, T, prm->a_eq_e,
                                       (double)prm->gray_absorption, gpic, gw);
   gcampos[0] = gcampos[1] = gcampos[2] = 0.0;
@@ -1143,8 +1170,10 @@ int spo_fd_particles(const spo_params *prm, const spo_particle *raw, const spo_p
   const int xres = prm->xres, yres = prm->yres, a_eq_e = prm->a_eq_e;
   const double gray = prm->gray_absorption;
   double *w = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
-  if (!w) return -2;
-  model_all(&m, raw, cov, n, w);
+  double *off = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  if (!w || !off) { free(w); free(off); return -2; }
+  model_offsets(&m, raw, cov, n, off);
+  model_all(&m, raw, cov, n, off, w);
   bins b;
   if (make_bins(cov, order, n, xres, yres, T, &b)) { free(w); return -1; }
   const double h2s = h2sigma_f();
@@ -1223,6 +1252,7 @@ int spo_fd_particles(const spo_params *prm, const spo_particle *raw, const spo_p
         double wq[6];
         model_fwd st;
         model_eval(&m, &q, &st, wq);
+        for (int jj = 0; jj < 6; ++jj) wq[jj] += off[6 * (size_t)i + jj];
         segs[sg] = st.seg;
         double acc = 0.0;
         for (int64_t k = 0; k < np; ++k) {
@@ -1245,6 +1275,7 @@ int spo_fd_particles(const spo_params *prm, const spo_particle *raw, const spo_p
   }
   free_bins(&b);
   free(w);
+  free(off);
   return err ? -3 : 0;
 }
 
@@ -1255,16 +1286,22 @@ int spo_fd_campos(const spo_params *prm, const spo_particle *raw, const spo_part
                   double fd[3]) {
   const size_t npix = (size_t)prm->xres * prm->yres * 3;
   double *w = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
+  double *off = (double *)malloc((size_t)(n > 0 ? n : 1) * 6 * sizeof(double));
   double *pp = (double *)malloc(npix * sizeof(double));
   double *pm = (double *)malloc(npix * sizeof(double));
-  if (!w || !pp || !pm) { free(w); free(pp); free(pm); return -2; }
+  if (!w || !off || !pp || !pm) { free(w); free(off); free(pp); free(pm); return -2; }
   int rc = 0;
+  {
+    spo_model m0;
+    if (spo_model_setup(prm, &m0)) rc = -1;
+    else model_offsets(&m0, raw, cov, n, off);  /* anchored at the base camera */
+  }
   for (int k = 0; k < 3 && rc == 0; ++k) {
     for (int sg = 0; sg < 2 && rc == 0; ++sg) {
       spo_model m;
       if (spo_model_setup(prm, &m)) { rc = -1; break; }
       m.campos[k] += sg ? -h : h;
-      model_all(&m, raw, cov, n, w);
+      model_all(&m, raw, cov, n, off, w);
       if (spo_render_frozen_fp64(cov, w, order, n, prm->xres, prm->yres, T, prm->a_eq_e,
                                  (double)prm->gray_absorption, sg ? pm : pp) < 0)
         rc = -1;
@@ -1274,16 +1311,20 @@ int spo_fd_campos(const spo_params *prm, const spo_particle *raw, const spo_part
       acc += (pp[j] - pm[j]) * (pp[j] + pm[j] - 2.0 * (double)target[j]);
     fd[k] = acc / (2.0 * h);
   }
-  free(w); free(pp); free(pm);
+  free(w); free(off); free(pp); free(pm);
   return rc;
 }
 
-/* The model's X, Y, R, E for every active particle (zeros elsewhere). */
+/* The smooth model's X, Y, R, E for every active particle (zeros elsewhere),
+   without the anchoring offsets. */
 int spo_model_project_all(const spo_params *prm, const spo_particle *raw,
                           const spo_particle *cov, int64_t n, double *w) {
   spo_model m;
   if (spo_model_setup(prm, &m)) return -1;
-  model_all(&m, raw, cov, n, w);
+  double *zero = (double *)calloc((size_t)(n > 0 ? n : 1) * 6, sizeof(double));
+  if (!zero) return -2;
+  model_all(&m, raw, cov, n, zero, w);
+  free(zero);
   return 0;
 }
 

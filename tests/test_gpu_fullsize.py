@@ -73,16 +73,16 @@ def _large_target(p: np.ndarray, seed: int) -> np.ndarray:
 
 # Gradient criteria of the large-render shape.  The bound of the render's
 # specification holds against both FP64 references: max-normalised L-inf
-# max|g - g_ref| / max|g_ref| <= 1e-3.  Per element, this frame is harder than
-# the differentiable workload: particles spanning up to a few thousand tiles
-# sum their per-tile partial gradients, of both signs, in FP32, so an element
-# far below its field's scale keeps only what that cancellation leaves --
-# element error with a 1%-of-max floor <= 5e-2 (measured up to 2.2e-2).  The
-# FP64 finite differences (step 1e-4) are themselves 2.6e-4 to 4.3e-4 (median)
-# from the exact FP64 adjoint on this frame, so their median bound is 1e-3;
-# against the FP64 adjoint the median bound stays 2e-4.
+# max|g - g_ref| / max|g_ref| <= 1e-3, and the median element error stays
+# <= 2e-4.  Per element, this frame is harder than the differentiable
+# workload: particles spanning up to a few thousand tiles sum their per-tile
+# partial gradients, of both signs, in FP32, so an element far below its
+# field's scale keeps only what that cancellation leaves -- element error with
+# a 1%-of-max floor <= 5e-2.  (The two FP64 references agree with each other
+# to ~1e-8 in the median once the model is anchored at the render's float
+# values.)
 LARGE_ELEM = 5e-2
-FD_MEDIAN = 1e-3
+FD_MEDIAN = 2e-4
 
 
 def _check_large(g, ref, what: str, median: float) -> list:

@@ -1,7 +1,8 @@
 """The oracle's FP64 adjoint (model chain rule + exact reverse-mode splat)
 against FP64 central finite differences of the same frozen-coverage model, on
 small frames in both modes and both projections.  This pins the checker that
-the GPU gradients are compared with."""
+the GPU gradients are compared with.  The model is anchored at the render's
+float-rounded projected values, so the loss is formed there too."""
 import numpy as np
 import pytest
 
@@ -21,8 +22,10 @@ def _case(port, mode, projection, n=4000, xres=96, yres=64):
     torder = None if mode == "additive" else port.sort_perm(tp, 1)
     target, _ = port.render_fp64(tp, torder, xres, yres, 16, mode == "additive", 0.2)
     target = target.astype(np.float32)
-    W = port.model_project(prm, w.rc, raw, cov)
-    pic = port.render_frozen_fp64(prm, cov, W, order)
+    # the loss at the render's own values (the model is anchored there)
+    W = np.stack([cov[k].astype(np.float64) for k in ("x", "y", "r", "er", "eg", "eb")], 1)
+    W[~cov["active"].astype(bool)] = 0.0
+    pic = port.render_frozen_fp64(prm, cov, np.ascontiguousarray(W), order)
     return w, prm, raw, cov, order, target, 2.0 * (pic - target)
 
 
