@@ -20,7 +20,9 @@ roofline: the dominant kernel of the frame, algorithmic work / its CUDA-event
 cpu_baseline: the CPU restatement of the reference (bit-exact with it) timed
         on this host's cores on the whole frame; the same leg, as the checker,
         measures the timed frame's image against the FP64 oracle
-        (image_rel_linf) and the reference's own FP32 arithmetic beside it.
+        (image_rel_linf) and the reference's own FP32 arithmetic beside it, and
+        times the reference's legacy GPU kernels (cuda/, additive frames) as
+        the GPU floor (legacy_gpu_floor).
 drop_in_default: the frame through host_rendering() with the drop-in's
         defaults (front-to-back compositing, every particle projected,
         colourised and sorted back into the caller's array), from pageable
@@ -250,6 +252,80 @@ def cpu_baseline(w, pic_gpu: np.ndarray, steps: int = 2, warmup: int = 1) -> dic
         "reference_fp32_rel_linf": rel_linf(pic32, pic64),
         "tolerance": 1e-4, "floor": "1e-6 x max|pixel|",
         "against": f"FP64 oracle at the GPU tile size {T}, same coverage and order"}
+    return out
+
+
+def legacy_gpu_floor(args, local: int) -> dict:
+    """The reference's legacy GPU renderer (cuda/, additive only), the GPU
+    floor: its own kernels built from the reference sources (PTX, by
+    oracle/build_ref.sh) under the oracle's driver, on the plain additive frame
+    (1M particles, 800x800) and on the batched workload's additive frames
+    (4 sets x 12 poses), inputs pre-clamped to [0, 1] as its normalisation
+    requires.  Each frame as cuda_rendering makes it: particle_sim records from
+    pageable host memory, three kernels, the image back; host wall time.  The
+    plain path renders the same frames through the C ABI from the same
+    pageable host records, timed the same way."""
+    import torch
+
+    import splotch_gb300 as sg
+    from oracle.oracle import LEGACY_PTX, LegacyGPU
+    from splotch_gb300 import synth
+
+    if not LEGACY_PTX.exists():
+        return {"unavailable": "the legacy kernels' PTX was not built (reference sources "
+                               "absent where build() ran)"}
+    port = _oracle_port()
+    leg = LegacyGPU()
+    r = sg.Renderer(local)
+
+    def both(p, params, rc, reps: int) -> tuple:
+        prm = dict(params.params)
+        p = p.copy()
+        p["I"] = np.minimum(p["I"], np.float32(1.0))
+        fr = leg.frame(port, prm, rc)
+        keep: list = []
+        desc = sg.frame_desc(sg.ParamFile(dict(prm)), rc, keep)
+        pic = np.zeros((desc.xres, desc.yres, 3), np.float32)
+        leg.render(port, prm, rc, p, frame=fr)
+        r.render_aos(desc, p, pic)
+        lt, gt, lst = [], [], None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            _, lst = leg.render(port, prm, rc, p, frame=fr)
+            lt.append(time.perf_counter() - t0)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r.render_aos(desc, p, pic)
+            gt.append(time.perf_counter() - t0)
+        return statistics.median(lt), statistics.median(gt), lst
+
+    out = {"kind": "reference", "note": "the reference's cuda/ kernels (k_range, k_process, "
+           "full-atomics k_render) compiled from its sources; the host driver restates "
+           "cuda_rendering for one chunk"}
+    w = synth.plain_additive()
+    lt, gt, lst = both(w.particles, w.params, w.rc, max(3, args.steps))
+    n = len(w.particles)
+    out["plain_additive_1M_800"] = {
+        "legacy_ms": lt * 1e3, "legacy_mparticles_per_s": n / lt / 1e6,
+        "legacy_stages_ms": {k: round(v, 3) for k, v in lst.items()},
+        "ours_ms": gt * 1e3, "ours_mparticles_per_s": n / gt / 1e6, "speedup": lt / gt}
+    bw = synth.batched(scale=args.batch_scale, tile=16, order=args.order)
+    lsum = gsum = 0.0
+    nfr = 0
+    pf = 0
+    for s, params, rc in bw.frames:
+        if params.params.get("a_eq_e") != "T":
+            continue
+        lt, gt, _ = both(bw.sets[s], params, rc, 1)
+        lsum += lt
+        gsum += gt
+        nfr += 1
+        pf += len(bw.sets[s])
+    r.close()
+    out["batched_additive_frames"] = {
+        "frames": nfr, "particle_frames": pf, "legacy_ms": lsum * 1e3,
+        "legacy_frames_per_s": nfr / lsum, "ours_ms": gsum * 1e3,
+        "ours_frames_per_s": nfr / gsum, "speedup": lsum / gsum}
     return out
 
 
@@ -622,7 +698,7 @@ def batched(args, local: int) -> dict:
         plain_pass()
     e1.record(stream)
     torch.cuda.synchronize()
-    r.set_split_tiles(False)
+    r.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
     out["plain_split_tiles_ms"] = e0.elapsed_time(e1) / reps
     out["plain_split_tiles_frames_per_s"] = nf / (out["plain_split_tiles_ms"] * 1e-3)
 
@@ -837,6 +913,7 @@ def run_gpu(args):
     cb = None
     if world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(w, pic_host)
+        cb["legacy_gpu_floor"] = legacy_gpu_floor(args, local)
     del w
     fb = None if args.no_fwd_bwd else fwd_bwd(args, local)
     bt = None if args.no_batched else batched(args, local)

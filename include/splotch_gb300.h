@@ -158,12 +158,22 @@ spl_status spl_prefetch(spl_context *ctx, const spl_particles *p);
    counterpart in the reference, whose tiles are dynamically scheduled CPU
    work items): one GPU block per segment instead of per tile, so that a few
    dense tiles do not keep most of the GPU idle; the segments' results are
-   then folded per pixel in list order.  Applies to additive and front-to-back
-   frames (not to ordered frames kept for spl_render_backward).  Off by
-   default: each pixel's sums are then grouped by segment, which changes
-   float rounding (within the usual tolerance) and so breaks the bit-for-bit
-   equality between spl_render and spl_batch_render frames. */
-spl_status spl_context_set_split_tiles(spl_context *ctx, int enable);
+   then folded per pixel in list order.  Each pixel's sums are then grouped by
+   segment, which changes float rounding within the usual tolerance (the
+   image stays deterministic), so a split frame is not bit-equal to the same
+   frame of spl_batch_render.
+     SPL_SPLIT_ADDITIVE (default): additive frames only.  Their segments add
+       up exactly the work of the whole tile.
+     SPL_SPLIT_ON: also front-to-back frames, whose tiles are cut only when
+       their list is at least 8x the frame's mean; a segment behind the front
+       one cannot stop early until the front one is opaque, so dense ordered
+       frames may render slower.
+     SPL_SPLIT_OFF: never.
+   Ordered frames kept for spl_render_backward are never split. */
+#define SPL_SPLIT_OFF 0
+#define SPL_SPLIT_ON 1
+#define SPL_SPLIT_ADDITIVE 2
+spl_status spl_context_set_split_tiles(spl_context *ctx, int mode);
 spl_status spl_get_stats(const spl_context *ctx, spl_stats *s);
 
 /* ---- test hooks: state of the last spl_render (host destinations) ----- */

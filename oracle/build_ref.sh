@@ -5,11 +5,13 @@
 # Reads the reference sources where they lie ($SPLOTCH_REF_DIR, else the
 # reference checkout named below -- the one place that names it) and writes
 # only under oracle/_ref/.  `build_ref.sh --where` prints that location.
-# Two libraries:
+# Two libraries and one PTX module:
 #   libsplotch_ref.so         default flags (on x86-64 __SSE2__ is defined, so
 #                             render_new takes its V4sf absorption branch)
 #   libsplotch_ref_scalar.so  the same with -U__SSE2__: the scalar branch that
 #                             an AArch64 (Grace) host compiles
+#   legacy_cuda_kernel.ptx    the legacy GPU kernels (cuda/cuda_kernel.cu), run by
+#                             oracle/legacy_gpu.cc as the GPU floor
 # Flags follow the reference's own plain build without -Ofast: -O2 -fopenmp,
 # plus -ffp-contract=off so no fused multiply-add changes its rounding.
 set -euo pipefail
@@ -50,4 +52,13 @@ build_variant() {  # $1 = output name, $2.. = extra flags
 
 build_variant libsplotch_ref
 build_variant libsplotch_ref_scalar -U__SSE2__
-echo "built $OUT/libsplotch_ref.so $OUT/libsplotch_ref_scalar.so"
+# The reference's legacy GPU kernels (cuda/cuda_kernel.cu, whose header
+# selects the full-atomics renderer and the classic kernel) as PTX for sm_103a:
+# text that the GPU host's driver compiles when oracle/legacy_gpu.cc loads it.
+# Flags of the reference's generic CUDA build (Makefile: -std=c++11, no fast
+# math), without its relocatable-device-code split: the one file holds every
+# kernel and constant it needs.
+NVCC="${NVCC:-$(command -v nvcc || echo /usr/local/cuda/bin/nvcc)}"
+"$NVCC" -ptx -arch=compute_103a -std=c++11 -I"$REF" -I"$REF/cxxsupport" -I"$REF/c_utils" \
+    "$REF/cuda/cuda_kernel.cu" -o "$OUT/legacy_cuda_kernel.ptx"
+echo "built $OUT/libsplotch_ref.so $OUT/libsplotch_ref_scalar.so $OUT/legacy_cuda_kernel.ptx"

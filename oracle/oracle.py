@@ -49,6 +49,33 @@ def build_port(force: bool = False) -> Path:
     return PORT_LIB
 
 
+LEGACY_LIB = BUILD / "liblegacy_gpu.so"
+LEGACY_PTX = REF_DIR / "legacy_cuda_kernel.ptx"
+
+
+def build_legacy() -> bool:
+    """Compile the host driver of the reference's legacy GPU kernels
+    (legacy_gpu.cc; CUDA runtime only, so it builds on the GPU host too)."""
+    BUILD.mkdir(exist_ok=True)
+    src = HERE / "legacy_gpu.cc"
+    if LEGACY_LIB.exists() and LEGACY_LIB.stat().st_mtime >= src.stat().st_mtime:
+        return True
+    nvcc = None
+    for cand in ("nvcc", "/usr/local/cuda/bin/nvcc"):
+        r = subprocess.run(["bash", "-c", f"command -v {cand}"], capture_output=True, text=True)
+        if r.returncode == 0:
+            nvcc = r.stdout.strip()
+            break
+    if nvcc is None:
+        return False
+    r = subprocess.run([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-x", "cu",
+                        str(src), "-o", str(LEGACY_LIB), "-lcudart"], capture_output=True,
+                       text=True)
+    if r.returncode:
+        raise RuntimeError(f"legacy driver build failed:\n{r.stderr}")
+    return True
+
+
 def ref_dir() -> Path:
     """Where the reference sources are read from (build_ref.sh decides)."""
     r = subprocess.run(["bash", str(HERE / "build_ref.sh"), "--where"], capture_output=True,
@@ -548,3 +575,82 @@ def rel_linf(a: np.ndarray, b: np.ndarray, floor_frac: float = 1e-6) -> float:
     m = float(np.max(np.abs(b))) if b.size else 0.0
     floor = max(floor_frac * m, 1e-30)
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor))) if b.size else 0.0
+
+
+class LegFrame(C.Structure):
+    _fields_ = [("mat", C.c_float * 12), ("projection", C.c_int), ("xres", C.c_int),
+                ("yres", C.c_int), ("fovfct", C.c_float), ("dist", C.c_float),
+                ("xfac", C.c_float), ("minrad_pix", C.c_float), ("xshift", C.c_double),
+                ("yshift", C.c_double), ("ptypes", C.c_int), ("col_vector", C.c_int * 8),
+                ("brightness", C.c_float * 8), ("smooth_fac", C.c_float * 8),
+                ("inorm_min", C.c_float * 8), ("inorm_max", C.c_float * 8),
+                ("cnorm_min", C.c_float * 8), ("cnorm_max", C.c_float * 8)]
+
+
+class LegacyGPU:
+    """The reference's legacy GPU renderer (cuda/: k_range, k_process and the
+    full-atomics k_render), compiled from its sources to PTX by build_ref.sh
+    and driven by legacy_gpu.cc the way cuda_rendering drives it for one
+    chunk.  Additive frames only, as that path renders them.  Its
+    normalisation needs intensity_min/max and color_min/max per type
+    (cuda/cuda_utils.cu:56-59); render() passes [0, 1] for both, so inputs
+    pre-clamped to [0, 1] render as the plain path renders them."""
+
+    def __init__(self):
+        if not LEGACY_PTX.exists():
+            raise FileNotFoundError(f"{LEGACY_PTX} is absent (built by build_ref.sh where "
+                                    "the reference sources are)")
+        build_legacy()
+        self.lib = C.CDLL(str(LEGACY_LIB))
+        self.lib.leg_open.restype = C.c_int
+        self.lib.leg_open.argtypes = [C.c_char_p]
+        self.lib.leg_render.restype = C.c_int
+        self.lib.leg_render.argtypes = [C.POINTER(LegFrame), C.c_void_p, C.c_int64, C.c_void_p,
+                                        C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        rc = self.lib.leg_open(str(LEGACY_PTX).encode())
+        if rc:
+            raise RuntimeError(f"loading the legacy kernels failed ({rc})")
+
+    def frame(self, port: "Port", params: dict, rc) -> tuple:
+        """The constant block's inputs (cu_get_trans_params, cu_init_transform)
+        and the colour map (setup_colormap) of one frame."""
+        cam = port.camera(params, rc)
+        f = LegFrame()
+        f.mat[:] = list(cam.mat)
+        f.projection = 1 if _get(params, "projection", True) else 0
+        f.xres = _get(params, "xres", 800)
+        f.yres = _get(params, "yres", f.xres)
+        f.fovfct, f.xfac = cam.fovfct, cam.xfac
+        d = np.asarray(rc.centerpos, np.float64) - np.asarray(rc.lookat, np.float64)
+        f.dist = float(np.float32(np.sqrt((d * d).sum())))
+        f.minrad_pix = float(_get(params, "minrad_pix", 1.0))
+        f.xshift, f.yshift = cam.xshift, cam.yshift
+        f.ptypes = _get(params, "ptypes", 1)
+        vals, points = [], []
+        for t in range(f.ptypes):
+            f.col_vector[t] = 1 if _get(params, f"color_is_vector{t}", False) else 0
+            f.brightness[t] = float(np.float32(_get(params, f"brightness{t}", 1.0) *
+                                               float(getattr(rc, "b_brightness", 1.0))))
+            f.smooth_fac[t] = float(_get(params, f"smooth_factor{t}", 1.0))
+            f.inorm_min[t], f.inorm_max[t], f.cnorm_min[t], f.cnorm_max[t] = 0.0, 1.0, 0.0, 1.0
+            points.append(len(vals))
+            pal = rc.amap[t] if t < len(rc.amap) else None
+            if pal is not None:
+                for x, c in zip(pal.x, pal.rgb):
+                    vals.append((np.float32(x), c[0], c[1], c[2]))
+        cmap = np.ascontiguousarray(np.array(vals, dtype=np.float32).reshape(-1, 4))
+        return f, cmap, np.ascontiguousarray(np.array(points, dtype=np.int32))
+
+    def render(self, port: "Port", params: dict, rc, particles: np.ndarray,
+               frame=None) -> tuple:
+        """(image x-major float32, stage milliseconds dict)."""
+        f, cmap, points = frame if frame is not None else self.frame(port, params, rc)
+        pic = np.zeros((f.xres, f.yres, 3), np.float32)
+        ms = np.zeros(6)
+        p = np.ascontiguousarray(particles)
+        rc_ = self.lib.leg_render(C.byref(f), _vp(p), len(p), _vp(cmap), len(cmap),
+                                  _vp(points), _vp(pic), _vp(ms))
+        if rc_:
+            raise RuntimeError(f"legacy render failed ({rc_})")
+        keys = ("copy_in", "k_range", "k_process", "k_render", "copy_out", "total")
+        return pic, dict(zip(keys, ms.tolist()))

@@ -361,11 +361,14 @@ class Renderer:
         _abi.check(self.lib.spl_get_stats(self.ctx, C.byref(s)))
         return s.as_dict()
 
-    def set_split_tiles(self, enable: bool = True) -> None:
-        """Cut heavy tiles into list segments in later renders (additive and
-        front-to-back frames): one GPU block per segment, results folded per
-        pixel.  Off by default (it regroups each pixel's float sums)."""
-        _abi.check(self.lib.spl_context_set_split_tiles(self.ctx, 1 if enable else 0))
+    def set_split_tiles(self, mode: bool | int = True) -> None:
+        """Which frames have heavy tiles cut into list segments in later
+        renders (one GPU block per segment, results folded per pixel): True or
+        SPL_SPLIT_ON additive and front-to-back frames, False or SPL_SPLIT_OFF
+        none, SPL_SPLIT_ADDITIVE (the default) additive frames only."""
+        m = mode if not isinstance(mode, bool) else (_abi.SPL_SPLIT_ON if mode
+                                                      else _abi.SPL_SPLIT_OFF)
+        _abi.check(self.lib.spl_context_set_split_tiles(self.ctx, int(m)))
 
     # -- gradients ------------------------------------------------------------
     def set_differentiable(self, enable: bool = True) -> None:

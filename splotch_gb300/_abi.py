@@ -17,6 +17,7 @@ SPL_MEM_HOST, SPL_MEM_DEVICE = 0, 1
 SPL_LAYOUT_AOS, SPL_LAYOUT_SOA = 0, 1
 SPL_WRITEBACK_NONE, SPL_WRITEBACK_FULL = 0, 1
 SPL_ORDER_BACK_TO_FRONT, SPL_ORDER_FRONT_TO_BACK = 0, 1
+SPL_SPLIT_OFF, SPL_SPLIT_ON, SPL_SPLIT_ADDITIVE = 0, 1, 2
 
 LIB_PATH = Path(__file__).resolve().parent / "libsplgpu.so"
 

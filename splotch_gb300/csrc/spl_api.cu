@@ -45,7 +45,7 @@ struct spl_context {
   spl::RayFrame *rays = nullptr;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
-  bool split_tiles = false;     // heavy tiles cut into list segments
+  int split_mode = SPL_SPLIT_ADDITIVE;  // which frames have heavy tiles cut into segments
   // state of the last frame (for the debug getters)
   int64_t n = 0, na = 0, ne = 0, ntiles = 0;
   bool has_order = false, writeback_done = false;
@@ -655,7 +655,9 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   }
   // Heavy tiles cut into list segments when asked (additive and front-to-back
   // frames whose per-pixel data the adjoint does not need)
-  const bool split = c->split_tiles && !sa.aux && (sa.a_eq_e || sa.order_mode == 1) && ntiles > 0;
+  const bool split = !sa.aux && ntiles > 0 &&
+                     ((sa.a_eq_e && c->split_mode != SPL_SPLIT_OFF) ||
+                      (!sa.a_eq_e && sa.order_mode == 1 && c->split_mode == SPL_SPLIT_ON));
   if (split) {
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
@@ -811,9 +813,12 @@ spl_status spl_prefetch(spl_context *c, const spl_particles *p) {
   return SPL_OK;
 }
 
-spl_status spl_context_set_split_tiles(spl_context *c, int enable) {
+spl_status spl_context_set_split_tiles(spl_context *c, int mode) {
   if (!c) return fail(SPL_ERR_INVALID, "null ctx");
-  c->split_tiles = enable != 0;
+  if (mode != SPL_SPLIT_OFF && mode != SPL_SPLIT_ON && mode != SPL_SPLIT_ADDITIVE)
+    return fail(SPL_ERR_INVALID, "spl_context_set_split_tiles: unknown mode " +
+                                     std::to_string(mode));
+  c->split_mode = mode;
   return SPL_OK;
 }
 

@@ -83,13 +83,15 @@ __device__ __forceinline__ float warp_sum6(const float v[6], int lane, int &j, b
 // Segments of each tile's list for the adjoint: ceil(len / seg_len), 0 for an
 // empty tile.
 // (split_min: a tile shorter than this stays one segment.)
+// Segments per tile: an empty list has empty_cnt (the adjoint skips it; the
+// forward still writes the tile's pixels from one empty segment).
 __global__ void k_adj_seg_count(const uint32_t *__restrict__ tile_start, int64_t ntiles,
-                                uint32_t seg_len, uint32_t split_min,
+                                uint32_t seg_len, uint32_t split_min, uint32_t empty_cnt,
                                 uint32_t *__restrict__ cnt) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntiles;
        t += (int64_t)gridDim.x * blockDim.x) {
     const uint32_t len = tile_start[t + 1] - tile_start[t];
-    cnt[t] = len == 0 ? 0u : len < split_min ? 1u : 1u + (len - 1u) / seg_len;
+    cnt[t] = len == 0 ? empty_cnt : len < split_min ? 1u : 1u + (len - 1u) / seg_len;
   }
 }
 
@@ -714,7 +716,7 @@ int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
   a.seg_len = seg_len;
   int launches = 1;
   int cb = (int)std::min<int64_t>((ntiles + 255) / 256, 152 * 8);
-  k_adj_seg_count<<<cb, 256, 0, s>>>(a.f.tile_start, ntiles, seg_len, 0u, a.seg_cnt);
+  k_adj_seg_count<<<cb, 256, 0, s>>>(a.f.tile_start, ntiles, seg_len, 0u, 0u, a.seg_cnt);
   scan_counts(a.seg_cnt, a.f.tile_order, ntiles, a.seg_off, a.scan_scratch, s, &launches);
   const uint32_t grid = (uint32_t)std::min<int64_t>(grid64, 0x7fffffff);
   switch (cfg) {
@@ -731,7 +733,8 @@ void launch_seg_count(const uint32_t *tile_start, int64_t ntiles, uint32_t seg_l
                       uint32_t split_min, uint32_t *cnt, cudaStream_t s) {
   if (ntiles <= 0) return;
   const int cb = (int)std::min<int64_t>((ntiles + 255) / 256, 152 * 8);
-  k_adj_seg_count<<<cb, 256, 0, s>>>(tile_start, ntiles, seg_len, split_min, cnt);
+  // every tile of the forward has a segment: an empty one writes zeros
+  k_adj_seg_count<<<cb, 256, 0, s>>>(tile_start, ntiles, seg_len, split_min, 1u, cnt);
 }
 
 int launch_project_adjoint(const ProjAdjArgs &a, cudaStream_t s) {

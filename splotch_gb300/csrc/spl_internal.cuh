@@ -446,8 +446,8 @@ struct SplatSegs {
 };
 int launch_splat_split(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s);
 int splat_batch_size(const SplatArgs &a);  // list entries staged per batch
-// Segments per tile: ceil(len / seg_len), 0 for an empty tile, 1 for a tile
-// shorter than split_min.
+// Segments per tile of the forward split: ceil(len / seg_len), 1 for an empty
+// tile (its segment writes the tile's zeros) or one shorter than split_min.
 void launch_seg_count(const uint32_t *tile_start, int64_t ntiles, uint32_t seg_len,
                       uint32_t split_min, uint32_t *cnt, cudaStream_t s);
 int splat_config_count();

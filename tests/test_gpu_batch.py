@@ -12,7 +12,7 @@ import pytest
 
 import splotch_gb300 as sg
 from oracle.oracle import rel_linf
-from splotch_gb300 import synth
+from splotch_gb300 import _abi, synth
 
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
@@ -44,7 +44,12 @@ def _plain(renderer, sets, s, desc, T, cfg):
     d.splat_config = cfg
     pic = torch.zeros((d.xres, d.yres, 3), dtype=torch.float32, device="cuda")
     torch.cuda.synchronize()
-    renderer.render_soa(d, sets[s], pic, device=True)
+    # the batch renders every tile whole: so does its per-frame counterpart
+    renderer.set_split_tiles(False)
+    try:
+        renderer.render_soa(d, sets[s], pic, device=True)
+    finally:
+        renderer.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
     torch.cuda.synchronize()
     return pic.cpu().numpy()
 

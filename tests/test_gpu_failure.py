@@ -100,7 +100,11 @@ def test_batch_allocation_failure_is_reported(renderer):
             want = torch.zeros_like(pic)
             d = type(desc).from_buffer_copy(desc)
             d.tile_size, d.splat_config = 16, 0 if desc.a_eq_e else 2
-            renderer.render_soa(d, sets[s], want, device=True)
+            renderer.set_split_tiles(False)  # the batch renders every tile whole
+            try:
+                renderer.render_soa(d, sets[s], want, device=True)
+            finally:
+                renderer.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
             torch.cuda.synchronize()
             assert np.array_equal(pic.cpu().numpy(), want.cpu().numpy())
     finally:

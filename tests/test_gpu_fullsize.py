@@ -26,7 +26,7 @@ import pytest
 
 import splotch_gb300 as sg
 from oracle.oracle import rel_linf
-from splotch_gb300 import synth
+from splotch_gb300 import _abi, synth
 
 from .helpers import IMAGE_TOL, assert_parity, gpu_frame, oracle_frame
 from .test_gpu_grad import (FIELDS, GRAD_MEDIAN, GRAD_TOL, _frame, _gpu_matrix, describe,
@@ -167,7 +167,11 @@ def test_batch_real_resolutions(renderer, port):
             d = type(desc).from_buffer_copy(desc)
             d.tile_size, d.splat_config = T, cfg
             want = torch.zeros_like(pic)
-            renderer.render_soa(d, sets[s], want, device=True)
+            renderer.set_split_tiles(False)  # the batch renders every tile whole
+            try:
+                renderer.render_soa(d, sets[s], want, device=True)
+            finally:
+                renderer.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
             torch.cuda.synchronize()
             assert np.array_equal(got, want.cpu().numpy()), f"frame {k} differs from spl_render"
             _, params, rc = bw.frames[k]

@@ -12,7 +12,7 @@ import pytest
 
 import splotch_gb300 as sg
 from oracle.oracle import rel_linf
-from splotch_gb300 import synth
+from splotch_gb300 import _abi, synth
 
 from .helpers import oracle_frame
 
@@ -35,7 +35,7 @@ def test_split_tiles_match_unsplit_and_oracle(renderer, port, mode):
         renderer.render_aos(desc, w.particles.copy(), split)
         launches_split = renderer.stats()["kernel_launches"]
     finally:
-        renderer.set_split_tiles(False)
+        renderer.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
     assert launches_split > launches_plain
     assert rel_linf(split, plain) <= 1e-5
     o = oracle_frame(port, dict(w.params.params), w.rc, w.particles, fp32=False)
@@ -54,6 +54,24 @@ def test_split_tiles_leave_differentiable_ordered_frames_whole(renderer):
     try:
         renderer.render_aos(desc, w.particles.copy(), pic)
     finally:
-        renderer.set_split_tiles(False)
+        renderer.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
         renderer.set_differentiable(False)
     assert np.array_equal(pic, want)  # the same unsplit render
+
+
+@pytest.mark.parametrize("mode", ["additive", "absorption"])
+def test_split_tiles_on_sparse_frames(renderer, port, mode):
+    """A frame with many empty tiles, split in both modes: every empty tile
+    still writes its zeros, and the image is the oracle's."""
+    from .helpers import assert_parity, gpu_frame
+
+    w = synth.differentiable(n=300, mode=mode, xres=320, yres=200, tile=16, order="ftb")
+    prm = dict(w.params.params)
+    renderer.set_split_tiles(True)
+    try:
+        g = gpu_frame(renderer, prm, w.rc, w.particles)
+    finally:
+        renderer.set_split_tiles(_abi.SPL_SPLIT_ADDITIVE)
+    ntiles = (320 // 16) * (200 // 16 + 1)
+    assert (np.diff(g.tile_start) == 0).sum() > ntiles // 4, "expected many empty tiles"
+    assert_parity(g, oracle_frame(port, prm, w.rc, w.particles, fp32=False))
