@@ -642,7 +642,7 @@ def batched(args, local: int) -> dict:
     import torch
 
     import splotch_gb300 as sg
-    from splotch_gb300 import synth
+    from splotch_gb300 import _abi, synth
 
     dev = f"cuda:{local}"
     bw = synth.batched(scale=args.batch_scale, tile=16, order=args.order)

@@ -48,8 +48,10 @@ enum { SPL_WRITEBACK_NONE = 0, SPL_WRITEBACK_FULL = 1 };
 /* Compositing order for the ordered (a_eq_e=false) splat.  BACK_TO_FRONT
    applies particles in list order exactly like render_new; FRONT_TO_BACK
    (the default) evaluates the same sum, term for term, in reverse and stops
-   once every channel's transmittance is below spl_frame_desc.ftb_epsilon
-   (1e-9: what lies behind then adds less than 1e-9 of its colour).  Both are
+   a pixel once every channel's transmittance is below spl_frame_desc.
+   ftb_epsilon (1e-9: what lies behind then adds less than 1e-9 of its colour)
+   or below ftb_relative (1e-5) times the colour the channel has composited
+   (what lies behind then adds at most 1e-5 of the pixel).  Both orders are
    within 1e-4 of the FP64 oracle; front-to-back skips the opaque depths of
    dense tiles, which back-to-front must walk in full. */
 enum { SPL_ORDER_BACK_TO_FRONT = 0, SPL_ORDER_FRONT_TO_BACK = 1 };
@@ -90,6 +92,11 @@ typedef struct {
   float ftb_epsilon;        /* transmittance cut for FRONT_TO_BACK (1e-9) */
   int splat_config;         /* splat launch configuration, -1 = default for the
                                tile size (see spl_splat_config_valid) */
+  float ftb_relative;       /* FRONT_TO_BACK also stops a pixel once each channel's
+                               transmittance is below ftb_relative times the colour
+                               it has composited (1e-5): all that lies behind adds
+                               at most that fraction of the pixel (q <= 1).  Not
+                               applied to frames kept for spl_render_backward. */
 } spl_frame_desc;
 
 /* Particle input.  AoS: aos points at n particle_sim records.  SoA: x..I,

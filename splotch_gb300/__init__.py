@@ -240,6 +240,8 @@ def frame_desc(params: ParamFile, rc: RenderContext, keep: list | None = None) -
                         else _abi.SPL_ORDER_BACK_TO_FRONT)
     if params.param_present("gpu_ftb_epsilon"):
         d.ftb_epsilon = params.find("gpu_ftb_epsilon", 1e-9)
+    if params.param_present("gpu_ftb_relative"):
+        d.ftb_relative = params.find("gpu_ftb_relative", 1e-5)
     if params.param_present("gpu_splat_config"):
         d.splat_config = params.find("gpu_splat_config", -1)
     d.b_brightness = float(rc.b_brightness)

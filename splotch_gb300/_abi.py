@@ -59,7 +59,7 @@ class FrameDesc(C.Structure):
         ("gray_absorption", C.c_float), ("sort_type", C.c_int), ("tile_size", C.c_int),
         ("campos", C.c_double * 3), ("lookat", C.c_double * 3), ("sky", C.c_double * 3),
         ("centerpos", C.c_double * 3), ("order_mode", C.c_int), ("ftb_epsilon", C.c_float),
-        ("splat_config", C.c_int),
+        ("splat_config", C.c_int), ("ftb_relative", C.c_float),
     ]
 
 

@@ -646,6 +646,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   sa.a_eq_e = d->a_eq_e ? 1 : 0;
   sa.order_mode = d->order_mode;
   sa.ftb_eps = d->ftb_epsilon;
+  sa.ftb_rel = d->ftb_relative;
   sa.config = d->splat_config;
   sa.pic = out->memspace == SPL_MEM_DEVICE ? out->pic : as<float>(c->pic);
   sa.aux = nullptr;

@@ -584,6 +584,7 @@ spl_status plan(spl_batch *b, int T, int64_t cap_add, int64_t cap_ord, int64_t c
     a.order_mode = d.order_mode;
     if (!d.a_eq_e && d.order_mode != 1) b->ord_all_ftb = false;
     a.ftb_eps = d.ftb_epsilon;
+    a.ftb_rel = d.ftb_relative;
     a.config = -1;
     a.pic = b->frames[f].pic;
   }

@@ -97,6 +97,7 @@ extern "C" void spl_frame_desc_defaults(spl_frame_desc *d) {
   d->sky[1] = 1.0;
   d->order_mode = SPL_ORDER_FRONT_TO_BACK;
   d->ftb_epsilon = 1e-9f;
+  d->ftb_relative = 1e-5f;
   d->splat_config = -1;
 }
 

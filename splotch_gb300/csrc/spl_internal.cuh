@@ -424,6 +424,7 @@ struct SplatArgs {
   int a_eq_e;
   int order_mode;
   float ftb_eps;
+  float ftb_rel;               // relative transmittance cut (front-to-back)
   int config;                  // launch configuration (-1: default for T)
   float *pic;                  // device, x-major xres*yres*3
   // ordered frames kept for the adjoint (null: not kept): per pixel, x-major,

@@ -194,6 +194,10 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
         }
       }
       if (FTB) {
+        // a pixel is done once each channel's transmittance is below the
+        // absolute cut or below ftb_rel times the colour it has composited
+        // (acc); frames kept for the adjoint use the absolute cut alone
+        const float rel = AUX ? 0.f : a.ftb_rel;
         bool mine_done = true;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
@@ -201,7 +205,8 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const float t = (k & 1) ? f2hi(tr[k / 2][c]) : f2lo(tr[k / 2][c]);
-              mine_done = mine_done && t < a.ftb_eps;
+              const float v = (k & 1) ? f2hi(acc[k / 2][c]) : f2lo(acc[k / 2][c]);
+              mine_done = mine_done && (t < a.ftb_eps || t < rel * v);
             }
           }
         }

@@ -17,7 +17,8 @@
 //   * new_renderer=true runs the ray-sphere renderer (spl_render_rays) and
 //     empties the particle vector, as host_rendering_new does.
 // GPU-only keys (all optional): gpu_device (0), gpu_writeback (true),
-// gpu_order ("ftb" | "btf"; default ftb), gpu_ftb_epsilon (1e-9), gpu_splat_config (-1).
+// gpu_order ("ftb" | "btf"; default ftb), gpu_ftb_epsilon (1e-9), gpu_ftb_relative
+// (1e-5), gpu_splat_config (-1).
 #include <string>
 #include <vector>
 
@@ -169,6 +170,8 @@ void host_rendering(paramfile &params, std::vector<particle_sim> &particles,
                                                                  : SPL_ORDER_BACK_TO_FRONT;
   if (params.param_present("gpu_ftb_epsilon"))
     d.ftb_epsilon = params.find<float32>("gpu_ftb_epsilon");
+  if (params.param_present("gpu_ftb_relative"))
+    d.ftb_relative = params.find<float32>("gpu_ftb_relative");
   if (params.param_present("gpu_splat_config"))
     d.splat_config = params.find<int>("gpu_splat_config");
 
