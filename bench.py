@@ -58,11 +58,11 @@ METRIC = "Mparticles/s & frames/s (plain, batched, fwd+bwd) on 1 GB300 at ≤1e-
 # committed one-kernel ncu capture (the bench itself runs no profiler); the
 # traffic is scaled to the timed frame by its reference fragment count.
 SPLAT_CAPTURE = {
-    "source": "profiles/k_splat_ftb_pairs_10M.md",
+    "source": "profiles/k_splat_ftb_10M.md",
     "fragments": 7.53e8,          # reference fragments of the captured launch
-    "dram_bytes": 90.4e6,         # dram__bytes_read.sum + dram__bytes_write.sum
-    "issue_frac": 0.744,          # issue slots busy per SMSP while active
-    "smem_wavefront_frac": 0.19,  # shared wavefronts / (SM cycles x SMs)
+    "dram_bytes": 84.2e6,         # dram__bytes (read + write) of the launch
+    "issue_frac": 0.76,           # issue slots busy per SMSP while active
+    "smem_wavefront_frac": 0.249,  # L1 data-pipe (shared) wavefronts, of peak
 }
 
 
