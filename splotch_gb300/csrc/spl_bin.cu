@@ -21,11 +21,17 @@ namespace {
 
 constexpr int kWideTiles = 64;
 
-// Each thread takes kEmitUnroll records per step (a grid stride apart) and
-// issues their loads together: in visiting order the particles' positions
-// are gathered at scattered indices, and the independent loads overlap.
-constexpr int kEmitUnroll = 4;
-
+// One warp per 32 consecutive visiting positions.  The candidate cells of the
+// warp's narrow particles (each particle's tile rectangle, column-major like
+// the reference loop) are laid end to end and dealt to the lanes 32 at a
+// time: a lane finds its cell's particle by binary search over the warp's
+// cell prefix, runs the circle test, and the passing cells take consecutive
+// slots in visiting order (a ballot prefix).  Every lane does useful work,
+// whatever the mix of footprints, and a warp's stores are contiguous.
+//
+// A particle's passing cells fill exactly its slots [off, off + count): the
+// count came from the same test (for_each_tile) in the same arithmetic; a
+// store is also checked against the particle's count before it is made.
 __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ pos,
                                                      const uint32_t *__restrict__ count,
                                                      const uint32_t *__restrict__ order,
@@ -35,34 +41,98 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
                                                      uint32_t *__restrict__ tval,
                                                      uint32_t *__restrict__ wide_list,
                                                      uint32_t *__restrict__ wide_n) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s0 < n;
-       s0 += stride * kEmitUnroll) {
-    uint32_t c[kEmitUnroll], i[kEmitUnroll];
-    float4 p[kEmitUnroll];
-#pragma unroll
-    for (int k = 0; k < kEmitUnroll; ++k) {
-      const int64_t s = s0 + k * stride;
-      c[k] = s < n ? __ldg(count + s) : 0u;  // counts are in visiting order
-      i[k] = s < n ? (order ? __ldg(order + s) : (uint32_t)s) : 0u;
-    }
-#pragma unroll
-    for (int k = 0; k < kEmitUnroll; ++k)
-      if (c[k] > 0 && c[k] <= (uint32_t)kWideTiles) p[k] = __ldg(pos + i[k]);
-#pragma unroll
-    for (int k = 0; k < kEmitUnroll; ++k) {
-      const int64_t s = s0 + k * stride;
-      if (c[k] == 0) continue;
-      if (c[k] > (uint32_t)kWideTiles) {  // handed to the warp-per-particle path
-        wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
-        continue;
-      }
+  __shared__ uint32_t cpre[256 / 32][33];  // per warp: exclusive cell prefix of its lanes
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const int T = g.T;
+  const int64_t nchunk = (n + 31) / 32;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t ch = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; ch < nchunk;
+       ch += nwarp) {
+    const int64_t s = ch * 32 + lane;
+    const uint32_t c = s < n ? __ldg(count + s) : 0u;  // counts are in visiting order
+    const uint32_t i = s < n ? (order ? __ldg(order + s) : (uint32_t)s) : 0u;
+    const bool narrow = c > 0u && c <= (uint32_t)kWideTiles;
+    if (c > (uint32_t)kWideTiles)  // handed to the warp-per-particle path
+      wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
+    float px = 0.f, py = 0.f, sumsq = 0.f;
+    int minx = 0, miny = 0, wy = 1;
+    uint32_t cells = 0, magic = 0, olo = 0, ohi = 0;
+    if (narrow) {
+      const float4 p = __ldg(pos + i);
+      px = p.x;
+      py = p.y;
+      const float rfacr = fmul(0.75f, p.z);
+      minx = max(0, f2i(fadd(fsub(px, rfacr), 1.f)) / T);
+      const int maxx = min(g.ncx - 1, f2i(fadd(px, rfacr)) / T);
+      miny = max(0, f2i(fadd(fsub(py, rfacr), 1.f)) / T);
+      const int maxy = min(g.ncy - 1, f2i(fadd(py, rfacr)) / T);
+      const float rs = fadd(g.rcell, rfacr);
+      sumsq = fmul(rs, rs);
+      wy = maxy - miny + 1;
+      cells = (uint32_t)((maxx - minx + 1) * wy);
+      // q / wy = umulhi(q, ceil(2^32 / wy)), exact for q, wy < 2^16
+      magic = wy > 1 ? 0xffffffffu / (uint32_t)wy + 1u : 0u;
       const uint64_t o = __ldg(off + s);
-      const uint32_t ii = i[k];
-      for_each_tile(p[k].x, p[k].y, p[k].z, g, [&](int tile, int j) {
-        tkey[o + j] = (uint32_t)tile;
-        tval[o + j] = ii;
-      });
+      olo = (uint32_t)o;
+      ohi = (uint32_t)(o >> 32);
+    }
+    // inclusive warp scans: candidate cells, and the narrow particles' counts
+    uint32_t cin = cells, nin = narrow ? c : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t0 = __shfl_up_sync(0xffffffffu, cin, d);
+      const uint32_t t1 = __shfl_up_sync(0xffffffffu, nin, d);
+      if (lane >= d) {
+        cin += t0;
+        nin += t1;
+      }
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, cin, 31);
+    const uint32_t nexcl = nin - (narrow ? c : 0u);  // passing cells before this lane's particle
+    __syncwarp();  // the previous chunk's readers of cpre are done
+    cpre[w][lane] = cin - cells;
+    __syncwarp();
+    uint32_t carry = 0;  // passing cells dealt so far in this chunk
+    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+      const uint32_t k = k0 + (uint32_t)lane;
+      int l = 0;  // the last lane whose cells start at or before k
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (cpre[w][l + step] <= k) l += step;
+      const int lminx = __shfl_sync(0xffffffffu, minx, l);
+      const int lminy = __shfl_sync(0xffffffffu, miny, l);
+      const int lwy = __shfl_sync(0xffffffffu, wy, l);
+      const uint32_t lmag = __shfl_sync(0xffffffffu, magic, l);
+      const float lpx = __shfl_sync(0xffffffffu, px, l);
+      const float lpy = __shfl_sync(0xffffffffu, py, l);
+      const float lsq = __shfl_sync(0xffffffffu, sumsq, l);
+      const uint32_t lc = __shfl_sync(0xffffffffu, c, l);
+      const uint32_t lnex = __shfl_sync(0xffffffffu, nexcl, l);
+      const uint32_t li = __shfl_sync(0xffffffffu, i, l);
+      const uint32_t lolo = __shfl_sync(0xffffffffu, olo, l);
+      const uint32_t lohi = __shfl_sync(0xffffffffu, ohi, l);
+      const uint32_t q = k - cpre[w][l];
+      const uint32_t qx = lwy > 1 ? __umulhi(q, lmag) : q;
+      const int ix = lminx + (int)qx;
+      const int iy = lminy + (int)(q - qx * (uint32_t)lwy);
+      bool pass = false;
+      if (k < total) {  // the test of for_each_tile, operation for operation
+        const float cx = fadd(g.cmid0, (float)(ix * T));
+        const float dx = fsub(lpx, cx);
+        const float dx2 = fmul(dx, dx);
+        const float cy = fadd(g.cmid0, (float)(iy * T));
+        const float dy = fsub(lpy, cy);
+        pass = fadd(dx2, fmul(dy, dy)) < lsq;
+      }
+      const uint32_t b = __ballot_sync(0xffffffffu, pass);
+      const uint32_t j = carry + __popc(b & lt) - lnex;  // rank among the particle's tiles
+      if (pass && j < lc) {
+        const uint64_t slot = (((uint64_t)lohi << 32) | lolo) + j;
+        tkey[slot] = (uint32_t)(iy * g.ncx + ix);
+        tval[slot] = li;
+      }
+      carry += __popc(b);
     }
   }
 }

@@ -83,6 +83,22 @@ __device__ __forceinline__ unsigned long long os_word(uint32_t epoch, uint32_t k
 // and each digit's global offset comes from the global digit base plus a
 // decoupled look-back over earlier tiles' published counts.  A tile only ever
 // waits on tiles that started before it, and every wait is bounded.
+//
+// Per tile: load the keys; rank each key among the equal digits before it
+// (stable); publish the tile's digit counts at once (onesweep); sort the tile
+// into shared memory by digit; look back (by then the keys' registers are
+// dead, and the tiles in front have had the ranking's time to publish their
+// own prefixes); write each digit's run to its global offset.
+//
+// Ranking: the lanes of a warp holding the same digit find each other
+// through a per-warp table of 256 lane masks in shared memory (each lane ORs
+// its bit into its digit's slot, then reads the slot back); the group's
+// lowest lane claims the group's slots in the warp's digit count and clears
+// the slot.  Items are ranked in order, so equal digits keep input order.
+// (A warp match instruction gives the same masks, at several times the cost
+// per item with the ~30 distinct digits a warp of 32 keys usually holds.)
+constexpr int OS_WINDOW = 8;  // look-back: predecessor states read per round
+
 template <bool OS>
 __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     const uint32_t *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
@@ -97,13 +113,16 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
   __shared__ uint32_t skey[RS_TILE];
   __shared__ uint32_t sval[RS_TILE];
   __shared__ uint32_t tile_sh;
+  // the ranking's lane-mask table lives in skey, which is written only after
+  // the ranking (behind a barrier)
+  static_assert(RS_TILE >= RS_WARPS * RS_BINS, "the mask table fits in skey");
+  uint32_t(*mtab)[RS_BINS] = reinterpret_cast<uint32_t(*)[RS_BINS]>(skey);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) (&whist[0][0])[i] = 0;
-  if (OS) {
-    if (threadIdx.x == 0) tile_sh = atomicAdd(tile_ctr, 1u);
-  } else {
-    boff[threadIdx.x] = offsets[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+  for (int i = threadIdx.x; i < RS_WARPS * RS_BINS; i += RS_THREADS) {
+    (&whist[0][0])[i] = 0;
+    skey[i] = 0;
   }
+  if (OS && threadIdx.x == 0) tile_sh = atomicAdd(tile_ctr, 1u);
   __syncthreads();
   const int blk = OS ? (int)tile_sh : (int)blockIdx.x;
   const uint32_t mask = (1u << nbits) - 1u;
@@ -115,30 +134,38 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     const bool valid = idx < n;
     key[j] = valid ? __ldg(keys_in + idx) : 0xffffffffu;
     val[j] = valid ? (vals_in ? __ldg(vals_in + idx) : (uint32_t)idx) : 0u;
-    const uint32_t d = valid ? (key[j] >> shift) & mask : RS_BINS + lane;
-    // the lanes holding digit d: the lowest one claims their slots in the
-    // warp's histogram with one shared atomic and passes the old count on.
-    // Successive items' claims are performed in the warp's issue order, which
-    // keeps item order for equal digits (the stable-order GPU tests against
-    // the oracle's permutation check this).
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+  }
+#pragma unroll
+  for (int j = 0; j < RS_ITEMS; ++j) {
+    const bool valid = base + j * 32 + lane < n;
+    const uint32_t d = (key[j] >> shift) & mask;
+    uint32_t *slot = &mtab[w][d];
+    __syncwarp();  // the previous item's slot clears are visible
+    if (valid) atomicOr(slot, 1u << lane);
+    __syncwarp();
+    const uint32_t peers = valid ? *slot : 0u;
     const int leader = __ffs(peers) - 1;
     uint32_t prior = 0;
     if (valid && lane == leader) prior = atomicAdd(&whist[w][d], (uint32_t)__popc(peers));
-    prior = __shfl_sync(0xffffffffu, prior, leader);
+    __syncwarp();  // every peer has read the slot
+    if (valid && lane == leader) *slot = 0u;
+    prior = __shfl_sync(0xffffffffu, prior, leader & 31);
     rank[j] = prior + __popc(peers & lanemask_lt());
   }
   __syncthreads();
+  const int d = threadIdx.x;
+  unsigned long long *st = OS ? state + (size_t)blk * RS_BINS + d : nullptr;
+  uint32_t run = 0;
   {  // per digit: exclusive prefix over warps, then over digits (block-local)
-    const int d = threadIdx.x;
-    uint32_t run = 0;
 #pragma unroll
     for (int ww = 0; ww < RS_WARPS; ++ww) {
       const uint32_t t = whist[ww][d];
       whist[ww][d] = run;
       run += t;
     }
-    // exclusive scan of the block's digit totals across the 256 threads
+    // onesweep: publish this tile's count of digit d (tile 0: its prefix)
+    if (OS)
+      *reinterpret_cast<volatile unsigned long long *>(st) = os_word(epoch, blk == 0 ? 2u : 1u, run);
     uint32_t inc = run;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -150,58 +177,74 @@ __global__ void __launch_bounds__(RS_THREADS, 3) k_rs_downsweep(
     uint32_t wpre = 0;
     for (int ww = 0; ww < w; ++ww) wpre += wtot[ww];
     lstart[d] = wpre + inc - run;
-    if (OS) {  // decoupled look-back for digit d
-      volatile unsigned long long *st = state + (size_t)blk * RS_BINS + d;
-      unsigned long long excl = 0;
-      if (blk == 0) {
-        *st = os_word(epoch, 2u, run);
-      } else {
-        *st = os_word(epoch, 1u, run);
-        int t = blk - 1;
-        uint32_t spins = 0;
-        while (t >= 0) {
-          const unsigned long long v =
-              reinterpret_cast<volatile unsigned long long *>(state)[(size_t)t * RS_BINS + d];
-          const uint32_t kind = (uint32_t)(v >> OS_KIND_SHIFT) & 3u;
-          if ((uint32_t)(v >> OS_EPOCH_SHIFT) != epoch || kind == 0u) {
-            // give up: this tile's offsets come from a partial prefix (never
-            // above the true one, so its writes stay inside [0, n)); the
-            // results are invalid and the host reports it
-            if (++spins > spin_limit) {
-              atomicOr(err, 2u);
-              break;
-            }
-            if (spins > 64) __nanosleep(64);
-            continue;
-          }
-          excl += v & OS_VALUE_MASK;
-          if (kind == 2u) break;
-          --t;
-        }
-        *st = os_word(epoch, 2u, excl + run);
-      }
-      boff[d] = (uint32_t)(digit_base[d] + excl);
-    }
   }
   __syncthreads();
   // stable local sort into shared memory ...
 #pragma unroll
   for (int j = 0; j < RS_ITEMS; ++j) {
-    const int64_t idx = base + j * 32 + lane;
-    if (idx < n) {
-      const uint32_t d = (key[j] >> shift) & mask;
-      const uint32_t lpos = lstart[d] + whist[w][d] + rank[j];
+    if (base + j * 32 + lane < n) {
+      const uint32_t dd = (key[j] >> shift) & mask;
+      const uint32_t lpos = lstart[dd] + whist[w][dd] + rank[j];
       skey[lpos] = key[j];
       sval[lpos] = val[j];
     }
+  }
+  // ... the digit's global offset ...
+  unsigned long long excl = 0;
+  if (OS) {
+    if (blk > 0) {  // decoupled look-back, OS_WINDOW tiles per round
+      int t = blk - 1;
+      uint32_t spins = 0;
+      while (t >= 0) {
+        unsigned long long v[OS_WINDOW];
+#pragma unroll
+        for (int i = 0; i < OS_WINDOW; ++i)  // before tile 0: an inclusive zero
+          v[i] = t - i >= 0 ? *reinterpret_cast<const volatile unsigned long long *>(
+                                  state + (size_t)(t - i) * RS_BINS + d)
+                            : os_word(epoch, 2u, 0ull);
+        bool go = true, found = false;
+        int used = 0;
+#pragma unroll
+        for (int i = 0; i < OS_WINDOW; ++i) {
+          if (go) {
+            const uint32_t kind = (uint32_t)(v[i] >> OS_KIND_SHIFT) & 3u;
+            if ((uint32_t)(v[i] >> OS_EPOCH_SHIFT) != epoch || kind == 0u) {
+              go = false;  // not published yet: read again from here
+            } else {
+              excl += v[i] & OS_VALUE_MASK;
+              used = i + 1;
+              if (kind == 2u) {
+                found = true;
+                go = false;
+              }
+            }
+          }
+        }
+        if (found) break;
+        t -= used;
+        if (used < OS_WINDOW && t >= 0) {
+          // give up: this tile's offsets come from a partial prefix (never
+          // above the true one, so its writes stay inside [0, n)); the
+          // results are invalid and the host reports it
+          if (++spins > spin_limit) {
+            atomicOr(err, 2u);
+            break;
+          }
+          if (spins > 64) __nanosleep(64);
+        }
+      }
+      *reinterpret_cast<volatile unsigned long long *>(st) = os_word(epoch, 2u, excl + run);
+    }
+    boff[d] = (uint32_t)(digit_base[d] + excl) - lstart[d];
+  } else {
+    boff[d] = offsets[(int64_t)d * nblocks + blk] - lstart[d];
   }
   __syncthreads();
   // ... then consecutive threads write consecutive slots of each digit run
   const int nloc = (int)min((int64_t)RS_TILE, n - (int64_t)blk * RS_TILE);
   for (int i = threadIdx.x; i < nloc; i += RS_THREADS) {
     const uint32_t k = skey[i];
-    const uint32_t d = (k >> shift) & mask;
-    const uint32_t dst = boff[d] + (uint32_t)i - lstart[d];
+    const uint32_t dst = boff[(k >> shift) & mask] + (uint32_t)i;
     if (keys_out) keys_out[dst] = k;
     vals_out[dst] = sval[i];
   }
