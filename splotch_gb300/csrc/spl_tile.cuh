@@ -3,8 +3,8 @@
 //
 // A tile's particle list is streamed through shared memory B entries at a
 // time.  Each entry is staged once per tile: tile-local position, Gaussian
-// width, clipped bounding box, colour, and the exact column runs of the
-// footprint inside the tile, decided as the reference decides coverage
+// width, colour, the exact column runs of the footprint inside the tile and
+// the rows they cover, decided as the reference decides coverage
 // (splotch/splotch_host.cc:580-606: tile-local coordinates, truncating int
 // conversion, the column run y in [int(py-dy+1), int(py+dy+1)) with
 // dy = sqrt(r^2 - dx^2)), in non-contracted float arithmetic.
@@ -25,7 +25,8 @@ struct Stage {
   float4 e12[B];   // e1, e1, e2, e2                (negated when additive)
   float4 q01[B];   // q0, q0, q1, q1 (q = e/(e+grayabsorb); negated on request)
   float2 q2[B];    // q2, q2
-  uint32_t bb[B];  // clipped bounding box minx | maxx<<8 | miny<<16 | maxy<<24
+  uint32_t bb[B];  // minx | maxx<<8 | miny<<16 | maxy<<24: the clipped bounding box's
+                   // columns, the covered rows (0: none covered)
 };
 
 // Run-table row length: T rounded up to whole 8-pixel items, so that every
@@ -57,8 +58,6 @@ __device__ __forceinline__ uint32_t stage_entry(Stage<B> &S, uint16_t *srun, int
     const float sigma = fmul(a.h2sigma, p.z);
     const float stp = fdiv(-1.f, fmul(sigma, sigma));
     if (minx < maxx && miny < maxy) {
-      bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((uint32_t)miny << 16) |
-           ((uint32_t)maxy << 24);
       uint16_t *run = srun + slot * RS;
       uint4 *row16 = reinterpret_cast<uint4 *>(run);
       for (int i = 0; i < RS / 8; ++i) row16[i] = make_uint4(0u, 0u, 0u, 0u);
@@ -70,6 +69,18 @@ __device__ __forceinline__ uint32_t stage_entry(Stage<B> &S, uint16_t *srun, int
         const int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
         run[x] = (uint16_t)(lo | (max(hi - lo, 0) << 8));
       }
+      // The rows the particle covers.  Every step from |dx| to the run is
+      // monotone, so a column nearer the centre holds the runs of the columns
+      // beyond it: the union of all runs is the longer run of the two columns
+      // next to posx (clamped to the box).  A warp whose rows it misses gets
+      // no hit; the columns stay those of the bounding box.
+      const int xa = min(max(f2i(floorf(posx)), minx), maxx - 1);
+      const int xb = min(xa + 1, maxx - 1);
+      const uint32_t ra = run[xa], rb = run[xb];
+      const uint32_t rc = (rb >> 8) > (ra >> 8) ? rb : ra;
+      if ((rc >> 8) > 0u)
+        bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((rc & 255u) << 16) |
+             (((rc & 255u) + (rc >> 8)) << 24);
     }
     const float s2 = stp * kLog2e;
     S.pxy[slot] = make_float4(posx, posx, posy, posy);
