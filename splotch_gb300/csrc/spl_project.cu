@@ -384,7 +384,7 @@ __device__ __forceinline__ void dense_block(const L &load, int64_t n, const Proj
                                             uint32_t *s_list, uint32_t *s_cnt);
 
 template <class L>
-__global__ void __launch_bounds__(256) k_project_dense(L load, int64_t n, ProjConst c,
+__global__ void __launch_bounds__(256, 4) k_project_dense(L load, int64_t n, ProjConst c,
                                                        const uint32_t *__restrict__ flags,
                                                        const uint32_t *__restrict__ word_off,
                                                        ProjectOut o) {
@@ -403,12 +403,10 @@ __device__ __forceinline__ void dense_block(const L &load, int64_t n, const Proj
                                             uint32_t *s_list, uint32_t *s_cnt) {
   const int64_t nwords = (n + 31) / 32;
   const int nw = (int)min((int64_t)DW, nwords - w0);
-  uint32_t f = 0;
-  if ((int)threadIdx.x < nw) f = __ldg(flags + w0 + threadIdx.x);
-  if (threadIdx.x < DW) s_cnt[threadIdx.x] = __popc(f);
-  __syncthreads();
   if ((int)threadIdx.x < nw) {  // expand word t's set bits at its local offset
+    uint32_t f = __ldg(flags + w0 + threadIdx.x);
     uint32_t pos = __ldg(word_off + w0 + threadIdx.x) - __ldg(word_off + w0);
+    if ((int)threadIdx.x == nw - 1) s_cnt[0] = pos + (uint32_t)__popc(f);  // the block's count
     const int64_t ibase = (w0 + threadIdx.x) * 32;
     while (f) {
       const int b = __ffs(f) - 1;
@@ -416,9 +414,8 @@ __device__ __forceinline__ void dense_block(const L &load, int64_t n, const Proj
       s_list[pos++] = (uint32_t)(ibase + b);
     }
   }
-  uint32_t nloc = 0;
-  for (int k = 0; k < nw; ++k) nloc += s_cnt[k];
   __syncthreads();
+  const uint32_t nloc = nw > 0 ? s_cnt[0] : 0u;
   const uint32_t base = nw > 0 ? __ldg(word_off + w0) : 0u;
   for (uint32_t k = threadIdx.x; k < nloc; k += blockDim.x) {
     const uint32_t i = s_list[k];
