@@ -364,7 +364,7 @@ __device__ __forceinline__ void flags_word(const L &load, int64_t n, const ProjC
 }
 
 template <class L>
-__global__ void __launch_bounds__(256) k_project_flags(L load, int64_t n, ProjConst c,
+__global__ void __launch_bounds__(256, 5) k_project_flags(L load, int64_t n, ProjConst c,
                                                        uint32_t *__restrict__ flags,
                                                        uint32_t *err) {
   const int lane = threadIdx.x & 31;
