@@ -104,62 +104,125 @@ __global__ void k_compose_order(const uint32_t *__restrict__ perm_ord, uint32_t 
     order[s] = s < cap_add ? (uint32_t)s : cap_add + perm_ord[s - cap_add];
 }
 
-// Each thread takes kEmitUnroll records per step (a grid stride apart) and
-// issues their scattered loads together, as k_emit_narrow does.
-constexpr int kEmitUnroll = 4;
-
+// One warp per 32 consecutive visiting positions, the cells of its narrow
+// records dealt to the lanes 32 at a time, as k_emit_narrow does for one
+// frame; each record brings its frame's tiling and global tile base.  A
+// record whose slots pass the capacity is not dealt: it raises the status bit
+// and turns its slots below the capacity into sentinels (the render is redone
+// after a re-plan).
 __global__ void __launch_bounds__(256) k_emit_batch_narrow(
     const float4 *__restrict__ pos, const uint32_t *__restrict__ count,
     const uint32_t *__restrict__ order, const uint64_t *__restrict__ off, int64_t n,
     const uint32_t *__restrict__ frame, const FrameTile *__restrict__ ft, uint64_t cap,
     uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval, uint32_t *__restrict__ wide_list,
     uint32_t *__restrict__ wide_n, uint32_t *status) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s0 < n;
-       s0 += stride * kEmitUnroll) {
-    uint32_t c[kEmitUnroll], i[kEmitUnroll], fr[kEmitUnroll];
-    uint64_t o[kEmitUnroll];
-    float4 p[kEmitUnroll];
-#pragma unroll
-    for (int k = 0; k < kEmitUnroll; ++k) {
-      const int64_t s = s0 + k * stride;
-      c[k] = s < n ? __ldg(count + s) : 0u;
-      o[k] = s < n ? __ldg(off + s) : 0u;
-      i[k] = s < n ? (order ? __ldg(order + s) : (uint32_t)s) : 0u;
-    }
-#pragma unroll
-    for (int k = 0; k < kEmitUnroll; ++k) {
-      if (c[k] > 0 && c[k] <= (uint32_t)kWide && o[k] + c[k] <= cap) {
-        p[k] = __ldg(pos + i[k]);
-        fr[k] = __ldg(frame + i[k]);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < kEmitUnroll; ++k) {
-      const int64_t s = s0 + k * stride;
-      if (c[k] == 0) continue;
-      if (o[k] + c[k] > cap) {
-        // over capacity: this render is redone after a re-plan; the slots it
-        // would have used below the capacity become sentinels (sorted last,
-        // never read as entries)
+  __shared__ uint32_t cpre[256 / 32][32];  // per warp: exclusive cell prefix of its lanes
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const uint32_t lt = (1u << lane) - 1u;
+  const int64_t nchunk = (n + 31) / 32;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t ch = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; ch < nchunk;
+       ch += nwarp) {
+    const int64_t s = ch * 32 + lane;
+    const uint32_t c = s < n ? __ldg(count + s) : 0u;
+    const uint64_t o = s < n ? __ldg(off + s) : 0u;
+    const uint32_t i = s < n ? (order ? __ldg(order + s) : (uint32_t)s) : 0u;
+    bool narrow = false;
+    if (c > 0u) {
+      if (o + c > cap) {
         atomicOr(status, 2u);
-        for (uint64_t q = o[k]; q < cap && q < o[k] + c[k]; ++q) {
+        for (uint64_t q = o; q < cap && q < o + c; ++q) {
           tkey[q] = 0xffffffffu;
           tval[q] = 0u;
         }
-        continue;
-      }
-      if (c[k] > (uint32_t)kWide) {
+      } else if (c > (uint32_t)kWide) {
         wide_list[atomicAdd(wide_n, 1u)] = (uint32_t)s;
-        continue;
+      } else {
+        narrow = true;
       }
-      const FrameTile t = ft[fr[k]];
-      const uint32_t ii = i[k];
-      const uint64_t ok = o[k];
-      for_each_tile(p[k].x, p[k].y, p[k].z, t.g, [&](int tile, int j) {
-        tkey[ok + j] = t.tile_base + (uint32_t)tile;
-        tval[ok + j] = ii;
-      });
+    }
+    float px = 0.f, py = 0.f, sumsq = 0.f, cmid0 = 0.f;
+    int minx = 0, miny = 0, wy = 1, T = 1, ncx = 0;
+    uint32_t cells = 0, magic = 0, base = 0;
+    if (narrow) {
+      const float4 p = __ldg(pos + i);
+      const FrameTile t = ft[__ldg(frame + i)];
+      px = p.x;
+      py = p.y;
+      T = t.g.T;
+      ncx = t.g.ncx;
+      cmid0 = t.g.cmid0;
+      base = t.tile_base;
+      const float rfacr = fmul(0.75f, p.z);
+      minx = max(0, f2i(fadd(fsub(px, rfacr), 1.f)) / T);
+      const int maxx = min(t.g.ncx - 1, f2i(fadd(px, rfacr)) / T);
+      miny = max(0, f2i(fadd(fsub(py, rfacr), 1.f)) / T);
+      const int maxy = min(t.g.ncy - 1, f2i(fadd(py, rfacr)) / T);
+      const float rs = fadd(t.g.rcell, rfacr);
+      sumsq = fmul(rs, rs);
+      wy = maxy - miny + 1;
+      cells = (uint32_t)((maxx - minx + 1) * wy);
+      magic = wy > 1 ? 0xffffffffu / (uint32_t)wy + 1u : 0u;  // q / wy = umulhi(q, magic)
+    }
+    uint32_t cin = cells, nin = narrow ? c : 0u;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t t0 = __shfl_up_sync(0xffffffffu, cin, d);
+      const uint32_t t1 = __shfl_up_sync(0xffffffffu, nin, d);
+      if (lane >= d) {
+        cin += t0;
+        nin += t1;
+      }
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, cin, 31);
+    const uint32_t nexcl = nin - (narrow ? c : 0u);
+    __syncwarp();
+    cpre[w][lane] = cin - cells;
+    __syncwarp();
+    uint32_t carry = 0;
+    for (uint32_t k0 = 0; k0 < total; k0 += 32) {
+      const uint32_t k = k0 + (uint32_t)lane;
+      int l = 0;
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1)
+        if (cpre[w][l + step] <= k) l += step;
+      const int lminx = __shfl_sync(0xffffffffu, minx, l);
+      const int lminy = __shfl_sync(0xffffffffu, miny, l);
+      const int lwy = __shfl_sync(0xffffffffu, wy, l);
+      const int lT = __shfl_sync(0xffffffffu, T, l);
+      const int lncx = __shfl_sync(0xffffffffu, ncx, l);
+      const uint32_t lmag = __shfl_sync(0xffffffffu, magic, l);
+      const float lpx = __shfl_sync(0xffffffffu, px, l);
+      const float lpy = __shfl_sync(0xffffffffu, py, l);
+      const float lsq = __shfl_sync(0xffffffffu, sumsq, l);
+      const float lcm = __shfl_sync(0xffffffffu, cmid0, l);
+      const uint32_t lbase = __shfl_sync(0xffffffffu, base, l);
+      const uint32_t lc = __shfl_sync(0xffffffffu, c, l);
+      const uint32_t lnex = __shfl_sync(0xffffffffu, nexcl, l);
+      const uint32_t li = __shfl_sync(0xffffffffu, i, l);
+      const uint32_t lolo = __shfl_sync(0xffffffffu, (uint32_t)o, l);
+      const uint32_t lohi = __shfl_sync(0xffffffffu, (uint32_t)(o >> 32), l);
+      const uint32_t q = k - cpre[w][l];
+      const uint32_t qx = lwy > 1 ? __umulhi(q, lmag) : q;
+      const int ix = lminx + (int)qx;
+      const int iy = lminy + (int)(q - qx * (uint32_t)lwy);
+      bool pass = false;
+      if (k < total) {  // the test of for_each_tile, operation for operation
+        const float cx = fadd(lcm, (float)(ix * lT));
+        const float dx = fsub(lpx, cx);
+        const float dx2 = fmul(dx, dx);
+        const float cy = fadd(lcm, (float)(iy * lT));
+        const float dy = fsub(lpy, cy);
+        pass = fadd(dx2, fmul(dy, dy)) < lsq;
+      }
+      const uint32_t b = __ballot_sync(0xffffffffu, pass);
+      const uint32_t j = carry + __popc(b & lt) - lnex;
+      if (pass && j < lc) {
+        const uint64_t slot = (((uint64_t)lohi << 32) | lolo) + j;
+        tkey[slot] = lbase + (uint32_t)(iy * lncx + ix);
+        tval[slot] = li;
+      }
+      carry += __popc(b);
     }
   }
 }
