@@ -99,6 +99,15 @@ __device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
 // expm1(-u) for u >= 0 on a pair, lane for lane the value of expm1_neg(-u):
 // the same Taylor polynomial (its coefficients negated with u) below 0.05 and
 // ex2(-u*log2e)-1 above.
+// The Taylor form of expm1_neg2 alone (u < 0.05 in every component).
+__device__ __forceinline__ F2 expm1_neg2_poly(F2 u) {
+  F2 p = fma2(u, f2(1.f / 24.f), f2(-1.f / 6.f));
+  p = fma2(p, u, f2(0.5f));
+  p = fma2(p, u, f2(-1.f));
+  return mul2(p, u);
+}
+constexpr float kExpm1TaylorCut = 0.05f;
+
 __device__ __forceinline__ F2 expm1_neg2(F2 u) {
   F2 p = fma2(u, f2(1.f / 24.f), f2(-1.f / 6.f));
   p = fma2(p, u, f2(0.5f));

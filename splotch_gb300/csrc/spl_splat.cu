@@ -162,31 +162,67 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
               continue;
             const bool in0 = covered(run, col[2 * p], row[2 * p]);
             const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
-            if (in0 || in1) {
-              // a pixel the particle does not cover gets att = 0: its update is
-              // the identity in every mode
+            // a pixel the particle does not cover gets att = 0: its update is
+            // the identity in every mode
+            if (ADD) {
+              if (in0 || in1) {
+                const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
+                const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
+                const F2 arg = mul2(f2(es.z, es.w), fma2(dy, dy, mul2(dx, dx)));
+                const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
+                acc[p][0] = fma2(f2(es.x, es.y), att, acc[p][0]);  // e negated
+                acc[p][1] = fma2(f2(e12.x, e12.y), att, acc[p][1]);
+                acc[p][2] = fma2(f2(e12.z, e12.w), att, acc[p][2]);
+              }
+            } else if (AUX) {
+              if (in0 || in1) {  // frames kept for the adjoint (register-bound: no vote)
+                const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
+                const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
+                const F2 arg = mul2(f2(es.z, es.w), fma2(dy, dy, mul2(dx, dx)));
+                const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
+                const F2 e[3] = {f2(es.x, es.y), f2(e12.x, e12.y), f2(e12.z, e12.w)};
+                const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                  const F2 u = mul2(e[c], att);
+                  od[AUX ? p : 0][c] = add2(od[AUX ? p : 0][c], u);
+                  const F2 m = expm1_neg2(u);
+                  if (!FTB) {
+                    acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
+                  } else {
+                    const F2 nw = mul2(tr[p][c], m);
+                    acc[p][c] = fma2(nw, q[c], acc[p][c]);
+                    tr[p][c] = add2(tr[p][c], nw);
+                  }
+                }
+              }
+            } else {
+              // every lane updates (uncovered pixels with att = 0), so that the
+              // warp can vote: when all its optical depths e*att are below the
+              // Taylor cut, expm1 takes the polynomial alone (the same values
+              // the per-component choice gives)
               const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
               const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
               const F2 arg = mul2(f2(es.z, es.w), fma2(dy, dy, mul2(dx, dx)));
               const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
               const F2 e[3] = {f2(es.x, es.y), f2(e12.x, e12.y), f2(e12.z, e12.w)};
               const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
+              F2 u[3];
+#pragma unroll
+              for (int c = 0; c < 3; ++c) u[c] = mul2(e[c], att);
+              const float um = fmaxf(fmaxf(fmaxf(f2lo(u[0]), f2hi(u[0])), fmaxf(f2lo(u[1]), f2hi(u[1]))),
+                                     fmaxf(f2lo(u[2]), f2hi(u[2])));
+              const bool poly = __all_sync(0xffffffffu, um < kExpm1TaylorCut);
 #pragma unroll
               for (int c = 0; c < 3; ++c) {
-                if (ADD) {
-                  acc[p][c] = fma2(e[c], att, acc[p][c]);  // e negated
+                const F2 m = poly ? expm1_neg2_poly(u[c]) : expm1_neg2(u[c]);
+                if (!FTB) {
+                  acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
                 } else {
-                  const F2 u = mul2(e[c], att);
-                  if (AUX) od[AUX ? p : 0][c] = add2(od[AUX ? p : 0][c], u);
-                  const F2 m = expm1_neg2(u);
-                  if (!FTB) {
-                    acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
-                  } else {
-                    // -w = Tr*expm1(-e*att); C += w*q (q negated); Tr -= w
-                    const F2 nw = mul2(tr[p][c], m);
-                    acc[p][c] = fma2(nw, q[c], acc[p][c]);
-                    tr[p][c] = add2(tr[p][c], nw);
-                  }
+                  // -w = Tr*expm1(-e*att); C += w*q (q negated); Tr -= w
+                  const F2 nw = mul2(tr[p][c], m);
+                  acc[p][c] = fma2(nw, q[c], acc[p][c]);
+                  tr[p][c] = add2(tr[p][c], nw);
                 }
               }
             }
