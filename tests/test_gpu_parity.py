@@ -128,6 +128,32 @@ def test_edge_cases(name, mode, renderer, port):
     assert_parity(g, o)
 
 
+@pytest.mark.parametrize("tile", [8, 16, 32])
+@pytest.mark.parametrize("mode", ["add", "ftb"])
+def test_bins_across_footprint_sizes(tile, mode, renderer, port):
+    """Bin emission deals each warp's candidate tiles across its lanes and hands
+    particles of more than 64 tiles to the warp-per-particle path: footprints
+    from one tile to well past 64 (both paths in every warp), partial tiles at
+    the right and bottom edges, three tile sizes; bins bit-exact."""
+    rng = np.random.default_rng(11 + tile)
+    xres, yres = (203, 137) if tile < 32 else (403, 297)  # more than 64 tiles either way
+    prm, rc = _edge_setup(xres=xres, yres=yres, tile=tile, a_eq_e=(mode == "add"),
+                          gpu_order="ftb")
+    # radius in pixels reaching ~1 to ~100 tiles at this tile size
+    rmax = 7.0 * tile
+    n = 600
+    specs = [(float(rng.uniform(-10, xres + 10)), float(rng.uniform(-10, yres + 10)),
+              float(rmax * rng.random() ** 2 + 0.3), float(rng.uniform(-20, 20)),
+              float(rng.uniform(0.2, 1.5)), float(rng.random())) for _ in range(n)]
+    p = _particles(prm, specs)
+    g = gpu_frame(renderer, prm, rc, p)
+    o = oracle_frame(port, prm, rc, p, fp32=False)
+    assert_parity(g, o)
+    counts = np.diff(o.tile_start.astype(np.int64))
+    assert g.stats["n_wide"] > 0, "no particle took the many-tile path"
+    assert len(o.entries) > n, counts.max()
+
+
 def test_zmin_and_all_culled(renderer, port):
     # both particles sit at depth -z = 100 and 99.5 in camera space: zmin=100.5
     # culls them (splotch_host.cc:123, cull when -z <= zmin)
