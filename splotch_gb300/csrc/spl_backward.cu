@@ -99,7 +99,7 @@ __global__ void k_adj_seg_count(const uint32_t *__restrict__ tile_start, int64_t
 // AdjArgs::seg_off); the forward's pixel layout: 8x4 items, WX x WY items per
 // warp, pixels processed in pairs (items 2p, 2p+1) with packed arithmetic.
 template <int NT, int WX, int WY, int B, bool ADD>
-__global__ void __launch_bounds__(NT) k_splat_adj(AdjArgs a) {
+__global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(AdjArgs a) {
   constexpr int K = WX * WY;
   constexpr int NP = (K + 1) / 2;
   constexpr int NO = ADD ? 1 : NP;  // ordered-only state
