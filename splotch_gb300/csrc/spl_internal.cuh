@@ -257,6 +257,53 @@ __device__ __forceinline__ int for_each_tile(float x, float y, float r, const Ti
   return cnt;
 }
 
+// The number of tiles for_each_tile visits, without visiting each one.  In a
+// column the passing rows are one interval around the row nearest y (cy rises
+// with iy, |dy| has one minimum, and every rounded step of the test is
+// monotone), found by binary search with the same test; rectangles of up to 64
+// cells are walked as for_each_tile walks them.
+__device__ __forceinline__ int count_tiles(float x, float y, float r, const Tiling &g) {
+  const int T = g.T;
+  const float rfacr = fmul(0.75f, r);
+  const int minx = max(0, f2i(fadd(fsub(x, rfacr), 1.f)) / T);
+  const int maxx = min(g.ncx - 1, f2i(fadd(x, rfacr)) / T);
+  const int miny = max(0, f2i(fadd(fsub(y, rfacr), 1.f)) / T);
+  const int maxy = min(g.ncy - 1, f2i(fadd(y, rfacr)) / T);
+  if (maxx < minx || maxy < miny) return 0;
+  if ((maxx - minx + 1) * (maxy - miny + 1) <= 64) return for_each_tile(x, y, r, g, [](int, int) {});
+  const float rs = fadd(g.rcell, rfacr);
+  const float sumsq = fmul(rs, rs);
+  auto dy2 = [&](int iy) {
+    const float dy = fsub(y, fadd(g.cmid0, (float)(iy * T)));
+    return fmul(dy, dy);
+  };
+  // the row nearest y: an estimate, then the smaller of its two candidates' dy^2
+  const int t = (int)floorf((y - g.cmid0) / (float)T);
+  const int ra = min(max(t, miny), maxy), rb = min(max(t + 1, miny), maxy);
+  const int c0 = dy2(rb) < dy2(ra) ? rb : ra;
+  const float d0 = dy2(c0);
+  int cnt = 0;
+  for (int ix = minx; ix <= maxx; ++ix) {
+    const float dx = fsub(x, fadd(g.cmid0, (float)(ix * T)));
+    const float dx2 = fmul(dx, dx);
+    if (!(fadd(dx2, d0) < sumsq)) continue;
+    int lo = miny, hi = c0;  // first passing row
+    while (lo < hi) {
+      const int m = (lo + hi) >> 1;
+      if (fadd(dx2, dy2(m)) < sumsq) hi = m; else lo = m + 1;
+    }
+    const int first = lo;
+    lo = c0;
+    hi = maxy;  // last passing row
+    while (lo < hi) {
+      const int m = (lo + hi + 1) >> 1;
+      if (fadd(dx2, dy2(m)) < sumsq) lo = m; else hi = m - 1;
+    }
+    cnt += lo - first + 1;
+  }
+  return cnt;
+}
+
 // ---------------------------------------------------------------------------
 // Launch wrappers (defined in the .cu files).
 struct ProjectOut {

@@ -283,7 +283,7 @@ __device__ __forceinline__ POut project_core(const ProjConst &c, const PIn &in, 
   o.count = 0;
   if (active) {
     Tiling g{c.T, c.ncx, c.ncy, c.rcell, c.cmid0};
-    o.count = (uint32_t)for_each_tile(x, y, r, g, [](int, int) {});
+    o.count = (uint32_t)count_tiles(x, y, r, g);
   }
   switch (c.sort_type) {
     case 1: o.key = fkey_asc(z); break;    // zcmp: z ascending
