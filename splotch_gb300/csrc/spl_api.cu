@@ -629,7 +629,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   if (ne > 0) {
     spl::launch_emit(as<float4>(c->pos_c), count_seq, order, off, na, g,
                      as<uint32_t>(c->tkey), as<uint32_t>(c->tval), as<uint32_t>(c->wide_list),
-                     d_wide_n, s);
+                     d_wide_n, d_err, s);
     launches += 2;
     const int tb = spl::bits_for(ntiles);
     if (tb > 0) {
@@ -765,6 +765,9 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   const uint32_t err = words[0];
   if (err & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
   if (err & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
+  if (err & 8u) return fail(SPL_ERR_CAPACITY, "the compacted particle arrays overflowed");
+  if (err & 16u)
+    return fail(SPL_ERR_CAPACITY, "bin emission found more tiles than a particle's count");
   c->stats.n_fallback = words[2];
   c->stats.n_wide = words[1];
 

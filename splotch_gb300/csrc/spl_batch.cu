@@ -221,6 +221,8 @@ __global__ void __launch_bounds__(256) k_emit_batch_narrow(
         const uint64_t slot = (((uint64_t)lohi << 32) | lolo) + j;
         tkey[slot] = lbase + (uint32_t)(iy * lncx + ix);
         tval[slot] = li;
+      } else if (pass) {
+        atomicOr(status, 4u);  // more passing tiles than counted: reported, not stored
       }
       carry += __popc(b);
     }
@@ -907,6 +909,8 @@ spl_status check_status(spl_batch *b, bool &overflow) {
   overflow = (h[0] & 3u) != 0 || (h[4] & 8u) != 0;
   if (h[4] & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
   if (h[4] & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
+  if (h[0] & 4u)
+    return fail(SPL_ERR_CAPACITY, "bin emission found more tiles than a record's count");
   return SPL_OK;
 }
 

@@ -30,8 +30,9 @@ constexpr int kWideTiles = 64;
 // whatever the mix of footprints, and a warp's stores are contiguous.
 //
 // A particle's passing cells fill exactly its slots [off, off + count): the
-// count came from the same test (for_each_tile) in the same arithmetic; a
-// store is also checked against the particle's count before it is made.
+// count came from the same test in the same arithmetic; a store is also
+// checked against the particle's count before it is made (one past it sets
+// bit 4 (16) of *err instead).
 __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ pos,
                                                      const uint32_t *__restrict__ count,
                                                      const uint32_t *__restrict__ order,
@@ -40,7 +41,8 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
                                                      uint32_t *__restrict__ tkey,
                                                      uint32_t *__restrict__ tval,
                                                      uint32_t *__restrict__ wide_list,
-                                                     uint32_t *__restrict__ wide_n) {
+                                                     uint32_t *__restrict__ wide_n,
+                                                     uint32_t *err) {
   __shared__ uint32_t cpre[256 / 32][33];  // per warp: exclusive cell prefix of its lanes
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const uint32_t lt = (1u << lane) - 1u;
@@ -131,6 +133,8 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
         const uint64_t slot = (((uint64_t)lohi << 32) | lolo) + j;
         tkey[slot] = (uint32_t)(iy * g.ncx + ix);
         tval[slot] = li;
+      } else if (pass) {
+        atomicOr(err, 16u);  // more passing tiles than counted: reported, not stored
       }
       carry += __popc(b);
     }
@@ -241,11 +245,11 @@ int grid_for(int64_t n, int per_block) {
 
 void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order,
                  const uint64_t *off, int64_t n, Tiling g, uint32_t *tkey, uint32_t *tval,
-                 uint32_t *wide_list, uint32_t *wide_n, cudaStream_t s) {
+                 uint32_t *wide_list, uint32_t *wide_n, uint32_t *err, cudaStream_t s) {
   if (n <= 0) return;
   cudaMemsetAsync(wide_n, 0, sizeof(uint32_t), s);
   k_emit_narrow<<<grid_for(n, 256), 256, 0, s>>>(pos, count, order, off, n, g, tkey, tval,
-                                                 wide_list, wide_n);
+                                                 wide_list, wide_n, err);
   k_emit_wide<<<152 * 4, 256, 0, s>>>(pos, order, off, wide_list, wide_n, g, tkey, tval);
 }
 

@@ -459,7 +459,7 @@ void launch_gather_u32(const uint32_t *src, const uint32_t *perm, int64_t n, uin
                        cudaStream_t s, int64_t nsrc = 0, uint32_t *err = nullptr);
 void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order,
                  const uint64_t *off, int64_t n, Tiling g, uint32_t *tkey, uint32_t *tval,
-                 uint32_t *wide_list, uint32_t *wide_n, cudaStream_t s);
+                 uint32_t *wide_list, uint32_t *wide_n, uint32_t *err, cudaStream_t s);
 void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
                         uint32_t *tile_start, cudaStream_t s);
 // 8-bit longest-first scheduling key per tile (sort ascending with
