@@ -232,8 +232,10 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
       if (FTB) {
         // a pixel is done once each channel's transmittance is below the
         // absolute cut or below ftb_rel times the colour it has composited
-        // (acc); frames kept for the adjoint use the absolute cut alone
-        const float rel = AUX ? 0.f : a.ftb_rel;
+        // (acc).  Frames kept for the adjoint stop the same way: the list
+        // position where a warp stopped is kept, and the adjoint walks exactly
+        // the fragments composited before it.
+        const float rel = a.ftb_rel;
         bool mine_done = true;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
