@@ -43,11 +43,6 @@ struct spl_context {
   };
   RayKey ray_key{};
   spl::RayFrame *rays = nullptr;
-  // pinned staging of the palette tables, so that their upload needs no host
-  // wait; pal_ev marks the end of the last upload's copies
-  void *pal_host = nullptr;
-  size_t pal_host_cap = 0;
-  cudaEvent_t pal_ev = nullptr;
   int debug_flags = 0;  // SPL_DEBUG_* bits
   bool differentiable = false;  // ordered forwards keep SplatArgs::aux
   int split_mode = SPL_SPLIT_ADDITIVE;  // which frames have heavy tiles cut into segments
@@ -399,8 +394,6 @@ spl_status spl_context_destroy(spl_context *c) {
     if (b.p) cudaFree(b.p);
   for (auto &e : c->ev)
     if (e) cudaEventDestroy(e);
-  if (c->pal_ev) cudaEventDestroy(c->pal_ev);
-  if (c->pal_host) cudaFreeHost(c->pal_host);
   if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
   for (auto &q : c->pf) {
     if (q.aos.p) cudaFree(q.aos.p);
@@ -484,36 +477,18 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   if ((st = ensure(c->pal_thr, (npal + 1) * 4)) || (st = ensure(c->pal_xff, (npal + 1) * 8)) ||
       (st = ensure(c->pal_invff, (npal + 1) * 8)))
     return st;
-  {  // through the pinned staging buffer, after the previous upload's copies
-    const size_t sz[5] = {(size_t)(npal + 1) * 8, (size_t)(npal + 1) * 12,
-                          (size_t)(npal + 1) * 4, (size_t)(npal + 1) * 8,
-                          (size_t)(npal + 1) * 8};
-    const void *src[5] = {fs.pal_x.data(), fs.pal_rgb.data(), fs.thr.data(), fs.xff.data(),
-                          fs.invff.data()};
-    void *dst[5] = {c->pal_x.p, c->pal_rgb.p, c->pal_thr.p, c->pal_xff.p, c->pal_invff.p};
-    size_t total = 0;
-    for (size_t b : sz) total += (b + 15) & ~(size_t)15;
-    if (!c->pal_ev) SPL_CK(cudaEventCreateWithFlags(&c->pal_ev, cudaEventDisableTiming));
-    SPL_CK(cudaEventSynchronize(c->pal_ev));
-    if (total > c->pal_host_cap) {
-      if (c->pal_host) cudaFreeHost(c->pal_host);
-      c->pal_host = nullptr;
-      c->pal_host_cap = 0;
-      if (cudaMallocHost(&c->pal_host, total) != cudaSuccess) {
-        cudaGetLastError();
-        c->pal_host = nullptr;
-        return fail(SPL_ERR_ALLOC, "pinned host memory for the palette tables");
-      }
-      c->pal_host_cap = total;
-    }
-    uint8_t *h = static_cast<uint8_t *>(c->pal_host);
-    for (int k = 0; k < 5; ++k) {
-      std::memcpy(h, src[k], sz[k]);
-      SPL_CK(cudaMemcpyAsync(dst[k], h, sz[k], cudaMemcpyHostToDevice, s));
-      h += (sz[k] + 15) & ~(size_t)15;
-    }
-    SPL_CK(cudaEventRecord(c->pal_ev, s));
-  }
+  // small copies from pageable memory: they travel in the command stream, not
+  // behind a large copy-engine transfer (a next frame's prefetch) as copies
+  // from pinned memory would
+  SPL_CK(cudaMemcpyAsync(c->pal_x.p, fs.pal_x.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_rgb.p, fs.pal_rgb.data(), (npal + 1) * 12, cudaMemcpyHostToDevice,
+                         s));
+  SPL_CK(cudaMemcpyAsync(c->pal_thr.p, fs.thr.data(), (npal + 1) * 4, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_xff.p, fs.xff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice, s));
+  SPL_CK(cudaMemcpyAsync(c->pal_invff.p, fs.invff.data(), (npal + 1) * 8, cudaMemcpyHostToDevice,
+                         s));
+  // the host tables live in fs: wait for the copies before anything else
+  SPL_CK(cudaStreamSynchronize(s));
   pc.pal_x = as<double>(c->pal_x);
   pc.pal_rgb = as<float>(c->pal_rgb);
   pc.pal_thr = as<float>(c->pal_thr);
