@@ -174,28 +174,6 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
                 acc[p][1] = fma2(f2(e12.x, e12.y), att, acc[p][1]);
                 acc[p][2] = fma2(f2(e12.z, e12.w), att, acc[p][2]);
               }
-            } else if (AUX) {
-              if (in0 || in1) {  // frames kept for the adjoint (register-bound: no vote)
-                const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
-                const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
-                const F2 arg = mul2(f2(es.z, es.w), fma2(dy, dy, mul2(dx, dx)));
-                const F2 att = f2(in0 ? ex2(f2lo(arg)) : 0.f, in1 ? ex2(f2hi(arg)) : 0.f);
-                const F2 e[3] = {f2(es.x, es.y), f2(e12.x, e12.y), f2(e12.z, e12.w)};
-                const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                  const F2 u = mul2(e[c], att);
-                  od[AUX ? p : 0][c] = add2(od[AUX ? p : 0][c], u);
-                  const F2 m = expm1_neg2(u);
-                  if (!FTB) {
-                    acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
-                  } else {
-                    const F2 nw = mul2(tr[p][c], m);
-                    acc[p][c] = fma2(nw, q[c], acc[p][c]);
-                    tr[p][c] = add2(tr[p][c], nw);
-                  }
-                }
-              }
             } else {
               // every lane updates (uncovered pixels with att = 0), so that the
               // warp can vote: when all its optical depths e*att are below the
@@ -215,6 +193,7 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
               const bool poly = __all_sync(0xffffffffu, um < kExpm1TaylorCut);
 #pragma unroll
               for (int c = 0; c < 3; ++c) {
+                if (AUX) od[AUX ? p : 0][c] = add2(od[AUX ? p : 0][c], u[c]);
                 const F2 m = poly ? expm1_neg2_poly(u[c]) : expm1_neg2(u[c]);
                 if (!FTB) {
                   acc[p][c] = fma2(m, sub2(acc[p][c], q[c]), acc[p][c]);
