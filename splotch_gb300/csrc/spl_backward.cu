@@ -296,8 +296,11 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
               continue;
             const bool in0 = covered(run, col[2 * p], row[2 * p]);
             const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
-            if (!(in0 || in1)) continue;
-            any = true;
+            // additive: lanes without a covered pixel skip; ordered: every lane
+            // runs the terms (they vanish), so that the warp can vote on the
+            // Taylor range of expm1 below
+            if (ADD && !(in0 || in1)) continue;
+            any = any || in0 || in1;
             // an uncovered pixel of the pair gets att = 0 (and g = 0 outside
             // the tile): its terms vanish
             const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
@@ -317,16 +320,23 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
               const F2 q[3] = {f2(q01.x, q01.y), f2(q01.z, q01.w), f2(q2.x, q2.y)};
               const F2 nw[3] = {f2(nw01.x, nw01.y), f2(nw01.z, nw01.w), f2(nw2.x, nw2.y)};
               gatt = f2(0.f);
+              F2 u[3];
+#pragma unroll
+              for (int c = 0; c < 3; ++c) u[c] = mul2(e[c], att);  // u as the forward forms it
+              const float um =
+                  fmaxf(fmaxf(fmaxf(f2lo(u[0]), f2hi(u[0])), fmaxf(f2lo(u[1]), f2hi(u[1]))),
+                        fmaxf(f2lo(u[2]), f2hi(u[2])));
+              const bool poly = __all_sync(0xffffffffu, um < kExpm1TaylorCut);
 #pragma unroll
               for (int c = 0; c < 3; ++c) {
                 F2 &sbc = sb[ADD ? 0 : p][c], &nbgc = nbg[ADD ? 0 : p][c];
-                // u as the forward forms it; transmittance in front of the
-                // particle from the stored optical depth, Tr = exp(-(od - sb))
-                const F2 u = mul2(e[c], att);
-                sbc = add2(sbc, u);
+                // transmittance in front of the particle from the stored
+                // optical depth, Tr = exp(-(od - sb))
+                sbc = add2(sbc, u[c]);
                 const F2 ta = mul2(sub2(sbc, od[ADD ? 0 : p][c]), f2(kLog2e));
                 const F2 trm = f2(ex2(f2lo(ta)), ex2(f2hi(ta)));
-                const F2 nwt = mul2(trm, expm1_neg2(u));  // -(Tr - Tr')
+                const F2 nwt =
+                    mul2(trm, poly ? expm1_neg2_poly(u[c]) : expm1_neg2(u[c]));  // -(Tr - Tr')
                 const F2 trn = add2(trm, nwt);            // Tr' = Tr*T
                 // dC/du = q*Tr' - B, dC/dq = Tr - Tr'  (B: composite behind)
                 const F2 ga = mul2(g[p][c], fma2(q[c], trn, nbgc));
