@@ -98,6 +98,9 @@ __global__ void k_adj_seg_count(const uint32_t *__restrict__ tile_start, int64_t
 // One CTA per segment of a tile's list (segments numbered in tile order,
 // AdjArgs::seg_off); the forward's pixel layout: 8x4 items, WX x WY items per
 // warp, pixels processed in pairs (items 2p, 2p+1) with packed arithmetic.
+// The ordered 128-thread form is held to 6 CTAs per SM (80 registers): with
+// heavy tiles cut into segments it is throughput-bound, and more resident
+// warps pay for the few spilled values.  Other forms choose their registers.
 template <int NT, int WX, int WY, int B, bool ADD>
 __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(AdjArgs a) {
   constexpr int K = WX * WY;

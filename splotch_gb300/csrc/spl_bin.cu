@@ -9,10 +9,11 @@
 // stable radix sort by tile id groups them without reordering, which gives the
 // same per-tile order bit-for-bit.
 //
-// Two emission paths: one thread per particle for footprints of up to
-// kWideTiles tiles, and one warp per particle (rows of its tile rectangle
-// spread over the lanes) for wide particles, so a particle covering thousands
-// of tiles does not serialise a whole warp behind one thread.
+// Two emission paths: footprints of up to kWideTiles tiles are dealt across
+// the lanes of a warp (the candidate tiles of its 32 particles laid end to
+// end), and a wide particle gets a warp of its own (rows of its tile rectangle
+// spread over the lanes), so a particle covering thousands of tiles does not
+// hold up the particles beside it.
 #include "spl_internal.cuh"
 
 namespace spl {
