@@ -31,8 +31,11 @@
 // Absorption: back-to-front applies C += expm1(-e*att)*(C - q) in list order
 // (splotch_host.cc:663-665).  Front-to-back visits the list in reverse and
 // accumulates C += Tr*q*(1-T), Tr *= T -- the same sum term by term -- and stops
-// a warp once every pixel's transmittance in all channels is below epsilon,
-// and the tile once every warp has stopped.
+// a warp once every pixel's transmittance in all channels is below epsilon or
+// below ftb_rel times the colour it has composited, and the tile once every
+// warp has stopped.  expm1(-u) is a Taylor polynomial below u = 0.05 and the
+// exponential form above; a warp evaluates only the polynomial when all its
+// fragments of a hit are below the cut (one vote per hit).
 #include "spl_tile.cuh"
 
 namespace spl {
