@@ -95,8 +95,9 @@ typedef struct {
   float ftb_relative;       /* FRONT_TO_BACK also stops a pixel once each channel's
                                transmittance is below ftb_relative times the colour
                                it has composited (1e-5): all that lies behind adds
-                               at most that fraction of the pixel (q <= 1).  Not
-                               applied to frames kept for spl_render_backward. */
+                               at most that fraction of the pixel (q <= 1).  Frames
+                               kept for spl_render_backward stop the same way; the
+                               backward differentiates what they composited. */
 } spl_frame_desc;
 
 /* Particle input.  AoS: aos points at n particle_sim records.  SoA: x..I,
