@@ -231,10 +231,11 @@ __global__ void __launch_bounds__(256) k_emit_batch_narrow(
 
 // One warp per wide record: lane l takes tile rows miny + l, +32, ...
 __global__ void __launch_bounds__(256) k_emit_batch_wide(
-    const float4 *__restrict__ pos, const uint32_t *__restrict__ order,
-    const uint64_t *__restrict__ off, const uint32_t *__restrict__ wide_list,
-    const uint32_t *__restrict__ wide_n, const uint32_t *__restrict__ frame,
-    const FrameTile *__restrict__ ft, uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval) {
+    const float4 *__restrict__ pos, const uint32_t *__restrict__ count,
+    const uint32_t *__restrict__ order, const uint64_t *__restrict__ off,
+    const uint32_t *__restrict__ wide_list, const uint32_t *__restrict__ wide_n,
+    const uint32_t *__restrict__ frame, const FrameTile *__restrict__ ft,
+    uint32_t *__restrict__ tkey, uint32_t *__restrict__ tval, uint32_t *status) {
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -245,6 +246,7 @@ __global__ void __launch_bounds__(256) k_emit_batch_wide(
     const FrameTile t = ft[__ldg(frame + i)];
     const Tiling &g = t.g;
     const uint64_t o = __ldg(off + s);
+    const uint64_t oend = o + __ldg(count + s);  // the record's slots end here
     const float4 p = __ldg(pos + i);
     const int T = g.T;
     const float rfacr = fmul(0.75f, p.z);
@@ -279,8 +281,12 @@ __global__ void __launch_bounds__(256) k_emit_batch_wide(
         for (int ix = minx; ix <= maxx; ++ix) {
           const float dx = fsub(p.x, fadd(g.cmid0, (float)(ix * T)));
           if (fadd(fmul(dx, dx), dy2) < sumsq) {
-            tkey[slot] = t.tile_base + (uint32_t)(iy * g.ncx + ix);
-            tval[slot] = i;
+            if (slot < oend) {
+              tkey[slot] = t.tile_base + (uint32_t)(iy * g.ncx + ix);
+              tval[slot] = i;
+            } else {
+              atomicOr(status, 4u);  // more passing tiles than counted: reported, not stored
+            }
             ++slot;
           }
         }
@@ -818,9 +824,9 @@ spl_status enqueue(spl_batch *b, cudaStream_t s, int splat_class = -1) {
       as<spl::FrameTile>(b->ft), capE, as<uint32_t>(b->tkey), as<uint32_t>(b->tval),
       as<uint32_t>(b->wide_list), status + 1, status);
   spl::k_emit_batch_wide<<<152 * 4, 256, 0, s>>>(
-      as<float4>(b->pos_c), order, off, as<uint32_t>(b->wide_list), status + 1,
+      as<float4>(b->pos_c), count_seq, order, off, as<uint32_t>(b->wide_list), status + 1,
       as<uint32_t>(b->frame_c), as<spl::FrameTile>(b->ft), as<uint32_t>(b->tkey),
-      as<uint32_t>(b->tval));
+      as<uint32_t>(b->tval), status);
   spl::k_fill_tail<<<spl::grid_for(capE), 256, 0, s>>>(as<uint32_t>(b->tkey), off + capA, capE);
   launches += 3;
   spl::radix_sort_pairs(as<uint32_t>(b->tkey), as<uint32_t>(b->tval), as<uint32_t>(b->tkey2),

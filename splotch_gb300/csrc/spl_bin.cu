@@ -148,12 +148,13 @@ __global__ void __launch_bounds__(256) k_emit_narrow(const float4 *__restrict__ 
 // slot range does not matter: the stable tile sort only orders entries of the
 // same tile, and a particle contributes at most one entry per tile.
 __global__ void __launch_bounds__(256) k_emit_wide(const float4 *__restrict__ pos,
+                                                   const uint32_t *__restrict__ count,
                                                    const uint32_t *__restrict__ order,
                                                    const uint64_t *__restrict__ off,
                                                    const uint32_t *__restrict__ wide_list,
                                                    const uint32_t *__restrict__ wide_n,
                                                    Tiling g, uint32_t *__restrict__ tkey,
-                                                   uint32_t *__restrict__ tval) {
+                                                   uint32_t *__restrict__ tval, uint32_t *err) {
   const int lane = threadIdx.x & 31;
   const int64_t warp0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -162,6 +163,7 @@ __global__ void __launch_bounds__(256) k_emit_wide(const float4 *__restrict__ po
     const uint32_t s = wide_list[w];
     const uint32_t i = order ? __ldg(order + s) : s;
     const uint64_t o = __ldg(off + s);
+    const uint64_t oend = o + __ldg(count + s);  // the particle's slots end here
     const float4 p = __ldg(pos + i);
     const int T = g.T;
     const float rfacr = fmul(0.75f, p.z);
@@ -200,8 +202,12 @@ __global__ void __launch_bounds__(256) k_emit_wide(const float4 *__restrict__ po
           const float cx = fadd(g.cmid0, (float)(ix * T));
           const float dx = fsub(p.x, cx);
           if (fadd(fmul(dx, dx), dy2) < sumsq) {
-            tkey[slot] = (uint32_t)(iy * g.ncx + ix);
-            tval[slot] = i;
+            if (slot < oend) {
+              tkey[slot] = (uint32_t)(iy * g.ncx + ix);
+              tval[slot] = i;
+            } else {
+              atomicOr(err, 16u);  // more passing tiles than counted: reported, not stored
+            }
             ++slot;
           }
         }
@@ -251,7 +257,8 @@ void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order
   cudaMemsetAsync(wide_n, 0, sizeof(uint32_t), s);
   k_emit_narrow<<<grid_for(n, 256), 256, 0, s>>>(pos, count, order, off, n, g, tkey, tval,
                                                  wide_list, wide_n, err);
-  k_emit_wide<<<152 * 4, 256, 0, s>>>(pos, order, off, wide_list, wide_n, g, tkey, tval);
+  k_emit_wide<<<152 * 4, 256, 0, s>>>(pos, count, order, off, wide_list, wide_n, g, tkey, tval,
+                                      err);
 }
 
 void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
