@@ -210,10 +210,15 @@ spl_status spl_debug_count_fragments(spl_context *ctx, int64_t *frags_out);
    test): the depth sort's first scatter pass never takes its first tile, so
    the next tile's look-back finds that status unpublished and gives up after
    a short bounded spin; spl_render then returns SPL_ERR_TIMEOUT before the
-   invalid permutation is used, and the context stays usable. */
+   invalid permutation is used, and the context stays usable.  Bit 4 (failure
+   test): the first active particle's tile count is stored one short (when it
+   covers 2 to 64 tiles), so bin emission finds one passing tile more than
+   counted; it stores nothing outside the particle's slots and spl_render
+   returns SPL_ERR_CAPACITY. */
 #define SPL_DEBUG_EXACT_FP64 1
 #define SPL_DEBUG_RADIX_REDUCE_SCAN 2
 #define SPL_DEBUG_LOOKBACK_STALL 4
+#define SPL_DEBUG_SHORT_COUNT 16
 spl_status spl_debug_set_options(spl_context *ctx, int flags);
 
 /* Failure test of device allocation (process-wide): the nth device buffer

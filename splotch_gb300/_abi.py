@@ -39,6 +39,7 @@ SPL_NOALLOC_MAX_PAIRS = 1 << 21
 SPL_DEBUG_EXACT_FP64 = 1
 SPL_DEBUG_RADIX_REDUCE_SCAN = 2
 SPL_DEBUG_LOOKBACK_STALL = 4
+SPL_DEBUG_SHORT_COUNT = 16
 
 
 class Camera(C.Structure):

@@ -440,6 +440,7 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   spl::FrameSetup fs;
   if ((st = spl::frame_setup(d, T, (c->debug_flags & 1) != 0, fs))) return st;
   spl::ProjConst pc = fs.pc;
+  pc.debug_short_count = (c->debug_flags & SPL_DEBUG_SHORT_COUNT) != 0;
   const spl::Tiling g = fs.g;
   const bool onesweep = (c->debug_flags & 2) == 0;
   const int npal = fs.npal;

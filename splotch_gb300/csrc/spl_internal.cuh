@@ -220,6 +220,9 @@ struct ProjConst {
   // per particle of the set, the palette colour of palette types (computed
   // once for frames sharing the set and its palettes), or null
   const float4 *pal_cache;
+  // failure test (spl_debug_set_options): the first compact record's tile count
+  // is stored one short when it is 2..64, so the emission finds a tile more
+  int debug_short_count;
 };
 
 struct Tiling {

@@ -11,6 +11,9 @@ purpose, both in bounded, in-range ways:
   unpublished and gives up after a short spin limit (every write of the pass
   stays in bounds); spl_render must return SPL_ERR_TIMEOUT before anything
   uses the invalid permutation, and the next frame must be exact;
+* a bin entry past its particle's counted tiles (a count stored one short by
+  a test hook): the emission stores nothing outside the particle's slots and
+  spl_render must return SPL_ERR_CAPACITY, the next frame exact;
 * a device allocation that fails: spl_debug_fail_alloc makes the n-th buffer
   allocation fail without calling cudaMalloc; the call must return
   SPL_ERR_ALLOC, and the next call must allocate what is missing and render
@@ -49,6 +52,30 @@ def test_lookback_timeout_is_reported_and_the_context_recovers(renderer, port):
     # the same context renders the frame exactly afterwards
     g = gpu_frame(renderer, prm, w.rc, w.particles)
     assert_parity(g, o)
+
+
+def test_tile_count_mismatch_is_reported_and_the_context_recovers(renderer, port):
+    """Bin emission checks every entry against its particle's counted tiles: with
+    the first active particle's count stored one short (a test hook), the extra
+    passing tile is not stored and spl_render returns SPL_ERR_CAPACITY."""
+    from .test_gpu_parity import _edge_setup, _particles
+    prm, rc = _edge_setup(a_eq_e=False, gpu_order="ftb")
+    # particle 0 sits on a tile corner: four tiles; then a few others
+    specs = [(16.0, 16.0, 6.0, 0.0, 1.0, 0.5)] + [
+        (10.0 + 9.0 * k, 40.0 + 3.0 * (k % 4), 4.0 + k % 3, 0.1 * k, 1.0, 0.1 * k)
+        for k in range(8)]
+    p = _particles(prm, specs)
+    o = oracle_frame(port, prm, rc, p, fp32=False)
+    assert 2 <= np.count_nonzero(o.entries == 0) <= 64  # the first active particle
+    renderer.set_debug(_abi.SPL_DEBUG_SHORT_COUNT)
+    try:
+        with pytest.raises(_abi.SplotchError) as e:
+            gpu_frame(renderer, prm, rc, p)
+    finally:
+        renderer.set_debug(0)
+    assert e.value.code == _abi.SPL_ERR_CAPACITY, e.value
+    assert "more tiles than" in str(e.value)
+    assert_parity(gpu_frame(renderer, prm, rc, p), o)
 
 
 @pytest.mark.parametrize("nth", [1, 3, 8, 17])
