@@ -267,8 +267,9 @@ typedef struct {
    Coverage, tile lists and order are held at the forward's decisions (their
    derivative is zero almost everywhere).  Needs that frame's inputs and, for
    a device image, its output unchanged, and a forward without writeback.
-   Absorption frames are differentiated front to back from the stored final
-   image (no per-particle intermediates are kept). */
+   Ordered absorption frames need spl_context_set_differentiable: the adjoint
+   walks each pixel's composited fragments back to front from the optical
+   depth and stop position the forward kept (no per-particle intermediates). */
 spl_status spl_render_backward(spl_context *ctx, const spl_image *grad_pic, spl_grads *g);
 /* Ordered (a_eq_e = false) frames can only be differentiated when they were
    rendered with this switch on: the forward then also keeps, per pixel, the
