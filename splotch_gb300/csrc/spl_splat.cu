@@ -54,7 +54,8 @@ size_t smem_bytes(int T) {
 // the persistent batch kernel).
 // AUX (ordered frames only): also accumulate each pixel's optical depth and
 // record where the warp stopped, for the adjoint (SplatArgs::aux).
-template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false>
+// MK: the run table holds row masks (tiles of 9 to 16 pixels).
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX = false, bool MK = false>
 // [start, end): the part of the tile's list to composite (the whole list, or
 // one segment of a heavy tile).  partial: null to write the tile into the
 // image, else the segment's own result per tile pixel (x*T + y): its
@@ -89,9 +90,11 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
   const int wbx0 = wx * WX * IW, wby0 = wy * WY * IH;  // warp box, tile-local
   const int wbx1 = min(wbx0 + WX * IW, tw), wby1 = min(wby0 + WY * IH, th);
 
-  // Pixel (k) of this lane: run-table column and row; a pixel outside the
-  // tile reads column 0 with row 255, which no run contains.
+  // Pixel (k) of this lane: run-table column and row (MK: the row's bit); a
+  // pixel outside the tile reads column 0 with row 255 (bit 0), which no run
+  // contains.
   int col[K], row[K];
+  uint32_t rbit[K];
   F2 px2[NP], py2[NP];                   // pixel coordinates of each pair
   F2 acc[NP][3], tr[NP][3];              // per channel: (pixel 2p, pixel 2p+1)
   F2 od[AUX ? NP : 1][3];                // optical depth (AUX)
@@ -103,6 +106,7 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
     const bool valid = warp_has_pixels && x < tw && y < th;
     col[k] = valid ? x : 0;
     row[k] = valid ? y : 255;
+    rbit[k] = valid ? 1u << y : 0u;
   }
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
@@ -126,8 +130,8 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
     // ---- stage B particles ------------------------------------------------
 #pragma unroll 1
     for (int slot = threadIdx.x; slot < B; slot += NT)
-      stage_entry<B, ADD, FTB>(S, srun, RS, slot, a, start + (uint32_t)bi * B + slot, end, x0s,
-                               y0s, tw, th);
+      stage_entry<B, ADD, FTB, MK>(S, srun, RS, slot, a, start + (uint32_t)bi * B + slot, end,
+                                   x0s, y0s, tw, th);
     if (FTB && opaque && threadIdx.x == 0)
       s_opaque = *reinterpret_cast<volatile uint32_t *>(opaque);
     __syncthreads();
@@ -163,8 +167,20 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
             if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
                                           wby0 + ((2 * p) / WX) * IH))
               continue;
-            const bool in0 = covered(run, col[2 * p], row[2 * p]);
-            const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
+            bool in0, in1;
+            if (MK && 2 * p + 1 < K) {
+              // the pair's columns x < 8 and x + 8 share the word at x (a
+              // pixel outside the tile has bit 0)
+              const uint32_t w2 = reinterpret_cast<const uint32_t *>(run)[col[2 * p] & 7];
+              in0 = (w2 & rbit[2 * p]) != 0u;
+              in1 = ((w2 >> 16) & rbit[2 * p + 1]) != 0u;
+            } else if (MK) {
+              in0 = covered_mask(run, col[2 * p], rbit[2 * p]);
+              in1 = false;
+            } else {
+              in0 = covered(run, col[2 * p], row[2 * p]);
+              in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
+            }
             // a pixel the particle does not cover gets att = 0: its update is
             // the identity in every mode
             if (ADD) {
@@ -221,7 +237,7 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
         bool mine_done = true;
 #pragma unroll
         for (int k = 0; k < K; ++k) {
-          if (row[k] != 255) {
+          if (MK ? rbit[k] != 0u : row[k] != 255) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
               const float t = (k & 1) ? f2hi(tr[k / 2][c]) : f2lo(tr[k / 2][c]);
@@ -245,6 +261,10 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
   }
 
   // ---- write the tile (pic is x-major: pixel (x,y) at (x*yres + y)*3) ----
+  if (MK) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) row[k] = rbit[k] ? __ffs(rbit[k]) - 1 : 255;
+  }
 #pragma unroll
   for (int k = 0; k < K; ++k) {
     if (row[k] != 255 && partial) {
@@ -274,11 +294,11 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
   }
 }
 
-template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX>
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX, bool MK>
 __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const int tile = a.tile_order ? (int)__ldg(a.tile_order + blockIdx.x) : (int)blockIdx.x;
-  splat_tile<NT, WX, WY, B, ADD, FTB, AUX>(a, tile, smem_raw, a.tile_start[tile],
+  splat_tile<NT, WX, WY, B, ADD, FTB, AUX, MK>(a, tile, smem_raw, a.tile_start[tile],
                                            a.tile_start[tile + 1], nullptr);
 }
 
@@ -326,7 +346,7 @@ __global__ void __launch_bounds__(NT) k_splat_queue(BatchSplatArgs q) {
 // tile of one segment is rendered into the image directly; each segment of a
 // longer tile writes its own composite and transmittance, and
 // k_splat_combine folds them.
-template <int NT, int WX, int WY, int B, bool ADD, bool FTB>
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool MK>
 __global__ void __launch_bounds__(NT) k_splat_seg(SplatArgs a, SplatSegs g) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const uint64_t item = blockIdx.x;
@@ -349,7 +369,8 @@ __global__ void __launch_bounds__(NT) k_splat_seg(SplatArgs a, SplatSegs g) {
   float4 *part =
       nseg > 1 ? g.partial + (g.seg_off[o] + ls) * (size_t)(a.T * a.T) * 2 : nullptr;
   uint32_t *opq = (FTB && nseg > 1) ? g.opaque + o : nullptr;
-  splat_tile<NT, WX, WY, B, ADD, FTB>(a, tile, smem_raw, s0, s1, part, opq, ls == nseg - 1);
+  splat_tile<NT, WX, WY, B, ADD, FTB, false, MK>(a, tile, smem_raw, s0, s1, part, opq,
+                                                ls == nseg - 1);
 }
 
 // One CTA per tile (tile order): a tile of several segments gets, per pixel,
@@ -424,25 +445,36 @@ __global__ void __launch_bounds__(256) k_count_fragments(SplatArgs a,
   if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(total, cnt);
 }
 
-template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX>
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool AUX, bool MK>
 void launch_one(const SplatArgs &a, size_t sm, cudaStream_t s) {
-  auto k = k_splat<NT, WX, WY, B, ADD, FTB, AUX>;
+  auto k = k_splat<NT, WX, WY, B, ADD, FTB, AUX, MK>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<a.ncx * a.ncy, NT, sm, s>>>(a);
 }
 
-template <int NT, int WX, int WY, int B>
-int launch_cfg(const SplatArgs &a, cudaStream_t s) {
-  const size_t sm = smem_bytes<B>(a.T);
+template <int NT, int WX, int WY, int B, bool MK>
+void launch_form(const SplatArgs &a, size_t sm, cudaStream_t s) {
   const bool aux = a.aux != nullptr;
   if (a.a_eq_e)
-    launch_one<NT, WX, WY, B, true, false, false>(a, sm, s);
+    launch_one<NT, WX, WY, B, true, false, false, MK>(a, sm, s);
   else if (a.order_mode == 1)
-    aux ? launch_one<NT, WX, WY, B, false, true, true>(a, sm, s)
-        : launch_one<NT, WX, WY, B, false, true, false>(a, sm, s);
+    aux ? launch_one<NT, WX, WY, B, false, true, true, MK>(a, sm, s)
+        : launch_one<NT, WX, WY, B, false, true, false, MK>(a, sm, s);
   else
-    aux ? launch_one<NT, WX, WY, B, false, false, true>(a, sm, s)
-        : launch_one<NT, WX, WY, B, false, false, false>(a, sm, s);
+    aux ? launch_one<NT, WX, WY, B, false, false, true, MK>(a, sm, s)
+        : launch_one<NT, WX, WY, B, false, false, false, MK>(a, sm, s);
+}
+
+// MKOK: tiles of 9 to 16 pixels take the row-mask form of the run table in
+// this configuration (its warp boxes start at column 0 or 8, and a pixel
+// pair's columns are x < 8 and x + 8).
+template <int NT, int WX, int WY, int B, bool MKOK>
+int launch_cfg(const SplatArgs &a, cudaStream_t s) {
+  const size_t sm = smem_bytes<B>(a.T);
+  if (MKOK && a.T > 8 && a.T <= 16)
+    launch_form<NT, WX, WY, B, MKOK>(a, sm, s);
+  else
+    launch_form<NT, WX, WY, B, false>(a, sm, s);
   return 1;
 }
 
@@ -491,30 +523,33 @@ int launch_splat(const SplatArgs &a, cudaStream_t s) {
                 ? a.config
                 : splat_default_config(a.T, a.a_eq_e != 0);
   switch (cfg) {
-    case 0: return launch_cfg<256, 1, 1, 256>(a, s);
-    case 1: return launch_cfg<64, 2, 2, 128>(a, s);
-    case 2: return launch_cfg<128, 2, 1, 128>(a, s);
-    case 3: return launch_cfg<256, 2, 2, 256>(a, s);
-    default: return launch_cfg<256, 4, 4, 256>(a, s);
+    case 0: return launch_cfg<256, 1, 1, 256, true>(a, s);
+    case 1: return launch_cfg<64, 2, 2, 128, true>(a, s);
+    case 2: return launch_cfg<128, 2, 1, 128, true>(a, s);
+    case 3: return launch_cfg<256, 2, 2, 256, false>(a, s);
+    default: return launch_cfg<256, 4, 4, 256, false>(a, s);
   }
 }
 
 namespace {
 
-template <int NT, int WX, int WY, int B, bool ADD, bool FTB>
+template <int NT, int WX, int WY, int B, bool ADD, bool FTB, bool MK>
 void launch_seg_one(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s) {
   const size_t sm = smem_bytes<B>(a.T);
-  auto k = k_splat_seg<NT, WX, WY, B, ADD, FTB>;
+  auto k = k_splat_seg<NT, WX, WY, B, ADD, FTB, MK>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   k<<<grid, NT, sm, s>>>(a, g);
 }
 
-template <int NT, int WX, int WY, int B>
+template <int NT, int WX, int WY, int B, bool MKOK>
 void launch_seg_cfg(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cudaStream_t s) {
+  const bool mk = MKOK && a.T > 8 && a.T <= 16;
   if (a.a_eq_e)
-    launch_seg_one<NT, WX, WY, B, true, false>(a, g, grid, s);
+    mk ? launch_seg_one<NT, WX, WY, B, true, false, MKOK>(a, g, grid, s)
+       : launch_seg_one<NT, WX, WY, B, true, false, false>(a, g, grid, s);
   else
-    launch_seg_one<NT, WX, WY, B, false, true>(a, g, grid, s);
+    mk ? launch_seg_one<NT, WX, WY, B, false, true, MKOK>(a, g, grid, s)
+       : launch_seg_one<NT, WX, WY, B, false, true, false>(a, g, grid, s);
 }
 
 }  // namespace
@@ -532,11 +567,11 @@ int launch_splat_split(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cu
                       ? a.config
                       : splat_default_config(a.T, a.a_eq_e != 0);
   switch (cfg) {
-    case 0: launch_seg_cfg<256, 1, 1, 256>(a, g, grid, s); break;
-    case 1: launch_seg_cfg<64, 2, 2, 128>(a, g, grid, s); break;
-    case 2: launch_seg_cfg<128, 2, 1, 128>(a, g, grid, s); break;
-    case 3: launch_seg_cfg<256, 2, 2, 256>(a, g, grid, s); break;
-    default: launch_seg_cfg<256, 4, 4, 256>(a, g, grid, s); break;
+    case 0: launch_seg_cfg<256, 1, 1, 256, true>(a, g, grid, s); break;
+    case 1: launch_seg_cfg<64, 2, 2, 128, true>(a, g, grid, s); break;
+    case 2: launch_seg_cfg<128, 2, 1, 128, true>(a, g, grid, s); break;
+    case 3: launch_seg_cfg<256, 2, 2, 256, false>(a, g, grid, s); break;
+    default: launch_seg_cfg<256, 4, 4, 256, false>(a, g, grid, s); break;
   }
   if (a.a_eq_e)
     k_splat_combine<true><<<a.ncx * a.ncy, 256, 0, s>>>(a, g);

@@ -31,13 +31,17 @@ struct Stage {
 
 // Run-table row length: T rounded up to whole 8-pixel items, so that every
 // column an item can address lies in the row and rows stay 16-byte aligned.
-// Per column the covered rows lo | (hi-lo)<<8, zero outside the bounding box.
+// Per column the covered rows [lo, hi): as lo | (hi-lo)<<8, or (tiles of 9
+// to 16 pixels, MK) as the row mask with bits lo..hi-1 set, column c at slot
+// mask_slot(c) so that columns c and c + 8 share one 32-bit word; zero
+// outside the bounding box.
 __host__ __device__ constexpr int run_stride(int T) { return (T + 7) & ~7; }
+__host__ __device__ constexpr int mask_slot(int c) { return (c & 7) * 2 + (c >> 3); }
 
 // Stage list entry jj of the tile at (x0s, y0s), tw x th pixels, into slot;
 // an entry past the list end stages an empty box.  Returns the particle index
 // (0xffffffff past the end); *colour receives the particle's colour.
-template <int B, bool ADD, bool NEGQ>
+template <int B, bool ADD, bool NEGQ, bool MK = false>
 __device__ __forceinline__ uint32_t stage_entry(Stage<B> &S, uint16_t *srun, int RS, int slot,
                                                 const SplatArgs &a, uint32_t jj, uint32_t end,
                                                 int x0s, int y0s, int tw, int th,
@@ -67,7 +71,11 @@ __device__ __forceinline__ uint32_t stage_entry(Stage<B> &S, uint16_t *srun, int
         const float dy = fsqrt(fsub(radsq, dxsq));
         const int lo = max(miny, f2i(fadd(fsub(posy, dy), 1.f)));
         const int hi = min(maxy, f2i(fadd(fadd(posy, dy), 1.f)));
-        run[x] = (uint16_t)(lo | (max(hi - lo, 0) << 8));
+        if (MK)  // 0 <= lo < hi <= th <= 16 when the run is not empty
+          run[mask_slot(x)] =
+              hi > lo ? (uint16_t)(((1u << hi) - 1u) & ~((1u << lo) - 1u)) : (uint16_t)0;
+        else
+          run[x] = (uint16_t)(lo | (max(hi - lo, 0) << 8));
       }
       // The rows the particle covers.  Every step from |dx| to the run is
       // monotone, so a column nearer the centre holds the runs of the columns
@@ -76,11 +84,18 @@ __device__ __forceinline__ uint32_t stage_entry(Stage<B> &S, uint16_t *srun, int
       // no hit; the columns stay those of the bounding box.
       const int xa = min(max(f2i(floorf(posx)), minx), maxx - 1);
       const int xb = min(xa + 1, maxx - 1);
-      const uint32_t ra = run[xa], rb = run[xb];
-      const uint32_t rc = (rb >> 8) > (ra >> 8) ? rb : ra;
-      if ((rc >> 8) > 0u)
-        bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((rc & 255u) << 16) |
-             (((rc & 255u) + (rc >> 8)) << 24);
+      const uint32_t ra = run[MK ? mask_slot(xa) : xa], rb = run[MK ? mask_slot(xb) : xb];
+      if (MK) {
+        const uint32_t rc = ra | rb;  // nested runs: the union is the longer
+        if (rc)
+          bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((uint32_t)(__ffs(rc) - 1) << 16) |
+               ((uint32_t)(32 - __clz(rc)) << 24);
+      } else {
+        const uint32_t rc = (rb >> 8) > (ra >> 8) ? rb : ra;
+        if ((rc >> 8) > 0u)
+          bb = (uint32_t)minx | ((uint32_t)maxx << 8) | ((rc & 255u) << 16) |
+               (((rc & 255u) + (rc >> 8)) << 24);
+      }
     }
     const float s2 = stp * kLog2e;
     S.pxy[slot] = make_float4(posx, posx, posy, posy);
@@ -108,6 +123,12 @@ __device__ __forceinline__ uint32_t stage_entry(Stage<B> &S, uint16_t *srun, int
 __device__ __forceinline__ bool covered(const uint16_t *run, int col, int row) {
   const uint32_t r = run[col];
   return (uint32_t)(row - (int)(r & 255)) < (r >> 8);
+}
+
+// The same test on a row-mask table: bit is the pixel's row bit (0 outside
+// the tile).
+__device__ __forceinline__ bool covered_mask(const uint16_t *run, int col, uint32_t bit) {
+  return (run[mask_slot(col)] & bit) != 0u;
 }
 
 // Does a bounding box reach the 16x4 pixels of the pair whose left item
