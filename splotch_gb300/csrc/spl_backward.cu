@@ -101,7 +101,8 @@ __global__ void k_adj_seg_count(const uint32_t *__restrict__ tile_start, int64_t
 // The ordered 128-thread form is held to 6 CTAs per SM (80 registers): with
 // heavy tiles cut into segments it is throughput-bound, and more resident
 // warps pay for the few spilled values.  Other forms choose their registers.
-template <int NT, int WX, int WY, int B, bool ADD>
+// MK: the staged coverage is held as row masks (tiles of 9 to 16 pixels).
+template <int NT, int WX, int WY, int B, bool ADD, bool MK>
 __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(AdjArgs a) {
   constexpr int K = WX * WY;
   constexpr int NP = (K + 1) / 2;
@@ -145,6 +146,7 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
   // g: dL/dpic; od: the forward's optical depth; sb: optical depth behind
   // and at the current particle; nbg: minus the composite behind it
   int col[K], row[K];
+  uint32_t rbit[K];  // the row's bit (0 outside the tile)
   F2 px2[NP], py2[NP];
   F2 g[NP][3], od[NO][3], sb[NO][3], nbg[NO][3];
   uint32_t mystop = 0xffffffffu;
@@ -155,6 +157,7 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
     const bool valid = warp_has_pixels && x < tw && y < th;
     col[k] = valid ? x : 0;
     row[k] = valid ? y : 255;
+    rbit[k] = valid ? 1u << y : 0u;
   }
 #pragma unroll
   for (int p = 0; p < NP; ++p) {
@@ -249,9 +252,9 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
 #pragma unroll 1
     for (int slot = threadIdx.x; slot < B; slot += NT) {
       float4 c;
-      const uint32_t idx = stage_entry<B, ADD, false>(St, srun, RS, slot, f,
-                                                      start + (uint32_t)bi * B + slot, end, x0s,
-                                                      y0s, tw, th, &c);
+      const uint32_t idx = stage_entry<B, ADD, false, MK>(St, srun, RS, slot, f,
+                                                          start + (uint32_t)bi * B + slot, end,
+                                                          x0s, y0s, tw, th, &c);
       if (!ADD && idx != 0xffffffffu) {
         const float d0 = fadd(c.x, f.gray), d1 = fadd(c.y, f.gray), d2 = fadd(c.z, f.gray);
         const float w0 = -(f.gray / (d0 * d0)), w1 = -(f.gray / (d1 * d1));
@@ -297,8 +300,10 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
             if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
                                           wby0 + ((2 * p) / WX) * IH))
               continue;
-            const bool in0 = covered(run, col[2 * p], row[2 * p]);
-            const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
+            const int k1 = 2 * p + 1 < K ? 2 * p + 1 : 0;
+            bool in0, in1;
+            covered_pair<MK>(run, col[2 * p], row[2 * p], rbit[2 * p], 2 * p + 1 < K, col[k1],
+                             row[k1], rbit[k1], in0, in1);
             // additive: lanes without a covered pixel skip; ordered: every lane
             // runs the terms (they vanish), so that the warp can vote on the
             // Taylor range of expm1 below
@@ -387,7 +392,7 @@ __global__ void __launch_bounds__(NT, (NT == 128 && !ADD) ? 6 : 0) k_splat_adj(A
 // and their own back-to-front composite V (V <- V*T + q*(1-T), from 0), into
 // seg_state[segment][pixel] = (U, V).  Same item mapping and pixel layout as
 // k_splat_adj.
-template <int NT, int WX, int WY, int B>
+template <int NT, int WX, int WY, int B, bool MK>
 __global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
   constexpr int K = WX * WY;
   constexpr int NP = (K + 1) / 2;
@@ -422,6 +427,7 @@ __global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
   const int wbx1 = min(wbx0 + WX * IW, tw), wby1 = min(wby0 + WY * IH, th);
 
   int col[K], row[K];
+  uint32_t rbit[K];
   F2 px2[NP], py2[NP], U[NP][3], V[NP][3];
   uint32_t mystop = 0xffffffffu;
 #pragma unroll
@@ -431,6 +437,7 @@ __global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
     const bool valid = warp_has_pixels && x < tw && y < th;
     col[k] = valid ? x : 0;
     row[k] = valid ? y : 255;
+    rbit[k] = valid ? 1u << y : 0u;
     if (valid)
       mystop = min(mystop, __float_as_uint(
                                __ldg(f.aux + (size_t)(x0s + x) * f.yres + (y0s + y)).w));
@@ -449,8 +456,8 @@ __global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
   for (int bi = 0; bi < nbatch; ++bi) {
 #pragma unroll 1
     for (int slot = threadIdx.x; slot < B; slot += NT)
-      stage_entry<B, false, false>(St, srun, RS, slot, f, start + (uint32_t)bi * B + slot, end,
-                                   x0s, y0s, tw, th);
+      stage_entry<B, false, false, MK>(St, srun, RS, slot, f, start + (uint32_t)bi * B + slot,
+                                       end, x0s, y0s, tw, th);
     __syncthreads();
     if (warp_has_pixels && rel0 + (uint32_t)bi * B >= wstop) {
 #pragma unroll 1
@@ -472,8 +479,10 @@ __global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
             if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
                                           wby0 + ((2 * p) / WX) * IH))
               continue;
-            const bool in0 = covered(run, col[2 * p], row[2 * p]);
-            const bool in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
+            const int k1 = 2 * p + 1 < K ? 2 * p + 1 : 0;
+            bool in0, in1;
+            covered_pair<MK>(run, col[2 * p], row[2 * p], rbit[2 * p], 2 * p + 1 < K, col[k1],
+                             row[k1], rbit[k1], in0, in1);
             if (!(in0 || in1)) continue;
             const F2 dx = sub2(px2[p], f2(pxy.x, pxy.y));
             const F2 dy = sub2(py2[p], f2(pxy.z, pxy.w));
@@ -509,24 +518,34 @@ __global__ void __launch_bounds__(NT) k_adj_ordered_state(AdjArgs a) {
   }
 }
 
-template <int NT, int WX, int WY, int B>
-void launch_adj_cfg(const AdjArgs &a, uint32_t grid, cudaStream_t s) {
+template <int NT, int WX, int WY, int B, bool MK>
+void launch_adj_form(const AdjArgs &a, uint32_t grid, cudaStream_t s) {
   const size_t sm = adj_smem_bytes<B>(a.f.T);
   if (a.f.a_eq_e) {
-    auto k = k_splat_adj<NT, WX, WY, B, true>;
+    auto k = k_splat_adj<NT, WX, WY, B, true, MK>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, NT, sm, s>>>(a);
   } else {
     if (a.seg_len != 0xffffffffu) {  // split ordered tiles: the state pass first
-      auto k1 = k_adj_ordered_state<NT, WX, WY, B>;
+      auto k1 = k_adj_ordered_state<NT, WX, WY, B, MK>;
       const size_t sm1 = sizeof(Stage<B>) + (size_t)B * run_stride(a.f.T) * 2;
       cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1);
       k1<<<grid, NT, sm1, s>>>(a);
     }
-    auto k = k_splat_adj<NT, WX, WY, B, false>;
+    auto k = k_splat_adj<NT, WX, WY, B, false, MK>;
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k<<<grid, NT, sm, s>>>(a);
   }
+}
+
+// MKOK: tiles of 9 to 16 pixels take row masks in this configuration (warp
+// boxes at column 0 or 8).
+template <int NT, int WX, int WY, int B, bool MKOK>
+void launch_adj_cfg(const AdjArgs &a, uint32_t grid, cudaStream_t s) {
+  if (MKOK && a.f.T > 8 && a.f.T <= 16)
+    launch_adj_form<NT, WX, WY, B, MKOK>(a, grid, s);
+  else
+    launch_adj_form<NT, WX, WY, B, false>(a, grid, s);
 }
 
 // ---- chain rule through colourisation and projection ------------------------
@@ -733,11 +752,11 @@ int launch_splat_adjoint(const AdjArgs &a0, cudaStream_t s) {
   scan_counts(a.seg_cnt, a.f.tile_order, ntiles, a.seg_off, a.scan_scratch, s, &launches);
   const uint32_t grid = (uint32_t)std::min<int64_t>(grid64, 0x7fffffff);
   switch (cfg) {
-    case 0: launch_adj_cfg<256, 1, 1, 256>(a, grid, s); break;
-    case 1: launch_adj_cfg<64, 2, 2, 128>(a, grid, s); break;
-    case 2: launch_adj_cfg<128, 2, 1, 128>(a, grid, s); break;
-    case 3: launch_adj_cfg<256, 2, 2, 256>(a, grid, s); break;
-    default: launch_adj_cfg<256, 4, 4, 256>(a, grid, s); break;
+    case 0: launch_adj_cfg<256, 1, 1, 256, true>(a, grid, s); break;
+    case 1: launch_adj_cfg<64, 2, 2, 128, true>(a, grid, s); break;
+    case 2: launch_adj_cfg<128, 2, 1, 128, true>(a, grid, s); break;
+    case 3: launch_adj_cfg<256, 2, 2, 256, false>(a, grid, s); break;
+    default: launch_adj_cfg<256, 4, 4, 256, false>(a, grid, s); break;
   }
   return launches + (!add && seg_len != 0xffffffffu ? 2 : 1);
 }

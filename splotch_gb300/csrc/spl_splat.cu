@@ -167,20 +167,10 @@ __device__ __forceinline__ void splat_tile(const SplatArgs &a, const int tile,
             if (NP > 1 && !box_meets_pair(bbj, wbx0 + ((2 * p) % WX) * IW,
                                           wby0 + ((2 * p) / WX) * IH))
               continue;
+            const int k1 = 2 * p + 1 < K ? 2 * p + 1 : 0;
             bool in0, in1;
-            if (MK && 2 * p + 1 < K) {
-              // the pair's columns x < 8 and x + 8 share the word at x (a
-              // pixel outside the tile has bit 0)
-              const uint32_t w2 = reinterpret_cast<const uint32_t *>(run)[col[2 * p] & 7];
-              in0 = (w2 & rbit[2 * p]) != 0u;
-              in1 = ((w2 >> 16) & rbit[2 * p + 1]) != 0u;
-            } else if (MK) {
-              in0 = covered_mask(run, col[2 * p], rbit[2 * p]);
-              in1 = false;
-            } else {
-              in0 = covered(run, col[2 * p], row[2 * p]);
-              in1 = 2 * p + 1 < K && covered(run, col[2 * p + 1], row[2 * p + 1]);
-            }
+            covered_pair<MK>(run, col[2 * p], row[2 * p], rbit[2 * p], 2 * p + 1 < K, col[k1],
+                             row[k1], rbit[k1], in0, in1);
             // a pixel the particle does not cover gets att = 0: its update is
             // the identity in every mode
             if (ADD) {
@@ -307,8 +297,9 @@ __global__ void __launch_bounds__(NT) k_splat(SplatArgs a) {
 // longest-list-first order across all frames; every frame's own arguments
 // (image, tiling, mode, tile-range slice) come from a per-frame table.  MODE
 // 0 / 1: every item is additive / front-to-back (one splat form compiled in);
-// 2: the form is chosen per item.
-template <int NT, int WX, int WY, int B, int MODE>
+// 2: the form is chosen per item.  MK: row-mask coverage (the batch's tile
+// size is 9 to 16 pixels).
+template <int NT, int WX, int WY, int B, int MODE, bool MK>
 __global__ void __launch_bounds__(NT) k_splat_queue(BatchSplatArgs q) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   __shared__ uint32_t s_item;
@@ -328,15 +319,15 @@ __global__ void __launch_bounds__(NT) k_splat_queue(BatchSplatArgs q) {
     const int tile = (int)(gt - q.tile_base[f]);
     const uint32_t t0 = a.tile_start[tile], t1 = a.tile_start[tile + 1];
     if (MODE == 0)
-      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw, t0, t1, nullptr);
+      splat_tile<NT, WX, WY, B, true, false, false, MK>(a, tile, smem_raw, t0, t1, nullptr);
     else if (MODE == 1)
-      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw, t0, t1, nullptr);
+      splat_tile<NT, WX, WY, B, false, true, false, MK>(a, tile, smem_raw, t0, t1, nullptr);
     else if (a.a_eq_e)
-      splat_tile<NT, WX, WY, B, true, false>(a, tile, smem_raw, t0, t1, nullptr);
+      splat_tile<NT, WX, WY, B, true, false, false, MK>(a, tile, smem_raw, t0, t1, nullptr);
     else if (a.order_mode == 1)
-      splat_tile<NT, WX, WY, B, false, true>(a, tile, smem_raw, t0, t1, nullptr);
+      splat_tile<NT, WX, WY, B, false, true, false, MK>(a, tile, smem_raw, t0, t1, nullptr);
     else
-      splat_tile<NT, WX, WY, B, false, false>(a, tile, smem_raw, t0, t1, nullptr);
+      splat_tile<NT, WX, WY, B, false, false, false, MK>(a, tile, smem_raw, t0, t1, nullptr);
     __syncthreads();  // s_item and the staging buffers are reused
   }
 }
@@ -582,10 +573,10 @@ int launch_splat_split(const SplatArgs &a, const SplatSegs &g, uint32_t grid, cu
 
 namespace {
 
-template <int NT, int WX, int WY, int B, int MODE>
+template <int NT, int WX, int WY, int B, int MODE, bool MK>
 int launch_queue_mode(const BatchSplatArgs &q, cudaStream_t s) {
   const size_t sm = smem_bytes<B>(q.T);
-  auto k = k_splat_queue<NT, WX, WY, B, MODE>;
+  auto k = k_splat_queue<NT, WX, WY, B, MODE, MK>;
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int per_sm = 0, dev = 0, nsm = 0;
   cudaGetDevice(&dev);
@@ -599,13 +590,19 @@ int launch_queue_mode(const BatchSplatArgs &q, cudaStream_t s) {
   return 1;
 }
 
-template <int NT, int WX, int WY, int B>
-int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
+template <int NT, int WX, int WY, int B, bool MK>
+int launch_queue_form(const BatchSplatArgs &q, cudaStream_t s) {
   switch (q.mode) {
-    case 0: return launch_queue_mode<NT, WX, WY, B, 0>(q, s);
-    case 1: return launch_queue_mode<NT, WX, WY, B, 1>(q, s);
-    default: return launch_queue_mode<NT, WX, WY, B, 2>(q, s);
+    case 0: return launch_queue_mode<NT, WX, WY, B, 0, MK>(q, s);
+    case 1: return launch_queue_mode<NT, WX, WY, B, 1, MK>(q, s);
+    default: return launch_queue_mode<NT, WX, WY, B, 2, MK>(q, s);
   }
+}
+
+template <int NT, int WX, int WY, int B, bool MKOK>
+int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
+  return MKOK && q.T > 8 && q.T <= 16 ? launch_queue_form<NT, WX, WY, B, MKOK>(q, s)
+                                      : launch_queue_form<NT, WX, WY, B, false>(q, s);
 }
 
 }  // namespace
@@ -613,11 +610,11 @@ int launch_queue_cfg(const BatchSplatArgs &q, cudaStream_t s) {
 int launch_splat_queue(const BatchSplatArgs &q, int cfg, cudaStream_t s) {
   if (q.nwork == 0) return 0;
   switch (cfg) {
-    case 0: return launch_queue_cfg<256, 1, 1, 256>(q, s);
-    case 1: return launch_queue_cfg<64, 2, 2, 128>(q, s);
-    case 2: return launch_queue_cfg<128, 2, 1, 128>(q, s);
-    case 3: return launch_queue_cfg<256, 2, 2, 256>(q, s);
-    default: return launch_queue_cfg<256, 4, 4, 256>(q, s);
+    case 0: return launch_queue_cfg<256, 1, 1, 256, true>(q, s);
+    case 1: return launch_queue_cfg<64, 2, 2, 128, true>(q, s);
+    case 2: return launch_queue_cfg<128, 2, 1, 128, true>(q, s);
+    case 3: return launch_queue_cfg<256, 2, 2, 256, false>(q, s);
+    default: return launch_queue_cfg<256, 4, 4, 256, false>(q, s);
   }
 }
 

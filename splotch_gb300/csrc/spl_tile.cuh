@@ -131,6 +131,26 @@ __device__ __forceinline__ bool covered_mask(const uint16_t *run, int col, uint3
   return (run[mask_slot(col)] & bit) != 0u;
 }
 
+// Coverage of a lane's pixel pair: pixel 0 at column c0, row r0 (row bit b0),
+// pixel 1 (when has1) at c1, r1, b1.  Row masks (MK): the pair's columns are
+// c0 < 8 and c0 + 8, whose masks share the 32-bit word at c0.
+template <bool MK>
+__device__ __forceinline__ void covered_pair(const uint16_t *run, int c0, int r0, uint32_t b0,
+                                             bool has1, int c1, int r1, uint32_t b1, bool &in0,
+                                             bool &in1) {
+  if (MK && has1) {
+    const uint32_t w2 = reinterpret_cast<const uint32_t *>(run)[c0 & 7];
+    in0 = (w2 & b0) != 0u;
+    in1 = ((w2 >> 16) & b1) != 0u;
+  } else if (MK) {
+    in0 = covered_mask(run, c0, b0);
+    in1 = false;
+  } else {
+    in0 = covered(run, c0, r0);
+    in1 = has1 && covered(run, c1, r1);
+  }
+}
+
 // Does a bounding box reach the 16x4 pixels of the pair whose left item
 // starts at (ix0, iy0)?
 __device__ __forceinline__ bool box_meets_pair(uint32_t bb, int ix0, int iy0) {
