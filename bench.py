@@ -75,9 +75,9 @@ def parse():
     ap.add_argument("--workload", default="absorption", choices=["absorption", "additive"])
     ap.add_argument("--tile", type=int, default=16)
     ap.add_argument("--order", default="ftb", choices=["ftb", "btf"])
-    ap.add_argument("--e2e-steps", type=int, default=10,
-                    help="frames in the host-memory sequence (the first frame's copy is "
-                         "not hidden behind an earlier frame)")
+    ap.add_argument("--e2e-steps", type=int, default=30,
+                    help="frames in the host-memory sequence (the first frame's copy and "
+                         "the last frame's render are not hidden behind another frame)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fwd-bwd", action="store_true")
     ap.add_argument("--no-batched", action="store_true")

@@ -499,10 +499,11 @@ bool splat_config_valid(int cfg, int T) {
 }
 
 // Measured on GB300 (50M-particle absorption frame and 1M additive frame at
-// T=16): 4 warps x 16x4 is fastest for the absorption splat, 8 warps x 8x4 for
-// the additive one; larger tiles need the wider configurations.
-int splat_default_config(int T, bool additive) {
-  if (!additive && splat_config_valid(2, T)) return 2;
+// T=16): 4 warps x 16x4 is fastest for both splats (absorption 4.34 ms against
+// 5.33 for 2 warps x 16x8 and 7.08 for 8 warps x 8x4; additive 0.30 ms against
+// 0.34 for both); larger tiles need the wider configurations.
+int splat_default_config(int T, bool /*additive*/) {
+  if (splat_config_valid(2, T)) return 2;
   if (splat_config_valid(0, T)) return 0;
   if (splat_config_valid(3, T)) return 3;
   return 4;
