@@ -53,7 +53,7 @@ def test_stage_parity(name, renderer, port):
 
 
 @pytest.mark.parametrize("mode", ["add", "btf", "ftb"])
-@pytest.mark.parametrize("tile", [8, 16, 32, 50])
+@pytest.mark.parametrize("tile", [8, 12, 16, 32, 50])
 def test_every_splat_config(tile, mode, renderer, port):
     """Every launch configuration that covers the tile size gives a parity image."""
     from splotch_gb300 import _abi

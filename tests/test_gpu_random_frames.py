@@ -23,7 +23,7 @@ def _case(seed: int):
     rng = np.random.default_rng(1000 + seed)
     xres = int(rng.integers(33, 301))
     yres = int(rng.integers(33, 301))
-    tile = int(rng.choice([8, 16, 32]))
+    tile = int(rng.choice([8, 12, 16, 32]))
     additive = bool(rng.random() < 0.4)
     if additive:
         w = synth.plain_additive(n=6000, seed=seed, xres=xres, yres=yres, tile=tile)

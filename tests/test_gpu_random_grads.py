@@ -24,7 +24,7 @@ def _case(seed: int):
     mode = str(rng.choice(["additive", "absorption"]))
     xres = int(rng.integers(96, 257))
     yres = int(rng.integers(96, 257))
-    tile = int(rng.choice([8, 16, 32]))
+    tile = int(rng.choice([8, 12, 16, 32]))
     w = synth.differentiable(n=20_000, mode=mode, seed=seed, xres=xres, yres=yres, tile=tile)
     c = np.full(3, 50.0)  # the differentiable workload's box is [0,100]^3
     d = rng.normal(size=3)
