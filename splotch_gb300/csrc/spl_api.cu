@@ -1094,7 +1094,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
   cudaEventRecord(c->ev[1], s);
 
   // ---- particle pass, then the particles sorted by level and direction -------
-  spl::RayParts rp{as<double4>(c->ray_rc), as<float4>(c->ray_cf), as<float4>(c->ray_clo),
+  spl::RayParts rp{as<double4_16a>(c->ray_rc), as<float4>(c->ray_cf), as<float4>(c->ray_clo),
                    as<float4>(c->ray_pod), as<float2>(c->ray_cov), as<uint32_t>(c->ray_code),
                    d_err};
   spl::launch_rays_prep(aos_dev, &soa, n, pc, k, rp, s);
@@ -1107,7 +1107,7 @@ spl_status spl_render_rays(spl_context *c, const spl_frame_desc *d, const spl_ra
                           order, n, 0, 32, true, c->scratch.p, s, &launches, d_err,
                           (c->debug_flags & 2) == 0);
   }
-  spl::RayParts rs{as<double4>(c->ray_rc2), as<float4>(c->ray_cf2), as<float4>(c->ray_clo2),
+  spl::RayParts rs{as<double4_16a>(c->ray_rc2), as<float4>(c->ray_cf2), as<float4>(c->ray_clo2),
                    as<float4>(c->ray_pod2), as<float2>(c->ray_cov2), key_s, d_err};
   spl::launch_rays_sorted(key_s, order, n, nlev, lev_start, rp, rs, s);
   launches += 2;

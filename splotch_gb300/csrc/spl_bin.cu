@@ -217,15 +217,38 @@ __global__ void __launch_bounds__(256) k_emit_wide(const float4 *__restrict__ po
   }
 }
 
-// tile_start[t] = first sorted position whose key is >= t.
+// tile_start[t] = first sorted position whose key is >= t.  A thread takes
+// four consecutive positions 4q..4q+3 (one 16-byte load when the keys are
+// 16-byte aligned and all four exist) and the key before them; positions run
+// to ne inclusive, where the key is taken as ntiles.
 __global__ void __launch_bounds__(256) k_tile_ranges(const uint32_t *__restrict__ key,
                                                      int64_t ne, int64_t ntiles,
                                                      uint32_t *__restrict__ tile_start) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p <= ne;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t kprev = p > 0 ? (int64_t)key[p - 1] : -1;
-    const int64_t kcur = p < ne ? (int64_t)key[p] : ntiles;
-    for (int64_t t = kprev + 1; t <= kcur; ++t) tile_start[t] = (uint32_t)p;
+  const bool vec = (reinterpret_cast<uintptr_t>(key) & 15u) == 0;
+  const int64_t nq = ne / 4 + 1;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nq;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p0 = q * 4;
+    uint32_t k4[4];
+    if (vec && p0 + 4 <= ne) {
+      const uint4 v = __ldg(reinterpret_cast<const uint4 *>(key + p0));
+      k4[0] = v.x;
+      k4[1] = v.y;
+      k4[2] = v.z;
+      k4[3] = v.w;
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) k4[i] = p0 + i < ne ? __ldg(key + p0 + i) : 0u;
+    }
+    int64_t kprev = p0 > 0 ? (int64_t)__ldg(key + p0 - 1) : -1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int64_t p = p0 + i;
+      if (p > ne) break;
+      const int64_t kcur = p < ne ? (int64_t)k4[i] : ntiles;
+      for (int64_t t = kprev + 1; t <= kcur; ++t) tile_start[t] = (uint32_t)p;
+      kprev = kcur;
+    }
   }
 }
 
@@ -263,7 +286,7 @@ void launch_emit(const float4 *pos, const uint32_t *count, const uint32_t *order
 
 void launch_tile_ranges(const uint32_t *sorted_tkey, int64_t ne, int64_t ntiles,
                         uint32_t *tile_start, cudaStream_t s) {
-  k_tile_ranges<<<grid_for(ne + 1, 256), 256, 0, s>>>(sorted_tkey, ne, ntiles, tile_start);
+  k_tile_ranges<<<grid_for(ne / 4 + 1, 256), 256, 0, s>>>(sorted_tkey, ne, ntiles, tile_start);
 }
 
 __global__ void __launch_bounds__(256) k_gather_u32(const uint32_t *__restrict__ src,

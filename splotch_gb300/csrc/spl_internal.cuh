@@ -639,7 +639,7 @@ struct RayConst {
 // walk then follow neighbouring paths, and a leaf's list is close in memory.
 constexpr int kRayCodeShift = 27;
 struct RayParts {
-  double4 *rc;     // unit direction c and angular radius r, as the reference has them
+  double4_16a *rc;  // unit direction c and angular radius r, as the reference has them
   float4 *cf;      // the same rounded to float
   float4 *clo;     // c - cf (float), the low parts of c as a float-float pair
   float4 *pod;     // colour after the radius correction

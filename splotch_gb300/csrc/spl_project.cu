@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(256) k_rays_prep(L load, int64_t n, ProjConst 
     r = dmul(r, rcorr);
     const float rc1 = (float)rcorr;
     const float f2 = fac / (rc1 * rc1);  // brightness / rcorr^2
-    const double4 rc = make_double4(cc[0], cc[1], cc[2], r);
+    const double4_16a rc = make_double4_16a(cc[0], cc[1], cc[2], r);
     const float4 cf = make_float4(__double2float_rn(cc[0]), __double2float_rn(cc[1]),
                                   __double2float_rn(cc[2]), __double2float_rn(r));
     uint32_t code = (uint32_t)k.nlev + 1;

@@ -413,7 +413,7 @@ __device__ __noinline__ double3 ray_dir3(const RayConst *__restrict__ kd, int X,
 // pixel (X, Y), out of line (a chord within the float screen's margin): the
 // weight on a hit, -1 on a miss.
 __device__ __noinline__ float ray_plane_exact(const RayConst *__restrict__ kd, int X, int Y,
-                                              double4 rc) {
+                                              double4_16a rc) {
   double d[3];
   ray_pix_dir_plane(*kd, X, Y, d);
   float w;
@@ -425,14 +425,14 @@ __device__ __noinline__ float ray_plane_exact(const RayConst *__restrict__ kd, i
 // of its near half (no coverage test).
 __device__ __noinline__ float4 ray_overlap(const RayConst *__restrict__ kd, int X, int Y,
                                            uint32_t s0, uint32_t s1,
-                                           const double4 *__restrict__ rcs,
+                                           const double4_16a *__restrict__ rcs,
                                            const float4 *__restrict__ pods) {
   double d[3];
   ray_pix_dir(*kd, X, Y, d);
   const double h2 = kd->h2sigma;
   float o0 = 0.f, o1 = 0.f, o2 = 0.f;
   for (uint32_t i = s0; i < s1; ++i) {
-    const double4 rc = rcs[i];
+    const double4_16a rc = rcs[i];
     const double c[3] = {rc.x, rc.y, rc.z};
     const double cosang = ddot3(d, c);
     const double sasq = dmul(dsub(1.0, cosang), dadd(1.0, cosang));

@@ -29,7 +29,7 @@ struct RayPart {
   bool th_ready;  // th_hi, th_lo computed (on first use)
 };
 
-__device__ __forceinline__ RayPart ray_part(const RayConst &k, double4 rc, float4 cf) {
+__device__ __forceinline__ RayPart ray_part(const RayConst &k, double4_16a rc, float4 cf) {
   RayPart p;
   p.c[0] = rc.x;
   p.c[1] = rc.y;
@@ -123,7 +123,7 @@ __device__ __forceinline__ void ray_pix_dir(const RayConst &k, int ix, int iy, d
 // The sphere-vs-ray test of subrender4 (new_renderer.cc:303-312) in double;
 // on a hit, w = exp(-sin^2/(r*h2sigma)^2) (1 for a NaN argument, which is
 // what the reference's exptable returns for it).
-__device__ __forceinline__ bool ray_exact_hit(const double d[3], double4 rc, double h2sigma,
+__device__ __forceinline__ bool ray_exact_hit(const double d[3], double4_16a rc, double h2sigma,
                                               float &w) {
   const double c[3] = {rc.x, rc.y, rc.z};
   const double r = rc.w;

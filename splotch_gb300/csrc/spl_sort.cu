@@ -261,15 +261,26 @@ __global__ void __launch_bounds__(RS_THREADS) k_os_hist(const uint32_t *__restri
   for (int i = threadIdx.x; i < OS_MAX_PASS * RS_BINS; i += RS_THREADS) (&h[0][0])[i] = 0;
   __syncthreads();
   const int npass = (bit1 - bit0 + 7) / 8;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t k = __ldg(keys + i);
+  auto count = [&](uint32_t k) {
     for (int p = 0; p < npass; ++p) {
       const int sh = bit0 + 8 * p;
       const int nb = min(8, bit1 - sh);
       atomicAdd(&h[p][(k >> sh) & ((1u << nb) - 1u)], 1u);
     }
+  };
+  // four keys per 16-byte load when the keys are 16-byte aligned, the
+  // remainder one at a time
+  const int64_t nq = (reinterpret_cast<uintptr_t>(keys) & 15u) == 0 ? n / 4 : 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < nq; q += stride) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(keys) + q);
+    count(v.x);
+    count(v.y);
+    count(v.z);
+    count(v.w);
   }
+  for (int64_t i = nq * 4 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += stride)
+    count(__ldg(keys + i));
   __syncthreads();
   for (int p = 0; p < npass; ++p)
     if (h[p][threadIdx.x]) atomicAdd(hist + p * RS_BINS + threadIdx.x, (unsigned long long)h[p][threadIdx.x]);
