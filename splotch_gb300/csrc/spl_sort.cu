@@ -376,24 +376,38 @@ template <typename T, typename L>
 __global__ void __launch_bounds__(SC_THREADS) k_scan_apply(L load, int64_t n,
                                                            const T *partials, T *out) {
   __shared__ T sm[33];
+  // the tile passes through shared memory both ways, so that a warp's loads
+  // and stores are consecutive elements while each thread scans SC_ITEMS
+  // consecutive ones (rows padded by one element against bank conflicts)
+  __shared__ T stage[SC_THREADS * (SC_ITEMS + 1)];
   const int64_t base = (int64_t)blockIdx.x * SC_TILE;
-  // each thread owns SC_ITEMS consecutive elements
-  const int64_t my = base + (int64_t)threadIdx.x * SC_ITEMS;
+#pragma unroll 4
+  for (int r = 0; r < SC_ITEMS; ++r) {
+    const int e = r * SC_THREADS + threadIdx.x;
+    const int64_t i = base + e;
+    stage[(e / SC_ITEMS) * (SC_ITEMS + 1) + e % SC_ITEMS] = i < n ? load(i) : T(0);
+  }
+  __syncthreads();
   T v[SC_ITEMS];
   T s = 0;
 #pragma unroll
   for (int j = 0; j < SC_ITEMS; ++j) {
-    const int64_t i = my + j;
-    v[j] = i < n ? load(i) : T(0);
+    v[j] = stage[threadIdx.x * (SC_ITEMS + 1) + j];
     s += v[j];
   }
-  T tot;
+  T tot;  // (the scan's barriers also order the reads above before the writes below)
   T ex = block_excl_scan<T>(s, sm, tot) + partials[blockIdx.x];
 #pragma unroll
   for (int j = 0; j < SC_ITEMS; ++j) {
-    const int64_t i = my + j;
-    if (i < n) out[i] = ex;
+    stage[threadIdx.x * (SC_ITEMS + 1) + j] = ex;
     ex += v[j];
+  }
+  __syncthreads();
+#pragma unroll 4
+  for (int r = 0; r < SC_ITEMS; ++r) {
+    const int e = r * SC_THREADS + threadIdx.x;
+    const int64_t i = base + e;
+    if (i < n) out[i] = stage[(e / SC_ITEMS) * (SC_ITEMS + 1) + e % SC_ITEMS];
   }
 }
 
