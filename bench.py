@@ -60,9 +60,9 @@ METRIC = "Mparticles/s & frames/s (plain, batched, fwd+bwd) on 1 GB300 at ≤1e-
 SPLAT_CAPTURE = {
     "source": "profiles/k_splat_ftb_10M.md",
     "fragments": 7.53e8,          # reference fragments of the captured launch
-    "dram_bytes": 85.9e6,         # dram__bytes (read + write) of the launch
-    "issue_frac": 0.74,           # issue slots busy per SMSP while active
-    "smem_wavefront_frac": 0.283,  # L1 data-pipe (shared) wavefronts, of peak
+    "dram_bytes": 85.4e6,         # dram__bytes (read + write) of the launch
+    "issue_frac": 0.70,           # issue slots busy per SMSP while active
+    "smem_wavefront_frac": 0.274,  # L1 data-pipe (shared) wavefronts, of peak
 }
 
 
