@@ -191,6 +191,25 @@ def test_host_rendering_mirror(built, port):
     assert rel_linf(rc.pic, pic64) <= IMAGE_TOL
 
 
+def test_large_writeback_into_pageable_memory(renderer):
+    """A write-back of 108 MB (3M particles, not a round size) into pageable
+    host memory: its bytes equal the same write-back into device memory, the
+    images are equal, and the array did change."""
+    torch = pytest.importorskip("torch")
+    w = synth.plain_absorption(n_gas=2_400_001, n_star=600_000, xres=320, yres=200, tile=16)
+    keep: list = []
+    desc = sg.frame_desc(w.params, w.rc, keep)
+    host = w.particles.copy()
+    pic = np.zeros((320, 200, 3), np.float32)
+    renderer.render_aos(desc, host, pic, writeback=True)
+    dev = torch.from_numpy(w.particles.copy().view(np.uint8).reshape(-1)).cuda()
+    pic_d = torch.zeros((320, 200, 3), dtype=torch.float32, device="cuda")
+    renderer.render_aos(desc, dev, pic_d, device=True, writeback=True)
+    assert np.array_equal(host.view(np.uint8).reshape(-1), dev.cpu().numpy())
+    assert np.array_equal(pic, pic_d.cpu().numpy())
+    assert not np.array_equal(host.view(np.uint8), w.particles.view(np.uint8))
+
+
 def test_soa_device_matches_aos(renderer):
     torch = pytest.importorskip("torch")
     w = synth.plain_additive(n=30000, xres=128, yres=128, tile=16)
