@@ -33,7 +33,8 @@ enum {
   SPL_ERR_ALLOC = 3,       /* device or pinned allocation failed */
   SPL_ERR_CAPACITY = 4,    /* a fixed-capacity buffer overflowed */
   SPL_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
-  SPL_ERR_UNSUPPORTED = 6  /* option not implemented on this path */
+  SPL_ERR_UNSUPPORTED = 6, /* option not implemented on this path */
+  SPL_ERR_INTERNAL = 7     /* an internal consistency check failed */
 };
 
 /* Memory space of a caller buffer. */

@@ -12,7 +12,7 @@ import numpy as np
 
 SPL_MAX_TYPES = 8
 SPL_OK, SPL_ERR_INVALID, SPL_ERR_CUDA, SPL_ERR_ALLOC, SPL_ERR_CAPACITY, SPL_ERR_TIMEOUT, \
-    SPL_ERR_UNSUPPORTED = range(7)
+    SPL_ERR_UNSUPPORTED, SPL_ERR_INTERNAL = range(8)
 SPL_MEM_HOST, SPL_MEM_DEVICE = 0, 1
 SPL_LAYOUT_AOS, SPL_LAYOUT_SOA = 0, 1
 SPL_WRITEBACK_NONE, SPL_WRITEBACK_FULL = 0, 1

@@ -744,6 +744,8 @@ spl_status spl_render(spl_context *c, const spl_frame_desc *d, const spl_particl
   if (err & 8u) return fail(SPL_ERR_CAPACITY, "the compacted particle arrays overflowed");
   if (err & 16u)
     return fail(SPL_ERR_CAPACITY, "bin emission found more tiles than a particle's count");
+  if (err & 32u)
+    return fail(SPL_ERR_INTERNAL, "the activity screen kept a particle the projection culls");
   c->stats.n_fallback = words[2];
   c->stats.n_wide = words[1];
 

@@ -915,6 +915,8 @@ spl_status check_status(spl_batch *b, bool &overflow) {
   overflow = (h[0] & 3u) != 0 || (h[4] & 8u) != 0;
   if (h[4] & 1u) return fail(SPL_ERR_INVALID, "particle type outside [0, ptypes)");
   if (h[4] & 2u) return fail(SPL_ERR_TIMEOUT, "a look-back wait gave up");
+  if (h[4] & 32u)
+    return fail(SPL_ERR_INTERNAL, "the activity screen kept a particle the projection culls");
   if (h[0] & 4u)
     return fail(SPL_ERR_CAPACITY, "bin emission found more tiles than a record's count");
   return SPL_OK;

@@ -346,15 +346,73 @@ __global__ void __launch_bounds__(256) k_project_full(L load, int64_t n, ProjCon
 //   k_project_dense  : each block expands its words into a dense list of
 //                      active particles, projects and colourises them with
 //                      all lanes busy, and writes the compact records
-// One warp: the activity bits of word w (particles 32w .. 32w+31).
+// A float screen of project_geom's activity decision (perspective frames):
+// 1 when the particle is active and 0 when it is inactive whatever the
+// roundings of the exact computation, -1 when it cannot decide (near a z
+// plane or an image edge; a NaN, infinite or non-positive radius; a type
+// outside [0, ptypes); orthographic or exact-FP64 frames), which leaves the
+// particle to project_geom.  The camera transform is evaluated with fused
+// multiply-adds (within 2^-20 of its terms' magnitude); the projection
+// factor's relative error is then below ek = ez/(nz - ez) + 2^-18, and screen
+// position and radius are within (4 ek + 2^-16) of their magnitudes plus
+// 2^-6 pixel, bounds far above the float errors of both computations.  The
+// footprint test holds, or fails, for every value inside those bounds.
+__device__ __forceinline__ int screen_activity(const ProjConst &c, const PIn &in) {
+  if (c.exact_fp64 || !c.projection) return -1;
+  const int t = in.type;
+  if (t < 0 || t >= c.ptypes) return -1;
+  const float *m = c.mat;
+  const float zf = fmaf(m[10], in.z, fmaf(m[9], in.y, fmaf(m[8], in.x, m[11])));
+  const float ez = 0x1p-20f * (fabsf(m[8] * in.x) + fabsf(m[9] * in.y) +
+                               fabsf(m[10] * in.z) + fabsf(m[11]));
+  const float nz = -zf;  // the z cut keeps zmin < -z < zmax
+  if (nz + ez <= c.zmin || nz - ez >= c.zmax) return 0;
+  if (!(nz - ez > c.zmin && nz - ez > 0.f && nz + ez < c.zmax)) return -1;
+  const float xc = fmaf(m[2], in.z, fmaf(m[1], in.y, fmaf(m[0], in.x, m[3])));
+  const float yc = fmaf(m[6], in.z, fmaf(m[5], in.y, fmaf(m[4], in.x, m[7])));
+  const float sx = fabsf(m[0] * in.x) + fabsf(m[1] * in.y) + fabsf(m[2] * in.z) + fabsf(m[3]);
+  const float sy = fabsf(m[4] * in.x) + fabsf(m[5] * in.y) + fabsf(m[6] * in.z) + fabsf(m[7]);
+  const float k = c.res2 / (c.fovfct * nz);     // the projection factor xfac2
+  const float ek = ez / (nz - ez) + 0x1p-18f;  // its relative error, with margin
+  const float xs = (float)c.xsum, ys = (float)c.ysum;
+  const float X = xs + xc * k, Y = ys + yc * k;
+  const float r2 = 2.f * in.r * k * c.smooth[t];
+  const float R = sqrtf(r2 * r2 + c.minrad2);  // the radius after the minrad correction
+  const float e = 4.f * ek + 0x1p-16f;
+  const float mX = (fabsf(xs) + fabsf(xc * k) + R) * e + sx * k * 0x1p-19f + 0x1p-6f;
+  const float mY = (fabsf(ys) + fabsf(yc * k) + R) * e + sy * k * 0x1p-19f + 0x1p-6f;
+  const float ext = 0.75f * R;
+  if (!(fabsf(X) < 1e30f && fabsf(Y) < 1e30f && mX < 1e30f && mY < 1e30f && ext < 1e30f))
+    return -1;
+  // maxx <= 0 needs x + 0.75r + 1 < 1; minx >= xres needs x - 0.75r + 1 >= xres
+  if (X + ext + mX < 0.f || X - ext - mX + 1.f >= (float)c.xres || Y + ext + mY < 0.f ||
+      Y - ext - mY + 1.f >= (float)c.yres)
+    return 0;
+  if (!(in.r > 1e-30f && in.r < 1e30f && r2 > 1e-20f && c.smooth[t] > 0.f)) return -1;
+  // active: max(int(x - 0.75r + 1), 0) < min(int(x + 0.75r + 1), xres), and in y
+  const float ax = fmaxf(floorf(X - ext + 1.f + mX), 0.f);
+  const float bx = fminf(floorf(X + ext + 1.f - mX), (float)c.xres);
+  const float ay = fmaxf(floorf(Y - ext + 1.f + mY), 0.f);
+  const float by = fminf(floorf(Y + ext + 1.f - mY), (float)c.yres);
+  return (ax < bx && ay < by) ? 1 : -1;
+}
+
+// One warp: the activity bits of word w (particles 32w .. 32w+31).  The float
+// screen decides nearly every particle; the few it cannot go through
+// project_geom.
 template <class L>
 __device__ __forceinline__ void flags_word(const L &load, int64_t n, const ProjConst &c,
                                            uint32_t *__restrict__ flags, uint32_t *err,
                                            int64_t w, int lane) {
   const int64_t i = w * 32 + lane;
-  bool active = false;
+  int dec = 0;
+  PIn in{};
   if (i < n) {
-    const PIn in = load(i);
+    in = load(i);
+    dec = screen_activity(c, in);
+  }
+  bool active = dec == 1;
+  if (__any_sync(0xffffffffu, dec < 0) && dec < 0) {
     float x, y, z, r, I;
     bool fb = false;
     active = project_geom(c, in, x, y, z, r, I, fb, err);
@@ -372,6 +430,88 @@ __global__ void __launch_bounds__(256, 5) k_project_flags(L load, int64_t n, Pro
   for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < nwords;
        w += ((int64_t)gridDim.x * blockDim.x) >> 5)
     flags_word(load, n, c, flags, err, w, lane);
+}
+
+// SoA activity flags, four particles per lane: a warp step takes 128
+// particles (four flag words) with 16-byte loads of x, y, z, r and an 8-byte
+// load of the types, so each warp keeps four times the bytes in flight of the
+// one-particle-per-lane form (which the latency of its loads bounded, not its
+// arithmetic).  Needs x, y, z, r 16-byte and type 8-byte aligned.
+__global__ void __launch_bounds__(256) k_project_flags_soa4(SoAIn soa, int64_t n, ProjConst c,
+                                                            uint32_t *__restrict__ flags,
+                                                            uint32_t *err) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nwords = (n + 31) / 32;
+  const int64_t nsteps = (n + 127) / 128;
+  for (int64_t st = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; st < nsteps;
+       st += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t i0 = st * 128 + lane * 4;
+    float xs[4], ys[4], zs[4], rs[4];
+    int ts[4] = {0, 0, 0, 0};
+    if (i0 + 4 <= n) {
+      const float4 X = __ldg(reinterpret_cast<const float4 *>(soa.x + i0));
+      const float4 Y = __ldg(reinterpret_cast<const float4 *>(soa.y + i0));
+      const float4 Z = __ldg(reinterpret_cast<const float4 *>(soa.z + i0));
+      const float4 R = __ldg(reinterpret_cast<const float4 *>(soa.r + i0));
+      xs[0] = X.x; xs[1] = X.y; xs[2] = X.z; xs[3] = X.w;
+      ys[0] = Y.x; ys[1] = Y.y; ys[2] = Y.z; ys[3] = Y.w;
+      zs[0] = Z.x; zs[1] = Z.y; zs[2] = Z.z; zs[3] = Z.w;
+      rs[0] = R.x; rs[1] = R.y; rs[2] = R.z; rs[3] = R.w;
+      if (soa.type) {
+        const ushort4 T = __ldg(reinterpret_cast<const ushort4 *>(soa.type + i0));
+        ts[0] = T.x; ts[1] = T.y; ts[2] = T.z; ts[3] = T.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int64_t i = i0 + j;
+        xs[j] = i < n ? __ldg(soa.x + i) : 0.f;
+        ys[j] = i < n ? __ldg(soa.y + i) : 0.f;
+        zs[j] = i < n ? __ldg(soa.z + i) : 0.f;
+        rs[j] = i < n ? __ldg(soa.r + i) : 0.f;
+        ts[j] = (i < n && soa.type) ? (int)__ldg(soa.type + i) : 0;
+      }
+    }
+    uint32_t nib = 0;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      PIn in{};
+      in.x = xs[j];
+      in.y = ys[j];
+      in.z = zs[j];
+      in.r = rs[j];
+      in.I = 1.f;  // activity does not depend on the intensity or the colour
+      in.type = ts[j];
+      const bool here = i0 + j < n;
+      const int dec = here ? screen_activity(c, in) : 0;
+      bool active = dec == 1;
+      if (__any_sync(0xffffffffu, dec < 0) && dec < 0) {
+        float x, y, z, r, I;
+        bool fb = false;
+        active = project_geom(c, in, x, y, z, r, I, fb, err);
+      }
+      nib |= (active ? 1u : 0u) << j;
+    }
+    // word q of the step holds lanes 8q .. 8q+7, four bits each
+    uint32_t v = nib << (4 * (lane & 7));
+    v |= __shfl_xor_sync(0xffffffffu, v, 1);
+    v |= __shfl_xor_sync(0xffffffffu, v, 2);
+    v |= __shfl_xor_sync(0xffffffffu, v, 4);
+    const int64_t w = st * 4 + (lane >> 3);
+    if ((lane & 7) == 0 && w < nwords) flags[w] = v;
+  }
+}
+
+bool soa4_ok(const SoAIn *soa) {
+  auto a16 = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+  return soa && a16(soa->x) && a16(soa->y) && a16(soa->z) && a16(soa->r) &&
+         (!soa->type || (reinterpret_cast<uintptr_t>(soa->type) & 7u) == 0);
+}
+
+int soa4_grid(int64_t n) {
+  const int64_t nsteps = (n + 127) / 128;
+  const int64_t b = (nsteps + 7) / 8;
+  return (int)(b < 152 * 16 ? b : 152 * 16);
 }
 
 constexpr int DW = kDenseWordsPerBlock;  // flag words per dense block (2048 particles)
@@ -420,6 +560,7 @@ __device__ __forceinline__ void dense_block(const L &load, int64_t n, const Proj
   for (uint32_t k = threadIdx.x; k < nloc; k += blockDim.x) {
     const uint32_t i = s_list[k];
     const POut p = project_core(c, load(i), i, o.err);
+    if (!p.active) atomicOr(o.err, 32u);  // the activity pass and this one disagree
     const uint32_t dst = base + k;
     if (dst >= o.cap_c) {
       atomicOr(o.err, 8u);
@@ -670,7 +811,10 @@ void launch_project(const void *aos, const SoAIn *soa, int64_t n, const ProjCons
       scan_popc(o.flags, nwords, o.word_off, o.n_act, o.scan_scratch, s, launches);
       k_project_dense<<<db, 256, 0, s>>>(la, n, c, o.flags, o.word_off, o);
     } else {
-      k_project_flags<<<fb, 256, 0, s>>>(ls, n, c, o.flags, o.err);
+      if (soa4_ok(soa))
+        k_project_flags_soa4<<<soa4_grid(n), 256, 0, s>>>(*soa, n, c, o.flags, o.err);
+      else
+        k_project_flags<<<fb, 256, 0, s>>>(ls, n, c, o.flags, o.err);
       scan_popc(o.flags, nwords, o.word_off, o.n_act, o.scan_scratch, s, launches);
       k_project_dense<<<db, 256, 0, s>>>(ls, n, c, o.flags, o.word_off, o);
     }
@@ -693,6 +837,8 @@ void launch_project_flags(const void *aos, const SoAIn *soa, int64_t n, const Pr
   if (aos)
     k_project_flags<<<fb, 256, 0, s>>>(LoadAoS{static_cast<const uint8_t *>(aos)}, n, c,
                                        o.flags, o.err);
+  else if (soa4_ok(soa))
+    k_project_flags_soa4<<<soa4_grid(n), 256, 0, s>>>(*soa, n, c, o.flags, o.err);
   else
     k_project_flags<<<fb, 256, 0, s>>>(
         LoadSoA{soa->x, soa->y, soa->z, soa->r, soa->I, soa->cr, soa->cg, soa->cb, soa->type},

@@ -154,6 +154,38 @@ def test_bins_across_footprint_sizes(tile, mode, renderer, port):
     assert len(o.entries) > n, counts.max()
 
 
+@pytest.mark.parametrize("mode", ["add", "ftb"])
+def test_footprints_at_the_image_edges(mode, renderer, port):
+    """Footprint edges within +-0.02 pixel of each image border (where the
+    activity pass's float screen cannot decide and the exact arithmetic does),
+    and radii from below the minrad floor to several pixels: projection, order
+    and bins bit-exact."""
+    rng = np.random.default_rng(5)
+    prm, rc = _edge_setup(xres=97, yres=61, a_eq_e=(mode == "add"), gpu_order="ftb")
+    xres, yres = 97, 61
+    specs = []
+    for k in range(800):
+        rpix = float(rng.choice([0.3, 1.0, 1.7, 4.0, 9.0]) * rng.uniform(0.9, 1.1))
+        ext = 0.75 * float(np.sqrt(rpix * rpix + 1.0))  # radius after the minrad_pix=1 correction
+        d = float(rng.uniform(-0.02, 0.02))
+        side = k % 4
+        if side == 0:    # x - 0.75r + 1 = xres + d
+            px, py = xres + d - 1 + ext, float(rng.uniform(0, yres))
+        elif side == 1:  # x + 0.75r + 1 = 1 + d
+            px, py = d - ext, float(rng.uniform(0, yres))
+        elif side == 2:
+            px, py = float(rng.uniform(0, xres)), yres + d - 1 + ext
+        else:
+            px, py = float(rng.uniform(0, xres)), d - ext
+        specs.append((px, py, rpix, float(rng.uniform(-5, 5)), 1.0, float(rng.random())))
+    p = _particles(prm, specs)
+    g = gpu_frame(renderer, prm, rc, p)
+    o = oracle_frame(port, prm, rc, p, fp32=False)
+    assert_parity(g, o)
+    act = g.projected["active"].astype(bool)
+    assert 0 < act.sum() < len(p)
+
+
 def test_zmin_and_all_culled(renderer, port):
     # both particles sit at depth -z = 100 and 99.5 in camera space: zmin=100.5
     # culls them (splotch_host.cc:123, cull when -z <= zmin)
@@ -238,7 +270,9 @@ def test_determinism(renderer):
 @pytest.mark.parametrize("camera", ["outside", "inside_cluster"])
 def test_fast_projection_equals_fp64(camera, renderer):
     """The float-float projection (with per-particle FP64 fallback) is bit-identical
-    to the exact FP64 arithmetic over millions of particles."""
+    to the exact FP64 arithmetic over millions of particles, and the activity
+    pass's float screen (off under the FP64 hook) selects the same particles:
+    visiting order and tile bins are equal."""
     w = synth.plain_absorption(n_gas=1_600_000, n_star=400_000, xres=640, yres=360, tile=16)
     if camera == "inside_cluster":  # many particles near the camera axis and plane
         p = w.particles
@@ -250,15 +284,20 @@ def test_fast_projection_equals_fp64(camera, renderer):
     desc = sg.frame_desc(w.params, w.rc, keep)
     pic = np.zeros((640, 360, 3), np.float32)
     out = {}
+    ntiles = ((640 + 15) // 16) * ((360 + 15) // 16)
     for flags in (0, 1):
         renderer.set_debug(flags)
         try:
             renderer.render_aos(desc, w.particles.copy(), pic)
         finally:
             renderer.set_debug(0)
-        out[flags] = (renderer.projected(len(w.particles)), renderer.stats()["n_fallback"])
+        out[flags] = (renderer.projected(len(w.particles)), renderer.stats()["n_fallback"],
+                      renderer.order(len(w.particles)), renderer.bins(ntiles))
     a, b = out[0][0].view(np.uint8), out[1][0].view(np.uint8)
     assert np.array_equal(a, b)
+    assert np.array_equal(out[0][2], out[1][2])
+    for u, v in zip(out[0][3], out[1][3]):
+        assert np.array_equal(u, v)
     assert out[1][1] == 0
     assert out[0][1] < 0.01 * len(w.particles), f"{out[0][1]} FP64 fallbacks"
     print(camera, "fallbacks", out[0][1], "of", len(w.particles))
