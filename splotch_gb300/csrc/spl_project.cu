@@ -352,8 +352,10 @@ __global__ void __launch_bounds__(256) k_project_full(L load, int64_t n, ProjCon
 // plane or an image edge; a NaN, infinite or non-positive radius; a type
 // outside [0, ptypes); orthographic or exact-FP64 frames), which leaves the
 // particle to project_geom.  The camera transform is evaluated with fused
-// multiply-adds (within 2^-20 of its terms' magnitude); the projection
-// factor's relative error is then below ek = ez/(nz - ez) + 2^-18, and screen
+// multiply-adds, within 2^-20 of a bound on its terms' magnitude (the row's
+// absolute sum times max(|x|, |y|, |z|), plus the translation); the
+// projection factor's relative error is then below ek = ez/(nz - ez) + 2^-18
+// (the factor and ek use the fast division, within 2 ulp), and screen
 // position and radius are within (4 ek + 2^-16) of their magnitudes plus
 // 2^-6 pixel, bounds far above the float errors of both computations.  The
 // footprint test holds, or fails, for every value inside those bounds.
@@ -362,18 +364,23 @@ __device__ __forceinline__ int screen_activity(const ProjConst &c, const PIn &in
   const int t = in.type;
   if (t < 0 || t >= c.ptypes) return -1;
   const float *m = c.mat;
+  const float am = fmaxf(fmaxf(fabsf(in.x), fabsf(in.y)), fabsf(in.z));
   const float zf = fmaf(m[10], in.z, fmaf(m[9], in.y, fmaf(m[8], in.x, m[11])));
-  const float ez = 0x1p-20f * (fabsf(m[8] * in.x) + fabsf(m[9] * in.y) +
-                               fabsf(m[10] * in.z) + fabsf(m[11]));
+  const float ez =
+      0x1p-20f * fmaf(fabsf(m[8]) + fabsf(m[9]) + fabsf(m[10]), am, fabsf(m[11]));
   const float nz = -zf;  // the z cut keeps zmin < -z < zmax
   if (nz + ez <= c.zmin || nz - ez >= c.zmax) return 0;
-  if (!(nz - ez > c.zmin && nz - ez > 0.f && nz + ez < c.zmax)) return -1;
+  // (the fast division's bound holds for denominators in [2^-126, 2^126])
+  if (!(nz - ez > c.zmin && nz - ez > 1e-30f && nz + ez < c.zmax && nz + ez < 1e30f))
+    return -1;
+  const float den = c.fovfct * nz;
+  if (!(den > 1e-30f && den < 1e30f)) return -1;
   const float xc = fmaf(m[2], in.z, fmaf(m[1], in.y, fmaf(m[0], in.x, m[3])));
   const float yc = fmaf(m[6], in.z, fmaf(m[5], in.y, fmaf(m[4], in.x, m[7])));
-  const float sx = fabsf(m[0] * in.x) + fabsf(m[1] * in.y) + fabsf(m[2] * in.z) + fabsf(m[3]);
-  const float sy = fabsf(m[4] * in.x) + fabsf(m[5] * in.y) + fabsf(m[6] * in.z) + fabsf(m[7]);
-  const float k = c.res2 / (c.fovfct * nz);     // the projection factor xfac2
-  const float ek = ez / (nz - ez) + 0x1p-18f;  // its relative error, with margin
+  const float sx = fmaf(fabsf(m[0]) + fabsf(m[1]) + fabsf(m[2]), am, fabsf(m[3]));
+  const float sy = fmaf(fabsf(m[4]) + fabsf(m[5]) + fabsf(m[6]), am, fabsf(m[7]));
+  const float k = __fdividef(c.res2, den);                // the projection factor xfac2
+  const float ek = __fdividef(ez, nz - ez) + 0x1p-18f;  // its relative error, with margin
   const float xs = (float)c.xsum, ys = (float)c.ysum;
   const float X = xs + xc * k, Y = ys + yc * k;
   const float r2 = 2.f * in.r * k * c.smooth[t];
