@@ -389,7 +389,7 @@ def roofline(stage_ms: dict, n: int, n_act: int, n_entries: int, n_tiles: int, f
         v["ms"] = stage_ms[k + "_ms"]
         v["peak"] = hbm if v["bound"] == "hbm" else fp32_peak
         v["frac"] = v["achieved"] / v["peak"]
-    kernels = {"project": "k_project_flags+scan_popc+k_project_dense",
+    kernels = {"project": "k_project_flags_soa4+scan_popc+k_project_dense",
                "sort": "k_os_hist+k_os_prefix+k_rs_downsweep",
                "bin": "k_gather_u32+scan+k_emit_narrow+k_emit_wide+tile sort+k_tile_ranges",
                "splat": "k_splat"}
