@@ -102,7 +102,10 @@ typedef struct {
 } spl_frame_desc;
 
 /* Particle input.  AoS: aos points at n particle_sim records.  SoA: x..I,
-   cr/cg/cb (e.r/e.g/e.b) are float arrays; type may be NULL (all type 0). */
+   cr/cg/cb (e.r/e.g/e.b) are float arrays; type may be NULL (all type 0).
+   Any alignment of the element type works; x, y, z, r 16-byte aligned and type
+   8-byte aligned (as allocations are) let the activity pass read four
+   particles per 16-byte load. */
 typedef struct {
   int64_t n;
   int layout;   /* SPL_LAYOUT_* */
